@@ -1,0 +1,368 @@
+#!/usr/bin/env python
+"""Env-steps/s of the generalized-coordinates step on GB300.
+
+Workload (the headline configuration): the quadruped (free sphere torso, 4
+legs x 2 hinged capsules, nq 15, nv 14, 8 motors of gear 150, 9 geoms vs the
+ground plane), 4096 envs, one env step = 5 pipeline steps of 0.01 s with one
+action per env step (brax/envs/base.py:128-137), actions ~ U(-1, 1), resets
+as brax/envs/ant.py:209-213 (init_q + U(-0.1, 0.1), qd ~ 0.1 N(0, 1)).
+
+value  : env-steps/s with state and actions resident in HBM; each timed step
+         is one braxg_step launch (5 frames x 4096 envs) timed with CUDA
+         events on the launching stream; the L2 is flushed (a 256 MB write)
+         before every timed step, outside the events.
+e2e    : the same metric through the public API with host buffers: per step
+         the actions are copied from pinned host memory, the step runs, and
+         the observation (q, qd) is copied back and waited for.
+--impl reference: the CPU baseline (the numpy restatement of the reference
+         path, see oracle/) on all host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'env-steps/s fwd & fwd+adjoint, 4096-env quadruped, 1 GB300, at 1e-5 rel err'
+WORKLOAD = 'quadruped'
+N_FRAMES = 5
+
+
+def parse():
+  p = argparse.ArgumentParser()
+  p.add_argument('--gpus', type=int, default=1)
+  p.add_argument('--steps', type=int, default=200)
+  p.add_argument('--warmup', type=int, default=10)
+  p.add_argument('--impl', default='braxg', choices=['braxg', 'reference'])
+  p.add_argument('--envs', type=int, default=4096)
+  p.add_argument('--inverse', default='newton_schulz', choices=['newton_schulz', 'cholesky'])
+  p.add_argument('--threads-per-env', type=int, default=0)
+  p.add_argument('--envs-per-cta', type=int, default=0)
+  p.add_argument('--cpu-sample-envs', type=int, default=256)
+  p.add_argument('--no-cpu-baseline', action='store_true')
+  return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# algorithmic work per pipeline step (FLOPs and bytes), fixed formulas
+# ---------------------------------------------------------------------------
+
+
+def algorithmic(sys_, n_mv: float):
+  nl, nv, nq, nu = sys_.num_links(), sys_.qd_size(), sys_.q_size(), sys_.act_size()
+  ncon = sys_.contacts.n
+  m = sys_.n_constraint_rows()
+  f_tree = 400 * nl + 150 * nv
+  f_m = 11 * nv * nv + 33 * nv
+  f_fact = nv ** 3 / 3 + m * nv * nv
+  f_a = m * m * nv + 2 * m * nv + 100 * nv * ncon
+  f_pg = 2 * m * m * n_mv
+  f_tail = 2 * m * nv + 4 * nv * nv
+  flops = f_tree + f_m + f_fact + f_a + f_pg + f_tail
+  bytes_env_step = 4 * (nq + nv + nu) + 4 * (nq + nv + 13 * nl) + 2 * 4 * nv * nv
+  return flops, bytes_env_step
+
+
+def load_nmv():
+  path = os.path.join(ROOT, 'tests', 'golden', 'pg_matvecs.json')
+  with open(path) as f:
+    return json.load(f)
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+
+class ClockSampler:
+  Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+       'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+       'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+  def __init__(self, index: int):
+    self.index = index
+    self.proc = None
+    self.lines = []
+
+  def __enter__(self):
+    try:
+      self.proc = subprocess.Popen(
+          ['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.Q}',
+           '--format=csv,noheader,nounits', '-lms', '200'],
+          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+      self.t = threading.Thread(target=self._read, daemon=True)
+      self.t.start()
+    except (OSError, FileNotFoundError):
+      self.proc = None
+    return self
+
+  def _read(self):
+    for line in self.proc.stdout:
+      self.lines.append(line.strip())
+
+  def __exit__(self, *a):
+    if self.proc is not None:
+      self.proc.terminate()
+      try:
+        self.proc.wait(timeout=5)
+      except subprocess.TimeoutExpired:
+        self.proc.kill()
+      self.t.join(timeout=2)
+
+  def summary(self):
+    sm, mx, reasons = [], None, set()
+    names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+    for line in self.lines:
+      f = [x.strip() for x in line.split(',')]
+      if len(f) < 9:
+        continue
+      try:
+        sm.append(float(f[1]))
+        mx = float(f[2])
+      except ValueError:
+        continue
+      for k, nm in enumerate(names):
+        if f[5 + k].lower().startswith('active'):
+          reasons.add(nm)
+    if not sm:
+      return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled'], 'samples': 0}
+    return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': mx, 'reasons': sorted(reasons),
+            'samples': len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle restatement (numpy, FP32) on all host cores
+# ---------------------------------------------------------------------------
+
+
+def _cpu_worker(args):
+  name, n, steps, seed = args
+  os.environ.setdefault('OMP_NUM_THREADS', '1')
+  from brax_gb300 import mjcf
+  from oracle.pipeline import Oracle
+  sys_ = mjcf.load_asset(name)
+  o = Oracle(sys_, np.float32)
+  rng = np.random.default_rng(seed)
+  q = (sys_.init_q + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))).astype(np.float32)
+  qd = (0.1 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32)
+  s = o.init(q, qd)
+  t0 = time.perf_counter()
+  for _ in range(steps):
+    s = o.env_step(s, rng.uniform(-1, 1, (n, sys_.act_size())).astype(np.float32), N_FRAMES)
+  return time.perf_counter() - t0, n * steps
+
+
+def cpu_baseline(sample_envs: int, steps: int = 2):
+  cores = os.cpu_count() or 1
+  ctx = mp.get_context('spawn')
+  t0 = time.perf_counter()
+  with ctx.Pool(cores) as pool:
+    res = pool.map(_cpu_worker, [(WORKLOAD, sample_envs, steps, 100 + i) for i in range(cores)])
+  wall = time.perf_counter() - t0
+  busy = max(r[0] for r in res)
+  total = sum(r[1] for r in res)
+  return {'value': total / busy, 'unit': 'env-steps/s', 'cores': cores, 'kind': 'port',
+          'sample': f'{cores} processes x {sample_envs} envs x {steps} env steps '
+                    f'({N_FRAMES} frames each), numpy FP32 restatement of the reference path; '
+                    f'slowest process {busy:.1f} s, pool wall {wall:.1f} s'}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+
+def run_braxg(args):
+  import torch
+  import torch.distributed as dist
+  world = int(os.environ.get('WORLD_SIZE', '1'))
+  rank = int(os.environ.get('RANK', '0'))
+  local = int(os.environ.get('LOCAL_RANK', '0'))
+  torch.cuda.set_device(local)
+  if world > 1:
+    dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+  dev = torch.device('cuda', local)
+  from brax_gb300 import _native, mjcf, pipeline
+  sys_ = mjcf.load_asset(WORKLOAD)
+  n = args.envs
+  mode = pipeline.NEWTON_SCHULZ if args.inverse == 'newton_schulz' else pipeline.CHOLESKY
+  kw = dict(inverse_mode=mode, threads_per_env=args.threads_per_env,
+            envs_per_cta=args.envs_per_cta)
+  rng = np.random.default_rng(1234 + rank)
+  q0 = (sys_.init_q + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))).astype(np.float32)
+  qd0 = (0.1 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32)
+  total = args.warmup + args.steps
+  gen = torch.Generator(device=dev)
+  gen.manual_seed(77 + rank)
+  acts = torch.rand(total, n, sys_.act_size(), device=dev, generator=gen) * 2 - 1
+  model = pipeline.model_for(sys_, dev)
+  s0 = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
+  a_state = s0
+  b_state = pipeline._alloc(model, n, False, dev)
+  flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+  stream = torch.cuda.current_stream(dev)
+
+  def one(i, src, dst):
+    return pipeline.step(sys_, src, acts[i], n_frames=N_FRAMES, out=dst, **kw)
+
+  for i in range(args.warmup):
+    one(i, a_state, b_state)
+    a_state, b_state = b_state, a_state
+  torch.cuda.synchronize()
+  if world > 1:
+    dist.barrier()
+  torch.cuda.synchronize()
+  ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        for _ in range(args.steps)]
+  launches = 0
+  with ClockSampler(local) as clk:
+    for k in range(args.steps):
+      flush.zero_()
+      ev[k][0].record(stream)
+      one(args.warmup + k, a_state, b_state)
+      ev[k][1].record(stream)
+      launches += _native.lib().braxg_last_launch_count()
+      a_state, b_state = b_state, a_state
+    torch.cuda.synchronize()
+  if world > 1:
+    dist.barrier()
+  torch.cuda.synchronize()
+  times = [a.elapsed_time(b) for a, b in ev]
+  t_total = sum(times) / 1e3
+  if world > 1:
+    t = torch.tensor([t_total], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    t_total = float(t.item())
+  status = a_state.status.cpu().numpy()
+  value = args.steps * n * world / t_total
+  ms_per_step = 1e3 * t_total / args.steps
+
+  # ---- e2e through the public API with host buffers ----------------------
+  h_act = torch.empty(args.steps, n, sys_.act_size(), dtype=torch.float32).pin_memory()
+  h_act.copy_(acts[args.warmup:].cpu())
+  h_obs = torch.empty(n, sys_.q_size() + sys_.qd_size(), dtype=torch.float32).pin_memory()
+  d_act = torch.empty(n, sys_.act_size(), dtype=torch.float32, device=dev)
+  obs = torch.empty(n, sys_.q_size() + sys_.qd_size(), dtype=torch.float32, device=dev)
+  st = s0
+  st2 = pipeline._alloc(model, n, False, dev)
+  for k in range(min(args.warmup, 5)):
+    d_act.copy_(h_act[k], non_blocking=True)
+    pipeline.step(sys_, st, d_act, n_frames=N_FRAMES, out=st2, **kw)
+    st, st2 = st2, st
+  torch.cuda.synchronize()
+  if world > 1:
+    dist.barrier()
+  t0 = time.perf_counter()
+  for k in range(args.steps):
+    d_act.copy_(h_act[k], non_blocking=True)
+    pipeline.step(sys_, st, d_act, n_frames=N_FRAMES, out=st2, **kw)
+    st, st2 = st2, st
+    obs[:, :sys_.q_size()].copy_(st.q)
+    obs[:, sys_.q_size():].copy_(st.qd)
+    h_obs.copy_(obs, non_blocking=True)
+    torch.cuda.current_stream(dev).synchronize()
+  t_e2e = time.perf_counter() - t0
+  if world > 1:
+    t = torch.tensor([t_e2e], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    t_e2e = float(t.item())
+  e2e = {'value': args.steps * n * world / t_e2e, 'unit': 'env-steps/s',
+         'h2d_bytes_per_step': n * sys_.act_size() * 4,
+         'd2h_bytes_per_step': n * (sys_.q_size() + sys_.qd_size()) * 4}
+
+  # ---- roofline -----------------------------------------------------------
+  nmv = load_nmv()[WORKLOAD]
+  f_step, b_step = algorithmic(sys_, nmv['mean_matvecs_per_step'])
+  launch_s = t_total / args.steps
+  flops_launch = f_step * N_FRAMES * n
+  achieved = flops_launch / launch_s / 1e12
+  props = torch.cuda.get_device_properties(dev)
+  peaks = {}
+  try:
+    with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+      peaks = json.load(f)
+  except OSError:
+    pass
+  sm_max = peaks.get('sm_max_mhz', 2070.0)
+  peak_fp32 = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+  hbm_peak = peaks.get('hbm_gbs', 6800.0)
+  roofline = {
+      'bound': 'fp32', 'achieved': round(achieved, 3), 'peak': round(peak_fp32, 1),
+      'unit': 'TFLOP/s', 'frac': round(achieved / peak_fp32, 4), 'traffic': None,
+      'peak_source': (f'nominal FP32 CUDA-core peak ({props.multi_processor_count} SMs x 128 '
+                      f'FMA/clk x 2 x {sm_max:.0f} MHz); MEASURED_PEAKS.json has no FP32 figure'),
+      'flops_per_launch': flops_launch,
+      'hbm': {'achieved_gbs': round(b_step * n / launch_s / 1e9, 2), 'peak_gbs': hbm_peak,
+              'frac': round(b_step * n / launch_s / 1e9 / hbm_peak, 5),
+              'bytes_per_launch': b_step * n, 'peak_source': 'MEASURED_PEAKS.json hbm_gbs (of measured)'},
+  }
+  clocks = clk.summary()
+  out = {
+      'metric': METRIC, 'value': round(value, 1), 'unit': 'env-steps/s', 'n_gpus': world,
+      'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
+      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+      'data': 'synthetic (seeded resets and U(-1,1) actions)',
+      'config': {'workload': f'{WORKLOAD} nq 15 nv 14 nu 8, 9 geoms vs plane (17 contact slots), '
+                             f'{n} envs per GPU, env step = {N_FRAMES} x 0.01 s',
+                 'envs_per_gpu': n, 'n_frames': N_FRAMES, 'inverse_mode': args.inverse,
+                 'parallelism': f'replicas x{world}', 'l2': 'flushed (256 MB write) before every timed step',
+                 'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
+                                          model.launch_shape(mode, args.threads_per_env,
+                                                             args.envs_per_cta)))},
+      'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
+      'env_status_nonzero': int((status != 0).sum()),
+  }
+  if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    out['cpu_baseline'] = cpu_baseline(args.cpu_sample_envs)
+  if world > 1:
+    dist.destroy_process_group()
+  if rank == 0:
+    print(json.dumps(out))
+
+
+def run_reference(args):
+  rank = int(os.environ.get('RANK', '0'))
+  world = int(os.environ.get('WORLD_SIZE', '1'))
+  if rank != 0:
+    return
+  vals = []
+  cb = None
+  for _ in range(max(1, min(args.steps, 3))):
+    cb = cpu_baseline(args.cpu_sample_envs, steps=1)
+    vals.append(cb['value'])
+  value = statistics.median(vals)
+  cb['value'] = value
+  out = {
+      'metric': METRIC, 'value': round(value, 2), 'unit': 'env-steps/s', 'n_gpus': world,
+      'steps': len(vals), 'warmup': 0, 'ms_per_step': None, 'higher_is_better': True,
+      'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+      'impl': 'reference',
+      'config': {'workload': f'{WORKLOAD}, {N_FRAMES} frames per env step, CPU sample'},
+      'cpu_baseline': cb,
+      'e2e': {'value': round(value, 2), 'unit': 'env-steps/s', 'h2d_bytes_per_step': 0,
+              'd2h_bytes_per_step': 0},
+      'note': ('the reference is pure Python/JAX and jax/jaxlib/mujoco are not installable here; '
+               'this arm times the numpy restatement of the same path (oracle/), kind "port"'),
+  }
+  print(json.dumps(out))
+
+
+if __name__ == '__main__':
+  a = parse()
+  if a.impl == 'reference':
+    run_reference(a)
+  else:
+    run_braxg(a)

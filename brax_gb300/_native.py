@@ -1,0 +1,86 @@
+"""ctypes binding of the braxg C ABI (include/braxg.h).
+
+The shared library is built in-tree by ``brax_gb300.build``; if it is missing
+every entry point raises instead of falling back to any CPU path.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+LIB_DIR = os.path.join(os.path.dirname(__file__), '_lib')
+LIB_PATH = os.path.join(LIB_DIR, 'libbraxg.so')
+
+STATE_FIELDS = (
+    'q', 'qd', 'mass_mx_inv', 'x_pos', 'x_rot', 'xd_ang', 'xd_vel', 'qf_smooth',
+    'qf_constraint', 'qdd', 'root_com', 'cinr_pos', 'cinr_rot', 'cinr_i', 'cd',
+    'cdof', 'cdofd', 'mass_mx', 'con_jac', 'con_diag', 'con_aref', 'status')
+
+EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims',
+           'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_launch_shape',
+           'braxg_last_launch_count', 'braxg_last_error')
+
+OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED = 0, 1, 2, 3
+INV_NEWTON_SCHULZ, INV_CHOLESKY = 0, 1
+ENV_NONFINITE, ENV_NOT_SPD = 1, 2
+
+
+class State(ctypes.Structure):
+  _fields_ = [(n, ctypes.c_void_p) for n in STATE_FIELDS]
+
+
+class Dims(ctypes.Structure):
+  _fields_ = [(n, ctypes.c_int32) for n in ('nl', 'nq', 'nv', 'nu', 'ncon', 'nlim', 'm')]
+
+
+class Options(ctypes.Structure):
+  _fields_ = [('inverse_mode', ctypes.c_int32), ('threads_per_env', ctypes.c_int32),
+              ('envs_per_cta', ctypes.c_int32)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib() -> ctypes.CDLL:
+  """Loads libbraxg.so (raises if it has not been built)."""
+  global _lib
+  with _lock:
+    if _lib is not None:
+      return _lib
+    if not os.path.exists(LIB_PATH):
+      raise RuntimeError(
+          f'braxg CUDA library not built ({LIB_PATH} missing); run '
+          '`python -c "import brax_gb300.build as b; b.build()"`')
+    l = ctypes.CDLL(LIB_PATH)
+    vp, i32, P = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER
+    l.braxg_model_create.argtypes = [vp, ctypes.c_size_t, i32, P(vp)]
+    l.braxg_model_destroy.argtypes = [vp]
+    l.braxg_model_dims.argtypes = [vp, P(Dims)]
+    l.braxg_init.argtypes = [vp, vp, i32, vp, vp, P(State), P(Options)]
+    l.braxg_step.argtypes = [vp, vp, i32, i32, vp, P(State), P(State), P(Options)]
+    l.braxg_rollout.argtypes = [vp, vp, i32, i32, i32, vp, P(State), P(State), vp, vp,
+                                P(Options)]
+    l.braxg_launch_shape.argtypes = [vp, P(Options), P(ctypes.c_int32), P(ctypes.c_int32),
+                                     P(ctypes.c_int32)]
+    l.braxg_last_error.restype = ctypes.c_char_p
+    l.braxg_last_launch_count.restype = ctypes.c_int
+    for n in EXPORTS:
+      if n not in ('braxg_last_error', 'braxg_last_launch_count'):
+        getattr(l, n).restype = ctypes.c_int
+    _lib = l
+    return l
+
+
+def check(rc: int, what: str):
+  """Maps a braxg status code onto the exception the reference would raise."""
+  if rc == OK:
+    return
+  msg = f'{what}: {lib().braxg_last_error().decode()}'
+  if rc == ERR_INVALID:
+    raise ValueError(msg)
+  if rc == ERR_UNSUPPORTED:
+    raise NotImplementedError(msg)
+  raise RuntimeError(msg)

@@ -1,0 +1,71 @@
+"""Builds libbraxg.so in-tree with nvcc for sm_103a (no CPU fallback exists)."""
+
+from __future__ import annotations
+
+import concurrent.futures
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+CSRC = os.path.join(ROOT, 'brax_gb300', 'csrc')
+OUT_DIR = os.path.join(ROOT, 'brax_gb300', '_lib')
+BUILD_DIR = os.path.join(ROOT, 'brax_gb300', '_lib', 'obj')
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+# one translation unit per group of kernel instantiations so they compile in
+# parallel; braxg.cu holds the C ABI
+UNITS = ['braxg.cu', 'inst_t32_nv16.cu', 'inst_t32_nv32.cu', 'inst_t32_nv64.cu',
+         'inst_t16.cu']
+
+
+def _nvcc():
+  cand = os.environ.get('NVCC') or os.path.join(
+      os.environ.get('CUDA_HOME', '/usr/local/cuda'), 'bin', 'nvcc')
+  return cand if os.path.exists(cand) else 'nvcc'
+
+
+def _flags(extra=()):
+  return [*ARCH, '-lineinfo', '-O3', '-std=c++17', '-Xcompiler', '-fPIC',
+          '-I', os.path.join(ROOT, 'include'), '-I', CSRC, *extra]
+
+
+def _sources_newer(target, deps):
+  if not os.path.exists(target):
+    return True
+  t = os.path.getmtime(target)
+  return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose: bool = False, force: bool = False) -> str:
+  """Compiles (if stale) and returns the path of libbraxg.so."""
+  os.makedirs(BUILD_DIR, exist_ok=True)
+  headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.cuh', '.h'))]
+  headers.append(os.path.join(ROOT, 'include', 'braxg.h'))
+  nvcc = _nvcc()
+  jobs = []
+  objs = []
+  for u in UNITS:
+    src = os.path.join(CSRC, u)
+    obj = os.path.join(BUILD_DIR, u.replace('.cu', '.o'))
+    objs.append(obj)
+    if force or _sources_newer(obj, [src, *headers]):
+      jobs.append([nvcc, *_flags(['-Xptxas', '-v'] if verbose else []), '-c', src, '-o', obj])
+
+  def run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+      raise RuntimeError(f'nvcc failed: {" ".join(cmd)}\n{r.stdout}\n{r.stderr}')
+    return r.stdout + r.stderr
+
+  with concurrent.futures.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    for log in ex.map(run, jobs):
+      if verbose and log:
+        print(log, file=sys.stderr)
+  lib = os.path.join(OUT_DIR, 'libbraxg.so')
+  if force or jobs or _sources_newer(lib, objs):
+    run([nvcc, *ARCH, '-shared', '-o', lib, *objs, '-lcudart'])
+  return lib
+
+
+if __name__ == '__main__':
+  print(build(verbose='-v' in sys.argv, force='-f' in sys.argv))

@@ -1,0 +1,247 @@
+// C ABI (include/braxg.h) and the fused step kernel launches.
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "braxg.h"
+#include "braxg_launch.h"
+#include "braxg_step.cuh"
+
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct braxg_model {
+  int device;
+  int* d_desc;
+  int words;
+  std::vector<int> h;
+  braxg_dims dims;
+  int ns_iters;
+  braxg::Layout L;
+};
+
+namespace {
+
+thread_local std::string g_err;
+thread_local int g_launches = 0;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(BRAXG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+struct Shape {
+  int T, NVB, epc, smem;
+};
+
+constexpr int kMaxSmem = 227 * 1024;
+
+int choose_shape(const braxg_model* m, const braxg_options* opt, Shape* s) {
+  int nv = m->dims.nv;
+  s->NVB = nv <= 16 ? 16 : (nv <= 32 ? 32 : 64);
+  int T = (opt && opt->threads_per_env) ? opt->threads_per_env : 32;
+  if (T != 16 && T != 32) return fail(BRAXG_ERR_INVALID, "threads_per_env must be 0, 16 or 32 (got %d)", T);
+  if (T == 16 && s->NVB == 64) T = 32;
+  s->T = T;
+  int model_bytes = braxg::al4(m->words) * 4;
+  int env_bytes = m->L.total * 4;
+  int max_epc = 256 / T;
+  int fit = (kMaxSmem - model_bytes) / env_bytes;
+  if (fit < 1)
+    return fail(BRAXG_ERR_UNSUPPORTED, "model needs %d bytes of shared memory per env; at most %d fit",
+                env_bytes, kMaxSmem - model_bytes);
+  int epc = (opt && opt->envs_per_cta) ? opt->envs_per_cta : 0;
+  if (epc == 0) {
+    // default: about 100 KB per CTA so two CTAs share an SM
+    epc = (100 * 1024 - model_bytes) / env_bytes;
+    if (epc < 1) epc = 1;
+    if (epc > max_epc) epc = max_epc;
+  }
+  if (epc > max_epc || epc > fit || epc < 1)
+    return fail(BRAXG_ERR_INVALID, "envs_per_cta %d out of range [1, %d]", epc, fit < max_epc ? fit : max_epc);
+  s->epc = epc;
+  s->smem = model_bytes + epc * env_bytes;
+  return BRAXG_OK;
+}
+
+int launch(const braxg_model* m, const braxg_options* opt, braxg::StepArgs& a, cudaStream_t st) {
+  g_launches = 0;
+  Shape s;
+  int rc = choose_shape(m, opt, &s);
+  if (rc) return rc;
+  if (a.n_env == 0) return BRAXG_OK;
+  a.envs_per_cta = s.epc;
+  int grid = (a.n_env + s.epc - 1) / s.epc;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != m->device) {
+    cudaError_t e = cudaSetDevice(m->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+  }
+  cudaError_t e;
+  if (s.T == 16 && s.NVB == 16) e = braxg::launch_step<16, 16>(a, grid, s.smem, st);
+  else if (s.T == 16) e = braxg::launch_step<16, 32>(a, grid, s.smem, st);
+  else if (s.NVB == 16) e = braxg::launch_step<32, 16>(a, grid, s.smem, st);
+  else if (s.NVB == 32) e = braxg::launch_step<32, 32>(a, grid, s.smem, st);
+  else e = braxg::launch_step<32, 64>(a, grid, s.smem, st);
+  if (cur != m->device) cudaSetDevice(cur);
+  if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+  g_launches = 1;
+  return BRAXG_OK;
+}
+
+int check_common(const braxg_model* m, int n_env, const braxg_options* opt) {
+  if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model is NULL");
+  if (n_env < 0) return fail(BRAXG_ERR_INVALID, "n_env must be >= 0 (got %d)", n_env);
+  if (opt && opt->inverse_mode != BRAXG_INV_NEWTON_SCHULZ && opt->inverse_mode != BRAXG_INV_CHOLESKY)
+    return fail(BRAXG_ERR_INVALID, "unknown inverse_mode %d", opt->inverse_mode);
+  return BRAXG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* braxg_last_error(void) { return g_err.c_str(); }
+
+int braxg_last_launch_count(void) { return g_launches; }
+
+int braxg_model_create(const void* desc, size_t desc_bytes, int device, braxg_model** out) {
+  if (desc == nullptr || out == nullptr) return fail(BRAXG_ERR_INVALID, "NULL descriptor or output");
+  if (desc_bytes < BXM_HEADER_WORDS * 4 || desc_bytes % 4 != 0)
+    return fail(BRAXG_ERR_INVALID, "descriptor size %zu is not a whole header", desc_bytes);
+  const int* w = static_cast<const int*>(desc);
+  if ((unsigned)w[BXM_H_MAGIC] != (unsigned)BXM_MAGIC || w[BXM_H_VERSION] != BXM_VERSION)
+    return fail(BRAXG_ERR_INVALID, "bad descriptor magic/version");
+  int words = w[BXM_H_WORDS];
+  if ((size_t)words * 4 != desc_bytes) return fail(BRAXG_ERR_INVALID, "descriptor length mismatch");
+  for (int k = BXM_O_LINK_PARENT; k <= BXM_O_CON_SOLP; ++k)
+    if (w[k] < BXM_HEADER_WORDS || w[k] > words) return fail(BRAXG_ERR_INVALID, "descriptor offset %d out of range", k);
+  braxg_dims d{w[BXM_H_NL], w[BXM_H_NQ], w[BXM_H_NV], w[BXM_H_NU], w[BXM_H_NCON], w[BXM_H_NLIM], w[BXM_H_M]};
+  if (d.nl < 1 || d.nv < 1 || d.nv > 64 || d.nq < 1 || d.nu < 0 || d.ncon < 0 || d.nlim < 0 || d.nl > 64)
+    return fail(BRAXG_ERR_UNSUPPORTED, "model dims out of the supported envelope (nl %d, nv %d)", d.nl, d.nv);
+  if (d.m != 4 * d.ncon + d.nlim) return fail(BRAXG_ERR_INVALID, "inconsistent constraint row count");
+  auto* m = new braxg_model();
+  m->device = device;
+  m->words = words;
+  m->h.assign(w, w + words);
+  m->dims = d;
+  m->ns_iters = w[BXM_H_NS_ITERS];
+  m->L = braxg::make_layout(d.nl, d.nq, d.nv, d.nu, d.ncon, d.nlim);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_desc, (size_t)words * 4);
+  if (e == cudaSuccess) e = cudaMemcpy(m->d_desc, w, (size_t)words * 4, cudaMemcpyHostToDevice);
+  cudaSetDevice(cur);
+  if (e != cudaSuccess) {
+    delete m;
+    return cuda_fail(e, "braxg_model_create");
+  }
+  *out = m;
+  return BRAXG_OK;
+}
+
+int braxg_model_destroy(braxg_model* m) {
+  if (m == nullptr) return BRAXG_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(m->device);
+  cudaFree(m->d_desc);
+  cudaSetDevice(cur);
+  delete m;
+  return BRAXG_OK;
+}
+
+int braxg_model_dims(const braxg_model* m, braxg_dims* out) {
+  if (m == nullptr || out == nullptr) return fail(BRAXG_ERR_INVALID, "NULL argument");
+  *out = m->dims;
+  return BRAXG_OK;
+}
+
+int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int32_t* tpe, int32_t* epc, int32_t* smem) {
+  if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model is NULL");
+  Shape s;
+  int rc = choose_shape(m, opt, &s);
+  if (rc) return rc;
+  if (tpe) *tpe = s.T;
+  if (epc) *epc = s.epc;
+  if (smem) *smem = s.smem;
+  return BRAXG_OK;
+}
+
+int braxg_init(const braxg_model* m, void* stream, int n_env, const float* q, const float* qd, braxg_state* out,
+               const braxg_options* opt) {
+  int rc = check_common(m, n_env, opt);
+  if (rc) return rc;
+  if (out == nullptr || (n_env > 0 && (q == nullptr || qd == nullptr)))
+    return fail(BRAXG_ERR_INVALID, "q, qd and out are required");
+  braxg::StepArgs a{};
+  a.model = m->d_desc;
+  a.model_words = m->words;
+  a.n_env = n_env;
+  a.n_steps = 0;
+  a.n_frames = 0;
+  a.exact_inverse = 1;
+  a.init = 1;
+  a.q_in = q;
+  a.qd_in = qd;
+  a.out = *out;
+  return launch(m, opt, a, static_cast<cudaStream_t>(stream));
+}
+
+static int run_steps(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, const float* act,
+                     long long act_stride, const braxg_state* in, braxg_state* out, float* tq, float* tqd,
+                     const braxg_options* opt) {
+  int rc = check_common(m, n_env, opt);
+  if (rc) return rc;
+  if (in == nullptr || out == nullptr) return fail(BRAXG_ERR_INVALID, "in and out states are required");
+  if (n_frames < 1 || n_steps < 0) return fail(BRAXG_ERR_INVALID, "n_frames must be >= 1 and n_steps >= 0");
+  bool ns = !(opt && opt->inverse_mode == BRAXG_INV_CHOLESKY) && m->ns_iters > 0;
+  if (n_env > 0 && (in->q == nullptr || in->qd == nullptr || (ns && in->mass_mx_inv == nullptr)))
+    return fail(BRAXG_ERR_INVALID, "in->q, in->qd and (Newton-Schulz mode) in->mass_mx_inv are required");
+  braxg::StepArgs a{};
+  a.model = m->d_desc;
+  a.model_words = m->words;
+  a.n_env = n_env;
+  a.n_steps = n_steps;
+  a.n_frames = n_frames;
+  a.exact_inverse = ns ? 0 : 1;
+  a.init = 0;
+  a.q_in = in->q;
+  a.qd_in = in->qd;
+  a.minv_in = in->mass_mx_inv;
+  a.act = act;
+  a.act_step_stride = act_stride;
+  a.out = *out;
+  a.traj_q = tq;
+  a.traj_qd = tqd;
+  return launch(m, opt, a, static_cast<cudaStream_t>(stream));
+}
+
+int braxg_step(const braxg_model* m, void* stream, int n_env, int n_frames, const float* act, const braxg_state* in,
+               braxg_state* out, const braxg_options* opt) {
+  return run_steps(m, stream, n_env, 1, n_frames, act, 0, in, out, nullptr, nullptr, opt);
+}
+
+int braxg_rollout(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, const float* act_seq,
+                  const braxg_state* in, braxg_state* out, float* traj_q, float* traj_qd, const braxg_options* opt) {
+  long long stride = m ? (long long)n_env * m->dims.nu : 0;
+  return run_steps(m, stream, n_env, n_steps, n_frames, act_seq, stride, in, out, traj_q, traj_qd, opt);
+}
+
+}  // extern "C"

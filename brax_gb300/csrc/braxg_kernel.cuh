@@ -1,0 +1,165 @@
+// The fused step kernel: loads one env per team, runs n_steps x n_frames
+// pipeline steps (brax/generalized/pipeline.py:64-94) and writes the State.
+#pragma once
+#include "braxg_launch.h"
+#include "braxg_step.cuh"
+
+namespace braxg {
+
+template <int T>
+__device__ void load_vec(const Team<T>& tm, float* dst, const float* src, int n) {
+  for (int i = tm.lane; i < n; i += T) dst[i] = src[i];
+}
+template <int T>
+__device__ void store_vec(const Team<T>& tm, float* dst, const float* src, int n) {
+  if (dst == nullptr) return;
+  for (int i = tm.lane; i < n; i += T) dst[i] = src[i];
+}
+template <int T>
+__device__ void store_mat(const Team<T>& tm, float* dst, const float* src, int n, int ld) {
+  if (dst == nullptr) return;
+  for (int idx = tm.lane; idx < n * n; idx += T) {
+    int i = idx / n, j = idx - i * n;
+    dst[idx] = src[i * ld + j];
+  }
+}
+
+template <int T, int NVB>
+__device__ bool position_stage(const Model& md, const Team<T>& tm, const Ws& w, bool exact, int iters) {
+  stage_fk<T>(md, tm, w);
+  stage_com<T>(md, tm, w);
+  stage_crba<T>(md, tm, w);
+  bool ok = stage_inverse<T, NVB>(md, tm, w, exact, iters);
+  stage_jacobian<T>(md, tm, w);
+  return ok;
+}
+
+template <int T, int NVB>
+__global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) int smem[];
+  for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
+  __syncthreads();
+  const Model md(smem);
+  const Team<T> tm;
+  const int team = threadIdx.x / T;
+  const long long env = (long long)blockIdx.x * a.envs_per_cta + team;
+  if (team >= a.envs_per_cta || env >= a.n_env) return;
+  Ws w;
+  w.L = make_layout(md.nl, md.nq, md.nv, md.nu, md.ncon, md.nlim);
+  w.b = reinterpret_cast<float*>(smem + al4(a.model_words)) + (size_t)team * w.L.total;
+  const Layout& L = w.L;
+  const int nq = md.nq, nv = md.nv, nl = md.nl, nu = md.nu, ld = L.ldm;
+
+  load_vec<T>(tm, w.at(L.q), a.q_in + env * nq, nq);
+  load_vec<T>(tm, w.at(L.qd), a.qd_in + env * nv, nv);
+  const bool exact = a.exact_inverse || a.init || md.ns_iters == 0;
+  if (!exact) {
+    const float* src = a.minv_in + env * nv * nv;
+    for (int idx = tm.lane; idx < nv * nv; idx += T) {
+      int i = idx / nv, j = idx - i * nv;
+      w.at(L.Minv)[i * ld + j] = src[idx];
+    }
+  }
+  tm.sync();
+  bool ok = position_stage<T, NVB>(md, tm, w, exact, 0);
+  if (a.init) {
+    for (int d = tm.lane; d < nv; d += T) {
+      w.at(L.qfs)[d] = 0.f;
+      w.at(L.qfc)[d] = 0.f;
+      w.at(L.qdd)[d] = 0.f;
+    }
+    tm.sync();
+  } else {
+    for (int s = 0; s < a.n_steps; ++s) {
+      const bool has_act = a.act != nullptr && nu > 0;
+      if (has_act) load_vec<T>(tm, w.at(L.act), a.act + s * a.act_step_stride + env * nu, nu);
+      tm.sync();
+      for (int f = 0; f < a.n_frames; ++f) {
+        stage_smooth<T>(md, tm, w, has_act);
+        stage_constraint<T>(md, tm, w);
+        ok = stage_integrate<T>(md, tm, w) && ok;
+        ok = position_stage<T, NVB>(md, tm, w, a.exact_inverse || md.ns_iters == 0, md.ns_iters) && ok;
+      }
+      if (a.traj_q != nullptr) store_vec<T>(tm, a.traj_q + ((long long)s * a.n_env + env) * nq, w.at(L.q), nq);
+      if (a.traj_qd != nullptr)
+        store_vec<T>(tm, a.traj_qd + ((long long)s * a.n_env + env) * nv, w.at(L.qd), nv);
+    }
+  }
+  // outputs
+  const braxg_state& o = a.out;
+  store_vec<T>(tm, o.q ? o.q + env * nq : nullptr, w.at(L.q), nq);
+  store_vec<T>(tm, o.qd ? o.qd + env * nv : nullptr, w.at(L.qd), nv);
+  store_mat<T>(tm, o.mass_mx_inv ? o.mass_mx_inv + env * nv * nv : nullptr, w.at(L.Minv), nv, ld);
+  store_mat<T>(tm, o.mass_mx ? o.mass_mx + env * nv * nv : nullptr, w.at(L.M), nv, ld);
+  store_vec<T>(tm, o.x_pos ? o.x_pos + env * nl * 3 : nullptr, w.at(L.xp), 3 * nl);
+  store_vec<T>(tm, o.x_rot ? o.x_rot + env * nl * 4 : nullptr, w.at(L.xr), 4 * nl);
+  store_vec<T>(tm, o.xd_ang ? o.xd_ang + env * nl * 3 : nullptr, w.at(L.xa), 3 * nl);
+  store_vec<T>(tm, o.xd_vel ? o.xd_vel + env * nl * 3 : nullptr, w.at(L.xv), 3 * nl);
+  store_vec<T>(tm, o.qf_smooth ? o.qf_smooth + env * nv : nullptr, w.at(L.qfs), nv);
+  store_vec<T>(tm, o.qf_constraint ? o.qf_constraint + env * nv : nullptr, w.at(L.qfc), nv);
+  store_vec<T>(tm, o.qdd ? o.qdd + env * nv : nullptr, w.at(L.qdd), nv);
+  store_vec<T>(tm, o.root_com ? o.root_com + env * nl * 3 : nullptr, w.at(L.rc), 3 * nl);
+  store_vec<T>(tm, o.cinr_pos ? o.cinr_pos + env * nl * 3 : nullptr, w.at(L.cp), 3 * nl);
+  store_vec<T>(tm, o.cinr_i ? o.cinr_i + env * nl * 9 : nullptr, w.at(L.ci), 9 * nl);
+  store_vec<T>(tm, o.cd ? o.cd + env * nl * 6 : nullptr, w.at(L.cd), 6 * nl);
+  store_vec<T>(tm, o.cdof ? o.cdof + env * nv * 6 : nullptr, w.at(L.cdof), 6 * nv);
+  store_vec<T>(tm, o.cdofd ? o.cdofd + env * nv * 6 : nullptr, w.at(L.cdofd), 6 * nv);
+  if (o.cinr_rot != nullptr) {  // cinr.transform.rot = x_i.rot
+    for (int l = tm.lane; l < nl; l += T) {
+      f3 op;
+      q4 orr;
+      tf_do(ld3(w.at(L.xp) + 3 * l), ld4(w.at(L.xr) + 4 * l), ld3(md.F(BXM_O_LI_POS) + 3 * l),
+            ld4(md.F(BXM_O_LI_ROT) + 4 * l), op, orr);
+      st4(o.cinr_rot + (env * nl + l) * 4, orr);
+    }
+  }
+  if (o.con_jac != nullptr || o.con_diag != nullptr || o.con_aref != nullptr) {
+    const int m = md.m;
+    const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
+    const int* rmap = reinterpret_cast<const int*>(w.at(L.rmap));
+    int* inv = reinterpret_cast<int*>(w.at(L.scr));
+    for (int r = tm.lane; r < m; r += T) inv[r] = -1;
+    tm.sync();
+    for (int r = tm.lane; r < nrow; r += T) inv[rmap[r]] = r;
+    tm.sync();
+    if (o.con_jac != nullptr) {
+      for (long long idx = tm.lane; idx < (long long)m * nv; idx += T) {
+        int r = (int)(idx / nv), d = (int)(idx - (long long)r * nv);
+        int c = inv[r];
+        o.con_jac[env * m * nv + idx] = c >= 0 ? w.at(L.J)[c * L.ldj + d] : 0.f;
+      }
+    }
+    for (int r = tm.lane; r < m; r += T) {
+      int c = inv[r];
+      if (o.con_diag != nullptr) o.con_diag[env * m + r] = c >= 0 ? w.at(L.rdiag)[c] : 0.f;
+      if (o.con_aref != nullptr) o.con_aref[env * m + r] = c >= 0 ? w.at(L.raref)[c] : 0.f;
+    }
+  }
+  if (o.status != nullptr) {
+    bool fin = true;
+    for (int i = tm.lane; i < nq; i += T) fin = fin && isfinite(w.at(L.q)[i]);
+    for (int i = tm.lane; i < nv; i += T) fin = fin && isfinite(w.at(L.qd)[i]);
+    fin = tm.all(fin);
+    if (tm.lane == 0) o.status[env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
+  }
+}
+
+
+constexpr int kMaxSmemBytes = 227 * 1024;
+
+template <int T, int NVB>
+cudaError_t launch_step(const StepArgs& a, int grid, int smem, cudaStream_t st) {
+  auto k = step_kernel<T, NVB>;
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_set[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr_set[dev] = true;
+  }
+  k<<<grid, a.envs_per_cta * T, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace braxg

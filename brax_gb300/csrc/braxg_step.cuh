@@ -1,0 +1,1242 @@
+// The fused generalized-coordinates step: one team of T lanes per env, all
+// per-env working state in shared memory, the packed model in shared memory
+// once per CTA.  Each stage cites the reference function it restates.
+#pragma once
+#include "braxg_math.cuh"
+#include "model_layout.h"
+
+namespace braxg {
+
+// ---------------------------------------------------------------------------
+// model accessor
+// ---------------------------------------------------------------------------
+struct Model {
+  const int* w;
+  int nl, nq, nv, nu, ncon, nlim, m, nlevel, ns_iters, pg_iters, pg_maxls;
+  float dt, pg_tol;
+  f3 g;
+  __device__ explicit Model(const int* w_) : w(w_) {
+    nl = w[BXM_H_NL];
+    nq = w[BXM_H_NQ];
+    nv = w[BXM_H_NV];
+    nu = w[BXM_H_NU];
+    ncon = w[BXM_H_NCON];
+    nlim = w[BXM_H_NLIM];
+    m = w[BXM_H_M];
+    nlevel = w[BXM_H_NLEVEL];
+    ns_iters = w[BXM_H_NS_ITERS];
+    pg_iters = w[BXM_H_PG_ITERS];
+    pg_maxls = w[BXM_H_PG_MAXLS];
+    dt = __int_as_float(w[BXM_H_DT]);
+    pg_tol = __int_as_float(w[BXM_H_PG_TOL]);
+    g = mk3(__int_as_float(w[BXM_H_GX]), __int_as_float(w[BXM_H_GY]), __int_as_float(w[BXM_H_GZ]));
+  }
+  __device__ __forceinline__ const int* I(int k) const { return w + w[k]; }
+  __device__ __forceinline__ const float* F(int k) const {
+    return reinterpret_cast<const float*>(w + w[k]);
+  }
+  __device__ __forceinline__ uint64_t anc(int l) const {
+    const unsigned* a = reinterpret_cast<const unsigned*>(I(BXM_O_LINK_ANC));
+    return (uint64_t)a[2 * l] | ((uint64_t)a[2 * l + 1] << 32);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// per-env shared-memory layout (word offsets)
+// ---------------------------------------------------------------------------
+struct Layout {
+  int ldm, ldj;
+  int q, qd, act, qfs, qfc, qdd, tau, v1, v2, misc;
+  int xp, xr, xa, xv, rc, ci, cp, cd, cdof, cdofd;
+  int M, Minv;
+  int J, rdiag, raref, rmap;
+  int scr, scr_words;
+  int total;
+};
+
+__host__ __device__ inline int al4(int x) { return (x + 3) & ~3; }
+
+__host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim) {
+  Layout L;
+  int m = 4 * ncon + nlim;
+  L.ldm = nv | 1;  // odd leading dimension: conflict-free strided lane access
+  L.ldj = nv | 1;
+  int o = 0;
+  auto take = [&](int words) {
+    int at = o;
+    o += al4(words);
+    return at;
+  };
+  L.q = take(nq);
+  L.qd = take(nv);
+  L.act = take(nu);
+  L.qfs = take(nv);
+  L.qfc = take(nv);
+  L.qdd = take(nv);
+  L.tau = take(nv);
+  L.v1 = take(nv);
+  L.v2 = take(nv);
+  L.misc = take(8);
+  L.xp = take(3 * nl);
+  L.xr = take(4 * nl);
+  L.xa = take(3 * nl);
+  L.xv = take(3 * nl);
+  L.rc = take(3 * nl);
+  L.ci = take(9 * nl);
+  L.cp = take(3 * nl);
+  L.cd = take(6 * nl);
+  L.cdof = take(6 * nv);
+  L.cdofd = take(6 * nv);
+  L.M = take(nv * L.ldm);
+  L.Minv = take(nv * L.ldm);
+  L.J = take(m * L.ldj);
+  L.rdiag = take(m);
+  L.raref = take(m);
+  L.rmap = take(m);
+  int s = 14 * nl;                                   // FK / com temporaries
+  s = s > 13 * nl + 0 ? s : 13 * nl;                 // crb
+  s = s > 12 * nl + nu ? s : 12 * nl + nu;           // RNE
+  s = s > 2 * nv * L.ldm + 4 ? s : 2 * nv * L.ldm + 4;  // inverse temporaries
+  s = s > 14 * ncon + 16 ? s : 14 * ncon + 16;       // contacts
+  s = s > 8 * m + 4 * nv + 40 ? s : 8 * m + 4 * nv + 40;  // projected gradient
+  s = s > m + 4 ? s : m + 4;                         // output row map
+  L.scr_words = al4(s);
+  L.scr = take(L.scr_words);
+  L.total = al4(o);
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// team of T lanes (T in {8, 16, 32}) inside one warp
+// ---------------------------------------------------------------------------
+template <int T>
+struct Team {
+  unsigned mask;
+  int lane, base;
+  __device__ Team() {
+    int wl = threadIdx.x & 31;
+    base = (wl / T) * T;
+    lane = wl - base;
+    mask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << base);
+  }
+  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+  __device__ __forceinline__ float sum(float v) const {
+#pragma unroll
+    for (int o = T / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o, T);
+    return v;
+  }
+  __device__ __forceinline__ bool all(bool p) const {
+    return (__ballot_sync(mask, p) & mask) == mask;
+  }
+  __device__ __forceinline__ bool any(bool p) const { return (__ballot_sync(mask, p) & mask) != 0u; }
+  __device__ __forceinline__ unsigned ballot(bool p) const {
+    return (__ballot_sync(mask, p) & mask) >> base;
+  }
+};
+
+struct Ws {
+  float* b;  // env base
+  Layout L;
+  __device__ __forceinline__ float* at(int off) const { return b + off; }
+};
+
+// ---------------------------------------------------------------------------
+// kinematics.forward: brax/kinematics.py:31-108
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ void stage_fk(const Model& md, const Team<T>& tm, const Ws& w) {
+  const Layout& L = w.L;
+  float* q = w.at(L.q);
+  float* qd = w.at(L.qd);
+  float* jp_ = w.at(L.scr);
+  float* jr_ = jp_ + 3 * md.nl;
+  float* ja_ = jr_ + 4 * md.nl;
+  float* jv_ = ja_ + 3 * md.nl;
+  const int* ltype = md.I(BXM_O_LINK_TYPE);
+  const int* qadr = md.I(BXM_O_LINK_QADR);
+  const int* dadr = md.I(BXM_O_LINK_DADR);
+  const float* dang = md.F(BXM_O_D_ANG);
+  const float* dvel = md.F(BXM_O_D_VEL);
+  for (int l = tm.lane; l < md.nl; l += T) {
+    int typ = ltype[l], qa = qadr[l], da = dadr[l];
+    f3 jp, ja, jv;
+    q4 jr;
+    if (typ == 0) {  // kinematics.py:47-50
+      jp = ld3(q + qa);
+      jr = ld4(q + qa + 3);
+      ja = ld3(qd + da + 3);
+      jv = ld3(qd + da);
+    } else {  // kinematics.py:51-76
+      for (int k = 0; k < typ; ++k) {
+        int d = da + k;
+        f3 ang = ld3(dang + 3 * d), vel = ld3(dvel + 3 * d);
+        float qk = q[qa + k], qdk = qd[d];
+        q4 rk = qnormalize(quat_rot_axis(ang, qk));
+        f3 pk = vel * qk;
+        f3 dak = ang * qdk, dvk = vel * qdk;
+        if (k == 0) {
+          jp = pk;
+          jr = rk;
+          ja = dak;
+          jv = dvk;
+        } else {
+          f3 np_;
+          q4 nr;
+          tf_do(jp, jr, pk, rk, np_, nr);
+          jp = np_;
+          jr = nr;
+          ja = ja + rotate(dak, rk);
+          jv = jv + rotate(dvk + cross3(pk, dak), rk);
+        }
+      }
+    }
+    // joint anchor offset and link transform: kinematics.py:80-82
+    f3 jpos = ld3(md.F(BXM_O_LJ_POS) + 3 * l);
+    f3 anchor = rotate(jpos, jr);
+    jp = (jp + jpos) - anchor;
+    f3 op;
+    q4 orr;
+    tf_do(ld3(md.F(BXM_O_LT_POS) + 3 * l), ld4(md.F(BXM_O_LT_ROT) + 4 * l), jp, jr, op, orr);
+    st3(jp_ + 3 * l, op);
+    st4(jr_ + 4 * l, orr);
+    st3(ja_ + 3 * l, ja);
+    st3(jv_ + 3 * l, jv);
+  }
+  tm.sync();
+  // world transforms, root-to-leaf level order (kinematics.py:84-102)
+  const int* lstart = md.I(BXM_O_LEVEL_START);
+  const int* llinks = md.I(BXM_O_LEVEL_LINKS);
+  const int* parent = md.I(BXM_O_LINK_PARENT);
+  float* xp = w.at(L.xp);
+  float* xr = w.at(L.xr);
+  float* xa = w.at(L.xa);
+  float* xv = w.at(L.xv);
+  for (int lv = 0; lv < md.nlevel; ++lv) {
+    for (int idx = lstart[lv] + tm.lane; idx < lstart[lv + 1]; idx += T) {
+      int l = llinks[idx];
+      int p = parent[l];
+      f3 jp = ld3(jp_ + 3 * l), ja = ld3(ja_ + 3 * l), jv = ld3(jv_ + 3 * l);
+      q4 jr = ld4(jr_ + 4 * l);
+      if (p < 0) {
+        st3(xp + 3 * l, jp);
+        st4(xr + 4 * l, jr);
+        st3(xa + 3 * l, rotate(ja, jr));
+        st3(xv + 3 * l, jv);
+      } else {
+        f3 pp = ld3(xp + 3 * p), pa = ld3(xa + 3 * p), pv = ld3(xv + 3 * p);
+        q4 pr = ld4(xr + 4 * p);
+        f3 op;
+        q4 orr;
+        tf_do(pp, pr, jp, jr, op, orr);
+        f3 vel = pv + cross3(pa, op - pp);
+        vel = vel + rotate(jv, pr);
+        st3(xp + 3 * l, op);
+        st4(xr + 4 * l, orr);
+        st3(xa + 3 * l, pa + rotate(ja, orr));
+        st3(xv + 3 * l, vel);
+      }
+    }
+    tm.sync();
+  }
+  for (int l = tm.lane; l < md.nl; l += T) st4(xr + 4 * l, qnormalize(ld4(xr + 4 * l)));  // :106
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// dynamics.transform_com: brax/generalized/dynamics.py:27-134
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ void stage_com(const Model& md, const Team<T>& tm, const Ws& w) {
+  const Layout& L = w.L;
+  const int nl = md.nl;
+  float* xip = w.at(L.scr);
+  float* xir = xip + 3 * nl;
+  float* jjp = xir + 4 * nl;
+  float* jjr = jjp + 3 * nl;
+  const float* xp = w.at(L.xp);
+  const float* xr = w.at(L.xr);
+  const float* mass = md.F(BXM_O_LI_MASS);
+  const int* parent = md.I(BXM_O_LINK_PARENT);
+  const int* ltype = md.I(BXM_O_LINK_TYPE);
+  for (int l = tm.lane; l < nl; l += T) {  // x_i = x.do(inertia.transform)  :37
+    f3 op;
+    q4 orr;
+    tf_do(ld3(xp + 3 * l), ld4(xr + 4 * l), ld3(md.F(BXM_O_LI_POS) + 3 * l),
+          ld4(md.F(BXM_O_LI_ROT) + 4 * l), op, orr);
+    st3(xip + 3 * l, op);
+    st4(xir + 4 * l, orr);
+    // parent frame for the dof motions: :47-52
+    int pi = (ltype[l] == 0) ? l : parent[l];
+    f3 pp = pi >= 0 ? ld3(xp + 3 * pi) : mk3(0.f, 0.f, 0.f);
+    q4 pr = pi >= 0 ? ld4(xr + 4 * pi) : qident();
+    f3 ap;
+    q4 ar;
+    tf_do(pp, pr, ld3(md.F(BXM_O_LT_POS) + 3 * l), ld4(md.F(BXM_O_LT_ROT) + 4 * l), ap, ar);
+    st3(jjp + 3 * l, ap + rotate(ld3(md.F(BXM_O_LJ_POS) + 3 * l), ar));
+    st4(jjr + 4 * l, ar);  // joint rotation is identity
+  }
+  tm.sync();
+  const int* root = md.I(BXM_O_LINK_ROOT);
+  float* rc = w.at(L.rc);
+  float* ci = w.at(L.ci);
+  float* cp = w.at(L.cp);
+  for (int l = tm.lane; l < nl; l += T) {
+    // root_com by segment sum over the link's tree: :38-43
+    int r = root[l];
+    f3 s = mk3(0.f, 0.f, 0.f);
+    float ms = 0.f;
+    for (int j = 0; j < nl; ++j) {
+      if (root[j] != r) continue;
+      s = s + mass[j] * ld3(xip + 3 * j);
+      ms = ms + mass[j];
+    }
+    f3 com = mk3(s.x / ms, s.y / ms, s.z / ms);
+    st3(rc + 3 * l, com);
+    // cinr = x_i(pos - root_com).do(inertia): :44, brax/base.py:589-595
+    f3 off = ld3(xip + 3 * l) - com;
+    float R[9], RI[9];
+    quat_to_3x3(ld4(xir + 4 * l), R);
+    const float* I = md.F(BXM_O_LI_I) + 9 * l;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) RI[3 * a + b] = R[3 * a] * I[b] + R[3 * a + 1] * I[3 + b] + R[3 * a + 2] * I[6 + b];
+    f3 h[3];
+    h[0] = cross3(off, mk3(-1.f, -0.f, -0.f));
+    h[1] = cross3(off, mk3(-0.f, -1.f, -0.f));
+    h[2] = cross3(off, mk3(-0.f, -0.f, -1.f));
+    float m_ = mass[l];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        ci[9 * l + 3 * a + b] = (RI[3 * a] * R[3 * b] + RI[3 * a + 1] * R[3 * b + 1] + RI[3 * a + 2] * R[3 * b + 2]) +
+                                dot3(h[a], h[b]) * m_;
+    st3(cp + 3 * l, off * m_);
+  }
+  tm.sync();
+  // cdof via stacked joints: :55-89
+  const int* qadr = md.I(BXM_O_LINK_QADR);
+  const int* dadr = md.I(BXM_O_LINK_DADR);
+  const float* dang = md.F(BXM_O_D_ANG);
+  const float* dvel = md.F(BXM_O_D_VEL);
+  const float* q = w.at(L.q);
+  const float* qd = w.at(L.qd);
+  float* cdof = w.at(L.cdof);
+  for (int l = tm.lane; l < nl; l += T) {
+    int typ = ltype[l], da = dadr[l], qa = qadr[l];
+    q4 jr = ld4(jjr + 4 * l);
+    f3 off = ld3(rc + 3 * l) - ld3(jjp + 3 * l);
+    int nd = typ == 0 ? 6 : typ;
+    f3 ap = mk3(0.f, 0.f, 0.f);
+    q4 ar = qident();
+    for (int k = 0; k < nd; ++k) {
+      int d = da + k;
+      f3 ang = ld3(dang + 3 * d), vel = ld3(dvel + 3 * d);
+      f3 ca, cv;
+      if (typ == 0) {
+        ca = ang;
+        cv = vel;
+      } else {  // inv_do(Motion) of the accumulated joint transform, brax/base.py:580-584
+        ca = rotate(ang, ar);
+        cv = rotate(vel, ar) + cross3(ap, ca);
+        float qk = q[qa + k];
+        q4 rk = qnormalize(quat_rot_axis(ang, qk));
+        f3 np_;
+        q4 nr;
+        tf_do(ap, ar, vel * qk, rk, np_, nr);
+        ap = np_;
+        ar = nr;
+      }
+      ca = rotate(ca, jr);        // :86
+      cv = cv - cross3(off, ca);  // :88-89
+      float* c = cdof + 6 * d;
+      st3(c, ca);
+      st3(c + 3, cv);
+    }
+  }
+  tm.sync();
+  // cd: root-to-leaf, cd = cd[parent] + sum(cdof * qd): :93-103
+  const int* lstart = md.I(BXM_O_LEVEL_START);
+  const int* llinks = md.I(BXM_O_LEVEL_LINKS);
+  float* cd = w.at(L.cd);
+  for (int lv = 0; lv < md.nlevel; ++lv) {
+    for (int idx = lstart[lv] + tm.lane; idx < lstart[lv + 1]; idx += T) {
+      int l = llinks[idx];
+      int p = parent[l];
+      f3 a = p >= 0 ? ld3(cd + 6 * p) : mk3(0.f, 0.f, 0.f);
+      f3 v = p >= 0 ? ld3(cd + 6 * p + 3) : mk3(0.f, 0.f, 0.f);
+      int nd = ltype[l] == 0 ? 6 : ltype[l];
+      for (int k = 0; k < nd; ++k) {
+        int d = dadr[l] + k;
+        a = a + ld3(cdof + 6 * d) * qd[d];
+        v = v + ld3(cdof + 6 * d + 3) * qd[d];
+      }
+      st3(cd + 6 * l, a);
+      st3(cd + 6 * l + 3, v);
+    }
+    tm.sync();
+  }
+  // cdofd: :106-130
+  float* cdofd = w.at(L.cdofd);
+  for (int l = tm.lane; l < nl; l += T) {
+    int typ = ltype[l], da = dadr[l];
+    if (typ == 0) {
+      f3 sa = ld3(cdof + 6 * da) * qd[da] + ld3(cdof + 6 * (da + 1)) * qd[da + 1];
+      sa = sa + ld3(cdof + 6 * (da + 2)) * qd[da + 2];
+      f3 sv = ld3(cdof + 6 * da + 3) * qd[da] + ld3(cdof + 6 * (da + 1) + 3) * qd[da + 1];
+      sv = sv + ld3(cdof + 6 * (da + 2) + 3) * qd[da + 2];
+      for (int k = 0; k < 6; ++k) {
+        int d = da + k;
+        f3 ra = mk3(0.f, 0.f, 0.f), rv = mk3(0.f, 0.f, 0.f);
+        if (k >= 3) motion_cross(sa, sv, ld3(cdof + 6 * d), ld3(cdof + 6 * d + 3), ra, rv);
+        st3(cdofd + 6 * d, ra);
+        st3(cdofd + 6 * d + 3, rv);
+      }
+    } else {
+      int p = parent[l];
+      f3 sa = p >= 0 ? ld3(cd + 6 * p) : mk3(0.f, 0.f, 0.f);
+      f3 sv = p >= 0 ? ld3(cd + 6 * p + 3) : mk3(0.f, 0.f, 0.f);
+      for (int k = 0; k < typ; ++k) {
+        int d = da + k;
+        f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
+        f3 ra, rv;
+        motion_cross(sa, sv, ca, cv, ra, rv);
+        st3(cdofd + 6 * d, ra);
+        st3(cdofd + 6 * d + 3, rv);
+        sa = sa + ca * qd[d];
+        sv = sv + cv * qd[d];
+      }
+    }
+  }
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// mass.matrix (CRBA): brax/generalized/mass.py:27-83
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ void stage_crba(const Model& md, const Team<T>& tm, const Ws& w) {
+  const Layout& L = w.L;
+  const int nl = md.nl, nv = md.nv, ld = L.ldm;
+  float* crbi = w.at(L.scr);
+  float* crbp = crbi + 9 * nl;
+  float* crbm = crbp + 3 * nl;
+  const float* ci = w.at(L.ci);
+  const float* cp = w.at(L.cp);
+  const float* mass = md.F(BXM_O_LI_MASS);
+  const int* lstart = md.I(BXM_O_LEVEL_START);
+  const int* llinks = md.I(BXM_O_LEVEL_LINKS);
+  const int* cstart = md.I(BXM_O_CHILD_START);
+  const int* cidx = md.I(BXM_O_CHILD_IDX);
+  for (int lv = md.nlevel - 1; lv >= 0; --lv) {  // leaf-to-root: crb = cinr + sum(children)
+    for (int idx = lstart[lv] + tm.lane; idx < lstart[lv + 1]; idx += T) {
+      int l = llinks[idx];
+      float si[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      f3 sp = mk3(0.f, 0.f, 0.f);
+      float sm = 0.f;
+      for (int c = cstart[l]; c < cstart[l + 1]; ++c) {
+        int ch = cidx[c];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) si[k] += crbi[9 * ch + k];
+        sp = sp + ld3(crbp + 3 * ch);
+        sm += crbm[ch];
+      }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) crbi[9 * l + k] = ci[9 * l + k] + si[k];
+      st3(crbp + 3 * l, ld3(cp + 3 * l) + sp);
+      crbm[l] = mass[l] + sm;
+    }
+    tm.sync();
+  }
+  const int* dlink = md.I(BXM_O_DOF_LINK);
+  const float* cdof = w.at(L.cdof);
+  const float* arm = md.F(BXM_O_D_ARM);
+  float* M = w.at(L.M);
+  for (int r = tm.lane; r < nv; r += T) {
+    int l = dlink[r];
+    f3 fa, fv;
+    inertia_mul(crbi + 9 * l, ld3(crbp + 3 * l), crbm[l], ld3(cdof + 6 * r), ld3(cdof + 6 * r + 3), fa, fv);
+    uint64_t anc = md.anc(l);
+    for (int c = 0; c <= r; ++c) {
+      float v = 0.f;
+      if ((anc >> c) & 1ull) v = dot3(ld3(cdof + 6 * c + 3), fv) + dot3(ld3(cdof + 6 * c), fa);
+      if (c == r) v = v + arm[r];
+      M[r * ld + c] = v;
+      M[c * ld + r] = v;
+    }
+  }
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// dense helpers on nv x nv matrices (leading dimension ld)
+// ---------------------------------------------------------------------------
+// op 0: C = A B;  op 1: C = I - A B;  op 2: C = A (I + B)
+template <int T, int NVB>
+__device__ void matmul(const Team<T>& tm, int n, int ld, const float* A, const float* B, float* C, int op) {
+  for (int j = tm.lane; j < n; j += T) {
+    float acc[NVB];
+#pragma unroll
+    for (int i = 0; i < NVB; ++i) acc[i] = 0.f;
+    for (int k = 0; k < n; ++k) {
+      float b = B[k * ld + j];
+      if (op == 2 && k == j) b = b + 1.f;
+#pragma unroll
+      for (int i = 0; i < NVB; ++i)
+        if (i < n) acc[i] = fmaf(A[i * ld + k], b, acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < NVB; ++i)
+      if (i < n) C[i * ld + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[i]) : acc[i];
+  }
+  tm.sync();
+}
+
+// safe_norm (brax/math.py:308-328) of an n x n matrix
+template <int T>
+__device__ float safe_norm_mat(const Team<T>& tm, int n, int ld, const float* R) {
+  float s = 0.f;
+  bool small = true;
+  for (int idx = tm.lane; idx < n * n; idx += T) {
+    int i = idx / n, j = idx - i * n;
+    float v = R[i * ld + j];
+    small = small && (fabsf(v) <= 1e-8f);
+    s += v * v;
+  }
+  bool z = tm.all(small);
+  s = tm.sum(s);
+  return z ? 0.f : sqrtf(s);
+}
+
+// In-place lower Cholesky of the n x n matrix in A (lower triangle used).
+// Returns false (team-uniform) when a pivot is not positive.
+template <int T>
+__device__ bool cholesky(const Team<T>& tm, int n, int ld, float* A) {
+  bool ok = true;
+  for (int k = 0; k < n; ++k) {
+    float piv = A[k * ld + k];
+    ok = ok && (piv > 0.f);
+    float d = sqrtf(fmaxf(piv, 1e-30f));
+    tm.sync();
+    for (int i = k + 1 + tm.lane; i < n; i += T) A[i * ld + k] = A[i * ld + k] / d;
+    if (tm.lane == 0) A[k * ld + k] = d;
+    tm.sync();
+    for (int i = k + 1 + tm.lane; i < n; i += T) {
+      float lik = A[i * ld + k];
+      for (int j = k + 1; j <= i; ++j) A[i * ld + j] = A[i * ld + j] - lik * A[j * ld + k];
+    }
+    tm.sync();
+  }
+  return ok;
+}
+
+// Minv = L^-T L^-1 from the Cholesky factor L (lower, in Lm); Wt is scratch.
+template <int T, int NVB>
+__device__ void chol_inverse(const Team<T>& tm, int n, int ld, const float* Lm, float* Wt, float* Minv) {
+  // Wt = L^-1 (lower), one column per lane by forward substitution
+  for (int j = tm.lane; j < n; j += T) {
+    for (int i = 0; i < n; ++i) {
+      float v;
+      if (i < j) {
+        v = 0.f;
+      } else {
+        float s = (i == j) ? 1.f : 0.f;
+        for (int k = j; k < i; ++k) s = s - Lm[i * ld + k] * Wt[k * ld + j];
+        v = s / Lm[i * ld + i];
+      }
+      Wt[i * ld + j] = v;
+    }
+  }
+  tm.sync();
+  // Minv[i][j] = sum_k Wt[k][i] Wt[k][j]
+  for (int j = tm.lane; j < n; j += T) {
+    float acc[NVB];
+#pragma unroll
+    for (int i = 0; i < NVB; ++i) acc[i] = 0.f;
+    for (int k = 0; k < n; ++k) {
+      float b = Wt[k * ld + j];
+#pragma unroll
+      for (int i = 0; i < NVB; ++i)
+        if (i < n) acc[i] = fmaf(Wt[k * ld + i], b, acc[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < NVB; ++i)
+      if (i < n) Minv[i * ld + j] = acc[i];
+  }
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// mass.matrix_inv: brax/generalized/mass.py:86-106 + brax/math.py:278-305
+// mode 0 keeps/updates Minv by Newton-Schulz (num_iter iterations; 0 keeps
+// the input); mode 1 recomputes the exact SPD inverse.
+// ---------------------------------------------------------------------------
+template <int T, int NVB>
+__device__ bool stage_inverse(const Model& md, const Team<T>& tm, const Ws& w, bool exact, int num_iter) {
+  const Layout& L = w.L;
+  const int n = md.nv, ld = L.ldm;
+  float* M = w.at(L.M);
+  float* P = w.at(L.Minv);
+  float* S1 = w.at(L.scr);
+  float* S2 = S1 + n * ld;
+  if (n == 0) return true;
+  if (exact) {
+    for (int idx = tm.lane; idx < n * n; idx += T) {
+      int i = idx / n, j = idx - i * n;
+      S1[i * ld + j] = M[i * ld + j];
+    }
+    tm.sync();
+    bool ok = cholesky<T>(tm, n, ld, S1);
+    chol_inverse<T, NVB>(tm, n, ld, S1, S2, P);
+    return ok;
+  }
+  if (num_iter <= 0) return true;
+  float* cur = P;
+  float* R = S1;
+  float* nxt = S2;
+  matmul<T, NVB>(tm, n, ld, M, cur, R, 1);  // r0 = I - A A_inv
+  float nr0 = safe_norm_mat<T>(tm, n, ld, R);
+  if (nr0 > 1.f) {  // reset to 0.5 A^T / tr(A A^T) (r0 is kept, as the reference does)
+    float s = 0.f;
+    for (int idx = tm.lane; idx < n * n; idx += T) {
+      int i = idx / n, j = idx - i * n;
+      float v = M[i * ld + j];
+      s += v * v;
+    }
+    s = tm.sum(s);
+    for (int idx = tm.lane; idx < n * n; idx += T) {
+      int i = idx / n, j = idx - i * n;
+      cur[i * ld + j] = 0.5f * M[j * ld + i] / s;
+    }
+    tm.sync();
+  }
+  float err = 1.f;
+  for (int it = 0; it < num_iter; ++it) {
+    matmul<T, NVB>(tm, n, ld, cur, R, nxt, 2);  // a_inv (I + r)
+    matmul<T, NVB>(tm, n, ld, M, nxt, R, 1);    // I - a a_inv_next
+    float e = safe_norm_mat<T>(tm, n, ld, R);
+    if (e < err) {
+      float* t = cur;
+      cur = nxt;
+      nxt = t;
+    }
+    err = e;
+  }
+  if (cur != P) {
+    for (int idx = tm.lane; idx < n * n; idx += T) {
+      int i = idx / n, j = idx - i * n;
+      P[i * ld + j] = cur[i * ld + j];
+    }
+    tm.sync();
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// constraint._imp_aref: brax/generalized/constraint.py:29-65
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void imp_aref(const float* p, float pos, float vel, float& imp, float& aref) {
+  float timeconst = p[0], dampratio = p[1], dmin = p[2], dmax = p[3], width = p[4], mid = p[5], power = p[6];
+  float imp_x = fabsf(pos) / width;
+  float imp_a = (1.f / powf(mid, power - 1.f)) * powf(imp_x, power);
+  float imp_b = 1.f - (1.f / powf(1.f - mid, power - 1.f)) * powf(1.f - imp_x, power);
+  float imp_y = imp_x < mid ? imp_a : imp_b;
+  imp = dmin + imp_y * (dmax - dmin);
+  imp = fminf(fmaxf(imp, dmin), dmax);
+  imp = imp_x > 1.f ? dmax : imp;
+  float b = 2.f / (dmax * timeconst);
+  float k = 1.f / (dmax * dmax * timeconst * timeconst * dampratio * dampratio);
+  b = dampratio <= 0.f ? -dampratio / dmax : b;
+  k = timeconst <= 0.f ? -timeconst / (dmax * dmax) : k;
+  aref = -b * vel - k * imp * pos;
+}
+
+// ---------------------------------------------------------------------------
+// contact.get + mujoco.mjx primitive collisions: brax/contact.py:28-67
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void geom_pose(const float* xp, const float* xr, int link, const float* gp,
+                                         const float* gq, f3& pos, float* R) {
+  f3 lp = link >= 0 ? ld3(xp + 3 * link) : mk3(0.f, 0.f, 0.f);
+  q4 lr = link >= 0 ? ld4(xr + 4 * link) : qident();
+  pos = lp + rotate(ld3(gp), lr);
+  quat_to_3x3(qmul(lr, ld4(gq)), R);
+}
+
+__device__ __forceinline__ void plane_sphere(f3 n, f3 pp, f3 sp, float r, float& dist, f3& pos) {
+  dist = dot3(sp - pp, n) - r;
+  pos = sp - n * (r + 0.5f * dist);
+}
+
+__device__ __forceinline__ void sphere_sphere(f3 p1, float r1, f3 p2, float r2, float& dist, f3& pos, f3& n) {
+  float d;
+  n = normalize_with_norm(p2 - p1, d);
+  if (d == 0.f) n = mk3(1.f, 0.f, 0.f);
+  dist = d - (r1 + r2);
+  pos = p1 + n * (r1 + 0.5f * dist);
+}
+
+__device__ __forceinline__ f3 closest_segment_point(f3 a, f3 b, f3 pt) {
+  f3 ab = b - a;
+  float t = dot3(pt - a, ab) / (dot3(ab, ab) + 1e-6f);
+  return a + fminf(fmaxf(t, 0.f), 1.f) * ab;
+}
+
+__device__ __forceinline__ void closest_seg_seg(f3 a0, f3 a1, f3 b0, f3 b1, f3& ba, f3& bb) {
+  float la, lb;
+  f3 da = normalize_with_norm(a1 - a0, la);
+  f3 db = normalize_with_norm(b1 - b0, lb);
+  float ha = la * 0.5f, hb = lb * 0.5f;
+  f3 am = a0 + da * ha, bm = b0 + db * hb;
+  f3 tr = am - bm;
+  float dd = dot3(da, db), dat = dot3(da, tr), dbt = dot3(db, tr);
+  float denom = 1.f - dd * dd;
+  float ta0 = (-dat + dd * dbt) / (denom + 1e-6f);
+  float tb0 = dbt + ta0 * dd;
+  float ta = fminf(fmaxf(ta0, -ha), ha), tb = fminf(fmaxf(tb0, -hb), hb);
+  f3 besta = am + da * ta, bestb = bm + db * tb;
+  f3 na = closest_segment_point(a0, a1, bestb);
+  f3 nb = closest_segment_point(b0, b1, besta);
+  float d1 = dot3(bestb - na, bestb - na), d2 = dot3(besta - nb, besta - nb);
+  if (d1 < d2) {
+    ba = na;
+  } else {
+    ba = besta;
+    bestb = nb;
+  }
+  bb = bestb;
+}
+
+// Writes dist[k], pos[k*3], frame[k*9] for every contact slot.
+template <int T>
+__device__ void stage_contacts(const Model& md, const Team<T>& tm, const Ws& w, float* dist, float* cpos,
+                               float* frame) {
+  const Layout& L = w.L;
+  const float* xp = w.at(L.xp);
+  const float* xr = w.at(L.xr);
+  const int* kind = md.I(BXM_O_CON_KIND);
+  const int* sub = md.I(BXM_O_CON_SUB);
+  const int* la = md.I(BXM_O_CON_LA);
+  const int* lb = md.I(BXM_O_CON_LB);
+  const float* g1p = md.F(BXM_O_CON_G1POS);
+  const float* g1q = md.F(BXM_O_CON_G1QUAT);
+  const float* g1s = md.F(BXM_O_CON_G1SIZE);
+  const float* g2p = md.F(BXM_O_CON_G2POS);
+  const float* g2q = md.F(BXM_O_CON_G2QUAT);
+  const float* g2s = md.F(BXM_O_CON_G2SIZE);
+  for (int k = tm.lane; k < md.ncon; k += T) {
+    f3 p1, p2;
+    float R1[9], R2[9];
+    geom_pose(xp, xr, la[k], g1p + 3 * k, g1q + 4 * k, p1, R1);
+    geom_pose(xp, xr, lb[k], g2p + 3 * k, g2q + 4 * k, p2, R2);
+    float* F = frame + 9 * k;
+    float d = 0.f;
+    f3 pos = mk3(0.f, 0.f, 0.f);
+    int kd = kind[k];
+    if (kd == BXM_CON_PLANE_SPHERE) {
+      f3 n = mk3(R1[2], R1[5], R1[8]);
+      plane_sphere(n, p1, p2, g2s[3 * k], d, pos);
+      make_frame(n, F);
+    } else if (kd == BXM_CON_PLANE_CAPSULE) {
+      f3 n = mk3(R1[2], R1[5], R1[8]), axis = mk3(R2[2], R2[5], R2[8]);
+      float bn;
+      f3 b = normalize_with_norm(axis - n * dot3(n, axis), bn);
+      if (bn < 0.5f) b = (-0.5f < n.y && n.y < 0.5f) ? mk3(0.f, 1.f, 0.f) : mk3(0.f, 0.f, 1.f);
+      f3 seg = axis * g2s[3 * k + 1];
+      f3 c = sub[k] == 0 ? p2 + seg : p2 - seg;
+      plane_sphere(n, p1, c, g2s[3 * k], d, pos);
+      st3(F, n);
+      st3(F + 3, b);
+      st3(F + 6, cross3(n, b));
+    } else if (kd == BXM_CON_PLANE_BOX) {
+      f3 n = mk3(R1[2], R1[5], R1[8]);
+      // the sub-th deepest corner (ties broken by corner index)
+      float cd[8];
+      f3 cc[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        f3 loc = mk3((c & 4) ? g2s[3 * k] : -g2s[3 * k], (c & 2) ? g2s[3 * k + 1] : -g2s[3 * k + 1],
+                     (c & 1) ? g2s[3 * k + 2] : -g2s[3 * k + 2]);
+        cc[c] = p2 + mk3(R2[0] * loc.x + R2[1] * loc.y + R2[2] * loc.z, R2[3] * loc.x + R2[4] * loc.y + R2[5] * loc.z,
+                         R2[6] * loc.x + R2[7] * loc.y + R2[8] * loc.z);
+        cd[c] = dot3(cc[c] - p1, n);
+      }
+      int want = sub[k], pick = 0;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        int rank = 0;
+#pragma unroll
+        for (int e = 0; e < 8; ++e) rank += (cd[e] < cd[c]) || (cd[e] == cd[c] && e < c);
+        if (rank == want) pick = c;
+      }
+      d = cd[pick];
+      pos = cc[pick] - n * (0.5f * d);
+      make_frame(n, F);
+    } else if (kd == BXM_CON_SPHERE_SPHERE) {
+      f3 n;
+      sphere_sphere(p1, g1s[3 * k], p2, g2s[3 * k], d, pos, n);
+      make_frame(n, F);
+    } else if (kd == BXM_CON_SPHERE_CAPSULE) {
+      f3 seg = mk3(R2[2], R2[5], R2[8]) * g2s[3 * k + 1];
+      f3 pt = closest_segment_point(p2 - seg, p2 + seg, p1);
+      f3 n;
+      sphere_sphere(p1, g1s[3 * k], pt, g2s[3 * k], d, pos, n);
+      make_frame(n, F);
+    } else {  // capsule-capsule
+      f3 s1 = mk3(R1[2], R1[5], R1[8]) * g1s[3 * k + 1];
+      f3 s2 = mk3(R2[2], R2[5], R2[8]) * g2s[3 * k + 1];
+      f3 a, b, n;
+      closest_seg_seg(p1 - s1, p1 + s1, p2 - s2, p2 + s2, a, b);
+      sphere_sphere(a, g1s[3 * k], b, g2s[3 * k], d, pos, n);
+      make_frame(n, F);
+    }
+    dist[k] = d;
+    st3(cpos + 3 * k, pos);
+  }
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// constraint.jacobian (active rows only, compacted): constraint.py:101-191.
+// Rows whose mask (dist < 0 / pos < 0) is off are exactly zero in the
+// reference (jac, diag and aref are multiplied by the mask), so they add
+// nothing to A x + b; only the active rows are stored, in reference order.
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ void stage_jacobian(const Model& md, const Team<T>& tm, const Ws& w) {
+  const Layout& L = w.L;
+  const int nv = md.nv, ldj = L.ldj, ncon = md.ncon;
+  float* dist = w.at(L.scr);
+  float* cpos = dist + al4(ncon);
+  float* frame = cpos + al4(3 * ncon);
+  int* rcon = reinterpret_cast<int*>(frame + al4(9 * ncon));
+  int* rmap = reinterpret_cast<int*>(w.at(L.rmap));
+  float* J = w.at(L.J);
+  float* rdiag = w.at(L.rdiag);
+  float* raref = w.at(L.raref);
+  const float* qd = w.at(L.qd);
+  const float* q = w.at(L.q);
+  int nact = 0;
+  if (ncon > 0) {
+    stage_contacts<T>(md, tm, w, dist, cpos, frame);
+    for (int base = 0; base < ncon; base += T) {
+      int k = base + tm.lane;
+      bool a = k < ncon && dist[k] < 0.f;
+      unsigned bal = tm.ballot(a);
+      if (a) rcon[nact + __popc(bal & ((1u << tm.lane) - 1u))] = k;
+      nact += __popc(bal);
+    }
+    tm.sync();
+    const int* la = md.I(BXM_O_CON_LA);
+    const int* lb = md.I(BXM_O_CON_LB);
+    const float* fric = md.F(BXM_O_CON_FRIC);
+    const float* rc = w.at(L.rc);
+    const float* cdof = w.at(L.cdof);
+    for (int c = 0; c < nact; ++c) {  // constraint.py:154-164
+      int k = rcon[c];
+      int a = la[k], b = lb[k];
+      uint64_t ma = a >= 0 ? md.anc(a) : 0ull, mb = md.anc(b);
+      f3 p = ld3(cpos + 3 * k);
+      f3 offa = a >= 0 ? p - ld3(rc + 3 * a) : mk3(0.f, 0.f, 0.f);
+      f3 offb = p - ld3(rc + 3 * b);
+      f3 n = ld3(frame + 9 * k), t1 = ld3(frame + 9 * k + 3), t2 = ld3(frame + 9 * k + 6);
+      float mu = fric[k];
+      f3 v0 = (-t1) * (-mu) + n, v1 = (-t1) * mu + n, v2 = (-t2) * (-mu) + n, v3 = (-t2) * mu + n;
+      for (int d = tm.lane; d < nv; d += T) {
+        f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
+        f3 jb = ((mb >> d) & 1ull) ? cv - cross3(offb, ca) : mk3(0.f, 0.f, 0.f);
+        f3 ja = ((ma >> d) & 1ull) ? cv - cross3(offa, ca) : mk3(0.f, 0.f, 0.f);
+        f3 diff = jb - ja;
+        J[(4 * c + 0) * ldj + d] = dot3(diff, v0);
+        J[(4 * c + 1) * ldj + d] = dot3(diff, v1);
+        J[(4 * c + 2) * ldj + d] = dot3(diff, v2);
+        J[(4 * c + 3) * ldj + d] = dot3(diff, v3);
+      }
+      if (tm.lane < 4) rmap[4 * c + tm.lane] = 4 * k + tm.lane;
+    }
+  }
+  int nrow = 4 * nact;
+  if (md.nlim > 0) {  // constraint.py:101-132
+    const float* lo = md.F(BXM_O_LIM_LO);
+    const float* hi = md.F(BXM_O_LIM_HI);
+    const int* lq = md.I(BXM_O_LIM_QADR);
+    const int* ldof = md.I(BXM_O_LIM_DOF);
+    for (int base = 0; base < md.nlim; base += T) {
+      int i = base + tm.lane;
+      bool a = false;
+      float side = 0.f;
+      if (i < md.nlim) {
+        float pmin = q[lq[i]] - lo[i], pmax = hi[i] - q[lq[i]];
+        float pos = fminf(fminf(pmin, pmax), 0.f);
+        a = pos < 0.f;
+        side = pmin < pmax ? 1.f : -1.f;
+      }
+      unsigned bal = tm.ballot(a);
+      tm.sync();
+      if (a) {
+        int r = nrow + __popc(bal & ((1u << tm.lane) - 1u));
+        rmap[r] = 4 * ncon + i;
+        for (int d = 0; d < nv; ++d) J[r * ldj + d] = (d == ldof[i]) ? side : 0.f;
+      }
+      nrow += __popc(bal);
+    }
+  }
+  tm.sync();
+  // per-row impedance, reference acceleration and A diagonal
+  const float* csolp = md.F(BXM_O_CON_SOLP);
+  const float* cinvw = md.F(BXM_O_CON_INVW);
+  const float* fric = md.F(BXM_O_CON_FRIC);
+  for (int r = tm.lane; r < nrow; r += T) {
+    int orig = rmap[r];
+    float vel = 0.f;
+    for (int d = 0; d < nv; ++d) vel += J[r * ldj + d] * qd[d];
+    float imp, aref, diag;
+    if (orig < 4 * ncon) {  // constraint.py:167-174
+      int k = orig >> 2;
+      imp_aref(csolp + 7 * k, dist[k], vel, imp, aref);
+      float mu = fric[k], tw = cinvw[k];
+      diag = (tw + mu * mu * tw) * (2.f * mu * mu * (1.f - imp) / (imp + 1e-8f));
+    } else {  // constraint.py:121-130
+      int i = orig - 4 * ncon;
+      const int* lq = md.I(BXM_O_LIM_QADR);
+      float pmin = q[lq[i]] - md.F(BXM_O_LIM_LO)[i], pmax = md.F(BXM_O_LIM_HI)[i] - q[lq[i]];
+      float pos = fminf(fminf(pmin, pmax), 0.f);
+      imp_aref(md.F(BXM_O_LIM_SOLP) + 7 * i, pos, vel, imp, aref);
+      diag = md.F(BXM_O_LIM_INVW)[i] * (1.f - imp) / (imp + 1e-8f);
+    }
+    rdiag[r] = diag;
+    raref[r] = aref;
+  }
+  if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[0] = nrow;
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// actuator.to_tau (brax/actuator.py:23-57), dynamics.forward with _passive
+// and inverse/RNE (brax/generalized/dynamics.py:137-236) -> qf_smooth
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ void stage_smooth(const Model& md, const Team<T>& tm, const Ws& w, bool has_act) {
+  const Layout& L = w.L;
+  const int nl = md.nl, nv = md.nv;
+  float* cdd = w.at(L.scr);
+  float* cf = cdd + 6 * nl;
+  float* force = cf + 6 * nl;
+  const float* q = w.at(L.q);
+  const float* qd = w.at(L.qd);
+  const float* act = w.at(L.act);
+  const int* aqid = md.I(BXM_O_ACT_QID);
+  const int* aqdid = md.I(BXM_O_ACT_QDID);
+  if (has_act) {
+    for (int a = tm.lane; a < md.nu; a += T) {
+      const float* cr = md.F(BXM_O_ACT_CR) + 2 * a;
+      const float* fr = md.F(BXM_O_ACT_FR) + 2 * a;
+      float gear = md.F(BXM_O_ACT_GEAR)[a];
+      float u = fminf(fmaxf(act[a], cr[0]), cr[1]);
+      float bias = gear * (q[aqid[a]] * md.F(BXM_O_ACT_BQ)[a] + qd[aqdid[a]] * md.F(BXM_O_ACT_BQD)[a]);
+      float f = md.F(BXM_O_ACT_GAIN)[a] * u + bias;
+      f = fminf(fmaxf(f, fr[0]), fr[1]);
+      force[a] = f * gear;
+    }
+  }
+  // cdd root-to-leaf: dynamics.py:153-165
+  const int* lstart = md.I(BXM_O_LEVEL_START);
+  const int* llinks = md.I(BXM_O_LEVEL_LINKS);
+  const int* parent = md.I(BXM_O_LINK_PARENT);
+  const int* ltype = md.I(BXM_O_LINK_TYPE);
+  const int* dadr = md.I(BXM_O_LINK_DADR);
+  const float* cdofd = w.at(L.cdofd);
+  for (int lv = 0; lv < md.nlevel; ++lv) {
+    for (int idx = lstart[lv] + tm.lane; idx < lstart[lv + 1]; idx += T) {
+      int l = llinks[idx];
+      int p = parent[l];
+      f3 a = p >= 0 ? ld3(cdd + 6 * p) : mk3(0.f, 0.f, 0.f);
+      f3 v = p >= 0 ? ld3(cdd + 6 * p + 3) : -md.g;
+      int nd = ltype[l] == 0 ? 6 : ltype[l];
+      for (int k = 0; k < nd; ++k) {
+        int d = dadr[l] + k;
+        a = a + ld3(cdofd + 6 * d) * qd[d];
+        v = v + ld3(cdofd + 6 * d + 3) * qd[d];
+      }
+      st3(cdd + 6 * l, a);
+      st3(cdd + 6 * l + 3, v);
+    }
+    tm.sync();
+  }
+  // cfrc_flat = cinr * cdd + cd x (cinr * cd): dynamics.py:168-171
+  const float* ci = w.at(L.ci);
+  const float* cp = w.at(L.cp);
+  const float* cd = w.at(L.cd);
+  const float* mass = md.F(BXM_O_LI_MASS);
+  for (int l = tm.lane; l < nl; l += T) {
+    f3 p = ld3(cp + 3 * l);
+    f3 fa, fv, ga, gv, xa, xv;
+    inertia_mul(ci + 9 * l, p, mass[l], ld3(cdd + 6 * l), ld3(cdd + 6 * l + 3), fa, fv);
+    f3 cda = ld3(cd + 6 * l), cdv = ld3(cd + 6 * l + 3);
+    inertia_mul(ci + 9 * l, p, mass[l], cda, cdv, ga, gv);
+    force_cross(cda, cdv, ga, gv, xa, xv);
+    st3(cf + 6 * l, fa + xa);
+    st3(cf + 6 * l + 3, fv + xv);
+  }
+  tm.sync();
+  // leaf-to-root sum: dynamics.py:174-179
+  const int* cstart = md.I(BXM_O_CHILD_START);
+  const int* cidx = md.I(BXM_O_CHILD_IDX);
+  for (int lv = md.nlevel - 1; lv >= 0; --lv) {
+    for (int idx = lstart[lv] + tm.lane; idx < lstart[lv + 1]; idx += T) {
+      int l = llinks[idx];
+      if (cstart[l] == cstart[l + 1]) continue;
+      f3 sa = mk3(0.f, 0.f, 0.f), sv = mk3(0.f, 0.f, 0.f);
+      for (int c = cstart[l]; c < cstart[l + 1]; ++c) {
+        sa = sa + ld3(cf + 6 * cidx[c]);
+        sv = sv + ld3(cf + 6 * cidx[c] + 3);
+      }
+      st3(cf + 6 * l, ld3(cf + 6 * l) + sa);
+      st3(cf + 6 * l + 3, ld3(cf + 6 * l + 3) + sv);
+    }
+    tm.sync();
+  }
+  // qf_smooth = passive - bias + tau: dynamics.py:182, 190-196, 232-234
+  const int* dlink = md.I(BXM_O_DOF_LINK);
+  const float* cdof = w.at(L.cdof);
+  const float* stiff = md.F(BXM_O_D_STIFF);
+  const float* damp = md.F(BXM_O_D_DAMP);
+  const int* qadr = md.I(BXM_O_LINK_QADR);
+  float* qfs = w.at(L.qfs);
+  for (int d = tm.lane; d < nv; d += T) {
+    int l = dlink[d];
+    float bias = dot3(ld3(cdof + 6 * d + 3), ld3(cf + 6 * l + 3)) + dot3(ld3(cdof + 6 * d), ld3(cf + 6 * l));
+    float pas = 0.f;
+    if (ltype[l] != 0) pas = -q[qadr[l] + (d - dadr[l])] * stiff[d];
+    pas = pas - damp[d] * qd[d];
+    float tau = 0.f;
+    if (has_act)
+      for (int a = 0; a < md.nu; ++a)
+        if (aqdid[a] == d) tau = tau + force[a];
+    qfs[d] = (pas - bias) + tau;
+  }
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
+// constraint.force: brax/generalized/constraint.py:194-240, with the
+// jaxopt.ProjectedGradient (FISTA + backtracking) iteration restated.
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ void matvec_A(const Model& md, const Team<T>& tm, const Ws& w, int nrow, const float* v, float* out,
+                         float* t1, float* t2) {
+  const Layout& L = w.L;
+  const int nv = md.nv, ldj = L.ldj, ld = L.ldm;
+  const float* J = w.at(L.J);
+  const float* Minv = w.at(L.Minv);
+  const float* rdiag = w.at(L.rdiag);
+  for (int d = tm.lane; d < nv; d += T) {  // t1 = J^T v
+    float s = 0.f;
+    for (int r = 0; r < nrow; ++r) s = fmaf(J[r * ldj + d], v[r], s);
+    t1[d] = s;
+  }
+  tm.sync();
+  for (int d = tm.lane; d < nv; d += T) {  // t2 = Minv t1
+    float s = 0.f;
+    for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * ld + k], t1[k], s);
+    t2[d] = s;
+  }
+  tm.sync();
+  for (int r = tm.lane; r < nrow; r += T) {  // out = J t2 + diag v
+    float s = 0.f;
+    for (int k = 0; k < nv; ++k) s = fmaf(J[r * ldj + k], t2[k], s);
+    out[r] = s + rdiag[r] * v[r];
+  }
+  tm.sync();
+}
+
+template <int T>
+__device__ int stage_constraint(const Model& md, const Team<T>& tm, const Ws& w) {
+  const Layout& L = w.L;
+  const int nv = md.nv, ldj = L.ldj, ld = L.ldm;
+  const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
+  float* qfc = w.at(L.qfc);
+  if (nrow == 0) {
+    for (int d = tm.lane; d < nv; d += T) qfc[d] = 0.f;
+    tm.sync();
+    return 0;
+  }
+  const int m = md.m;
+  float* b = w.at(L.scr);
+  float* x = b + al4(m);
+  float* y = x + al4(m);
+  float* gy = y + al4(m);
+  float* r = gy + al4(m);
+  float* nx = r + al4(m);
+  float* gx = nx + al4(m);
+  float* ny = gx + al4(m);
+  float* t1 = ny + al4(m);
+  float* t2 = t1 + al4(nv);
+  const float* J = w.at(L.J);
+  const float* Minv = w.at(L.Minv);
+  const float* raref = w.at(L.raref);
+  const float* qfs = w.at(L.qfs);
+  // b = J Minv qf_smooth - aref
+  for (int d = tm.lane; d < nv; d += T) {
+    float s = 0.f;
+    for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * ld + k], qfs[k], s);
+    t2[d] = s;
+  }
+  tm.sync();
+  for (int i = tm.lane; i < nrow; i += T) {
+    float s = 0.f;
+    for (int k = 0; k < nv; ++k) s = fmaf(J[i * ldj + k], t2[k], s);
+    b[i] = s - raref[i];
+    x[i] = 0.f;
+    y[i] = 0.f;
+  }
+  tm.sync();
+  float t = 1.f, ss = 1.f, err = INFINITY;
+  int matvecs = 0;
+  for (int it = 0; it < md.pg_iters; ++it) {
+    if (it > 0 && !(err > md.pg_tol)) break;
+    // value and gradient at y
+    matvec_A<T>(md, tm, w, nrow, y, r, t1, t2);
+    float fs = 0.f;
+    for (int i = tm.lane; i < nrow; i += T) {
+      r[i] = r[i] + b[i];
+      fs += 0.5f * r[i] * r[i];
+    }
+    float fy = tm.sum(fs);
+    tm.sync();
+    matvec_A<T>(md, tm, w, nrow, r, gy, t1, t2);
+    matvecs += 2;
+    float cur = ss;
+    for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
+    tm.sync();
+    for (int ls = 0; ls < md.pg_maxls; ++ls) {
+      matvec_A<T>(md, tm, w, nrow, nx, r, t1, t2);
+      matvecs += 1;
+      float fn = 0.f, dv = 0.f, sq = 0.f;
+      for (int i = tm.lane; i < nrow; i += T) {
+        float ri = r[i] + b[i];
+        fn += 0.5f * ri * ri;
+        float dx = nx[i] - y[i];
+        dv += dx * gy[i];
+        sq += dx * dx;
+      }
+      fn = tm.sum(fn);
+      dv = tm.sum(dv);
+      sq = tm.sum(sq);
+      bool cond = cur * (fn - fy) > cur * dv + 0.5f * sq;
+      if (!cond) break;
+      cur = cur * 0.5f;
+      for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
+      tm.sync();
+    }
+    float nss = cur <= 1e-6f ? 1.f : cur / 0.5f;
+    float nt = 0.5f * (1.f + sqrtf(1.f + 4.f * t * t));
+    float beta = (t - 1.f) / nt;
+    for (int i = tm.lane; i < nrow; i += T) ny[i] = nx[i] + beta * (nx[i] - x[i]);
+    tm.sync();
+    // gradient at the new iterate and the stopping error
+    matvec_A<T>(md, tm, w, nrow, nx, r, t1, t2);
+    for (int i = tm.lane; i < nrow; i += T) r[i] = r[i] + b[i];
+    tm.sync();
+    matvec_A<T>(md, tm, w, nrow, r, gx, t1, t2);
+    matvecs += 2;
+    float es = 0.f;
+    for (int i = tm.lane; i < nrow; i += T) {
+      float e = fmaxf(nx[i] + (-1.f) * gx[i], 0.f) - nx[i];
+      es += e * e;
+      x[i] = nx[i];
+      y[i] = ny[i];
+    }
+    err = sqrtf(tm.sum(es));
+    tm.sync();
+    t = nt;
+    ss = nss;
+  }
+  // qf_constraint = J^T x
+  for (int d = tm.lane; d < nv; d += T) {
+    float s = 0.f;
+    for (int i = 0; i < nrow; ++i) s = fmaf(J[i * ldj + d], x[i], s);
+    qfc[d] = s;
+  }
+  tm.sync();
+  return matvecs;
+}
+
+// ---------------------------------------------------------------------------
+// integrator.integrate: brax/generalized/integrator.py:26-84
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ bool stage_integrate(const Model& md, const Team<T>& tm, const Ws& w) {
+  const Layout& L = w.L;
+  const int nv = md.nv, ld = L.ldm;
+  const float h = md.dt;
+  float* qfs = w.at(L.qfs);
+  float* qfc = w.at(L.qfc);
+  float* qdd = w.at(L.qdd);
+  float* v = w.at(L.v1);
+  float* qd = w.at(L.qd);
+  float* q = w.at(L.q);
+  bool ok = true;
+  for (int d = tm.lane; d < nv; d += T) v[d] = qfs[d] + qfc[d];
+  tm.sync();
+  if (md.ns_iters == 0) {  // (M + diag(damping) dt)^-1: integrator.py:58-62
+    float* A = w.at(L.scr);
+    const float* M = w.at(L.M);
+    const float* damp = md.F(BXM_O_D_DAMP);
+    for (int idx = tm.lane; idx < nv * nv; idx += T) {
+      int i = idx / nv, j = idx - i * nv;
+      A[i * ld + j] = M[i * ld + j] + (i == j ? damp[i] * h : 0.f);
+    }
+    tm.sync();
+    ok = cholesky<T>(tm, nv, ld, A);
+    // forward / backward substitution on the vector (single lane, nv small)
+    if (tm.lane == 0) {
+      for (int i = 0; i < nv; ++i) {
+        float s = v[i];
+        for (int k = 0; k < i; ++k) s -= A[i * ld + k] * qdd[k];
+        qdd[i] = s / A[i * ld + i];
+      }
+      for (int i = nv - 1; i >= 0; --i) {
+        float s = qdd[i];
+        for (int k = i + 1; k < nv; ++k) s -= A[k * ld + i] * qdd[k];
+        qdd[i] = s / A[i * ld + i];
+      }
+    }
+    tm.sync();
+  } else {
+    const float* Minv = w.at(L.Minv);
+    for (int d = tm.lane; d < nv; d += T) {
+      float s = 0.f;
+      for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * ld + k], v[k], s);
+      qdd[d] = s;
+    }
+    tm.sync();
+  }
+  for (int d = tm.lane; d < nv; d += T) qd[d] = qd[d] + qdd[d] * h;
+  tm.sync();
+  const int* ltype = md.I(BXM_O_LINK_TYPE);
+  const int* qadr = md.I(BXM_O_LINK_QADR);
+  const int* dadr = md.I(BXM_O_LINK_DADR);
+  for (int l = tm.lane; l < md.nl; l += T) {
+    int typ = ltype[l], qa = qadr[l], da = dadr[l];
+    if (typ == 0) {
+      q4 rot = ld4(q + qa + 3);
+      f3 ang = ld3(qd + da + 3);
+      float an = sqrtf(dot3(ang, ang)) + 1e-8f;
+      f3 axis = mk3(ang.x / an, ang.y / an, ang.z / an);
+      q4 qr = quat_rot_axis(axis, h * an);
+      rot = qmul(rot, qr);
+      float rn = sqrtf(rot.w * rot.w + rot.x * rot.x + rot.y * rot.y + rot.z * rot.z);
+      rot = q4{rot.w / rn, rot.x / rn, rot.y / rn, rot.z / rn};
+      f3 pos = ld3(q + qa) + ld3(qd + da) * h;
+      st3(q + qa, pos);
+      st4(q + qa + 3, rot);
+    } else {
+      for (int k = 0; k < typ; ++k) q[qa + k] = q[qa + k] + qd[da + k] * h;
+    }
+  }
+  tm.sync();
+  return ok;
+}
+
+}  // namespace braxg

@@ -1,0 +1,4 @@
+// Instantiation of the step kernel for 32 lanes per env, nv <= 64.
+#include "braxg_kernel.cuh"
+
+template cudaError_t braxg::launch_step<32, 64>(const braxg::StepArgs&, int, int, cudaStream_t);

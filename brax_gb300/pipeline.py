@@ -1,0 +1,225 @@
+"""Drop-in for brax.generalized.pipeline (init / step) on the GB300 kernels.
+
+Mirrors brax/generalized/pipeline.py:32-94: ``init(sys, q, qd)`` and
+``step(sys, state, act)`` with the same argument meaning, except that arrays
+are torch CUDA tensors and may carry a leading batch axis (the axis brax adds
+with ``jax.vmap``).  ``state`` fields follow brax/generalized/base.py:25-92.
+
+Every call goes through the braxg C ABI (include/braxg.h); there is no CPU
+fallback: without the built CUDA library or a CUDA device the calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from typing import Optional
+
+import torch
+
+from brax_gb300 import _native as N
+from brax_gb300 import model_pack
+from brax_gb300.system import System
+
+NEWTON_SCHULZ = N.INV_NEWTON_SCHULZ
+CHOLESKY = N.INV_CHOLESKY
+
+
+class Model:
+  """A System resident on one CUDA device (braxg_model_create)."""
+
+  def __init__(self, sys: System, device: Optional[torch.device] = None):
+    device = torch.device('cuda') if device is None else torch.device(device)
+    if device.type != 'cuda':
+      raise RuntimeError('braxg runs on CUDA devices only')
+    self.sys = sys
+    self.device = torch.device('cuda', device.index if device.index is not None
+                               else torch.cuda.current_device())
+    self.desc = model_pack.pack(sys)
+    h = ctypes.c_void_p()
+    lib = N.lib()
+    N.check(lib.braxg_model_create(self.desc.ctypes.data, self.desc.nbytes,
+                                   self.device.index, ctypes.byref(h)),
+            'braxg_model_create')
+    self._h = h
+    d = N.Dims()
+    N.check(lib.braxg_model_dims(h, ctypes.byref(d)), 'braxg_model_dims')
+    self.nl, self.nq, self.nv, self.nu = d.nl, d.nq, d.nv, d.nu
+    self.ncon, self.nlim, self.m = d.ncon, d.nlim, d.m
+
+  @property
+  def handle(self):
+    return self._h
+
+  def __del__(self):
+    h = getattr(self, '_h', None)
+    if h is not None and h.value:
+      try:
+        N.lib().braxg_model_destroy(h)
+      except Exception:  # interpreter shutdown
+        pass
+      self._h = None
+
+  def launch_shape(self, inverse_mode=NEWTON_SCHULZ, threads_per_env=0, envs_per_cta=0):
+    t, e, s = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    opt = N.Options(inverse_mode, threads_per_env, envs_per_cta)
+    N.check(N.lib().braxg_launch_shape(self._h, ctypes.byref(opt), ctypes.byref(t),
+                                       ctypes.byref(e), ctypes.byref(s)), 'braxg_launch_shape')
+    return t.value, e.value, s.value
+
+
+_MODELS = {}
+
+
+def model_for(sys, device=None) -> Model:
+  """Returns (and caches) the device-resident Model of a System."""
+  if isinstance(sys, Model):
+    return sys
+  dev = torch.device('cuda') if device is None else torch.device(device)
+  idx = dev.index if dev.index is not None else torch.cuda.current_device()
+  key = (id(sys), idx)
+  m = _MODELS.get(key)
+  if m is None or m.sys is not sys:
+    m = Model(sys, torch.device('cuda', idx))
+    _MODELS[key] = m
+  return m
+
+
+@dataclasses.dataclass
+class State:
+  """brax.generalized.base.State with a leading batch axis (torch tensors)."""
+  q: torch.Tensor
+  qd: torch.Tensor
+  x_pos: torch.Tensor
+  x_rot: torch.Tensor
+  xd_ang: torch.Tensor
+  xd_vel: torch.Tensor
+  mass_mx_inv: torch.Tensor
+  qf_smooth: torch.Tensor
+  qf_constraint: torch.Tensor
+  qdd: torch.Tensor
+  status: torch.Tensor
+  root_com: Optional[torch.Tensor] = None
+  cinr_pos: Optional[torch.Tensor] = None
+  cinr_rot: Optional[torch.Tensor] = None
+  cinr_i: Optional[torch.Tensor] = None
+  cd: Optional[torch.Tensor] = None
+  cdof: Optional[torch.Tensor] = None
+  cdofd: Optional[torch.Tensor] = None
+  mass_mx: Optional[torch.Tensor] = None
+  con_jac: Optional[torch.Tensor] = None
+  con_diag: Optional[torch.Tensor] = None
+  con_aref: Optional[torch.Tensor] = None
+  contact: None = None
+
+  def replace(self, **kw) -> 'State':
+    return dataclasses.replace(self, **kw)
+
+
+def _alloc(m: Model, n: int, full: bool, dev) -> State:
+  f = lambda *s: torch.empty(*s, dtype=torch.float32, device=dev)
+  s = State(q=f(n, m.nq), qd=f(n, m.nv), x_pos=f(n, m.nl, 3), x_rot=f(n, m.nl, 4),
+            xd_ang=f(n, m.nl, 3), xd_vel=f(n, m.nl, 3), mass_mx_inv=f(n, m.nv, m.nv),
+            qf_smooth=f(n, m.nv), qf_constraint=f(n, m.nv), qdd=f(n, m.nv),
+            status=torch.empty(n, dtype=torch.int32, device=dev))
+  if full:
+    s = s.replace(root_com=f(n, m.nl, 3), cinr_pos=f(n, m.nl, 3), cinr_rot=f(n, m.nl, 4),
+                  cinr_i=f(n, m.nl, 3, 3), cd=f(n, m.nl, 6), cdof=f(n, m.nv, 6),
+                  cdofd=f(n, m.nv, 6), mass_mx=f(n, m.nv, m.nv), con_jac=f(n, m.m, m.nv),
+                  con_diag=f(n, m.m), con_aref=f(n, m.m))
+  return s
+
+
+def _ptr(t):
+  return None if t is None else t.data_ptr()
+
+
+def _cstate(s: State) -> N.State:
+  return N.State(*[_ptr(getattr(s, f)) for f in N.STATE_FIELDS])
+
+
+def _as_batch(x: torch.Tensor, width: int, name: str, dev) -> torch.Tensor:
+  if not isinstance(x, torch.Tensor):
+    x = torch.as_tensor(x)
+  if x.dim() == 1:
+    x = x[None]
+  if x.dim() != 2 or x.shape[1] != width:
+    raise ValueError(f'{name} must have shape (..., {width}), got {tuple(x.shape)}')
+  if x.device != dev:
+    raise ValueError(f'{name} is on {x.device}, the model on {dev}')
+  return x.to(torch.float32).contiguous()
+
+
+def _opts(inverse_mode, threads_per_env, envs_per_cta):
+  return N.Options(int(inverse_mode), int(threads_per_env), int(envs_per_cta))
+
+
+def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
+         full: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0) -> State:
+  """brax/generalized/pipeline.py:32-61 for a batch of envs."""
+  if debug:
+    raise NotImplementedError('debug contacts are not materialised')
+  m = model_for(sys, q.device if isinstance(q, torch.Tensor) else None)
+  q = _as_batch(q, m.nq, 'q', m.device)
+  qd = _as_batch(qd, m.nv, 'qd', m.device)
+  if q.shape[0] != qd.shape[0]:
+    raise ValueError('q and qd batch sizes differ')
+  out = _alloc(m, q.shape[0], full, m.device)
+  cs = _cstate(out)
+  stream = torch.cuda.current_stream(m.device).cuda_stream
+  N.check(N.lib().braxg_init(m.handle, ctypes.c_void_p(stream), q.shape[0], q.data_ptr(),
+                             qd.data_ptr(), ctypes.byref(cs),
+                             ctypes.byref(_opts(NEWTON_SCHULZ, threads_per_env, envs_per_cta))),
+          'braxg_init')
+  return out
+
+
+def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
+         full: bool = False, inverse_mode: int = NEWTON_SCHULZ, out: Optional[State] = None,
+         threads_per_env: int = 0, envs_per_cta: int = 0) -> State:
+  """brax/generalized/pipeline.py:64-94; n_frames > 1 repeats it with the same
+  action (PipelineEnv.pipeline_step, brax/envs/base.py:128-137)."""
+  if debug:
+    raise NotImplementedError('debug contacts are not materialised')
+  m = model_for(sys, state.q.device)
+  n = state.q.shape[0]
+  act_p = None
+  if act is not None and m.nu > 0:
+    act = _as_batch(act, m.nu, 'act', m.device)
+    if act.shape[0] != n:
+      raise ValueError(f'act batch {act.shape[0]} != state batch {n}')
+    act_p = act.data_ptr()
+  if out is None:
+    out = _alloc(m, n, full, m.device)
+  cin = _cstate(state)
+  cout = _cstate(out)
+  stream = torch.cuda.current_stream(m.device).cuda_stream
+  N.check(N.lib().braxg_step(m.handle, ctypes.c_void_p(stream), n, int(n_frames), act_p,
+                             ctypes.byref(cin), ctypes.byref(cout),
+                             ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta))),
+          'braxg_step')
+  return out
+
+
+def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = NEWTON_SCHULZ,
+            trajectory: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0):
+  """len(act_seq) env steps in one launch; returns (final State, (traj_q, traj_qd))."""
+  m = model_for(sys, state.q.device)
+  n = state.q.shape[0]
+  act_seq = act_seq.to(torch.float32).contiguous()
+  if act_seq.dim() != 3 or act_seq.shape[1] != n or act_seq.shape[2] != m.nu:
+    raise ValueError(f'act_seq must be (n_steps, {n}, {m.nu})')
+  n_steps = act_seq.shape[0]
+  out = _alloc(m, n, False, m.device)
+  tq = tqd = None
+  if trajectory:
+    tq = torch.empty(n_steps, n, m.nq, dtype=torch.float32, device=m.device)
+    tqd = torch.empty(n_steps, n, m.nv, dtype=torch.float32, device=m.device)
+  cin, cout = _cstate(state), _cstate(out)
+  stream = torch.cuda.current_stream(m.device).cuda_stream
+  N.check(N.lib().braxg_rollout(m.handle, ctypes.c_void_p(stream), n, n_steps, int(n_frames),
+                                act_seq.data_ptr() if m.nu else None, ctypes.byref(cin),
+                                ctypes.byref(cout), _ptr(tq), _ptr(tqd),
+                                ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta))),
+          'braxg_rollout')
+  return out, (tq, tqd)

@@ -1,0 +1,134 @@
+/*
+ * braxg: C ABI of the GB300-native generalized-coordinates physics step.
+ *
+ * Drop-in boundary for brax's generalized pipeline:
+ *   brax/generalized/pipeline.py:32-61   init(sys, q, qd)      -> braxg_init
+ *   brax/generalized/pipeline.py:64-94   step(sys, state, act) -> braxg_step
+ *   brax/envs/base.py:128-137            pipeline_step (n_frames x step with
+ *                                        one action)            -> braxg_step
+ *   lax.scan over env steps (brax/training/agents/apg/train.py:188-198)
+ *                                                               -> braxg_rollout
+ * The System pytree (brax/base.py:415-540) is passed once, packed by
+ * brax_gb300/model_pack.py, to braxg_model_create.  The State pytree
+ * (brax/generalized/base.py:25-92) is a struct of per-field device pointers,
+ * env-major ([n_env, ...], float32, contiguous).
+ *
+ * All entry points are stream-ordered on the caller's cudaStream_t (passed as
+ * void*), never synchronise the host, and allocate no device memory after
+ * braxg_model_create.  Every call returns 0 on success or a braxg_status code;
+ * braxg_last_error() returns a message for the calling thread's last failure.
+ */
+#ifndef BRAXG_H_
+#define BRAXG_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct braxg_model braxg_model;
+
+enum braxg_status_code {
+  BRAXG_OK = 0,
+  BRAXG_ERR_INVALID = 1,     /* bad argument or descriptor (ValueError) */
+  BRAXG_ERR_CUDA = 2,        /* a CUDA call failed (RuntimeError) */
+  BRAXG_ERR_UNSUPPORTED = 3  /* model outside the supported envelope (NotImplementedError) */
+};
+
+/* How mass_mx_inv is produced after each step (brax/generalized/mass.py:86-106). */
+enum braxg_inverse_mode {
+  /* Newton-Schulz warm start from the previous inverse with the reference's
+   * iteration count and best-iterate acceptance (brax/math.py:278-305). */
+  BRAXG_INV_NEWTON_SCHULZ = 0,
+  /* Exact SPD inverse from a per-env Cholesky factorisation. */
+  BRAXG_INV_CHOLESKY = 1
+};
+
+/* Per-env status bits written to braxg_state.status. */
+enum braxg_env_flags {
+  BRAXG_ENV_NONFINITE = 1,   /* q or qd not finite after the call */
+  BRAXG_ENV_NOT_SPD = 2      /* a Cholesky pivot was <= 0 */
+};
+
+typedef struct {
+  int32_t nl, nq, nv, nu, ncon, nlim, m;
+} braxg_dims;
+
+/* Fields of brax.generalized.base.State.  q, qd and mass_mx_inv are the
+ * state carried between steps; every other pointer is an optional output
+ * (NULL skips it). */
+typedef struct {
+  float* q;             /* [n, nq] */
+  float* qd;            /* [n, nv] */
+  float* mass_mx_inv;   /* [n, nv, nv] */
+  float* x_pos;         /* [n, nl, 3] */
+  float* x_rot;         /* [n, nl, 4] */
+  float* xd_ang;        /* [n, nl, 3] */
+  float* xd_vel;        /* [n, nl, 3] */
+  float* qf_smooth;     /* [n, nv] */
+  float* qf_constraint; /* [n, nv] */
+  float* qdd;           /* [n, nv] */
+  float* root_com;      /* [n, nl, 3] */
+  float* cinr_pos;      /* [n, nl, 3]  cinr.transform.pos */
+  float* cinr_rot;      /* [n, nl, 4]  cinr.transform.rot */
+  float* cinr_i;        /* [n, nl, 9]  cinr.i */
+  float* cd;            /* [n, nl, 6]  ang(3), vel(3) */
+  float* cdof;          /* [n, nv, 6] */
+  float* cdofd;         /* [n, nv, 6] */
+  float* mass_mx;       /* [n, nv, nv] */
+  float* con_jac;       /* [n, m, nv] */
+  float* con_diag;      /* [n, m] */
+  float* con_aref;      /* [n, m] */
+  int32_t* status;      /* [n] braxg_env_flags */
+} braxg_state;
+
+typedef struct {
+  int32_t inverse_mode;     /* braxg_inverse_mode */
+  int32_t threads_per_env;  /* 0 = tuned, else 16 or 32 lanes per env */
+  int32_t envs_per_cta;     /* 0 = tuned */
+} braxg_options;
+
+/* Copies a packed System descriptor to `device`.  Replaces tracing the
+ * System pytree into the jitted step (brax/io/mjcf.py:317-489 builds it). */
+int braxg_model_create(const void* desc, size_t desc_bytes, int device, braxg_model** out);
+int braxg_model_destroy(braxg_model* model);
+int braxg_model_dims(const braxg_model* model, braxg_dims* out);
+
+/* brax/generalized/pipeline.py:32-61.  Reads q [n, nq], qd [n, nv]; writes the
+ * State fields of `out` (mass_mx_inv is the exact SPD inverse, the forces are
+ * zero). */
+int braxg_init(const braxg_model* model, void* stream, int n_env, const float* q,
+               const float* qd, braxg_state* out, const braxg_options* opt);
+
+/* n_frames x brax/generalized/pipeline.py:64-94 with one action per env
+ * (brax/envs/base.py:128-137).  act is [n, nu] (NULL = no actuation).  Reads
+ * in->q, in->qd, in->mass_mx_inv; `out` may alias `in`. */
+int braxg_step(const braxg_model* model, void* stream, int n_env, int n_frames,
+               const float* act, const braxg_state* in, braxg_state* out,
+               const braxg_options* opt);
+
+/* n_steps env steps of n_frames pipeline steps each, act_seq [n_steps, n, nu].
+ * traj_q [n_steps, n, nq] and traj_qd [n_steps, n, nv] (optional) receive the
+ * state after every env step; `out` receives the final state. */
+int braxg_rollout(const braxg_model* model, void* stream, int n_env, int n_steps,
+                  int n_frames, const float* act_seq, const braxg_state* in,
+                  braxg_state* out, float* traj_q, float* traj_qd,
+                  const braxg_options* opt);
+
+/* Launch shape the tuner picks for this model: lanes per env, envs per CTA,
+ * dynamic shared memory bytes per CTA. */
+int braxg_launch_shape(const braxg_model* model, const braxg_options* opt,
+                       int32_t* threads_per_env, int32_t* envs_per_cta,
+                       int32_t* smem_bytes);
+
+/* Number of kernel launches the last successful call on this thread issued. */
+int braxg_last_launch_count(void);
+
+const char* braxg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BRAXG_H_ */

@@ -848,6 +848,14 @@ class Oracle:
     s = self.jacobian(s)
     return s
 
+  def restore(self, q, qd, minv) -> State:
+    """The full State the reference holds for (q, qd, mass_mx_inv): every
+    other field is the position-level function of (q, qd) computed at the end
+    of the previous step (pipeline.py:86-92)."""
+    s = self.init(q, qd)
+    s = s.replace(mass_mx_inv=np.asarray(minv, self.dt_))
+    return s
+
   def step(self, s: State, act) -> State:
     act = None if act is None else np.asarray(act, self.dt_)
     tau = self.to_tau(act, s.q, s.qd)

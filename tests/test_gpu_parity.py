@@ -1,0 +1,168 @@
+"""GPU parity: the sm_103a kernels (through the braxg C ABI) against the
+oracle on the same seeded inputs.
+
+Tolerances (FP32 kernel vs FP32 / FP64 oracle):
+* position-level State fields after init: max-abs error <= 1e-5 x max(|ref|, 1);
+* single-step q / qd: relative error (max-abs diff / max(max |ref|, 1)) <=
+  1e-5 for at least 99 % of envs and <= 1e-3 for all envs.  The remaining
+  1 % allowance covers FP32 line-search accept/reject flips of the projected-
+  gradient solver (a step-size decision taken on two nearly equal FP32
+  values), which both FP32 implementations can take differently;
+* the active-contact mask is identical except for slots within 1e-6 of the
+  penetration threshold.
+"""
+
+import numpy as np
+import pytest
+
+from tests.parity_util import WORKLOADS, actions, load, rel_err, seeded_inputs
+
+torch = pytest.importorskip('torch')
+pytestmark = pytest.mark.gpu
+
+
+def _pipeline():
+  if not torch.cuda.is_available():
+    pytest.skip('no CUDA device')
+  from brax_gb300 import pipeline
+  return pipeline
+
+
+def _t(x):
+  return torch.as_tensor(np.asarray(x, np.float32), device='cuda')
+
+
+def _np(x):
+  return x.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize('name', WORKLOADS)
+def test_init_full_state(name):
+  P = _pipeline()
+  from oracle.pipeline import Oracle
+  sys = load(name)
+  n = 64
+  q, qd = seeded_inputs(sys, n)
+  q, qd = q.astype(np.float32).astype(np.float64), qd.astype(np.float32).astype(np.float64)
+  o = Oracle(sys, np.float64)
+  ref = o.init(q, qd)
+  got = P.init(sys, _t(q), _t(qd), full=True)
+  torch.cuda.synchronize()
+  assert (_np(got.status) == 0).all()
+  pairs = [('x_pos', ref.x_pos), ('x_rot', ref.x_rot), ('xd_ang', ref.xd_ang),
+           ('xd_vel', ref.xd_vel), ('root_com', ref.root_com), ('cinr_pos', ref.cinr_pos),
+           ('cinr_rot', ref.cinr_rot), ('cinr_i', ref.cinr_i),
+           ('cd', np.concatenate([ref.cd_ang, ref.cd_vel], -1)),
+           ('cdof', np.concatenate([ref.cdof_ang, ref.cdof_vel], -1)),
+           ('cdofd', np.concatenate([ref.cdofd_ang, ref.cdofd_vel], -1)),
+           ('mass_mx', ref.mass_mx), ('con_jac', ref.con_jac), ('con_diag', ref.con_diag),
+           ('con_aref', ref.con_aref)]
+  for field, r in pairs:
+    g = _np(getattr(got, field)).reshape(r.shape)
+    e = rel_err(g, r)
+    assert e.max() <= 1e-5, (field, e.max())
+  # mass_mx_inv: exact SPD inverse; compare relative to its own scale
+  e = rel_err(_np(got.mass_mx_inv), ref.mass_mx_inv)
+  assert e.max() <= 1e-5, e.max()
+
+
+def _states(sys, o, n, steps, seed):
+  """Oracle states reached after `steps` env steps from seeded resets."""
+  rng = np.random.default_rng(seed + 1)
+  q, qd = seeded_inputs(sys, n, seed)
+  s = o.init(q, qd)
+  for _ in range(steps):
+    s = o.step(s, actions(sys, n, rng))
+  return s, rng
+
+
+@pytest.mark.parametrize('name', WORKLOADS)
+@pytest.mark.parametrize('steps', [0, 7])
+def test_single_step_parity(name, steps):
+  P = _pipeline()
+  from oracle.pipeline import Oracle
+  sys = load(name)
+  n = 256
+  o32 = Oracle(sys, np.float32)
+  o64 = Oracle(sys, np.float64)
+  s64, rng = _states(sys, o64, n, steps, seed=3)
+  act = actions(sys, n, rng)
+  # the same input state for all three: q, qd and mass_mx_inv (FP32-rounded)
+  q, qd, minv = (s64.q.astype(np.float32), s64.qd.astype(np.float32),
+                 s64.mass_mx_inv.astype(np.float32))
+  r32 = o32.step(o32.restore(q, qd, minv), act.astype(np.float32))
+  r64 = o64.step(o64.restore(q.astype(np.float64), qd.astype(np.float64),
+                             minv.astype(np.float64)), act)
+  st = P.State(q=_t(q), qd=_t(qd), mass_mx_inv=_t(minv), x_pos=None, x_rot=None, xd_ang=None,
+               xd_vel=None, qf_smooth=None, qf_constraint=None, qdd=None, status=None)
+  got = P.step(sys, st, _t(act))
+  torch.cuda.synchronize()
+  assert (_np(got.status) == 0).all()
+  for field in ('q', 'qd'):
+    g = _np(getattr(got, field))
+    e32 = rel_err(g, getattr(r32, field))
+    e64 = rel_err(g, getattr(r64, field))
+    print(f'{name} steps={steps} {field}: vs fp32 p50 {np.median(e32):.2e} p99 '
+          f'{np.quantile(e32, 0.99):.2e} max {e32.max():.2e} | vs fp64 p50 '
+          f'{np.median(e64):.2e} max {e64.max():.2e}')
+    assert np.quantile(e32, 0.99) <= 1e-5, (field, np.sort(e32)[-5:])
+    assert e32.max() <= 1e-3, (field, e32.max())
+
+
+@pytest.mark.parametrize('name', ['quadruped', 'humanoid_like'])
+def test_contact_mask(name):
+  P = _pipeline()
+  from oracle.pipeline import Oracle
+  sys = load(name)
+  n = 256
+  o64 = Oracle(sys, np.float64)
+  s64, _ = _states(sys, o64, n, 10, seed=5)
+  got = P.init(sys, _t(s64.q), _t(s64.qd), full=True)
+  torch.cuda.synchronize()
+  ref = Oracle(sys, np.float64).init(s64.q.astype(np.float32).astype(np.float64),
+                                     s64.qd.astype(np.float32).astype(np.float64))
+  rows_ref = np.abs(ref.con_jac[:, :4 * sys.contacts.n]).reshape(n, sys.contacts.n, -1).max(-1) > 0
+  rows_got = np.abs(_np(got.con_jac)[:, :4 * sys.contacts.n]).reshape(n, sys.contacts.n, -1).max(-1) > 0
+  near = np.abs(ref.contact_dist) <= 1e-6
+  assert ((rows_ref == rows_got) | near).all()
+
+
+@pytest.mark.parametrize('name', WORKLOADS)
+def test_cholesky_mode_matches_newton_schulz(name):
+  P = _pipeline()
+  sys = load(name)
+  n = 256
+  q, qd = seeded_inputs(sys, n, seed=9)
+  rng = np.random.default_rng(10)
+  s_ns = P.init(sys, _t(q), _t(qd))
+  s_ch = s_ns
+  for _ in range(3):
+    a = _t(actions(sys, n, rng))
+    s_ns = P.step(sys, s_ns, a, n_frames=1, inverse_mode=P.NEWTON_SCHULZ)
+    s_ch = P.step(sys, s_ch, a, n_frames=1, inverse_mode=P.CHOLESKY)
+  torch.cuda.synchronize()
+  for field in ('q', 'qd'):
+    e = rel_err(_np(getattr(s_ch, field)), _np(getattr(s_ns, field)))
+    print(f'{name} cholesky vs NS {field}: p50 {np.median(e):.2e} max {e.max():.2e}')
+    assert np.quantile(e, 0.99) <= 1e-5
+
+
+@pytest.mark.parametrize('name', ['quadruped'])
+def test_multi_frame_step_matches_oracle_rollout(name):
+  P = _pipeline()
+  from oracle.pipeline import Oracle
+  sys = load(name)
+  n = 128
+  q, qd = seeded_inputs(sys, n, seed=11)
+  rng = np.random.default_rng(12)
+  o64 = Oracle(sys, np.float64)
+  ref = o64.init(q, qd)
+  got = P.init(sys, _t(q), _t(qd))
+  for _ in range(2):
+    a = actions(sys, n, rng)
+    ref = o64.env_step(ref, a, 5)
+    got = P.step(sys, got, _t(a), n_frames=5)
+  torch.cuda.synchronize()
+  e = rel_err(_np(got.q), ref.q)
+  print(f'2 env steps x 5 frames q: p50 {np.median(e):.2e} p90 {np.quantile(e, 0.9):.2e} max {e.max():.2e}')
+  assert np.median(e) <= 1e-4
