@@ -265,21 +265,32 @@ def run_braxg(args):
   torch.cuda.synchronize()
   if world > 1:
     dist.barrier()
+  e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+  api_s = 0.0
   t0 = time.perf_counter()
   for k in range(args.steps):
+    e_ev[k][0].record(stream)
     d_act.copy_(h_act[k], non_blocking=True)
+    ta = time.perf_counter()
     pipeline.step(sys_, st, d_act, n_frames=N_FRAMES, out=st2, **kw)
+    api_s += time.perf_counter() - ta
     st, st2 = st2, st
     obs[:, :sys_.q_size()].copy_(st.q)
     obs[:, sys_.q_size():].copy_(st.qd)
     h_obs.copy_(obs, non_blocking=True)
-    torch.cuda.current_stream(dev).synchronize()
+    e_ev[k][1].record(stream)
+    stream.synchronize()
   t_e2e = time.perf_counter() - t0
   if world > 1:
     t = torch.tensor([t_e2e], device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     t_e2e = float(t.item())
+  gpu_e2e = sum(a.elapsed_time(b) for a, b in e_ev) / 1e3
   e2e = {'value': args.steps * n * world / t_e2e, 'unit': 'env-steps/s',
+         'ms_per_step_wall': round(1e3 * t_e2e / args.steps, 4),
+         'ms_per_step_gpu': round(1e3 * gpu_e2e / args.steps, 4),
+         'ms_per_step_api_call': round(1e3 * api_s / args.steps, 4),
          'h2d_bytes_per_step': n * sys_.act_size() * 4,
          'd2h_bytes_per_step': n * (sys_.q_size() + sys_.qd_size()) * 4}
 

@@ -37,7 +37,13 @@ class Dims(ctypes.Structure):
 
 class Options(ctypes.Structure):
   _fields_ = [('inverse_mode', ctypes.c_int32), ('threads_per_env', ctypes.c_int32),
-              ('envs_per_cta', ctypes.c_int32)]
+              ('envs_per_cta', ctypes.c_int32), ('reserved', ctypes.c_int32),
+              ('stage_cycles', ctypes.c_void_p)]
+
+
+PROFILE_SLOTS = ('fk', 'com', 'crba', 'inverse', 'jacobian', 'smooth', 'constraint',
+                 'integrate', 'io', 'matvecs', 'rows', 'ns_resets', 'substeps')
+N_PROFILE_SLOTS = 16
 
 
 _lib = None

@@ -85,6 +85,7 @@ int launch(const braxg_model* m, const braxg_options* opt, braxg::StepArgs& a, c
   if (rc) return rc;
   if (a.n_env == 0) return BRAXG_OK;
   a.envs_per_cta = s.epc;
+  a.prof = opt ? opt->stage_cycles : nullptr;
   int grid = (a.n_env + s.epc - 1) / s.epc;
   int cur = 0;
   cudaGetDevice(&cur);

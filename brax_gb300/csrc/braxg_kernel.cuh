@@ -24,18 +24,45 @@ __device__ void store_mat(const Team<T>& tm, float* dst, const float* src, int n
   }
 }
 
+// Per-stage cycle accumulation (only when a profile buffer is passed).
+struct Prof {
+  bool on;
+  long long t;
+  unsigned long long acc[BRAXG_PROF_SLOTS];
+  __device__ explicit Prof(bool on_) : on(on_), t(0) {
+#pragma unroll
+    for (int i = 0; i < BRAXG_PROF_SLOTS; ++i) acc[i] = 0ull;
+    if (on) t = clock64();
+  }
+  __device__ __forceinline__ void mark(int slot) {
+    if (!on) return;
+    long long now = clock64();
+    acc[slot] += (unsigned long long)(now - t);
+    t = now;
+  }
+  __device__ __forceinline__ void count(int slot, unsigned long long v) {
+    if (on) acc[slot] += v;
+  }
+};
+
 template <int T, int NVB>
-__device__ bool position_stage(const Model& md, const Team<T>& tm, const Ws& w, bool exact, int iters) {
+__device__ bool position_stage(const Model& md, const Team<T>& tm, const Ws& w, bool exact, int iters, Prof& pf) {
   stage_fk<T>(md, tm, w);
+  pf.mark(BRAXG_PROF_FK);
   stage_com<T>(md, tm, w);
+  pf.mark(BRAXG_PROF_COM);
   stage_crba<T>(md, tm, w);
+  pf.mark(BRAXG_PROF_CRBA);
   bool ok = stage_inverse<T, NVB>(md, tm, w, exact, iters);
+  pf.mark(BRAXG_PROF_INVERSE);
   stage_jacobian<T>(md, tm, w);
+  pf.mark(BRAXG_PROF_JACOBIAN);
+  pf.count(BRAXG_PROF_ROWS, (unsigned long long)reinterpret_cast<const int*>(w.at(w.L.misc))[0]);
   return ok;
 }
 
 template <int T, int NVB>
-__global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   extern __shared__ __align__(16) int smem[];
   for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
   __syncthreads();
@@ -49,6 +76,7 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
   w.b = reinterpret_cast<float*>(smem + al4(a.model_words)) + (size_t)team * w.L.total;
   const Layout& L = w.L;
   const int nq = md.nq, nv = md.nv, nl = md.nl, nu = md.nu, ld = L.ldm;
+  Prof pf(a.prof != nullptr);
 
   load_vec<T>(tm, w.at(L.q), a.q_in + env * nq, nq);
   load_vec<T>(tm, w.at(L.qd), a.qd_in + env * nv, nv);
@@ -60,8 +88,10 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
       w.at(L.Minv)[i * ld + j] = src[idx];
     }
   }
+  if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] = 0;
   tm.sync();
-  bool ok = position_stage<T, NVB>(md, tm, w, exact, 0);
+  pf.mark(BRAXG_PROF_IO);
+  bool ok = position_stage<T, NVB>(md, tm, w, exact, 0, pf);
   if (a.init) {
     for (int d = tm.lane; d < nv; d += T) {
       w.at(L.qfs)[d] = 0.f;
@@ -76,9 +106,13 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
       tm.sync();
       for (int f = 0; f < a.n_frames; ++f) {
         stage_smooth<T>(md, tm, w, has_act);
-        stage_constraint<T>(md, tm, w);
+        pf.mark(BRAXG_PROF_SMOOTH);
+        pf.count(BRAXG_PROF_MATVECS, (unsigned long long)stage_constraint<T>(md, tm, w));
+        pf.mark(BRAXG_PROF_CONSTRAINT);
         ok = stage_integrate<T>(md, tm, w) && ok;
-        ok = position_stage<T, NVB>(md, tm, w, a.exact_inverse || md.ns_iters == 0, md.ns_iters) && ok;
+        pf.mark(BRAXG_PROF_INTEGRATE);
+        ok = position_stage<T, NVB>(md, tm, w, a.exact_inverse || md.ns_iters == 0, md.ns_iters, pf) && ok;
+        pf.count(BRAXG_PROF_SUBSTEPS, 1ull);
       }
       if (a.traj_q != nullptr) store_vec<T>(tm, a.traj_q + ((long long)s * a.n_env + env) * nq, w.at(L.q), nq);
       if (a.traj_qd != nullptr)
@@ -141,6 +175,12 @@ __global__ void __launch_bounds__(256) step_kernel(const StepArgs a) {
     for (int i = tm.lane; i < nv; i += T) fin = fin && isfinite(w.at(L.qd)[i]);
     fin = tm.all(fin);
     if (tm.lane == 0) o.status[env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
+  }
+  pf.mark(BRAXG_PROF_IO);
+  pf.count(BRAXG_PROF_NS_RESETS, (unsigned long long)reinterpret_cast<const int*>(w.at(L.misc))[1]);
+  if (a.prof != nullptr && tm.lane == 0) {
+    for (int i = 0; i < BRAXG_PROF_SLOTS; ++i)
+      if (pf.acc[i]) atomicAdd(a.prof + i, pf.acc[i]);
   }
 }
 

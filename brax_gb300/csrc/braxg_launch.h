@@ -24,6 +24,7 @@ struct StepArgs {
   braxg_state out;
   float* traj_q;
   float* traj_qd;
+  unsigned long long* prof;
 };
 
 // Launches step_kernel<T, NVB> (defined in braxg_kernel.cuh, instantiated in

@@ -473,22 +473,69 @@ __device__ void stage_crba(const Model& md, const Team<T>& tm, const Ws& w) {
 // dense helpers on nv x nv matrices (leading dimension ld)
 // ---------------------------------------------------------------------------
 // op 0: C = A B;  op 1: C = I - A B;  op 2: C = A (I + B)
+// Register-tiled: the lanes form an RB x CB grid, each lane owns a TR x TC
+// block of C (TR = NVB / RB, TC = NVB / CB).  Shapes whose tile would hold
+// more than 32 accumulators use one column per lane instead.
+template <int T, int NVB>
+struct MMTile {
+  static constexpr int RB = (T == 32) ? 8 : 4;
+  static constexpr int CB = T / RB;
+  static constexpr int TR = NVB / RB;
+  static constexpr int TC = NVB / CB;
+  static constexpr bool tiled = TR * TC <= 32;
+};
+
 template <int T, int NVB>
 __device__ void matmul(const Team<T>& tm, int n, int ld, const float* A, const float* B, float* C, int op) {
-  for (int j = tm.lane; j < n; j += T) {
-    float acc[NVB];
+  using G = MMTile<T, NVB>;
+  if constexpr (G::tiled) {
+    const int rb = tm.lane / G::CB, cb = tm.lane - (tm.lane / G::CB) * G::CB;
+    const int i0 = rb * G::TR, j0 = cb * G::TC;
+    if (i0 < n && j0 < n) {
+      float acc[G::TR][G::TC];
 #pragma unroll
-    for (int i = 0; i < NVB; ++i) acc[i] = 0.f;
-    for (int k = 0; k < n; ++k) {
-      float b = B[k * ld + j];
-      if (op == 2 && k == j) b = b + 1.f;
+      for (int r = 0; r < G::TR; ++r)
+#pragma unroll
+        for (int c = 0; c < G::TC; ++c) acc[r][c] = 0.f;
+      for (int k = 0; k < n; ++k) {
+        float a[G::TR], b[G::TC];
+#pragma unroll
+        for (int r = 0; r < G::TR; ++r) a[r] = (i0 + r < n) ? A[(i0 + r) * ld + k] : 0.f;
+#pragma unroll
+        for (int c = 0; c < G::TC; ++c) {
+          float v = (j0 + c < n) ? B[k * ld + j0 + c] : 0.f;
+          if (op == 2 && k == j0 + c) v = v + 1.f;
+          b[c] = v;
+        }
+#pragma unroll
+        for (int r = 0; r < G::TR; ++r)
+#pragma unroll
+          for (int c = 0; c < G::TC; ++c) acc[r][c] = fmaf(a[r], b[c], acc[r][c]);
+      }
+#pragma unroll
+      for (int r = 0; r < G::TR; ++r)
+#pragma unroll
+        for (int c = 0; c < G::TC; ++c) {
+          int i = i0 + r, j = j0 + c;
+          if (i < n && j < n) C[i * ld + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[r][c]) : acc[r][c];
+        }
+    }
+  } else {
+    for (int j = tm.lane; j < n; j += T) {
+      float acc[NVB];
+#pragma unroll
+      for (int i = 0; i < NVB; ++i) acc[i] = 0.f;
+      for (int k = 0; k < n; ++k) {
+        float b = B[k * ld + j];
+        if (op == 2 && k == j) b = b + 1.f;
+#pragma unroll
+        for (int i = 0; i < NVB; ++i)
+          if (i < n) acc[i] = fmaf(A[i * ld + k], b, acc[i]);
+      }
 #pragma unroll
       for (int i = 0; i < NVB; ++i)
-        if (i < n) acc[i] = fmaf(A[i * ld + k], b, acc[i]);
+        if (i < n) C[i * ld + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[i]) : acc[i];
     }
-#pragma unroll
-    for (int i = 0; i < NVB; ++i)
-      if (i < n) C[i * ld + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[i]) : acc[i];
   }
   tm.sync();
 }
@@ -531,40 +578,64 @@ __device__ bool cholesky(const Team<T>& tm, int n, int ld, float* A) {
   return ok;
 }
 
-// Minv = L^-T L^-1 from the Cholesky factor L (lower, in Lm); Wt is scratch.
-template <int T, int NVB>
-__device__ void chol_inverse(const Team<T>& tm, int n, int ld, const float* Lm, float* Wt, float* Minv) {
-  // Wt = L^-1 (lower), one column per lane by forward substitution
-  for (int j = tm.lane; j < n; j += T) {
-    for (int i = 0; i < n; ++i) {
-      float v;
-      if (i < j) {
-        v = 0.f;
-      } else {
-        float s = (i == j) ? 1.f : 0.f;
-        for (int k = j; k < i; ++k) s = s - Lm[i * ld + k] * Wt[k * ld + j];
-        v = s / Lm[i * ld + i];
+// Exact SPD inverse by Cholesky: M = L L^T (right-looking, lanes over the
+// trailing entries), X = L^-1 (right-looking forward elimination, lanes over
+// the updated entries), Minv = X^T X (lanes over the lower triangle, mirrored).
+// Lw and X are n x ld scratch matrices.  Returns false (team-uniform) when a
+// pivot is not positive.
+template <int T>
+__device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc, float* Lw, float* X, float* Minv) {
+  for (int idx = tm.lane; idx < n * n; idx += T) {
+    int i = idx / n, j = idx - i * n;
+    Lw[i * ld + j] = Msrc[i * ld + j];
+    X[i * ld + j] = (i == j) ? 1.f : 0.f;
+  }
+  tm.sync();
+  bool ok = true;
+  for (int k = 0; k < n; ++k) {
+    float piv = Lw[k * ld + k];
+    ok = ok && (piv > 0.f);
+    float d = sqrtf(fmaxf(piv, 1e-30f));
+    for (int i = k + 1 + tm.lane; i < n; i += T) Lw[i * ld + k] = Lw[i * ld + k] / d;
+    tm.sync();
+    if (tm.lane == 0) Lw[k * ld + k] = d;
+    const int w = n - k - 1;
+    for (int p = tm.lane; p < w * w; p += T) {
+      int ii = p / w, jj = p - ii * w;
+      if (jj <= ii) {
+        int i = k + 1 + ii, j = k + 1 + jj;
+        Lw[i * ld + j] = Lw[i * ld + j] - Lw[i * ld + k] * Lw[j * ld + k];
       }
-      Wt[i * ld + j] = v;
     }
+    tm.sync();
+  }
+  for (int k = 0; k < n; ++k) {
+    const float lkk = Lw[k * ld + k];
+    for (int j = tm.lane; j <= k; j += T) X[k * ld + j] = X[k * ld + j] / lkk;
+    tm.sync();
+    const int rows = n - k - 1, cols = k + 1;
+    for (int p = tm.lane; p < rows * cols; p += T) {
+      int ii = p / cols, j = p - ii * cols, i = k + 1 + ii;
+      X[i * ld + j] = X[i * ld + j] - Lw[i * ld + k] * X[k * ld + j];
+    }
+    tm.sync();
+  }
+  for (int idx = tm.lane; idx < n * n; idx += T) {
+    int i = idx / n, j = idx - i * n;
+    if (j > i) continue;
+    float s0 = 0.f, s1 = 0.f;
+    int m = i;
+    for (; m + 1 < n; m += 2) {
+      s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
+      s1 = fmaf(X[(m + 1) * ld + i], X[(m + 1) * ld + j], s1);
+    }
+    if (m < n) s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
+    float v = s0 + s1;
+    Minv[i * ld + j] = v;
+    Minv[j * ld + i] = v;
   }
   tm.sync();
-  // Minv[i][j] = sum_k Wt[k][i] Wt[k][j]
-  for (int j = tm.lane; j < n; j += T) {
-    float acc[NVB];
-#pragma unroll
-    for (int i = 0; i < NVB; ++i) acc[i] = 0.f;
-    for (int k = 0; k < n; ++k) {
-      float b = Wt[k * ld + j];
-#pragma unroll
-      for (int i = 0; i < NVB; ++i)
-        if (i < n) acc[i] = fmaf(Wt[k * ld + i], b, acc[i]);
-    }
-#pragma unroll
-    for (int i = 0; i < NVB; ++i)
-      if (i < n) Minv[i * ld + j] = acc[i];
-  }
-  tm.sync();
+  return ok;
 }
 
 // ---------------------------------------------------------------------------
@@ -582,14 +653,7 @@ __device__ bool stage_inverse(const Model& md, const Team<T>& tm, const Ws& w, b
   float* S2 = S1 + n * ld;
   if (n == 0) return true;
   if (exact) {
-    for (int idx = tm.lane; idx < n * n; idx += T) {
-      int i = idx / n, j = idx - i * n;
-      S1[i * ld + j] = M[i * ld + j];
-    }
-    tm.sync();
-    bool ok = cholesky<T>(tm, n, ld, S1);
-    chol_inverse<T, NVB>(tm, n, ld, S1, S2, P);
-    return ok;
+    return spd_inverse<T>(tm, n, ld, M, S1, S2, P);
   }
   if (num_iter <= 0) return true;
   float* cur = P;
@@ -598,6 +662,7 @@ __device__ bool stage_inverse(const Model& md, const Team<T>& tm, const Ws& w, b
   matmul<T, NVB>(tm, n, ld, M, cur, R, 1);  // r0 = I - A A_inv
   float nr0 = safe_norm_mat<T>(tm, n, ld, R);
   if (nr0 > 1.f) {  // reset to 0.5 A^T / tr(A A^T) (r0 is kept, as the reference does)
+    if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] += 1;
     float s = 0.f;
     for (int idx = tm.lane; idx < n * n; idx += T) {
       int i = idx / n, j = idx - i * n;
@@ -1031,21 +1096,38 @@ __device__ void matvec_A(const Model& md, const Team<T>& tm, const Ws& w, int nr
   const float* Minv = w.at(L.Minv);
   const float* rdiag = w.at(L.rdiag);
   for (int d = tm.lane; d < nv; d += T) {  // t1 = J^T v
-    float s = 0.f;
-    for (int r = 0; r < nrow; ++r) s = fmaf(J[r * ldj + d], v[r], s);
-    t1[d] = s;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+    int r = 0;
+    for (; r + 3 < nrow; r += 4) {
+      s0 = fmaf(J[r * ldj + d], v[r], s0);
+      s1 = fmaf(J[(r + 1) * ldj + d], v[r + 1], s1);
+      s2 = fmaf(J[(r + 2) * ldj + d], v[r + 2], s2);
+      s3 = fmaf(J[(r + 3) * ldj + d], v[r + 3], s3);
+    }
+    for (; r < nrow; ++r) s0 = fmaf(J[r * ldj + d], v[r], s0);
+    t1[d] = (s0 + s1) + (s2 + s3);
   }
   tm.sync();
   for (int d = tm.lane; d < nv; d += T) {  // t2 = Minv t1
-    float s = 0.f;
-    for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * ld + k], t1[k], s);
-    t2[d] = s;
+    float s0 = 0.f, s1 = 0.f;
+    int k = 0;
+    for (; k + 1 < nv; k += 2) {
+      s0 = fmaf(Minv[d * ld + k], t1[k], s0);
+      s1 = fmaf(Minv[d * ld + k + 1], t1[k + 1], s1);
+    }
+    if (k < nv) s0 = fmaf(Minv[d * ld + k], t1[k], s0);
+    t2[d] = s0 + s1;
   }
   tm.sync();
   for (int r = tm.lane; r < nrow; r += T) {  // out = J t2 + diag v
-    float s = 0.f;
-    for (int k = 0; k < nv; ++k) s = fmaf(J[r * ldj + k], t2[k], s);
-    out[r] = s + rdiag[r] * v[r];
+    float s0 = 0.f, s1 = 0.f;
+    int k = 0;
+    for (; k + 1 < nv; k += 2) {
+      s0 = fmaf(J[r * ldj + k], t2[k], s0);
+      s1 = fmaf(J[r * ldj + k + 1], t2[k + 1], s1);
+    }
+    if (k < nv) s0 = fmaf(J[r * ldj + k], t2[k], s0);
+    out[r] = (s0 + s1) + rdiag[r] * v[r];
   }
   tm.sync();
 }

@@ -150,8 +150,20 @@ def _as_batch(x: torch.Tensor, width: int, name: str, dev) -> torch.Tensor:
   return x.to(torch.float32).contiguous()
 
 
-def _opts(inverse_mode, threads_per_env, envs_per_cta):
-  return N.Options(int(inverse_mode), int(threads_per_env), int(envs_per_cta))
+def _opts(inverse_mode, threads_per_env, envs_per_cta, profile=None):
+  return N.Options(int(inverse_mode), int(threads_per_env), int(envs_per_cta), 0,
+                   None if profile is None else profile.data_ptr())
+
+
+def profile_buffer(device=None) -> torch.Tensor:
+  """A zeroed per-stage profile buffer to pass as ``profile=``."""
+  return torch.zeros(N.N_PROFILE_SLOTS, dtype=torch.int64,
+                     device=device if device is not None else 'cuda')
+
+
+def profile_report(buf: torch.Tensor) -> dict:
+  v = buf.cpu().tolist()
+  return {k: v[i] for i, k in enumerate(N.PROFILE_SLOTS)}
 
 
 def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
@@ -176,7 +188,8 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
 
 def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
          full: bool = False, inverse_mode: int = NEWTON_SCHULZ, out: Optional[State] = None,
-         threads_per_env: int = 0, envs_per_cta: int = 0) -> State:
+         threads_per_env: int = 0, envs_per_cta: int = 0,
+         profile: Optional[torch.Tensor] = None) -> State:
   """brax/generalized/pipeline.py:64-94; n_frames > 1 repeats it with the same
   action (PipelineEnv.pipeline_step, brax/envs/base.py:128-137)."""
   if debug:
@@ -196,7 +209,8 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
   stream = torch.cuda.current_stream(m.device).cuda_stream
   N.check(N.lib().braxg_step(m.handle, ctypes.c_void_p(stream), n, int(n_frames), act_p,
                              ctypes.byref(cin), ctypes.byref(cout),
-                             ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta))),
+                             ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta,
+                                                profile))),
           'braxg_step')
   return out
 

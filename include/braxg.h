@@ -84,10 +84,23 @@ typedef struct {
   int32_t* status;      /* [n] braxg_env_flags */
 } braxg_state;
 
+/* Per-stage profile slots of braxg_options.stage_cycles (sums over envs of
+ * clock64 deltas taken by lane 0 of each env's team, plus event counters). */
+enum braxg_profile_slot {
+  BRAXG_PROF_FK = 0, BRAXG_PROF_COM, BRAXG_PROF_CRBA, BRAXG_PROF_INVERSE,
+  BRAXG_PROF_JACOBIAN, BRAXG_PROF_SMOOTH, BRAXG_PROF_CONSTRAINT, BRAXG_PROF_INTEGRATE,
+  BRAXG_PROF_IO, BRAXG_PROF_MATVECS, BRAXG_PROF_ROWS, BRAXG_PROF_NS_RESETS,
+  BRAXG_PROF_SUBSTEPS, BRAXG_PROF_SLOTS = 16
+};
+
 typedef struct {
   int32_t inverse_mode;     /* braxg_inverse_mode */
   int32_t threads_per_env;  /* 0 = tuned, else 16 or 32 lanes per env */
   int32_t envs_per_cta;     /* 0 = tuned */
+  int32_t reserved;
+  /* Optional device buffer of BRAXG_PROF_SLOTS uint64 counters the kernel
+   * adds its per-stage cycle counts into (NULL = no profiling). */
+  unsigned long long* stage_cycles;
 } braxg_options;
 
 /* Copies a packed System descriptor to `device`.  Replaces tracing the

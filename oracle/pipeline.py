@@ -216,8 +216,12 @@ class State:
 class Oracle:
   """Holds a System cast to ``dtype`` plus its static schedule."""
 
-  def __init__(self, sys: S.System, dtype=np.float64):
+  def __init__(self, sys: S.System, dtype=np.float64, exact_inverse: bool = False):
+    """exact_inverse=True replaces the Newton-Schulz update of mass_mx_inv by
+    the exact SPD inverse (the kernel's Cholesky mode); the reference path is
+    exact_inverse=False."""
     self.sys = sys
+    self.exact_inverse = exact_inverse
     self.dt_ = np.dtype(dtype)
     self.st = static(sys)
     f = lambda a: np.asarray(a, dtype=self.dt_)
@@ -466,7 +470,7 @@ class Oracle:
     mx = self.mass_matrix(s)
     if self.st.nv == 0:
       return s.replace(mass_mx=mx, mass_mx_inv=mx)
-    if num_iter > 0:
+    if num_iter > 0 and not self.exact_inverse:
       minv = self.inv_approximate(mx, s.mass_mx_inv, num_iter)
     else:
       minv = self.spd_inverse(mx)

@@ -241,3 +241,31 @@ def test_fp32_vs_fp64_single_step():
     for a, b in ((s32.q, s64.q), (s32.qd, s64.qd)):
       err = np.abs(a - b).max(-1) / np.maximum(np.abs(b).max(-1), 1.0)
       assert np.median(err) < 1e-5, (name, err)
+
+
+def test_humanoid_newton_schulz_loses_the_inverse():
+  """On the humanoid-like workload (gear-100 motors on light limbs, dt 3 ms)
+  one step moves M far relative to its smallest eigenvalues (~0.009), the
+  reference's Newton-Schulz update (K = 20, math.py:278-305) starts from a
+  residual > 1, resets, and its acceptance rule (err starts at 1) then never
+  accepts an iterate: mass_mx_inv stops being an inverse.  The exact-inverse
+  (Cholesky) mode does not reproduce this, by design; the quadruped stays in
+  the converged regime, where both modes agree."""
+  from tests.parity_util import actions, seeded_inputs
+  sys = mjcf.load_asset('humanoid_like')
+  o = Oracle(sys, np.float64)
+  q, qd = seeded_inputs(sys, 16, 3)
+  s = o.init(q, qd)
+  rng = np.random.default_rng(4)
+  for _ in range(3):
+    s = o.step(s, actions(sys, 16, rng))
+  resid = np.linalg.norm(np.eye(sys.qd_size()) - s.mass_mx @ s.mass_mx_inv, axis=(1, 2))
+  assert (resid > 1).mean() > 0.5
+  sys_q = mjcf.load_asset('quadruped')
+  oq = Oracle(sys_q, np.float64)
+  q, qd = seeded_inputs(sys_q, 16, 3)
+  s = oq.init(q, qd)
+  for _ in range(10):
+    s = oq.step(s, actions(sys_q, 16, rng))
+  resid = np.linalg.norm(np.eye(sys_q.qd_size()) - s.mass_mx @ s.mass_mx_inv, axis=(1, 2))
+  assert resid.max() < 1e-6
