@@ -57,7 +57,7 @@ int choose_shape(const braxg_model* m, const braxg_options* opt, Shape* s) {
   if (T != 16 && T != 32) return fail(BRAXG_ERR_INVALID, "threads_per_env must be 0, 16 or 32 (got %d)", T);
   if (T == 16 && s->NVB == 64) T = 32;
   s->T = T;
-  int model_bytes = braxg::al4(m->words) * 4;
+  int model_bytes = (braxg::al4(m->words) + braxg::kLayoutWords) * 4;
   int env_bytes = m->L.total * 4;
   int max_epc = 256 / T;
   int fit = (kMaxSmem - model_bytes) / env_bytes;

@@ -24,40 +24,47 @@ __device__ void store_mat(const Team<T>& tm, float* dst, const float* src, int n
   }
 }
 
-// Per-stage cycle accumulation (only when a profile buffer is passed).
+// Per-stage cycle accumulation (only when a profile buffer is passed): lane 0
+// of each team adds the clock64 delta of every stage straight into the buffer.
 struct Prof {
-  bool on;
+  unsigned long long* buf;  // null unless profiling; set only on lane 0 of each team
   long long t;
-  unsigned long long acc[BRAXG_PROF_SLOTS];
-  __device__ explicit Prof(bool on_) : on(on_), t(0) {
-#pragma unroll
-    for (int i = 0; i < BRAXG_PROF_SLOTS; ++i) acc[i] = 0ull;
-    if (on) t = clock64();
+  __device__ Prof(unsigned long long* b, bool lead) : buf(lead ? b : nullptr), t(0) {
+    if (buf != nullptr) t = clock64();
   }
   __device__ __forceinline__ void mark(int slot) {
-    if (!on) return;
+    if (buf == nullptr) return;
     long long now = clock64();
-    acc[slot] += (unsigned long long)(now - t);
+    atomicAdd(buf + slot, (unsigned long long)(now - t));
     t = now;
   }
   __device__ __forceinline__ void count(int slot, unsigned long long v) {
-    if (on) acc[slot] += v;
+    if (buf != nullptr) atomicAdd(buf + slot, v);
   }
 };
 
+// All teams of a CTA walk the stages in lockstep (a CTA barrier after every
+// stage), so the warps of an SM execute the same stage's code at the same time
+// and the instruction working set is one or two stages, not the whole kernel.
 template <int T, int NVB>
-__device__ bool position_stage(const Model& md, const Team<T>& tm, const Ws& w, bool exact, int iters, Prof& pf) {
-  stage_fk<T>(md, tm, w);
+__device__ __forceinline__ bool position_stage(const int* mw, Ws w, bool active, bool exact, int iters, Prof& pf) {
+  bool ok = true;
+  if (active) stage_fk<T>(mw, w);
+  __syncthreads();
   pf.mark(BRAXG_PROF_FK);
-  stage_com<T>(md, tm, w);
+  if (active) stage_com<T>(mw, w);
+  __syncthreads();
   pf.mark(BRAXG_PROF_COM);
-  stage_crba<T>(md, tm, w);
+  if (active) stage_crba<T>(mw, w);
+  __syncthreads();
   pf.mark(BRAXG_PROF_CRBA);
-  bool ok = stage_inverse<T, NVB>(md, tm, w, exact, iters);
+  if (active) ok = stage_inverse<T, NVB>(mw, w, exact, iters);
+  __syncthreads();
   pf.mark(BRAXG_PROF_INVERSE);
-  stage_jacobian<T>(md, tm, w);
+  if (active) stage_jacobian<T>(mw, w);
+  __syncthreads();
   pf.mark(BRAXG_PROF_JACOBIAN);
-  pf.count(BRAXG_PROF_ROWS, (unsigned long long)reinterpret_cast<const int*>(w.at(w.L.misc))[0]);
+  if (active) pf.count(BRAXG_PROF_ROWS, (unsigned long long)reinterpret_cast<const int*>(w.at(w.L->misc))[0]);
   return ok;
 }
 
@@ -65,23 +72,33 @@ template <int T, int NVB>
 __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   extern __shared__ __align__(16) int smem[];
   for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
+  Layout* shared_layout = reinterpret_cast<Layout*>(smem + al4(a.model_words));
+  if (threadIdx.x == 0) {
+    const int* w0 = a.model;
+    *shared_layout = make_layout(w0[BXM_H_NL], w0[BXM_H_NQ], w0[BXM_H_NV], w0[BXM_H_NU], w0[BXM_H_NCON],
+                                 w0[BXM_H_NLIM]);
+  }
   __syncthreads();
   const Model md(smem);
   const Team<T> tm;
   const int team = threadIdx.x / T;
-  const long long env = (long long)blockIdx.x * a.envs_per_cta + team;
-  if (team >= a.envs_per_cta || env >= a.n_env) return;
+  long long env = (long long)blockIdx.x * a.envs_per_cta + team;
+  // teams past the batch keep hitting the CTA barriers but do no work
+  const bool active = team < a.envs_per_cta && env < a.n_env;
+  if (!active) env = 0;
   Ws w;
-  w.L = make_layout(md.nl, md.nq, md.nv, md.nu, md.ncon, md.nlim);
-  w.b = reinterpret_cast<float*>(smem + al4(a.model_words)) + (size_t)team * w.L.total;
-  const Layout& L = w.L;
+  w.L = shared_layout;
+  w.b = reinterpret_cast<float*>(smem + al4(a.model_words) + kLayoutWords) + (size_t)team * w.L->total;
+  const Layout& L = *w.L;
   const int nq = md.nq, nv = md.nv, nl = md.nl, nu = md.nu, ld = L.ldm;
-  Prof pf(a.prof != nullptr);
+  Prof pf(a.prof, active && tm.lane == 0);
 
-  load_vec<T>(tm, w.at(L.q), a.q_in + env * nq, nq);
-  load_vec<T>(tm, w.at(L.qd), a.qd_in + env * nv, nv);
   const bool exact = a.exact_inverse || a.init || md.ns_iters == 0;
-  if (!exact) {
+  if (active) {
+    load_vec<T>(tm, w.at(L.q), a.q_in + env * nq, nq);
+    load_vec<T>(tm, w.at(L.qd), a.qd_in + env * nv, nv);
+  }
+  if (active && !exact) {
     const float* src = a.minv_in + env * nv * nv;
     for (int idx = tm.lane; idx < nv * nv; idx += T) {
       int i = idx / nv, j = idx - i * nv;
@@ -91,9 +108,9 @@ __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] = 0;
   tm.sync();
   pf.mark(BRAXG_PROF_IO);
-  bool ok = position_stage<T, NVB>(md, tm, w, exact, 0, pf);
+  bool ok = position_stage<T, NVB>(smem, w, active, exact, 0, pf);
   if (a.init) {
-    for (int d = tm.lane; d < nv; d += T) {
+    for (int d = tm.lane; active && d < nv; d += T) {
       w.at(L.qfs)[d] = 0.f;
       w.at(L.qfc)[d] = 0.f;
       w.at(L.qdd)[d] = 0.f;
@@ -102,23 +119,29 @@ __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   } else {
     for (int s = 0; s < a.n_steps; ++s) {
       const bool has_act = a.act != nullptr && nu > 0;
-      if (has_act) load_vec<T>(tm, w.at(L.act), a.act + s * a.act_step_stride + env * nu, nu);
+      if (has_act && active) load_vec<T>(tm, w.at(L.act), a.act + s * a.act_step_stride + env * nu, nu);
       tm.sync();
       for (int f = 0; f < a.n_frames; ++f) {
-        stage_smooth<T>(md, tm, w, has_act);
+        if (active) stage_smooth<T>(smem, w, has_act);
+        __syncthreads();
         pf.mark(BRAXG_PROF_SMOOTH);
-        pf.count(BRAXG_PROF_MATVECS, (unsigned long long)stage_constraint<T>(md, tm, w));
+        int mvs = 0;
+        if (active) mvs = stage_constraint<T>(smem, w);
+        __syncthreads();
+        pf.count(BRAXG_PROF_MATVECS, (unsigned long long)mvs);
         pf.mark(BRAXG_PROF_CONSTRAINT);
-        ok = stage_integrate<T>(md, tm, w) && ok;
+        if (active) ok = stage_integrate<T>(smem, w) && ok;
+        __syncthreads();
         pf.mark(BRAXG_PROF_INTEGRATE);
-        ok = position_stage<T, NVB>(md, tm, w, a.exact_inverse || md.ns_iters == 0, md.ns_iters, pf) && ok;
+        ok = position_stage<T, NVB>(smem, w, active, a.exact_inverse || md.ns_iters == 0, md.ns_iters, pf) && ok;
         pf.count(BRAXG_PROF_SUBSTEPS, 1ull);
       }
-      if (a.traj_q != nullptr) store_vec<T>(tm, a.traj_q + ((long long)s * a.n_env + env) * nq, w.at(L.q), nq);
-      if (a.traj_qd != nullptr)
+      if (active && a.traj_q != nullptr) store_vec<T>(tm, a.traj_q + ((long long)s * a.n_env + env) * nq, w.at(L.q), nq);
+      if (active && a.traj_qd != nullptr)
         store_vec<T>(tm, a.traj_qd + ((long long)s * a.n_env + env) * nv, w.at(L.qd), nv);
     }
   }
+  if (!active) return;  // no CTA barrier follows
   // outputs
   const braxg_state& o = a.out;
   store_vec<T>(tm, o.q ? o.q + env * nq : nullptr, w.at(L.q), nq);
@@ -178,10 +201,7 @@ __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   }
   pf.mark(BRAXG_PROF_IO);
   pf.count(BRAXG_PROF_NS_RESETS, (unsigned long long)reinterpret_cast<const int*>(w.at(L.misc))[1]);
-  if (a.prof != nullptr && tm.lane == 0) {
-    for (int i = 0; i < BRAXG_PROF_SLOTS; ++i)
-      if (pf.acc[i]) atomicAdd(a.prof + i, pf.acc[i]);
-  }
+
 }
 
 

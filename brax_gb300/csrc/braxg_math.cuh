@@ -54,10 +54,20 @@ __device__ __forceinline__ q4 qmul(q4 u, q4 v) {
             u.w * v.z + u.x * v.y - u.y * v.x + u.z * v.w};
 }
 
+// One out-of-line copy of the precise sine/cosine (keeps the kernel's code
+// footprint small: every call site would otherwise carry its own expansion).
+static __device__ __noinline__ void sincos_ool(float x, float* s, float* c) { sincosf(x, s, c); }
+static __device__ __noinline__ float pow_ool(float x, float y) { return powf(x, y); }
+// x^y with the exact shortcuts y == 1 and y == 2 (powf is correctly rounded
+// there, and so are x and x*x, so the results are identical).
+__device__ __forceinline__ float pow_fast(float x, float y) {
+  return y == 2.f ? x * x : (y == 1.f ? x : pow_ool(x, y));
+}
+
 // brax/math.py:134-148
 __device__ __forceinline__ q4 quat_rot_axis(f3 axis, float angle) {
   float s, c;
-  sincosf(angle * 0.5f, &s, &c);
+  sincos_ool(angle * 0.5f, &s, &c);
   return q4{c, axis.x * s, axis.y * s, axis.z * s};
 }
 

@@ -55,6 +55,8 @@ struct Layout {
 };
 
 __host__ __device__ inline int al4(int x) { return (x + 3) & ~3; }
+// words reserved after the model descriptor for the shared Layout
+constexpr int kLayoutWords = 64;
 
 __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim) {
   Layout L;
@@ -105,6 +107,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.total = al4(o);
   return L;
 }
+static_assert(sizeof(Layout) <= kLayoutWords * 4, "Layout must fit its shared slot");
 
 // ---------------------------------------------------------------------------
 // team of T lanes (T in {8, 16, 32}) inside one warp
@@ -134,9 +137,11 @@ struct Team {
   }
 };
 
+// Per-env workspace handle: the env's arena base and the (shared) layout.
+// Passed by value so out-of-line stages keep it in registers.
 struct Ws {
-  float* b;  // env base
-  Layout L;
+  float* b;
+  const Layout* L;
   __device__ __forceinline__ float* at(int off) const { return b + off; }
 };
 
@@ -144,8 +149,10 @@ struct Ws {
 // kinematics.forward: brax/kinematics.py:31-108
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ void stage_fk(const Model& md, const Team<T>& tm, const Ws& w) {
-  const Layout& L = w.L;
+__device__ __noinline__ void stage_fk(const int* mw, Ws w) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   float* q = w.at(L.q);
   float* qd = w.at(L.qd);
   float* jp_ = w.at(L.scr);
@@ -246,8 +253,10 @@ __device__ void stage_fk(const Model& md, const Team<T>& tm, const Ws& w) {
 // dynamics.transform_com: brax/generalized/dynamics.py:27-134
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ void stage_com(const Model& md, const Team<T>& tm, const Ws& w) {
-  const Layout& L = w.L;
+__device__ __noinline__ void stage_com(const int* mw, Ws w) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int nl = md.nl;
   float* xip = w.at(L.scr);
   float* xir = xip + 3 * nl;
@@ -416,8 +425,10 @@ __device__ void stage_com(const Model& md, const Team<T>& tm, const Ws& w) {
 // mass.matrix (CRBA): brax/generalized/mass.py:27-83
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ void stage_crba(const Model& md, const Team<T>& tm, const Ws& w) {
-  const Layout& L = w.L;
+__device__ __noinline__ void stage_crba(const int* mw, Ws w) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int nl = md.nl, nv = md.nv, ld = L.ldm;
   float* crbi = w.at(L.scr);
   float* crbp = crbi + 9 * nl;
@@ -644,8 +655,10 @@ __device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc,
 // the input); mode 1 recomputes the exact SPD inverse.
 // ---------------------------------------------------------------------------
 template <int T, int NVB>
-__device__ bool stage_inverse(const Model& md, const Team<T>& tm, const Ws& w, bool exact, int num_iter) {
-  const Layout& L = w.L;
+__device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int num_iter) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int n = md.nv, ld = L.ldm;
   float* M = w.at(L.M);
   float* P = w.at(L.Minv);
@@ -704,8 +717,8 @@ __device__ bool stage_inverse(const Model& md, const Team<T>& tm, const Ws& w, b
 __device__ __forceinline__ void imp_aref(const float* p, float pos, float vel, float& imp, float& aref) {
   float timeconst = p[0], dampratio = p[1], dmin = p[2], dmax = p[3], width = p[4], mid = p[5], power = p[6];
   float imp_x = fabsf(pos) / width;
-  float imp_a = (1.f / powf(mid, power - 1.f)) * powf(imp_x, power);
-  float imp_b = 1.f - (1.f / powf(1.f - mid, power - 1.f)) * powf(1.f - imp_x, power);
+  float imp_a = (1.f / pow_fast(mid, power - 1.f)) * pow_fast(imp_x, power);
+  float imp_b = 1.f - (1.f / pow_fast(1.f - mid, power - 1.f)) * pow_fast(1.f - imp_x, power);
   float imp_y = imp_x < mid ? imp_a : imp_b;
   imp = dmin + imp_y * (dmax - dmin);
   imp = fminf(fmaxf(imp, dmin), dmax);
@@ -774,9 +787,10 @@ __device__ __forceinline__ void closest_seg_seg(f3 a0, f3 a1, f3 b0, f3 b1, f3& 
 
 // Writes dist[k], pos[k*3], frame[k*9] for every contact slot.
 template <int T>
-__device__ void stage_contacts(const Model& md, const Team<T>& tm, const Ws& w, float* dist, float* cpos,
-                               float* frame) {
-  const Layout& L = w.L;
+__device__ __noinline__ void stage_contacts(const int* mw, Ws w, float* dist, float* cpos, float* frame) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const float* xp = w.at(L.xp);
   const float* xr = w.at(L.xr);
   const int* kind = md.I(BXM_O_CON_KIND);
@@ -827,10 +841,10 @@ __device__ void stage_contacts(const Model& md, const Team<T>& tm, const Ws& w, 
         cd[c] = dot3(cc[c] - p1, n);
       }
       int want = sub[k], pick = 0;
-#pragma unroll
+#pragma unroll 1
       for (int c = 0; c < 8; ++c) {
         int rank = 0;
-#pragma unroll
+#pragma unroll 1
         for (int e = 0; e < 8; ++e) rank += (cd[e] < cd[c]) || (cd[e] == cd[c] && e < c);
         if (rank == want) pick = c;
       }
@@ -868,8 +882,10 @@ __device__ void stage_contacts(const Model& md, const Team<T>& tm, const Ws& w, 
 // nothing to A x + b; only the active rows are stored, in reference order.
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ void stage_jacobian(const Model& md, const Team<T>& tm, const Ws& w) {
-  const Layout& L = w.L;
+__device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int nv = md.nv, ldj = L.ldj, ncon = md.ncon;
   float* dist = w.at(L.scr);
   float* cpos = dist + al4(ncon);
@@ -883,7 +899,7 @@ __device__ void stage_jacobian(const Model& md, const Team<T>& tm, const Ws& w) 
   const float* q = w.at(L.q);
   int nact = 0;
   if (ncon > 0) {
-    stage_contacts<T>(md, tm, w, dist, cpos, frame);
+    stage_contacts<T>(md.w, w, dist, cpos, frame);
     for (int base = 0; base < ncon; base += T) {
       int k = base + tm.lane;
       bool a = k < ncon && dist[k] < 0.f;
@@ -981,8 +997,10 @@ __device__ void stage_jacobian(const Model& md, const Team<T>& tm, const Ws& w) 
 // and inverse/RNE (brax/generalized/dynamics.py:137-236) -> qf_smooth
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ void stage_smooth(const Model& md, const Team<T>& tm, const Ws& w, bool has_act) {
-  const Layout& L = w.L;
+__device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int nl = md.nl, nv = md.nv;
   float* cdd = w.at(L.scr);
   float* cf = cdd + 6 * nl;
@@ -1088,9 +1106,11 @@ __device__ void stage_smooth(const Model& md, const Team<T>& tm, const Ws& w, bo
 // jaxopt.ProjectedGradient (FISTA + backtracking) iteration restated.
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ void matvec_A(const Model& md, const Team<T>& tm, const Ws& w, int nrow, const float* v, float* out,
-                         float* t1, float* t2) {
-  const Layout& L = w.L;
+__device__ __noinline__ void matvec_A(const int* mw, Ws w, int nrow, const float* v, float* out, float* t1,
+                                      float* t2) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int nv = md.nv, ldj = L.ldj, ld = L.ldm;
   const float* J = w.at(L.J);
   const float* Minv = w.at(L.Minv);
@@ -1133,8 +1153,10 @@ __device__ void matvec_A(const Model& md, const Team<T>& tm, const Ws& w, int nr
 }
 
 template <int T>
-__device__ int stage_constraint(const Model& md, const Team<T>& tm, const Ws& w) {
-  const Layout& L = w.L;
+__device__ __noinline__ int stage_constraint(const int* mw, Ws w) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int nv = md.nv, ldj = L.ldj, ld = L.ldm;
   const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
   float* qfc = w.at(L.qfc);
@@ -1178,7 +1200,7 @@ __device__ int stage_constraint(const Model& md, const Team<T>& tm, const Ws& w)
   for (int it = 0; it < md.pg_iters; ++it) {
     if (it > 0 && !(err > md.pg_tol)) break;
     // value and gradient at y
-    matvec_A<T>(md, tm, w, nrow, y, r, t1, t2);
+    matvec_A<T>(md.w, w, nrow, y, r, t1, t2);
     float fs = 0.f;
     for (int i = tm.lane; i < nrow; i += T) {
       r[i] = r[i] + b[i];
@@ -1186,13 +1208,13 @@ __device__ int stage_constraint(const Model& md, const Team<T>& tm, const Ws& w)
     }
     float fy = tm.sum(fs);
     tm.sync();
-    matvec_A<T>(md, tm, w, nrow, r, gy, t1, t2);
+    matvec_A<T>(md.w, w, nrow, r, gy, t1, t2);
     matvecs += 2;
     float cur = ss;
     for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
     tm.sync();
     for (int ls = 0; ls < md.pg_maxls; ++ls) {
-      matvec_A<T>(md, tm, w, nrow, nx, r, t1, t2);
+      matvec_A<T>(md.w, w, nrow, nx, r, t1, t2);
       matvecs += 1;
       float fn = 0.f, dv = 0.f, sq = 0.f;
       for (int i = tm.lane; i < nrow; i += T) {
@@ -1217,10 +1239,10 @@ __device__ int stage_constraint(const Model& md, const Team<T>& tm, const Ws& w)
     for (int i = tm.lane; i < nrow; i += T) ny[i] = nx[i] + beta * (nx[i] - x[i]);
     tm.sync();
     // gradient at the new iterate and the stopping error
-    matvec_A<T>(md, tm, w, nrow, nx, r, t1, t2);
+    matvec_A<T>(md.w, w, nrow, nx, r, t1, t2);
     for (int i = tm.lane; i < nrow; i += T) r[i] = r[i] + b[i];
     tm.sync();
-    matvec_A<T>(md, tm, w, nrow, r, gx, t1, t2);
+    matvec_A<T>(md.w, w, nrow, r, gx, t1, t2);
     matvecs += 2;
     float es = 0.f;
     for (int i = tm.lane; i < nrow; i += T) {
@@ -1248,8 +1270,10 @@ __device__ int stage_constraint(const Model& md, const Team<T>& tm, const Ws& w)
 // integrator.integrate: brax/generalized/integrator.py:26-84
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ bool stage_integrate(const Model& md, const Team<T>& tm, const Ws& w) {
-  const Layout& L = w.L;
+__device__ __noinline__ bool stage_integrate(const int* mw, Ws w) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
   const int nv = md.nv, ld = L.ldm;
   const float h = md.dt;
   float* qfs = w.at(L.qfs);

@@ -1,0 +1,51 @@
+"""The numpy restatement of the step's reverse-mode derivative (the checker
+for the CUDA adjoint) against FP64 central finite differences."""
+
+import numpy as np
+import pytest
+
+from oracle.adjoint import StepAdjoint
+from oracle.pipeline import Oracle
+from tests.parity_util import actions, load, seeded_inputs
+
+
+def _fd_check(name, steps, B=4, seed=5):
+  sys_ = load(name)
+  o = Oracle(sys_, np.float64, exact_inverse=True)
+  q, qd = seeded_inputs(sys_, B, seed)
+  s = o.init(q, qd)
+  rng = np.random.default_rng(seed + 1)
+  for _ in range(steps):
+    s = o.step(s, actions(sys_, B, rng))
+  q, qd = s.q.copy(), s.qd.copy()
+  act = actions(sys_, B, rng)
+  adj = StepAdjoint(sys_)
+  qn, qdn, T = adj.forward(q, qd, act)
+  qbo, qdbo = rng.normal(size=qn.shape), rng.normal(size=qdn.shape)
+  adj._xr = T['s'].x_rot
+  grads = adj.vjp(T, qbo, qdbo)
+
+  def f(q_, qd_, a_):
+    r = o.step(o.restore(q_, qd_, np.zeros((B, sys_.qd_size(), sys_.qd_size()))), a_)
+    return np.sum(qbo * r.q, -1) + np.sum(qdbo * r.qd, -1)
+
+  eps = 1e-6
+  for which, got in enumerate(grads):
+    base = [q, qd, act]
+    fd = np.zeros_like(got)
+    for j in range(got.shape[1]):
+      a = [x.copy() for x in base]
+      a[which][:, j] += eps
+      fp = f(*a)
+      a[which][:, j] -= 2 * eps
+      fd[:, j] = (fp - f(*a)) / (2 * eps)
+    err = np.abs(got - fd).max(-1) / np.maximum(np.abs(fd).max(-1), 1e-9)
+    assert err.max() < 1e-5, (name, which, err)
+  return T
+
+
+@pytest.mark.parametrize('name,steps', [('chain3', 3), ('quadruped', 6), ('quadruped', 40)])
+def test_step_vjp_matches_finite_differences(name, steps):
+  T = _fd_check(name, steps)
+  if steps == 40:  # the landed quadruped exercises contact and limit rows
+    assert (np.abs(T['s'].con_jac).max(-1) > 0).sum() > 0
