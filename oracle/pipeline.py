@@ -857,7 +857,8 @@ class Oracle:
     other field is the position-level function of (q, qd) computed at the end
     of the previous step (pipeline.py:86-92)."""
     s = self.init(q, qd)
-    s = s.replace(mass_mx_inv=np.asarray(minv, self.dt_))
+    if minv is not None:
+      s = s.replace(mass_mx_inv=np.asarray(minv, self.dt_))
     return s
 
   def step(self, s: State, act) -> State:

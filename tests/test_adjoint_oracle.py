@@ -26,7 +26,7 @@ def _fd_check(name, steps, B=4, seed=5):
   grads = adj.vjp(T, qbo, qdbo)
 
   def f(q_, qd_, a_):
-    r = o.step(o.restore(q_, qd_, np.zeros((B, sys_.qd_size(), sys_.qd_size()))), a_)
+    r = o.step(o.restore(q_, qd_, None), a_)  # exact inverse of M(q_)
     return np.sum(qbo * r.q, -1) + np.sum(qdbo * r.qd, -1)
 
   eps = 1e-6
