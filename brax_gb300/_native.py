@@ -19,12 +19,13 @@ STATE_FIELDS = (
     'cdof', 'cdofd', 'mass_mx', 'con_jac', 'con_diag', 'con_aref', 'status')
 
 EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims',
-           'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_launch_shape',
-           'braxg_last_launch_count', 'braxg_last_error')
+           'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_rollout_vjp_workspace',
+           'braxg_rollout_vjp', 'braxg_launch_shape', 'braxg_last_launch_count',
+           'braxg_last_error')
 
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED = 0, 1, 2, 3
 INV_NEWTON_SCHULZ, INV_CHOLESKY = 0, 1
-ENV_NONFINITE, ENV_NOT_SPD = 1, 2
+ENV_NONFINITE, ENV_NOT_SPD, ENV_NO_GRADIENT = 1, 2, 4
 
 
 class State(ctypes.Structure):
@@ -69,6 +70,9 @@ def lib() -> ctypes.CDLL:
     l.braxg_step.argtypes = [vp, vp, i32, i32, vp, P(State), P(State), P(Options)]
     l.braxg_rollout.argtypes = [vp, vp, i32, i32, i32, vp, P(State), P(State), vp, vp,
                                 P(Options)]
+    l.braxg_rollout_vjp_workspace.argtypes = [vp, i32, i32, i32, i32, P(ctypes.c_size_t)]
+    l.braxg_rollout_vjp.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp,
+                                    vp, vp, vp, ctypes.c_size_t, vp, P(Options)]
     l.braxg_launch_shape.argtypes = [vp, P(Options), P(ctypes.c_int32), P(ctypes.c_int32),
                                      P(ctypes.c_int32)]
     l.braxg_last_error.restype = ctypes.c_char_p

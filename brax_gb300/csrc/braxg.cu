@@ -10,6 +10,7 @@
 #include "braxg.h"
 #include "braxg_launch.h"
 #include "braxg_step.cuh"
+#include "braxg_adjoint.cuh"
 
 
 // ---------------------------------------------------------------------------
@@ -232,6 +233,88 @@ static int run_steps(const braxg_model* m, void* stream, int n_env, int n_steps,
   a.traj_q = tq;
   a.traj_qd = tqd;
   return launch(m, opt, a, static_cast<cudaStream_t>(stream));
+}
+
+static void vjp_sizes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, size_t* ckpt_floats,
+                      size_t* seg_floats) {
+  size_t S = (size_t)m->dims.nq + m->dims.nv;
+  size_t n_ckpt = (size_t)(n_steps + ckpt_every - 1) / ckpt_every;
+  *ckpt_floats = (n_ckpt * n_env * S + 63) / 64 * 64;
+  *seg_floats = (size_t)ckpt_every * n_frames * n_env * S;
+}
+
+int braxg_rollout_vjp_workspace(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every,
+                                size_t* bytes) {
+  if (m == nullptr || bytes == nullptr) return fail(BRAXG_ERR_INVALID, "NULL argument");
+  if (n_env < 0 || n_steps < 1 || n_frames < 1 || ckpt_every < 1)
+    return fail(BRAXG_ERR_INVALID, "n_env >= 0, n_steps, n_frames and ckpt_every >= 1 required");
+  size_t c, sg;
+  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, &c, &sg);
+  *bytes = (c + sg) * sizeof(float);
+  return BRAXG_OK;
+}
+
+int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, int ckpt_every,
+                      const float* act_seq, const float* q0, const float* qd0, const float* q_bar,
+                      const float* qd_bar, float* act_bar, float* q0_bar, float* qd0_bar, float* traj_q,
+                      float* traj_qd, void* workspace, size_t workspace_bytes, int32_t* status,
+                      const braxg_options* opt) {
+  (void)opt;
+  g_launches = 0;
+  size_t need = 0;
+  int rc = braxg_rollout_vjp_workspace(m, n_env, n_steps, n_frames, ckpt_every, &need);
+  if (rc) return rc;
+  if (n_env == 0) return BRAXG_OK;
+  if (q0 == nullptr || qd0 == nullptr) return fail(BRAXG_ERR_INVALID, "q0 and qd0 are required");
+  if (workspace == nullptr || workspace_bytes < need)
+    return fail(BRAXG_ERR_INVALID, "workspace of %zu bytes required (got %zu)", need, workspace_bytes);
+  if (m->dims.nv > 32) return fail(BRAXG_ERR_UNSUPPORTED, "gradients support nv <= 32");
+  for (int k = 0; k < m->dims.ncon; ++k) {
+    int kind = m->h[m->h[BXM_O_CON_KIND] + k], la = m->h[m->h[BXM_O_CON_LA] + k];
+    if ((kind != BXM_CON_PLANE_SPHERE && kind != BXM_CON_PLANE_CAPSULE) || la >= 0)
+      return fail(BRAXG_ERR_UNSUPPORTED, "gradients support world-plane sphere/capsule contacts only");
+  }
+  size_t c, sg;
+  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, &c, &sg);
+  braxg::VjpArgs a{};
+  a.model = m->d_desc;
+  a.model_words = m->words;
+  a.n_env = n_env;
+  a.n_steps = n_steps;
+  a.n_frames = n_frames;
+  a.ckpt_every = ckpt_every;
+  a.act = act_seq;
+  a.q0 = q0;
+  a.qd0 = qd0;
+  a.q_bar = q_bar;
+  a.qd_bar = qd_bar;
+  a.act_bar = act_bar;
+  a.q0_bar = q0_bar;
+  a.qd0_bar = qd0_bar;
+  a.ckpt = static_cast<float*>(workspace);
+  a.seg = static_cast<float*>(workspace) + c;
+  a.traj_q = traj_q;
+  a.traj_qd = traj_qd;
+  a.status = status;
+  braxg::AdjLayout A = braxg::make_adj_layout(m->dims.nl, m->dims.nq, m->dims.nv, m->dims.nu, m->dims.ncon,
+                                              m->dims.nlim, m->h[BXM_H_PG_ITERS]);
+  int head = (braxg::al4(m->words) + 2 * braxg::kLayoutWords) * 4;
+  int env_bytes = (m->L.total + A.total) * 4;
+  int epc = (kMaxSmem - head) / env_bytes;
+  if (epc < 1) return fail(BRAXG_ERR_UNSUPPORTED, "model too large for the gradient kernel's shared memory");
+  if (epc > 8) epc = 8;
+  a.envs_per_cta = epc;
+  int smem = head + epc * env_bytes;
+  int grid = (n_env + epc - 1) / epc;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != m->device) cudaSetDevice(m->device);
+  cudaError_t e = m->dims.nv <= 16 ? braxg::launch_vjp<32, 16>(a, grid, smem, static_cast<cudaStream_t>(stream))
+                                   : braxg::launch_vjp<32, 32>(a, grid, smem, static_cast<cudaStream_t>(stream));
+  if (cur != m->device) cudaSetDevice(cur);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient kernel launch");
+  g_launches = 1;
+  return BRAXG_OK;
 }
 
 int braxg_step(const braxg_model* m, void* stream, int n_env, int n_frames, const float* act, const braxg_state* in,

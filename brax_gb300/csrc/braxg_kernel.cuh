@@ -68,6 +68,72 @@ __device__ __forceinline__ bool position_stage(const int* mw, Ws w, bool active,
   return ok;
 }
 
+// Writes the State outputs of one env (out-of-line: runs once per launch).
+template <int T>
+__device__ __noinline__ void write_outputs(const StepArgs& a, const int* mw, Ws w, long long env, bool ok) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  const int nq = md.nq, nv = md.nv, nl = md.nl, ld = L.ldm;
+  // outputs
+  const braxg_state& o = a.out;
+  store_vec<T>(tm, o.q ? o.q + env * nq : nullptr, w.at(L.q), nq);
+  store_vec<T>(tm, o.qd ? o.qd + env * nv : nullptr, w.at(L.qd), nv);
+  store_mat<T>(tm, o.mass_mx_inv ? o.mass_mx_inv + env * nv * nv : nullptr, w.at(L.Minv), nv, ld);
+  store_mat<T>(tm, o.mass_mx ? o.mass_mx + env * nv * nv : nullptr, w.at(L.M), nv, ld);
+  store_vec<T>(tm, o.x_pos ? o.x_pos + env * nl * 3 : nullptr, w.at(L.xp), 3 * nl);
+  store_vec<T>(tm, o.x_rot ? o.x_rot + env * nl * 4 : nullptr, w.at(L.xr), 4 * nl);
+  store_vec<T>(tm, o.xd_ang ? o.xd_ang + env * nl * 3 : nullptr, w.at(L.xa), 3 * nl);
+  store_vec<T>(tm, o.xd_vel ? o.xd_vel + env * nl * 3 : nullptr, w.at(L.xv), 3 * nl);
+  store_vec<T>(tm, o.qf_smooth ? o.qf_smooth + env * nv : nullptr, w.at(L.qfs), nv);
+  store_vec<T>(tm, o.qf_constraint ? o.qf_constraint + env * nv : nullptr, w.at(L.qfc), nv);
+  store_vec<T>(tm, o.qdd ? o.qdd + env * nv : nullptr, w.at(L.qdd), nv);
+  store_vec<T>(tm, o.root_com ? o.root_com + env * nl * 3 : nullptr, w.at(L.rc), 3 * nl);
+  store_vec<T>(tm, o.cinr_pos ? o.cinr_pos + env * nl * 3 : nullptr, w.at(L.cp), 3 * nl);
+  store_vec<T>(tm, o.cinr_i ? o.cinr_i + env * nl * 9 : nullptr, w.at(L.ci), 9 * nl);
+  store_vec<T>(tm, o.cd ? o.cd + env * nl * 6 : nullptr, w.at(L.cd), 6 * nl);
+  store_vec<T>(tm, o.cdof ? o.cdof + env * nv * 6 : nullptr, w.at(L.cdof), 6 * nv);
+  store_vec<T>(tm, o.cdofd ? o.cdofd + env * nv * 6 : nullptr, w.at(L.cdofd), 6 * nv);
+  if (o.cinr_rot != nullptr) {  // cinr.transform.rot = x_i.rot
+    for (int l = tm.lane; l < nl; l += T) {
+      f3 op;
+      q4 orr;
+      tf_do(ld3(w.at(L.xp) + 3 * l), ld4(w.at(L.xr) + 4 * l), ld3(md.F(BXM_O_LI_POS) + 3 * l),
+            ld4(md.F(BXM_O_LI_ROT) + 4 * l), op, orr);
+      st4(o.cinr_rot + (env * nl + l) * 4, orr);
+    }
+  }
+  if (o.con_jac != nullptr || o.con_diag != nullptr || o.con_aref != nullptr) {
+    const int m = md.m;
+    const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
+    const int* rmap = reinterpret_cast<const int*>(w.at(L.rmap));
+    int* inv = reinterpret_cast<int*>(w.at(L.scr));
+    for (int r = tm.lane; r < m; r += T) inv[r] = -1;
+    tm.sync();
+    for (int r = tm.lane; r < nrow; r += T) inv[rmap[r]] = r;
+    tm.sync();
+    if (o.con_jac != nullptr) {
+      for (long long idx = tm.lane; idx < (long long)m * nv; idx += T) {
+        int r = (int)(idx / nv), d = (int)(idx - (long long)r * nv);
+        int c = inv[r];
+        o.con_jac[env * m * nv + idx] = c >= 0 ? w.at(L.J)[c * L.ldj + d] : 0.f;
+      }
+    }
+    for (int r = tm.lane; r < m; r += T) {
+      int c = inv[r];
+      if (o.con_diag != nullptr) o.con_diag[env * m + r] = c >= 0 ? w.at(L.rdiag)[c] : 0.f;
+      if (o.con_aref != nullptr) o.con_aref[env * m + r] = c >= 0 ? w.at(L.raref)[c] : 0.f;
+    }
+  }
+  if (o.status != nullptr) {
+    bool fin = true;
+    for (int i = tm.lane; i < nq; i += T) fin = fin && isfinite(w.at(L.q)[i]);
+    for (int i = tm.lane; i < nv; i += T) fin = fin && isfinite(w.at(L.qd)[i]);
+    fin = tm.all(fin);
+    if (tm.lane == 0) o.status[env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
+  }
+}
+
 template <int T, int NVB>
 __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   extern __shared__ __align__(16) int smem[];
@@ -142,63 +208,7 @@ __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
     }
   }
   if (!active) return;  // no CTA barrier follows
-  // outputs
-  const braxg_state& o = a.out;
-  store_vec<T>(tm, o.q ? o.q + env * nq : nullptr, w.at(L.q), nq);
-  store_vec<T>(tm, o.qd ? o.qd + env * nv : nullptr, w.at(L.qd), nv);
-  store_mat<T>(tm, o.mass_mx_inv ? o.mass_mx_inv + env * nv * nv : nullptr, w.at(L.Minv), nv, ld);
-  store_mat<T>(tm, o.mass_mx ? o.mass_mx + env * nv * nv : nullptr, w.at(L.M), nv, ld);
-  store_vec<T>(tm, o.x_pos ? o.x_pos + env * nl * 3 : nullptr, w.at(L.xp), 3 * nl);
-  store_vec<T>(tm, o.x_rot ? o.x_rot + env * nl * 4 : nullptr, w.at(L.xr), 4 * nl);
-  store_vec<T>(tm, o.xd_ang ? o.xd_ang + env * nl * 3 : nullptr, w.at(L.xa), 3 * nl);
-  store_vec<T>(tm, o.xd_vel ? o.xd_vel + env * nl * 3 : nullptr, w.at(L.xv), 3 * nl);
-  store_vec<T>(tm, o.qf_smooth ? o.qf_smooth + env * nv : nullptr, w.at(L.qfs), nv);
-  store_vec<T>(tm, o.qf_constraint ? o.qf_constraint + env * nv : nullptr, w.at(L.qfc), nv);
-  store_vec<T>(tm, o.qdd ? o.qdd + env * nv : nullptr, w.at(L.qdd), nv);
-  store_vec<T>(tm, o.root_com ? o.root_com + env * nl * 3 : nullptr, w.at(L.rc), 3 * nl);
-  store_vec<T>(tm, o.cinr_pos ? o.cinr_pos + env * nl * 3 : nullptr, w.at(L.cp), 3 * nl);
-  store_vec<T>(tm, o.cinr_i ? o.cinr_i + env * nl * 9 : nullptr, w.at(L.ci), 9 * nl);
-  store_vec<T>(tm, o.cd ? o.cd + env * nl * 6 : nullptr, w.at(L.cd), 6 * nl);
-  store_vec<T>(tm, o.cdof ? o.cdof + env * nv * 6 : nullptr, w.at(L.cdof), 6 * nv);
-  store_vec<T>(tm, o.cdofd ? o.cdofd + env * nv * 6 : nullptr, w.at(L.cdofd), 6 * nv);
-  if (o.cinr_rot != nullptr) {  // cinr.transform.rot = x_i.rot
-    for (int l = tm.lane; l < nl; l += T) {
-      f3 op;
-      q4 orr;
-      tf_do(ld3(w.at(L.xp) + 3 * l), ld4(w.at(L.xr) + 4 * l), ld3(md.F(BXM_O_LI_POS) + 3 * l),
-            ld4(md.F(BXM_O_LI_ROT) + 4 * l), op, orr);
-      st4(o.cinr_rot + (env * nl + l) * 4, orr);
-    }
-  }
-  if (o.con_jac != nullptr || o.con_diag != nullptr || o.con_aref != nullptr) {
-    const int m = md.m;
-    const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
-    const int* rmap = reinterpret_cast<const int*>(w.at(L.rmap));
-    int* inv = reinterpret_cast<int*>(w.at(L.scr));
-    for (int r = tm.lane; r < m; r += T) inv[r] = -1;
-    tm.sync();
-    for (int r = tm.lane; r < nrow; r += T) inv[rmap[r]] = r;
-    tm.sync();
-    if (o.con_jac != nullptr) {
-      for (long long idx = tm.lane; idx < (long long)m * nv; idx += T) {
-        int r = (int)(idx / nv), d = (int)(idx - (long long)r * nv);
-        int c = inv[r];
-        o.con_jac[env * m * nv + idx] = c >= 0 ? w.at(L.J)[c * L.ldj + d] : 0.f;
-      }
-    }
-    for (int r = tm.lane; r < m; r += T) {
-      int c = inv[r];
-      if (o.con_diag != nullptr) o.con_diag[env * m + r] = c >= 0 ? w.at(L.rdiag)[c] : 0.f;
-      if (o.con_aref != nullptr) o.con_aref[env * m + r] = c >= 0 ? w.at(L.raref)[c] : 0.f;
-    }
-  }
-  if (o.status != nullptr) {
-    bool fin = true;
-    for (int i = tm.lane; i < nq; i += T) fin = fin && isfinite(w.at(L.q)[i]);
-    for (int i = tm.lane; i < nv; i += T) fin = fin && isfinite(w.at(L.qd)[i]);
-    fin = tm.all(fin);
-    if (tm.lane == 0) o.status[env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
-  }
+  write_outputs<T>(a, smem, w, env, ok);
   pf.mark(BRAXG_PROF_IO);
   pf.count(BRAXG_PROF_NS_RESETS, (unsigned long long)reinterpret_cast<const int*>(w.at(L.misc))[1]);
 

@@ -57,6 +57,9 @@ struct Layout {
 __host__ __device__ inline int al4(int x) { return (x + 3) & ~3; }
 // words reserved after the model descriptor for the shared Layout
 constexpr int kLayoutWords = 64;
+// the projected-gradient solve forms A explicitly while at most this many
+// constraint rows are active (else it applies A = J Minv J^T + diag implicitly)
+constexpr int kMaxExplicitRows = 32;
 
 __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim) {
   Layout L;
@@ -100,7 +103,12 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   s = s > 12 * nl + nu ? s : 12 * nl + nu;           // RNE
   s = s > 2 * nv * L.ldm + 4 ? s : 2 * nv * L.ldm + 4;  // inverse temporaries
   s = s > 14 * ncon + 16 ? s : 14 * ncon + 16;       // contacts
-  s = s > 8 * m + 4 * nv + 40 ? s : 8 * m + 4 * nv + 40;  // projected gradient
+  s = s > 8 * m + 4 * nv + 40 ? s : 8 * m + 4 * nv + 40;  // projected gradient (implicit A)
+  {
+    const int na = m < kMaxExplicitRows ? m : kMaxExplicitRows;  // explicit A = (J Minv) J^T + diag
+    const int pg = na * (na | 1) + na * L.ldm + 8 * al4(na) + 2 * al4(nv) + 16;
+    s = s > pg ? s : pg;
+  }
   s = s > m + 4 ? s : m + 4;                         // output row map
   L.scr_words = al4(s);
   L.scr = take(L.scr_words);
@@ -556,12 +564,12 @@ template <int T>
 __device__ float safe_norm_mat(const Team<T>& tm, int n, int ld, const float* R) {
   float s = 0.f;
   bool small = true;
-  for (int idx = tm.lane; idx < n * n; idx += T) {
-    int i = idx / n, j = idx - i * n;
-    float v = R[i * ld + j];
-    small = small && (fabsf(v) <= 1e-8f);
-    s += v * v;
-  }
+  for (int j = tm.lane; j < n; j += T)
+    for (int i = 0; i < n; ++i) {
+      float v = R[i * ld + j];
+      small = small && (fabsf(v) <= 1e-8f);
+      s += v * v;
+    }
   bool z = tm.all(small);
   s = tm.sum(s);
   return z ? 0.f : sqrtf(s);
@@ -596,11 +604,12 @@ __device__ bool cholesky(const Team<T>& tm, int n, int ld, float* A) {
 // pivot is not positive.
 template <int T>
 __device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc, float* Lw, float* X, float* Minv) {
-  for (int idx = tm.lane; idx < n * n; idx += T) {
-    int i = idx / n, j = idx - i * n;
-    Lw[i * ld + j] = Msrc[i * ld + j];
-    X[i * ld + j] = (i == j) ? 1.f : 0.f;
-  }
+  // lanes own columns: no integer division in the index arithmetic
+  for (int j = tm.lane; j < n; j += T)
+    for (int i = 0; i < n; ++i) {
+      Lw[i * ld + j] = Msrc[i * ld + j];
+      X[i * ld + j] = (i == j) ? 1.f : 0.f;
+    }
   tm.sync();
   bool ok = true;
   for (int k = 0; k < n; ++k) {
@@ -610,13 +619,9 @@ __device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc,
     for (int i = k + 1 + tm.lane; i < n; i += T) Lw[i * ld + k] = Lw[i * ld + k] / d;
     tm.sync();
     if (tm.lane == 0) Lw[k * ld + k] = d;
-    const int w = n - k - 1;
-    for (int p = tm.lane; p < w * w; p += T) {
-      int ii = p / w, jj = p - ii * w;
-      if (jj <= ii) {
-        int i = k + 1 + ii, j = k + 1 + jj;
-        Lw[i * ld + j] = Lw[i * ld + j] - Lw[i * ld + k] * Lw[j * ld + k];
-      }
+    for (int j = k + 1 + tm.lane; j < n; j += T) {  // trailing update of column j
+      const float ljk = Lw[j * ld + k];
+      for (int i = j; i < n; ++i) Lw[i * ld + j] = Lw[i * ld + j] - Lw[i * ld + k] * ljk;
     }
     tm.sync();
   }
@@ -624,26 +629,25 @@ __device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc,
     const float lkk = Lw[k * ld + k];
     for (int j = tm.lane; j <= k; j += T) X[k * ld + j] = X[k * ld + j] / lkk;
     tm.sync();
-    const int rows = n - k - 1, cols = k + 1;
-    for (int p = tm.lane; p < rows * cols; p += T) {
-      int ii = p / cols, j = p - ii * cols, i = k + 1 + ii;
-      X[i * ld + j] = X[i * ld + j] - Lw[i * ld + k] * X[k * ld + j];
+    for (int j = tm.lane; j <= k; j += T) {  // eliminate column j below row k
+      const float xkj = X[k * ld + j];
+      for (int i = k + 1; i < n; ++i) X[i * ld + j] = X[i * ld + j] - Lw[i * ld + k] * xkj;
     }
     tm.sync();
   }
-  for (int idx = tm.lane; idx < n * n; idx += T) {
-    int i = idx / n, j = idx - i * n;
-    if (j > i) continue;
-    float s0 = 0.f, s1 = 0.f;
-    int m = i;
-    for (; m + 1 < n; m += 2) {
-      s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
-      s1 = fmaf(X[(m + 1) * ld + i], X[(m + 1) * ld + j], s1);
+  for (int j = tm.lane; j < n; j += T) {  // Minv = X^T X, column j, rows i >= j
+    for (int i = j; i < n; ++i) {
+      float s0 = 0.f, s1 = 0.f;
+      int m = i;
+      for (; m + 1 < n; m += 2) {
+        s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
+        s1 = fmaf(X[(m + 1) * ld + i], X[(m + 1) * ld + j], s1);
+      }
+      if (m < n) s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
+      float v = s0 + s1;
+      Minv[i * ld + j] = v;
+      Minv[j * ld + i] = v;
     }
-    if (m < n) s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
-    float v = s0 + s1;
-    Minv[i * ld + j] = v;
-    Minv[j * ld + i] = v;
   }
   tm.sync();
   return ok;
@@ -677,16 +681,14 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   if (nr0 > 1.f) {  // reset to 0.5 A^T / tr(A A^T) (r0 is kept, as the reference does)
     if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] += 1;
     float s = 0.f;
-    for (int idx = tm.lane; idx < n * n; idx += T) {
-      int i = idx / n, j = idx - i * n;
-      float v = M[i * ld + j];
-      s += v * v;
-    }
+    for (int j = tm.lane; j < n; j += T)
+      for (int i = 0; i < n; ++i) {
+        float v = M[i * ld + j];
+        s += v * v;
+      }
     s = tm.sum(s);
-    for (int idx = tm.lane; idx < n * n; idx += T) {
-      int i = idx / n, j = idx - i * n;
-      cur[i * ld + j] = 0.5f * M[j * ld + i] / s;
-    }
+    for (int j = tm.lane; j < n; j += T)
+      for (int i = 0; i < n; ++i) cur[i * ld + j] = 0.5f * M[j * ld + i] / s;
     tm.sync();
   }
   float err = 1.f;
@@ -702,10 +704,8 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
     err = e;
   }
   if (cur != P) {
-    for (int idx = tm.lane; idx < n * n; idx += T) {
-      int i = idx / n, j = idx - i * n;
-      P[i * ld + j] = cur[i * ld + j];
-    }
+    for (int j = tm.lane; j < n; j += T)
+      for (int i = 0; i < n; ++i) P[i * ld + j] = cur[i * ld + j];
     tm.sync();
   }
   return true;
@@ -1152,8 +1152,184 @@ __device__ __noinline__ void matvec_A(const int* mw, Ws w, int nrow, const float
   tm.sync();
 }
 
+// Projected gradient with A formed explicitly, in the reference's association:
+// W = J Minv, A = W J^T + diag(d), b = W qf_smooth - aref (constraint.py:208-210).
+// Used when nrow <= kMaxExplicitRows; each matvec is then one team pass.
+// PG tape (reverse pass only): [0] iterations run, then x* (al4(kMaxExplicitRows)
+// words), then per iteration 4 scalars (step, beta) and y, r(y), [z > 0],
+// each al4(kMaxExplicitRows) words.
+constexpr int kTapeIterWords = 4 + 3 * ((kMaxExplicitRows + 3) & ~3);
+constexpr int kTapeHeadWords = 4 + ((kMaxExplicitRows + 3) & ~3);
+
 template <int T>
-__device__ __noinline__ int stage_constraint(const int* mw, Ws w) {
+__device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* tape) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  const int nv = md.nv, ldj = L.ldj, ld = L.ldm, la = nrow | 1;
+  float* A = w.at(L.scr);
+  float* W = A + nrow * la;
+  float* b = W + nrow * ld;
+  float* x = b + al4(nrow);
+  float* y = x + al4(nrow);
+  float* gy = y + al4(nrow);
+  float* r = gy + al4(nrow);
+  float* nx = r + al4(nrow);
+  float* ny = nx + al4(nrow);
+  float* gx = ny + al4(nrow);
+  const float* J = w.at(L.J);
+  const float* Minv = w.at(L.Minv);
+  const float* rdiag = w.at(L.rdiag);
+  const float* raref = w.at(L.raref);
+  const float* qfs = w.at(L.qfs);
+  float* qfc = w.at(L.qfc);
+  for (int k = tm.lane; k < nv; k += T)  // W = J Minv (lanes over columns)
+    for (int i = 0; i < nrow; ++i) {
+      float s0 = 0.f, s1 = 0.f;
+      int d = 0;
+      for (; d + 1 < nv; d += 2) {
+        s0 = fmaf(J[i * ldj + d], Minv[d * ld + k], s0);
+        s1 = fmaf(J[i * ldj + d + 1], Minv[(d + 1) * ld + k], s1);
+      }
+      if (d < nv) s0 = fmaf(J[i * ldj + d], Minv[d * ld + k], s0);
+      W[i * ld + k] = s0 + s1;
+    }
+  tm.sync();
+  for (int c = tm.lane; c < nrow; c += T) {  // A[:, c] = W J[c]^T (+ diag)
+    for (int i = 0; i < nrow; ++i) {
+      float s0 = 0.f, s1 = 0.f;
+      int k = 0;
+      for (; k + 1 < nv; k += 2) {
+        s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+        s1 = fmaf(W[i * ld + k + 1], J[c * ldj + k + 1], s1);
+      }
+      if (k < nv) s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+      A[i * la + c] = (s0 + s1) + (i == c ? rdiag[i] : 0.f);
+    }
+    float s0 = 0.f, s1 = 0.f;  // b[c] = W[c] qf_smooth - aref[c]
+    int k = 0;
+    for (; k + 1 < nv; k += 2) {
+      s0 = fmaf(W[c * ld + k], qfs[k], s0);
+      s1 = fmaf(W[c * ld + k + 1], qfs[k + 1], s1);
+    }
+    if (k < nv) s0 = fmaf(W[c * ld + k], qfs[k], s0);
+    b[c] = (s0 + s1) - raref[c];
+    x[c] = 0.f;
+    y[c] = 0.f;
+  }
+  tm.sync();
+  // out = A v + b (lanes over rows)
+  auto resid = [&](const float* v, float* out) {
+    for (int i = tm.lane; i < nrow; i += T) {
+      float s0 = 0.f, s1 = 0.f;
+      int c = 0;
+      for (; c + 1 < nrow; c += 2) {
+        s0 = fmaf(A[i * la + c], v[c], s0);
+        s1 = fmaf(A[i * la + c + 1], v[c + 1], s1);
+      }
+      if (c < nrow) s0 = fmaf(A[i * la + c], v[c], s0);
+      out[i] = (s0 + s1) + b[i];
+    }
+    tm.sync();
+  };
+  // out = A^T v (lanes over columns)
+  auto grad = [&](const float* v, float* out) {
+    for (int c = tm.lane; c < nrow; c += T) {
+      float s0 = 0.f, s1 = 0.f;
+      int i = 0;
+      for (; i + 1 < nrow; i += 2) {
+        s0 = fmaf(A[i * la + c], v[i], s0);
+        s1 = fmaf(A[(i + 1) * la + c], v[i + 1], s1);
+      }
+      if (i < nrow) s0 = fmaf(A[i * la + c], v[i], s0);
+      out[c] = s0 + s1;
+    }
+    tm.sync();
+  };
+  float t = 1.f, ss = 1.f, err = INFINITY;
+  int matvecs = 0;
+  int iters = 0;
+  constexpr int kA = (kMaxExplicitRows + 3) & ~3;
+  for (int it = 0; it < md.pg_iters; ++it) {
+    if (it > 0 && !(err > md.pg_tol)) break;
+    resid(y, r);
+    float* rec = tape != nullptr ? tape + kTapeHeadWords + it * kTapeIterWords : nullptr;
+    if (rec != nullptr)
+      for (int i = tm.lane; i < nrow; i += T) {
+        rec[4 + i] = y[i];
+        rec[4 + kA + i] = r[i];
+      }
+    float fs = 0.f;
+    for (int i = tm.lane; i < nrow; i += T) fs += 0.5f * r[i] * r[i];
+    const float fy = tm.sum(fs);
+    grad(r, gy);
+    matvecs += 2;
+    float cur = ss;
+    for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
+    tm.sync();
+    for (int ls = 0; ls < md.pg_maxls; ++ls) {
+      resid(nx, r);
+      matvecs += 1;
+      float fn = 0.f, dv = 0.f, sq = 0.f;
+      for (int i = tm.lane; i < nrow; i += T) {
+        fn += 0.5f * r[i] * r[i];
+        float dx = nx[i] - y[i];
+        dv += dx * gy[i];
+        sq += dx * dx;
+      }
+      fn = tm.sum(fn);
+      dv = tm.sum(dv);
+      sq = tm.sum(sq);
+      if (!(cur * (fn - fy) > cur * dv + 0.5f * sq)) break;
+      cur = cur * 0.5f;
+      for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
+      tm.sync();
+    }
+    const float nss = cur <= 1e-6f ? 1.f : cur / 0.5f;
+    const float nt = 0.5f * (1.f + sqrtf(1.f + 4.f * t * t));
+    const float beta = (t - 1.f) / nt;
+    for (int i = tm.lane; i < nrow; i += T) ny[i] = nx[i] + beta * (nx[i] - x[i]);
+    if (rec != nullptr) {
+      for (int i = tm.lane; i < nrow; i += T) rec[4 + 2 * kA + i] = (y[i] + (-cur) * gy[i]) > 0.f ? 1.f : 0.f;
+      if (tm.lane == 0) {
+        rec[0] = cur;
+        rec[1] = beta;
+      }
+    }
+    iters = it + 1;
+    resid(nx, r);
+    grad(r, gx);
+    matvecs += 2;
+    float es = 0.f;
+    for (int i = tm.lane; i < nrow; i += T) {
+      float e = fmaxf(nx[i] + (-1.f) * gx[i], 0.f) - nx[i];
+      es += e * e;
+      x[i] = nx[i];
+      y[i] = ny[i];
+    }
+    err = sqrtf(tm.sum(es));
+    tm.sync();
+    t = nt;
+    ss = nss;
+  }
+  for (int d = tm.lane; d < nv; d += T) {  // qf_constraint = J^T x
+    float s = 0.f;
+    for (int i = 0; i < nrow; ++i) s = fmaf(J[i * ldj + d], x[i], s);
+    qfc[d] = s;
+  }
+  if (tape != nullptr) {
+    for (int i = tm.lane; i < nrow; i += T) tape[4 + i] = x[i];
+    if (tm.lane == 0) {
+      tape[0] = (float)iters;
+      tape[1] = (float)nrow;
+    }
+  }
+  tm.sync();
+  return matvecs;
+}
+
+template <int T>
+__device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = nullptr) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
@@ -1162,9 +1338,15 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w) {
   float* qfc = w.at(L.qfc);
   if (nrow == 0) {
     for (int d = tm.lane; d < nv; d += T) qfc[d] = 0.f;
+    if (tape != nullptr && tm.lane == 0) {
+      tape[0] = 0.f;
+      tape[1] = 0.f;
+    }
     tm.sync();
     return 0;
   }
+  if (nrow <= kMaxExplicitRows) return pg_explicit<T>(md.w, w, nrow, tape);
+  if (tape != nullptr && tm.lane == 0) tape[0] = -1.f;  // too many rows for the taped path
   const int m = md.m;
   float* b = w.at(L.scr);
   float* x = b + al4(m);

@@ -1,0 +1,229 @@
+// Fused forward + reverse of an n-step rollout (the gradient of a loss on the
+// trajectory w.r.t. the actions and the initial state), checkpointed every
+// ckpt_every env steps with recompute.  One team of 32 lanes per env; the CTA
+// walks the stages in lockstep like the forward kernel.
+#pragma once
+#include "braxg_adjoint.cuh"
+#include "braxg_kernel.cuh"
+
+namespace braxg {
+
+
+
+template <int T, int NVB>
+__device__ __forceinline__ void fwd_frame(const int* mw, Ws w, bool active, bool has_act, float* tape, bool& ok) {
+  if (active) stage_smooth<T>(mw, w, has_act);
+  __syncthreads();
+  if (active) stage_constraint<T>(mw, w, tape);
+  __syncthreads();
+  if (active) ok = stage_integrate<T>(mw, w) && ok;
+  __syncthreads();
+}
+
+template <int T, int NVB>
+__device__ __forceinline__ bool pos_stage(const int* mw, Ws w, bool active) {
+  bool ok = true;
+  if (active) stage_fk<T>(mw, w);
+  __syncthreads();
+  if (active) stage_com<T>(mw, w);
+  __syncthreads();
+  if (active) stage_crba<T>(mw, w);
+  __syncthreads();
+  if (active) ok = stage_inverse<T, NVB>(mw, w, true, 0);
+  __syncthreads();
+  if (active) stage_jacobian<T>(mw, w);
+  __syncthreads();
+  return ok;
+}
+
+template <int T>
+__device__ __forceinline__ void copy_vec(const Team<T>& tm, float* dst, const float* src, int n) {
+  for (int i = tm.lane; i < n; i += T) dst[i] = src[i];
+}
+
+template <int T, int NVB>
+__global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
+  extern __shared__ __align__(16) int smem[];
+  for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
+  Layout* sl = reinterpret_cast<Layout*>(smem + al4(a.model_words));
+  AdjLayout* sal = reinterpret_cast<AdjLayout*>(smem + al4(a.model_words) + kLayoutWords);
+  if (threadIdx.x == 0) {
+    const int* w0 = a.model;
+    *sl = make_layout(w0[BXM_H_NL], w0[BXM_H_NQ], w0[BXM_H_NV], w0[BXM_H_NU], w0[BXM_H_NCON], w0[BXM_H_NLIM]);
+    *sal = make_adj_layout(w0[BXM_H_NL], w0[BXM_H_NQ], w0[BXM_H_NV], w0[BXM_H_NU], w0[BXM_H_NCON], w0[BXM_H_NLIM],
+                           w0[BXM_H_PG_ITERS]);
+  }
+  __syncthreads();
+  const int* mw = smem;
+  const Model md(mw);
+  const Team<T> tm;
+  const int team = threadIdx.x / T;
+  long long env = (long long)blockIdx.x * a.envs_per_cta + team;
+  const bool active = env < a.n_env;
+  if (!active) env = 0;
+  Ws w;
+  w.L = sl;
+  AWs aw;
+  aw.A = sal;
+  float* base = reinterpret_cast<float*>(smem + al4(a.model_words) + 2 * kLayoutWords);
+  w.b = base + (size_t)team * (sl->total + sal->total);
+  aw.b = w.b + sl->total;
+  const Layout& L = *sl;
+  const AdjLayout& A = *sal;
+  const int nq = md.nq, nv = md.nv, nu = md.nu;
+  const int S = nq + nv;
+  const long long n = a.n_env;
+  const bool has_act = a.act != nullptr && nu > 0;
+  bool ok = true, taped = true;
+  // ---- forward with checkpoints ----
+  if (active) {
+    copy_vec<T>(tm, w.at(L.q), a.q0 + env * nq, nq);
+    copy_vec<T>(tm, w.at(L.qd), a.qd0 + env * nv, nv);
+  }
+  tm.sync();
+  __syncthreads();
+  ok = pos_stage<T, NVB>(mw, w, active) && ok;
+  for (int s = 0; s < a.n_steps; ++s) {
+    if (active && s % a.ckpt_every == 0) {
+      float* c = a.ckpt + ((long long)(s / a.ckpt_every) * n + env) * S;
+      copy_vec<T>(tm, c, w.at(L.q), nq);
+      copy_vec<T>(tm, c + nq, w.at(L.qd), nv);
+    }
+    if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
+    tm.sync();
+    for (int f = 0; f < a.n_frames; ++f) {
+      fwd_frame<T, NVB>(mw, w, active, has_act, nullptr, ok);
+      ok = pos_stage<T, NVB>(mw, w, active) && ok;
+    }
+    if (active && a.traj_q != nullptr) copy_vec<T>(tm, a.traj_q + ((long long)s * n + env) * nq, w.at(L.q), nq);
+    if (active && a.traj_qd != nullptr) copy_vec<T>(tm, a.traj_qd + ((long long)s * n + env) * nv, w.at(L.qd), nv);
+  }
+  // ---- backward ----
+  float* qbo = aw.at(A.qbo);
+  float* qdbo = aw.at(A.qdbo);
+  if (active) {
+    for (int i = tm.lane; i < nq; i += T)
+      qbo[i] = a.q_bar ? a.q_bar[((long long)(a.n_steps - 1) * n + env) * nq + i] : 0.f;
+    for (int i = tm.lane; i < nv; i += T)
+      qdbo[i] = a.qd_bar ? a.qd_bar[((long long)(a.n_steps - 1) * n + env) * nv + i] : 0.f;
+  }
+  tm.sync();
+  const int n_ckpt = (a.n_steps + a.ckpt_every - 1) / a.ckpt_every;
+  for (int sg = n_ckpt - 1; sg >= 0; --sg) {
+    const int s0 = sg * a.ckpt_every;
+    const int s1 = min(s0 + a.ckpt_every, a.n_steps);
+    if (active) {
+      const float* c = a.ckpt + ((long long)sg * n + env) * S;
+      copy_vec<T>(tm, w.at(L.q), c, nq);
+      copy_vec<T>(tm, w.at(L.qd), c + nq, nv);
+    }
+    tm.sync();
+    __syncthreads();
+    pos_stage<T, NVB>(mw, w, active);
+    for (int s = s0; s < s1; ++s) {  // recompute the segment, keeping every frame's input state
+      if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
+      for (int f = 0; f < a.n_frames; ++f) {
+        if (active) {
+          float* sp = a.seg + ((long long)((s - s0) * a.n_frames + f) * n + env) * S;
+          copy_vec<T>(tm, sp, w.at(L.q), nq);
+          copy_vec<T>(tm, sp + nq, w.at(L.qd), nv);
+        }
+        tm.sync();
+        bool dummy = true;
+        fwd_frame<T, NVB>(mw, w, active, has_act, nullptr, dummy);
+        pos_stage<T, NVB>(mw, w, active);
+      }
+    }
+    for (int s = s1 - 1; s >= s0; --s) {
+      if (active) {
+        if (has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
+        for (int i = tm.lane; i < nu; i += T) aw.at(A.actb)[i] = 0.f;
+      }
+      tm.sync();
+      for (int f = a.n_frames - 1; f >= 0; --f) {
+        if (active) {
+          const float* sp = a.seg + ((long long)((s - s0) * a.n_frames + f) * n + env) * S;
+          copy_vec<T>(tm, w.at(L.q), sp, nq);
+          copy_vec<T>(tm, w.at(L.qd), sp + nq, nv);
+          copy_vec<T>(tm, aw.at(A.q0), sp, nq);
+          copy_vec<T>(tm, aw.at(A.qd0), sp + nq, nv);
+          // zero the accumulated adjoints of this step
+          for (int i = tm.lane; i < nq; i += T) aw.at(A.qb)[i] = 0.f;
+          for (int i = tm.lane; i < nv; i += T) aw.at(A.qdb)[i] = 0.f;
+          for (int i = tm.lane; i < 3 * md.nl; i += T) {
+            aw.at(A.xpb)[i] = 0.f;
+            aw.at(A.cpb)[i] = 0.f;
+            aw.at(A.rcb)[i] = 0.f;
+          }
+          for (int i = tm.lane; i < 4 * md.nl; i += T) aw.at(A.xrb)[i] = 0.f;
+          for (int i = tm.lane; i < 9 * md.nl; i += T) aw.at(A.cib)[i] = 0.f;
+          for (int i = tm.lane; i < 6 * md.nl; i += T) aw.at(A.cdb)[i] = 0.f;
+          for (int i = tm.lane; i < 6 * nv; i += T) {
+            aw.at(A.cdofb)[i] = 0.f;
+            aw.at(A.cdofdb)[i] = 0.f;
+          }
+        }
+        tm.sync();
+        __syncthreads();
+        pos_stage<T, NVB>(mw, w, active);
+        bool dummy = true;
+        fwd_frame<T, NVB>(mw, w, active, has_act, aw.at(A.tape), dummy);
+        if (active) rev_integrate<T>(mw, w, aw);
+        __syncthreads();
+        if (active) rev_qdd<T>(mw, w, aw);
+        __syncthreads();
+        if (active) taped = rev_constraint<T>(mw, w, aw) && taped;
+        __syncthreads();
+        if (active) rev_smooth<T>(mw, w, aw, has_act);
+        __syncthreads();
+        if (active) rev_inverse<T, NVB>(mw, w, aw);
+        __syncthreads();
+        if (active) rev_crba<T>(mw, w, aw);
+        __syncthreads();
+        if (active) rev_rows<T>(mw, w, aw);
+        __syncthreads();
+        if (active) rev_com<T>(mw, w, aw);
+        __syncthreads();
+        if (active) rev_fk<T>(mw, w, aw);
+        __syncthreads();
+        if (active) {
+          copy_vec<T>(tm, qbo, aw.at(A.qb), nq);
+          copy_vec<T>(tm, qdbo, aw.at(A.qdb), nv);
+        }
+        tm.sync();
+      }
+      if (active) {
+        if (a.act_bar != nullptr) copy_vec<T>(tm, a.act_bar + ((long long)s * n + env) * nu, aw.at(A.actb), nu);
+        if (s > 0) {
+          for (int i = tm.lane; i < nq; i += T)
+            if (a.q_bar) qbo[i] += a.q_bar[((long long)(s - 1) * n + env) * nq + i];
+          for (int i = tm.lane; i < nv; i += T)
+            if (a.qd_bar) qdbo[i] += a.qd_bar[((long long)(s - 1) * n + env) * nv + i];
+        }
+      }
+      tm.sync();
+    }
+  }
+  if (!active) return;
+  if (a.q0_bar != nullptr) copy_vec<T>(tm, a.q0_bar + env * nq, qbo, nq);
+  if (a.qd0_bar != nullptr) copy_vec<T>(tm, a.qd0_bar + env * nv, qdbo, nv);
+  if (a.status != nullptr && tm.lane == 0)
+    a.status[env] = (ok ? 0 : BRAXG_ENV_NOT_SPD) | (taped ? 0 : BRAXG_ENV_NO_GRADIENT);
+}
+
+template <int T, int NVB>
+cudaError_t launch_vjp(const VjpArgs& a, int grid, int smem, cudaStream_t st) {
+  auto k = vjp_kernel<T, NVB>;
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 64 && !attr_set[dev]) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr_set[dev] = true;
+  }
+  k<<<grid, a.envs_per_cta * T, smem, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace braxg

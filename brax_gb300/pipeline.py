@@ -237,3 +237,73 @@ def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = N
                                 ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta))),
           'braxg_rollout')
   return out, (tq, tqd)
+
+
+def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int = 1,
+                 ckpt_every: int = 16, trajectory: bool = False):
+  """Reverse-mode gradient of a rollout through the hand-written adjoint.
+
+  Replaces ``jax.grad`` through ``lax.scan`` of ``pipeline_step``
+  (brax/training/agents/apg/train.py:188-198).  ``q_bar`` / ``qd_bar``
+  [n_steps, n, nq|nv] are the loss cotangents of the state after every env step.
+  Returns (act_bar, q0_bar, qd0_bar, status, (traj_q, traj_qd)).
+  """
+  m = model_for(sys, q0.device)
+  q0 = _as_batch(q0, m.nq, 'q0', m.device)
+  qd0 = _as_batch(qd0, m.nv, 'qd0', m.device)
+  n = q0.shape[0]
+  act_seq = act_seq.to(torch.float32).contiguous()
+  if act_seq.dim() != 3 or act_seq.shape[1] != n or act_seq.shape[2] != m.nu:
+    raise ValueError(f'act_seq must be (n_steps, {n}, {m.nu})')
+  n_steps = act_seq.shape[0]
+  dev = m.device
+  f = lambda *s: torch.zeros(*s, dtype=torch.float32, device=dev)
+  qb = None if q_bar is None else q_bar.to(torch.float32).contiguous()
+  qdb = None if qd_bar is None else qd_bar.to(torch.float32).contiguous()
+  act_bar, q0_bar, qd0_bar = f(n_steps, n, m.nu), f(n, m.nq), f(n, m.nv)
+  tq = tqd = None
+  if trajectory:
+    tq, tqd = f(n_steps, n, m.nq), f(n_steps, n, m.nv)
+  status = torch.zeros(n, dtype=torch.int32, device=dev)
+  nbytes = ctypes.c_size_t()
+  lib = N.lib()
+  N.check(lib.braxg_rollout_vjp_workspace(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
+                                          ctypes.byref(nbytes)), 'braxg_rollout_vjp_workspace')
+  ws = torch.empty(max(nbytes.value, 4), dtype=torch.uint8, device=dev)
+  stream = torch.cuda.current_stream(dev).cuda_stream
+  N.check(lib.braxg_rollout_vjp(
+      m.handle, ctypes.c_void_p(stream), n, n_steps, int(n_frames), int(ckpt_every),
+      act_seq.data_ptr() if m.nu else None, q0.data_ptr(), qd0.data_ptr(), _ptr(qb), _ptr(qdb),
+      act_bar.data_ptr() if m.nu else None, q0_bar.data_ptr(), qd0_bar.data_ptr(), _ptr(tq),
+      _ptr(tqd), ws.data_ptr(), nbytes.value, status.data_ptr(),
+      ctypes.byref(_opts(CHOLESKY, 0, 0))), 'braxg_rollout_vjp')
+  return act_bar, q0_bar, qd0_bar, status, (tq, tqd)
+
+
+class Rollout(torch.autograd.Function):
+  """Differentiable rollout for torch: (q0, qd0, act_seq) -> (traj_q, traj_qd).
+
+  The forward runs braxg_rollout (exact-inverse mode); the backward runs the
+  checkpointed hand-written adjoint (braxg_rollout_vjp).
+  """
+
+  @staticmethod
+  def forward(ctx, q0, qd0, act_seq, sys, n_frames, ckpt_every):
+    s = init(sys, q0, qd0)
+    _, (tq, tqd) = rollout(sys, s, act_seq, n_frames=n_frames, inverse_mode=CHOLESKY,
+                           trajectory=True)
+    ctx.save_for_backward(q0, qd0, act_seq)
+    ctx.sys, ctx.n_frames, ctx.ckpt_every = sys, n_frames, ckpt_every
+    return tq, tqd
+
+  @staticmethod
+  def backward(ctx, gq, gqd):
+    q0, qd0, act_seq = ctx.saved_tensors
+    act_bar, q0_bar, qd0_bar, _, _ = rollout_grad(
+        ctx.sys, q0, qd0, act_seq, gq, gqd, n_frames=ctx.n_frames, ckpt_every=ctx.ckpt_every)
+    return q0_bar, qd0_bar, act_bar, None, None, None
+
+
+def differentiable_rollout(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16):
+  """torch.autograd-enabled rollout returning (traj_q, traj_qd)."""
+  return Rollout.apply(q0, qd0, act_seq, sys, n_frames, ckpt_every)

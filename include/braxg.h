@@ -49,7 +49,8 @@ enum braxg_inverse_mode {
 /* Per-env status bits written to braxg_state.status. */
 enum braxg_env_flags {
   BRAXG_ENV_NONFINITE = 1,   /* q or qd not finite after the call */
-  BRAXG_ENV_NOT_SPD = 2      /* a Cholesky pivot was <= 0 */
+  BRAXG_ENV_NOT_SPD = 2,     /* a Cholesky pivot was <= 0 */
+  BRAXG_ENV_NO_GRADIENT = 4  /* a step ran more than 32 active constraint rows: no gradient */
 };
 
 typedef struct {
@@ -129,6 +130,29 @@ int braxg_rollout(const braxg_model* model, void* stream, int n_env, int n_steps
                   int n_frames, const float* act_seq, const braxg_state* in,
                   braxg_state* out, float* traj_q, float* traj_qd,
                   const braxg_options* opt);
+
+/* Device workspace braxg_rollout_vjp needs: the checkpoints (every
+ * ckpt_every env steps) and the per-frame states of one recomputed segment. */
+int braxg_rollout_vjp_workspace(const braxg_model* model, int n_env, int n_steps, int n_frames,
+                                int ckpt_every, size_t* bytes);
+
+/* Gradient of a rollout (the reverse of braxg_rollout), the replacement for
+ * jax.grad through lax.scan of pipeline_step (brax/training/agents/apg/
+ * train.py:188-198).  Runs the forward from (q0, qd0) with act_seq
+ * [n_steps, n, nu], checkpointing every ckpt_every env steps, then the
+ * hand-written reverse of every pipeline step with recompute.  q_bar / qd_bar
+ * [n_steps, n, nq|nv] are the loss cotangents of the state after each env step
+ * (NULL = zero); outputs are act_bar [n_steps, n, nu], q0_bar [n, nq],
+ * qd0_bar [n, nv] and, optionally, the forward trajectory traj_q / traj_qd.
+ * The mass-matrix inverse is exact (Cholesky); status bits as braxg_env_flags.
+ * Supports hinge/slide/free joints, world-plane sphere and capsule contacts and
+ * joint limits; envs whose steps exceed 32 active constraint rows get
+ * BRAXG_ENV_NO_GRADIENT. */
+int braxg_rollout_vjp(const braxg_model* model, void* stream, int n_env, int n_steps, int n_frames,
+                      int ckpt_every, const float* act_seq, const float* q0, const float* qd0,
+                      const float* q_bar, const float* qd_bar, float* act_bar, float* q0_bar,
+                      float* qd0_bar, float* traj_q, float* traj_qd, void* workspace,
+                      size_t workspace_bytes, int32_t* status, const braxg_options* opt);
 
 /* Launch shape the tuner picks for this model: lanes per env, envs per CTA,
  * dynamic shared memory bytes per CTA. */
