@@ -53,6 +53,7 @@ def parse():
   p.add_argument('--envs-per-cta', type=int, default=0)
   p.add_argument('--cpu-sample-envs', type=int, default=256)
   p.add_argument('--no-cpu-baseline', action='store_true')
+  p.add_argument('--no-adjoint', action='store_true')
   return p.parse_args()
 
 
@@ -321,6 +322,7 @@ def run_braxg(args):
               'bytes_per_launch': b_step * n, 'peak_source': 'MEASURED_PEAKS.json hbm_gbs (of measured)'},
   }
   clocks = clk.summary()
+  adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank)
   out = {
       'metric': METRIC, 'value': round(value, 1), 'unit': 'env-steps/s', 'n_gpus': world,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
@@ -334,6 +336,7 @@ def run_braxg(args):
                                           model.launch_shape(mode, args.threads_per_env,
                                                              args.envs_per_cta)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
+      'adjoint': adjoint,
       'env_status_nonzero': int((status != 0).sum()),
   }
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -342,6 +345,52 @@ def run_braxg(args):
     dist.destroy_process_group()
   if rank == 0:
     print(json.dumps(out))
+
+
+def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16, reps=3):
+  """Forward rollout vs fused forward + adjoint (the APG workload): quadruped,
+  512 envs, 128 env steps of 5 frames, loss -mean(torso x-velocity) +
+  1e-3 sum |u|^2, gradients w.r.t. the actions and qd0, checkpoint every 16."""
+  rng = np.random.default_rng(55 + rank)
+  q0 = torch.tensor((sys_.init_q + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))).astype(np.float32), device=dev)
+  qd0 = torch.tensor((0.1 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32), device=dev)
+  u = torch.tensor(rng.uniform(-1, 1, (horizon, n, sys_.act_size())).astype(np.float32), device=dev)
+  qd_bar = torch.zeros(horizon, n, sys_.qd_size(), device=dev)
+  qd_bar[:, :, 0] = -1.0 / horizon
+  stream = torch.cuda.current_stream(dev)
+
+  def timed(fn):
+    fn()
+    torch.cuda.synchronize()
+    best = []
+    for _ in range(reps):
+      e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+      e0.record(stream)
+      fn()
+      e1.record(stream)
+      torch.cuda.synchronize()
+      best.append(e0.elapsed_time(e1) / 1e3)
+    return statistics.median(best)
+
+  def fwd():
+    s = pipeline.init(sys_, q0, qd0)
+    pipeline.rollout(sys_, s, u, n_frames=N_FRAMES, inverse_mode=pipeline.CHOLESKY, trajectory=True)
+
+  status = [None]
+
+  def fwd_adj():
+    r = pipeline.rollout_grad(sys_, q0, qd0, u, None, qd_bar, n_frames=N_FRAMES, ckpt_every=ckpt)
+    status[0] = r[3]
+
+  t_f = timed(fwd)
+  t_b = timed(fwd_adj)
+  bad = int((status[0] != 0).sum().item())
+  return {'workload': f'quadruped, {n} envs, {horizon} env steps x {N_FRAMES} frames, checkpoint every {ckpt}',
+          'fwd_env_steps_per_s': round(n * horizon / t_f, 1),
+          'fwd_adj_env_steps_per_s': round(n * horizon / t_b, 1),
+          'fwd_ms': round(1e3 * t_f, 3), 'fwd_adj_ms': round(1e3 * t_b, 3),
+          'cost_ratio_fwd_adj_over_fwd': round(t_b / t_f, 3),
+          'envs_without_gradient': bad, 'gpu_launches_fwd_adj': 1}
 
 
 def run_reference(args):
