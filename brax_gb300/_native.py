@@ -20,8 +20,9 @@ STATE_FIELDS = (
 
 EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims',
            'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_rollout_vjp_workspace',
-           'braxg_rollout_vjp', 'braxg_launch_shape', 'braxg_last_launch_count',
-           'braxg_last_error')
+           'braxg_rollout_vjp', 'braxg_rollout_vjp_noalloc',
+           'braxg_rollout_vjp_noalloc_capacity', 'braxg_launch_shape',
+           'braxg_last_launch_count', 'braxg_last_error')
 
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED = 0, 1, 2, 3
 INV_NEWTON_SCHULZ, INV_CHOLESKY = 0, 1
@@ -73,12 +74,17 @@ def lib() -> ctypes.CDLL:
     l.braxg_rollout_vjp_workspace.argtypes = [vp, i32, i32, i32, i32, P(ctypes.c_size_t)]
     l.braxg_rollout_vjp.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp,
                                     vp, vp, vp, ctypes.c_size_t, vp, P(Options)]
+    l.braxg_rollout_vjp_noalloc.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp,
+                                            vp, vp, vp, vp, vp, P(Options)]
+    l.braxg_rollout_vjp_noalloc_capacity.restype = ctypes.c_size_t
+    l.braxg_rollout_vjp_noalloc_capacity.argtypes = []
     l.braxg_launch_shape.argtypes = [vp, P(Options), P(ctypes.c_int32), P(ctypes.c_int32),
                                      P(ctypes.c_int32)]
     l.braxg_last_error.restype = ctypes.c_char_p
     l.braxg_last_launch_count.restype = ctypes.c_int
     for n in EXPORTS:
-      if n not in ('braxg_last_error', 'braxg_last_launch_count'):
+      if n not in ('braxg_last_error', 'braxg_last_launch_count',
+                   'braxg_rollout_vjp_noalloc_capacity'):
         getattr(l, n).restype = ctypes.c_int
     _lib = l
     return l

@@ -4,6 +4,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -315,6 +316,56 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
   if (e != cudaSuccess) return cuda_fail(e, "gradient kernel launch");
   g_launches = 1;
   return BRAXG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free rollout gradient.  The checkpoint / segment workspace of
+// braxg_rollout_vjp lives in one fixed device array of this library, so the
+// caller passes only its inputs and outputs and nothing here allocates.  Each
+// device that loads the library holds the array until the process exits.
+// ---------------------------------------------------------------------------
+static constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB
+static __device__ __align__(256) unsigned char g_vjp_scratch[kNoAllocScratchBytes];
+static std::mutex g_scratch_mu;
+static void* g_scratch_addr[64] = {nullptr};  // device address of g_vjp_scratch, per device
+
+size_t braxg_rollout_vjp_noalloc_capacity(void) { return kNoAllocScratchBytes; }
+
+int braxg_rollout_vjp_noalloc(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames,
+                              int ckpt_every, const float* act_seq, const float* q0, const float* qd0,
+                              const float* q_bar, const float* qd_bar, float* act_bar, float* q0_bar,
+                              float* qd0_bar, float* traj_q, float* traj_qd, int32_t* status,
+                              const braxg_options* opt) {
+  size_t need = 0;
+  int rc = braxg_rollout_vjp_workspace(m, n_env, n_steps, n_frames, ckpt_every, &need);
+  if (rc) return rc;
+  if (need > kNoAllocScratchBytes)
+    return fail(BRAXG_ERR_INVALID,
+                "braxg_rollout_vjp_noalloc: %d envs x %d steps x %d frames (checkpoint every %d) need %zu bytes "
+                "of scratch; the fixed array holds %zu bytes (pass a workspace to braxg_rollout_vjp instead)",
+                n_env, n_steps, n_frames, ckpt_every, need, kNoAllocScratchBytes);
+  if (m->device < 0 || m->device >= 64) return fail(BRAXG_ERR_INVALID, "device ordinal %d out of range", m->device);
+  void* scratch = nullptr;
+  {
+    // first call on a device: look up the array's device address with that
+    // device current (once; later calls reuse it)
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (g_scratch_addr[m->device] == nullptr) {
+      int cur = 0;
+      cudaGetDevice(&cur);
+      cudaError_t e = cudaSetDevice(m->device);
+      void* addr = nullptr;
+      if (e == cudaSuccess) e = cudaGetSymbolAddress(&addr, g_vjp_scratch);
+      cudaSetDevice(cur);
+      if (e != cudaSuccess) return cuda_fail(e, "braxg_rollout_vjp_noalloc: cudaGetSymbolAddress");
+      g_scratch_addr[m->device] = addr;
+    }
+    scratch = g_scratch_addr[m->device];
+  }
+  // Every word of the checkpoint / segment workspace is written before it is
+  // read, so the array's previous contents need no clearing.
+  return braxg_rollout_vjp(m, stream, n_env, n_steps, n_frames, ckpt_every, act_seq, q0, qd0, q_bar, qd_bar,
+                           act_bar, q0_bar, qd0_bar, traj_q, traj_qd, scratch, kNoAllocScratchBytes, status, opt);
 }
 
 int braxg_step(const braxg_model* m, void* stream, int n_env, int n_frames, const float* act, const braxg_state* in,

@@ -154,6 +154,27 @@ int braxg_rollout_vjp(const braxg_model* model, void* stream, int n_env, int n_s
                       float* qd0_bar, float* traj_q, float* traj_qd, void* workspace,
                       size_t workspace_bytes, int32_t* status, const braxg_options* opt);
 
+/* braxg_rollout_vjp without a workspace argument, for callers that cannot
+ * allocate device memory: an XLA custom call registered without access to the
+ * scratch allocator, a plugin whose host framework owns every device
+ * allocation, or a control loop that must not enter the CUDA allocator.  The
+ * checkpoint / segment scratch is one fixed 8 MiB array inside this library
+ * (braxg_rollout_vjp_noalloc_capacity() bytes), held by every device that
+ * loads the library until the process exits; requests needing more
+ * (braxg_rollout_vjp_workspace) fail with BRAXG_ERR_INVALID.  Nothing is
+ * allocated or freed.  The first call on a device looks up the array's device
+ * address with that device current, so make one call on each device before
+ * any stream capture.  All calls share the one array: calls that overlap on
+ * the GPU (different streams, or different threads without ordering) race on
+ * it and corrupt each other's gradients.  No counterpart in the reference: it
+ * exists only for callers that cannot allocate. */
+size_t braxg_rollout_vjp_noalloc_capacity(void);
+int braxg_rollout_vjp_noalloc(const braxg_model* model, void* stream, int n_env, int n_steps,
+                              int n_frames, int ckpt_every, const float* act_seq, const float* q0,
+                              const float* qd0, const float* q_bar, const float* qd_bar,
+                              float* act_bar, float* q0_bar, float* qd0_bar, float* traj_q,
+                              float* traj_qd, int32_t* status, const braxg_options* opt);
+
 /* Launch shape the tuner picks for this model: lanes per env, envs per CTA,
  * dynamic shared memory bytes per CTA. */
 int braxg_launch_shape(const braxg_model* model, const braxg_options* opt,
