@@ -48,7 +48,7 @@ def parse():
   p.add_argument('--warmup', type=int, default=10)
   p.add_argument('--impl', default='braxg', choices=['braxg', 'reference'])
   p.add_argument('--envs', type=int, default=4096)
-  p.add_argument('--inverse', default='newton_schulz', choices=['newton_schulz', 'cholesky'])
+  p.add_argument('--inverse', default='cholesky', choices=['newton_schulz', 'cholesky'])
   p.add_argument('--threads-per-env', type=int, default=0)
   p.add_argument('--envs-per-cta', type=int, default=0)
   p.add_argument('--cpu-sample-envs', type=int, default=256)
@@ -62,7 +62,7 @@ def parse():
 # ---------------------------------------------------------------------------
 
 
-def algorithmic(sys_, n_mv: float):
+def algorithmic(sys_, n_mv: float, carried_minv: bool = True):
   nl, nv, nq, nu = sys_.num_links(), sys_.qd_size(), sys_.q_size(), sys_.act_size()
   ncon = sys_.contacts.n
   m = sys_.n_constraint_rows()
@@ -73,8 +73,31 @@ def algorithmic(sys_, n_mv: float):
   f_pg = 2 * m * m * n_mv
   f_tail = 2 * m * nv + 4 * nv * nv
   flops = f_tree + f_m + f_fact + f_a + f_pg + f_tail
-  bytes_env_step = 4 * (nq + nv + nu) + 4 * (nq + nv + 13 * nl) + 2 * 4 * nv * nv
+  # state in/out + actions + link outputs, plus mass_mx_inv written (and read
+  # back when it is carried, Newton-Schulz mode)
+  bytes_env_step = 4 * (nq + nv + nu) + 4 * (nq + nv + 13 * nl) + (2 if carried_minv else 1) * 4 * nv * nv
   return flops, bytes_env_step
+
+
+def profiled_traffic(kernel: str):
+  """DRAM bytes (read + write) per launch of `kernel` on this workload, from the
+  committed ncu summary profiles/<kernel>_quadruped_4096.md (a line
+  `traffic_bytes_per_launch: N`); None when no summary is present."""
+  path = os.path.join(ROOT, 'profiles', f'{kernel}_quadruped_4096.md')
+  try:
+    with open(path) as f:
+      for line in f:
+        if line.strip().startswith('traffic_bytes_per_launch:'):
+          return int(float(line.split(':', 1)[1]))
+  except OSError:
+    pass
+  return None
+
+
+def workload_config(n: int, world: int):
+  return {'workload': f'{WORKLOAD} nq 15 nv 14 nu 8, 9 geoms vs plane (17 contact slots), '
+                      f'{n} envs per GPU, env step = {N_FRAMES} x 0.01 s',
+          'envs_per_gpu': n, 'n_frames': N_FRAMES, 'parallelism': f'replicas x{world}'}
 
 
 def load_nmv():
@@ -257,11 +280,12 @@ def run_braxg(args):
   h_obs = torch.empty(n, sys_.q_size() + sys_.qd_size(), dtype=torch.float32).pin_memory()
   d_act = torch.empty(n, sys_.act_size(), dtype=torch.float32, device=dev)
   obs = torch.empty(n, sys_.q_size() + sys_.qd_size(), dtype=torch.float32, device=dev)
-  st = s0
+  # the same trajectory segment as the device-timed loop: a fresh reset, the
+  # same warm-up steps, then the timed steps with the actions read from host
+  st = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
   st2 = pipeline._alloc(model, n, False, dev)
-  for k in range(min(args.warmup, 5)):
-    d_act.copy_(h_act[k], non_blocking=True)
-    pipeline.step(sys_, st, d_act, n_frames=N_FRAMES, out=st2, **kw)
+  for k in range(args.warmup):
+    pipeline.step(sys_, st, acts[k], n_frames=N_FRAMES, out=st2, **kw)
     st, st2 = st2, st
   torch.cuda.synchronize()
   if world > 1:
@@ -297,7 +321,7 @@ def run_braxg(args):
 
   # ---- roofline -----------------------------------------------------------
   nmv = load_nmv()[WORKLOAD]
-  f_step, b_step = algorithmic(sys_, nmv['mean_matvecs_per_step'])
+  f_step, b_step = algorithmic(sys_, nmv['mean_matvecs_per_step'], args.inverse == 'newton_schulz')
   launch_s = t_total / args.steps
   flops_launch = f_step * N_FRAMES * n
   achieved = flops_launch / launch_s / 1e12
@@ -313,7 +337,8 @@ def run_braxg(args):
   hbm_peak = peaks.get('hbm_gbs', 6800.0)
   roofline = {
       'bound': 'fp32', 'achieved': round(achieved, 3), 'peak': round(peak_fp32, 1),
-      'unit': 'TFLOP/s', 'frac': round(achieved / peak_fp32, 4), 'traffic': None,
+      'unit': 'TFLOP/s', 'frac': round(achieved / peak_fp32, 4),
+      'traffic': profiled_traffic('step_kernel'),
       'peak_source': (f'nominal FP32 CUDA-core peak ({props.multi_processor_count} SMs x 128 '
                       f'FMA/clk x 2 x {sm_max:.0f} MHz); MEASURED_PEAKS.json has no FP32 figure'),
       'flops_per_launch': flops_launch,
@@ -328,10 +353,9 @@ def run_braxg(args):
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded resets and U(-1,1) actions)',
-      'config': {'workload': f'{WORKLOAD} nq 15 nv 14 nu 8, 9 geoms vs plane (17 contact slots), '
-                             f'{n} envs per GPU, env step = {N_FRAMES} x 0.01 s',
-                 'envs_per_gpu': n, 'n_frames': N_FRAMES, 'inverse_mode': args.inverse,
-                 'parallelism': f'replicas x{world}', 'l2': 'flushed (256 MB write) before every timed step',
+      'config': {**workload_config(n, world),
+                 'inverse_mode': args.inverse,
+                 'l2': 'flushed (256 MB write) before every timed step',
                  'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
                                           model.launch_shape(mode, args.threads_per_env,
                                                              args.envs_per_cta)))},
@@ -410,7 +434,8 @@ def run_reference(args):
       'steps': len(vals), 'warmup': 0, 'ms_per_step': None, 'higher_is_better': True,
       'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
       'impl': 'reference',
-      'config': {'workload': f'{WORKLOAD}, {N_FRAMES} frames per env step, CPU sample'},
+      'config': {**workload_config(args.envs, world), 'inverse_mode': 'newton_schulz (the reference algorithm)',
+                 'sample': cb['sample']},
       'cpu_baseline': cb,
       'e2e': {'value': round(value, 2), 'unit': 'env-steps/s', 'h2d_bytes_per_step': 0,
               'd2h_bytes_per_step': 0},
