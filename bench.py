@@ -54,6 +54,7 @@ def parse():
   p.add_argument('--cpu-sample-envs', type=int, default=256)
   p.add_argument('--no-cpu-baseline', action='store_true')
   p.add_argument('--no-adjoint', action='store_true')
+  p.add_argument('--no-uneven', action='store_true')
   return p.parse_args()
 
 
@@ -348,6 +349,7 @@ def run_braxg(args):
   }
   clocks = clk.summary()
   adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank)
+  uneven = None if args.no_uneven else bench_uneven(torch, dev, rank)
   out = {
       'metric': METRIC, 'value': round(value, 1), 'unit': 'env-steps/s', 'n_gpus': world,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
@@ -360,7 +362,7 @@ def run_braxg(args):
                                           model.launch_shape(mode, args.threads_per_env,
                                                              args.envs_per_cta)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
-      'adjoint': adjoint,
+      'adjoint': adjoint, 'uneven': uneven,
       'env_status_nonzero': int((status != 0).sum()),
   }
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -415,6 +417,73 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
           'fwd_ms': round(1e3 * t_f, 3), 'fwd_adj_ms': round(1e3 * t_b, 3),
           'cost_ratio_fwd_adj_over_fwd': round(t_b / t_f, 3),
           'envs_without_gradient': bad, 'gpu_launches_fwd_adj': 1}
+
+
+def bench_uneven(torch, dev, rank, total=8192, n_steps=256):
+  """The uneven batch: 8192 envs (60 % hinge chains of U{2..32} links with the
+  last link against a plane, 25 % quadrupeds, 15 % humanoid-like), 256 env
+  steps, shapes from the autotuner; timed as one persistent launch of all 256
+  steps and as 256 per-step launches captured in one CUDA graph."""
+  from brax_gb300 import autotune, workloads as W
+  from brax_gb300.batch import Batch, GraphRollout
+  mix = W.uneven_mix(total, seed=rank)
+  systems, n_env, n_frames = [m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix]
+  t0 = time.perf_counter()
+  shapes = autotune.tune_batch(systems, n_env, n_frames, device=dev)
+  tune_s = time.perf_counter() - t0
+  b = Batch(systems, n_env, n_frames, shapes=shapes, device=dev)
+  rng = np.random.default_rng(900 + rank)
+  qs, qds, acts = [], [], []
+  for s, n, _ in mix:
+    q, qd = W.reset(s, n, rng)
+    qs.append(q)
+    qds.append(qd)
+    acts.append(np.stack([W.actions(s, n, rng) for _ in range(n_steps)]).astype(np.float32))
+  table = b.concat_steps(acts, 'act')
+  s0 = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
+  stream = torch.cuda.current_stream(dev)
+  out = b.alloc()
+  b.rollout(s0, table[:4], out=out)  # warm-up
+  torch.cuda.synchronize()
+  e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+  e0.record(stream)
+  b.rollout(s0, table, out=out)
+  e1.record(stream)
+  torch.cuda.synchronize()
+  t_one = e0.elapsed_time(e1) / 1e3
+  bad = int((out.status != 0).sum().item())
+  bad_by_family = {}
+  for (s, _, _), st in zip(mix, b.split(out.status, 'status')):
+    st = st.cpu().numpy()
+    k = W.family(s)
+    e = bad_by_family.setdefault(k, {'nonfinite': 0, 'not_spd': 0})
+    e['nonfinite'] += int(((st & 1) != 0).sum())
+    e['not_spd'] += int(((st & 2) != 0).sum())
+
+  def policy(k, state, act):
+    act.copy_(table[k])
+
+  g = GraphRollout(b, s0, n_steps, policy)
+  for f in ('q', 'qd', 'mass_mx_inv'):
+    getattr(g.state, f).copy_(getattr(s0, f))
+  torch.cuda.synchronize()
+  e0.record(stream)
+  g.replay()
+  e1.record(stream)
+  torch.cuda.synchronize()
+  t_graph = e0.elapsed_time(e1) / 1e3
+  fam = {}
+  for s, n, f in mix:
+    k = W.family(s)
+    fam[k] = fam.get(k, 0) + n
+  return {'workload': f'{total} envs: ' + ', '.join(f'{n} {k}' for k, n in fam.items()) +
+                      f' ({len(mix)} models, nv 2-32), {n_steps} env steps (chains 1 frame, others 5)',
+          'env_steps_per_s_one_launch': round(total * n_steps / t_one, 1),
+          'env_steps_per_s_graph': round(total * n_steps / t_graph, 1),
+          'ms_one_launch': round(1e3 * t_one, 3), 'ms_graph': round(1e3 * t_graph, 3),
+          'graph_nodes_per_step': 3, 'shapes': shapes, 'launch': b.launch_info(),
+          'autotune_s': round(tune_s, 2), 'env_status_nonzero': bad,
+          'env_status_by_family': bad_by_family}
 
 
 def run_reference(args):

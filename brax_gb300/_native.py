@@ -22,11 +22,13 @@ EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims',
            'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_rollout_vjp_workspace',
            'braxg_rollout_vjp', 'braxg_rollout_vjp_noalloc',
            'braxg_rollout_vjp_noalloc_capacity', 'braxg_launch_shape',
+           'braxg_batch_create', 'braxg_batch_destroy', 'braxg_batch_get_offsets',
+           'braxg_batch_launch_info', 'braxg_batch_init', 'braxg_batch_rollout',
            'braxg_last_launch_count', 'braxg_last_error')
 
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED = 0, 1, 2, 3
 INV_NEWTON_SCHULZ, INV_CHOLESKY = 0, 1
-ENV_NONFINITE, ENV_NOT_SPD, ENV_NO_GRADIENT = 1, 2, 4
+ENV_NONFINITE, ENV_NOT_SPD, ENV_NO_GRADIENT, ENV_SKIPPED = 1, 2, 4, 8
 
 
 class State(ctypes.Structure):
@@ -43,9 +45,24 @@ class Options(ctypes.Structure):
               ('stage_cycles', ctypes.c_void_p)]
 
 
+class BucketShape(ctypes.Structure):
+  _fields_ = [('nv_max', ctypes.c_int32), ('threads_per_env', ctypes.c_int32),
+              ('envs_per_cta', ctypes.c_int32), ('reserved', ctypes.c_int32)]
+
+
+OFFSET_FIELDS = ('env', 'q', 'qd', 'mass_mx', 'link', 'act', 'row', 'jac')
+
+
+class BatchOffsets(ctypes.Structure):
+  _fields_ = [(n, ctypes.c_int64) for n in OFFSET_FIELDS]
+
+
 PROFILE_SLOTS = ('fk', 'com', 'crba', 'inverse', 'jacobian', 'smooth', 'constraint',
                  'integrate', 'io', 'matvecs', 'rows', 'ns_resets', 'substeps')
-N_PROFILE_SLOTS = 16
+VJP_PROFILE_SLOTS = {16: 'checkpoint_pass', 17: 'segment_recompute', 18: 'restore',
+                     19: 'rev_integrate', 20: 'rev_qdd', 21: 'rev_constraint', 22: 'rev_smooth',
+                     23: 'rev_inverse', 24: 'rev_crba', 25: 'rev_rows', 26: 'rev_com', 27: 'rev_fk'}
+N_PROFILE_SLOTS = 32
 
 
 _lib = None
@@ -80,6 +97,14 @@ def lib() -> ctypes.CDLL:
     l.braxg_rollout_vjp_noalloc_capacity.argtypes = []
     l.braxg_launch_shape.argtypes = [vp, P(Options), P(ctypes.c_int32), P(ctypes.c_int32),
                                      P(ctypes.c_int32)]
+    l.braxg_batch_create.argtypes = [P(vp), P(ctypes.c_int32), P(ctypes.c_int32), i32,
+                                     P(BucketShape), i32, ctypes.c_int32, P(vp)]
+    l.braxg_batch_destroy.argtypes = [vp]
+    l.braxg_batch_get_offsets.argtypes = [vp, i32, P(BatchOffsets)]
+    l.braxg_batch_launch_info.argtypes = [vp, P(ctypes.c_int32), P(ctypes.c_int32),
+                                          P(ctypes.c_int32), P(ctypes.c_int32)]
+    l.braxg_batch_init.argtypes = [vp, vp, vp, vp, P(State), P(Options)]
+    l.braxg_batch_rollout.argtypes = [vp, vp, i32, vp, P(State), P(State), vp, vp, P(Options)]
     l.braxg_last_error.restype = ctypes.c_char_p
     l.braxg_last_launch_count.restype = ctypes.c_int
     for n in EXPORTS:

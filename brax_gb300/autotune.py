@@ -1,0 +1,161 @@
+"""Launch-shape autotuner: lanes per env and envs per CTA for each nv bucket.
+
+For every nv bucket present in a batch (nv <= 8, 16, 32, 64) the tuner builds
+a batch of that bucket's models alone (with their env counts), times a short
+rollout of it for every candidate shape with CUDA events, and keeps the
+fastest.  Results are cached in a JSON file keyed by the GPU name, the bucket
+and the bucket's models and env counts, so a later process with the same batch
+reads them instead of timing again.  The cache lives next to the built library
+(``brax_gb300/_lib/autotune.json``) unless ``BRAXG_TUNE_CACHE`` names another
+file.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import threading
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from brax_gb300 import _native as N
+from brax_gb300 import model_pack
+from brax_gb300 import pipeline as P
+
+BUCKETS = (8, 16, 32, 64)
+# per-CTA shared memory of the tuned launch: two CTAs per SM, as the batch
+# default; shapes are timed under the same limit so that the combined launch
+# (which takes the largest group's CTA size) keeps two CTAs per SM
+SMEM_PER_CTA = 113 * 1024
+_lock = threading.Lock()
+
+
+def cache_path() -> str:
+  return os.environ.get('BRAXG_TUNE_CACHE') or os.path.join(N.LIB_DIR, 'autotune.json')
+
+
+def bucket_of(nv: int) -> int:
+  for b in BUCKETS:
+    if nv <= b:
+      return b
+  raise NotImplementedError(f'nv {nv} is above the largest bucket {BUCKETS[-1]}')
+
+
+def candidates(bucket: int) -> List[Tuple[int, int]]:
+  """(threads_per_env, envs_per_cta) pairs; envs_per_cta 0 = fit 113 KB per CTA."""
+  out = []
+  lanes = (16, 32) if bucket <= 32 else (32,)
+  for t in lanes:
+    for e in (0, 2, 4, 6, 8) if t == 32 else (0, 4, 8, 12, 16):
+      out.append((t, e))
+  return out
+
+
+def _key(device: torch.device, bucket: int, systems, n_env, n_frames) -> str:
+  h = hashlib.sha1()
+  for s, n, f in zip(systems, n_env, n_frames):
+    h.update(model_pack.pack(s).tobytes())
+    h.update(np.asarray([n, f], np.int64).tobytes())
+  name = torch.cuda.get_device_name(device)
+  return f'{name}|nv<={bucket}|{h.hexdigest()[:16]}'
+
+
+def _load() -> Dict:
+  try:
+    with open(cache_path()) as f:
+      return json.load(f)
+  except (OSError, ValueError):
+    return {}
+
+
+def _store(table: Dict):
+  path = cache_path()
+  os.makedirs(os.path.dirname(path), exist_ok=True)
+  tmp = path + f'.{os.getpid()}.tmp'
+  with open(tmp, 'w') as f:
+    json.dump(table, f, indent=1, sort_keys=True)
+  os.replace(tmp, path)
+
+
+def _time_shape(systems, n_env, n_frames, shape, device, n_steps: int, reps: int, smem: int) -> float:
+  from brax_gb300.batch import Batch
+  from brax_gb300 import workloads as W
+  b = Batch(systems, n_env, n_frames, shapes=[(BUCKETS[-1], shape[0], shape[1])], smem_per_cta=smem,
+            device=device)
+  rng = np.random.default_rng(0)
+  qs, qds, acts = [], [], []
+  for s, n in zip(systems, n_env):
+    q, qd = W.reset(s, n, rng)
+    qs.append(q)
+    qds.append(qd)
+    acts.append(np.stack([W.actions(s, n, rng) for _ in range(n_steps)]))
+  state = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
+  act = b.concat_steps(acts, 'act') if b.totals['act'] else None
+  out = b.alloc()
+  b.rollout(state, act, n_steps, out=out)  # warm-up
+  stream = torch.cuda.current_stream(device)
+  times = []
+  for _ in range(reps):
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.rollout(state, act, n_steps, out=out)
+    e1.record(stream)
+    e1.synchronize()
+    times.append(e0.elapsed_time(e1))
+  return float(np.median(times))
+
+
+def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Sequence[int]] = None,
+               device=None, n_steps: int = 2, reps: int = 3, use_cache: bool = True,
+               verbose: bool = False) -> List[Tuple[int, int, int]]:
+  """Shapes [(nv_max, threads_per_env, envs_per_cta)] for ``Batch(shapes=...)``,
+  one per nv bucket present, each the fastest candidate for that bucket's
+  models timed alone."""
+  device = torch.device('cuda') if device is None else torch.device(device)
+  if device.index is None:
+    device = torch.device('cuda', torch.cuda.current_device())
+  n_frames = [1] * len(systems) if n_frames is None else list(n_frames)
+  groups: Dict[int, List[int]] = {}
+  for g, s in enumerate(systems):
+    if n_env[g] > 0:
+      groups.setdefault(bucket_of(s.qd_size()), []).append(g)
+  with _lock:
+    table = _load() if use_cache else {}
+  shapes = []
+  dirty = False
+  for bucket in sorted(groups):
+    idx = groups[bucket]
+    sys_b = [systems[g] for g in idx]
+    ne_b = [n_env[g] for g in idx]
+    nf_b = [n_frames[g] for g in idx]
+    key = _key(device, bucket, sys_b, ne_b, nf_b)
+    hit = table.get(key)
+    if hit is None:
+      results = {}
+      for smem in (SMEM_PER_CTA, 0):  # 0: models too large for two CTAs per SM
+        for shape in candidates(bucket):
+          try:
+            results[shape] = _time_shape(sys_b, ne_b, nf_b, shape, device, n_steps, reps, smem)
+          except (ValueError, NotImplementedError):
+            continue  # shape does not fit this bucket's models
+          if verbose:
+            print(f'nv<={bucket} threads {shape[0]} envs/cta {shape[1]}: {results[shape]:.3f} ms')
+        if results:
+          break
+      if not results:
+        raise NotImplementedError(f'no launch shape fits the nv<={bucket} models')
+      best = min(results, key=results.get)
+      hit = {'threads_per_env': best[0], 'envs_per_cta': best[1], 'ms': results[best],
+             'timed': {f'{t}x{e}': ms for (t, e), ms in results.items()}}
+      table[key] = hit
+      dirty = True
+    shapes.append((bucket, hit['threads_per_env'], hit['envs_per_cta']))
+  if dirty and use_cache:
+    with _lock:
+      merged = _load()
+      merged.update(table)
+      _store(merged)
+  return shapes

@@ -15,7 +15,7 @@ ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # one translation unit per group of kernel instantiations so they compile in
 # parallel; braxg.cu holds the C ABI
 UNITS = ['braxg.cu', 'inst_t32_nv16.cu', 'inst_t32_nv32.cu', 'inst_t32_nv64.cu',
-         'inst_t16.cu', 'inst_vjp_nv16.cu', 'inst_vjp_nv32.cu']
+         'inst_t16.cu', 'inst_vjp_nv16.cu', 'inst_vjp_nv32.cu', 'inst_batch.cu']
 
 
 def _nvcc():

@@ -70,37 +70,38 @@ __device__ __forceinline__ bool position_stage(const int* mw, Ws w, bool active,
 
 // Writes the State outputs of one env (out-of-line: runs once per launch).
 template <int T>
-__device__ __noinline__ void write_outputs(const StepArgs& a, const int* mw, Ws w, long long env, bool ok) {
+__device__ __noinline__ void write_outputs(const StepArgs& a, const EnvBase& B, const int* mw, Ws w, long long env,
+                                           bool ok) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
   const int nq = md.nq, nv = md.nv, nl = md.nl, ld = L.ldm;
   // outputs
   const braxg_state& o = a.out;
-  store_vec<T>(tm, o.q ? o.q + env * nq : nullptr, w.at(L.q), nq);
-  store_vec<T>(tm, o.qd ? o.qd + env * nv : nullptr, w.at(L.qd), nv);
-  store_mat<T>(tm, o.mass_mx_inv ? o.mass_mx_inv + env * nv * nv : nullptr, w.at(L.Minv), nv, ld);
-  store_mat<T>(tm, o.mass_mx ? o.mass_mx + env * nv * nv : nullptr, w.at(L.M), nv, ld);
-  store_vec<T>(tm, o.x_pos ? o.x_pos + env * nl * 3 : nullptr, w.at(L.xp), 3 * nl);
-  store_vec<T>(tm, o.x_rot ? o.x_rot + env * nl * 4 : nullptr, w.at(L.xr), 4 * nl);
-  store_vec<T>(tm, o.xd_ang ? o.xd_ang + env * nl * 3 : nullptr, w.at(L.xa), 3 * nl);
-  store_vec<T>(tm, o.xd_vel ? o.xd_vel + env * nl * 3 : nullptr, w.at(L.xv), 3 * nl);
-  store_vec<T>(tm, o.qf_smooth ? o.qf_smooth + env * nv : nullptr, w.at(L.qfs), nv);
-  store_vec<T>(tm, o.qf_constraint ? o.qf_constraint + env * nv : nullptr, w.at(L.qfc), nv);
-  store_vec<T>(tm, o.qdd ? o.qdd + env * nv : nullptr, w.at(L.qdd), nv);
-  store_vec<T>(tm, o.root_com ? o.root_com + env * nl * 3 : nullptr, w.at(L.rc), 3 * nl);
-  store_vec<T>(tm, o.cinr_pos ? o.cinr_pos + env * nl * 3 : nullptr, w.at(L.cp), 3 * nl);
-  store_vec<T>(tm, o.cinr_i ? o.cinr_i + env * nl * 9 : nullptr, w.at(L.ci), 9 * nl);
-  store_vec<T>(tm, o.cd ? o.cd + env * nl * 6 : nullptr, w.at(L.cd), 6 * nl);
-  store_vec<T>(tm, o.cdof ? o.cdof + env * nv * 6 : nullptr, w.at(L.cdof), 6 * nv);
-  store_vec<T>(tm, o.cdofd ? o.cdofd + env * nv * 6 : nullptr, w.at(L.cdofd), 6 * nv);
+  store_vec<T>(tm, o.q ? o.q + B.q + env * nq : nullptr, w.at(L.q), nq);
+  store_vec<T>(tm, o.qd ? o.qd + B.v + env * nv : nullptr, w.at(L.qd), nv);
+  store_mat<T>(tm, o.mass_mx_inv ? o.mass_mx_inv + B.vv + env * nv * nv : nullptr, w.at(L.Minv), nv, ld);
+  store_mat<T>(tm, o.mass_mx ? o.mass_mx + B.vv + env * nv * nv : nullptr, w.at(L.M), nv, ld);
+  store_vec<T>(tm, o.x_pos ? o.x_pos + 3 * B.l + env * nl * 3 : nullptr, w.at(L.xp), 3 * nl);
+  store_vec<T>(tm, o.x_rot ? o.x_rot + 4 * B.l + env * nl * 4 : nullptr, w.at(L.xr), 4 * nl);
+  store_vec<T>(tm, o.xd_ang ? o.xd_ang + 3 * B.l + env * nl * 3 : nullptr, w.at(L.xa), 3 * nl);
+  store_vec<T>(tm, o.xd_vel ? o.xd_vel + 3 * B.l + env * nl * 3 : nullptr, w.at(L.xv), 3 * nl);
+  store_vec<T>(tm, o.qf_smooth ? o.qf_smooth + B.v + env * nv : nullptr, w.at(L.qfs), nv);
+  store_vec<T>(tm, o.qf_constraint ? o.qf_constraint + B.v + env * nv : nullptr, w.at(L.qfc), nv);
+  store_vec<T>(tm, o.qdd ? o.qdd + B.v + env * nv : nullptr, w.at(L.qdd), nv);
+  store_vec<T>(tm, o.root_com ? o.root_com + 3 * B.l + env * nl * 3 : nullptr, w.at(L.rc), 3 * nl);
+  store_vec<T>(tm, o.cinr_pos ? o.cinr_pos + 3 * B.l + env * nl * 3 : nullptr, w.at(L.cp), 3 * nl);
+  store_vec<T>(tm, o.cinr_i ? o.cinr_i + 9 * B.l + env * nl * 9 : nullptr, w.at(L.ci), 9 * nl);
+  store_vec<T>(tm, o.cd ? o.cd + 6 * B.l + env * nl * 6 : nullptr, w.at(L.cd), 6 * nl);
+  store_vec<T>(tm, o.cdof ? o.cdof + 6 * B.v + env * nv * 6 : nullptr, w.at(L.cdof), 6 * nv);
+  store_vec<T>(tm, o.cdofd ? o.cdofd + 6 * B.v + env * nv * 6 : nullptr, w.at(L.cdofd), 6 * nv);
   if (o.cinr_rot != nullptr) {  // cinr.transform.rot = x_i.rot
     for (int l = tm.lane; l < nl; l += T) {
       f3 op;
       q4 orr;
       tf_do(ld3(w.at(L.xp) + 3 * l), ld4(w.at(L.xr) + 4 * l), ld3(md.F(BXM_O_LI_POS) + 3 * l),
             ld4(md.F(BXM_O_LI_ROT) + 4 * l), op, orr);
-      st4(o.cinr_rot + (env * nl + l) * 4, orr);
+      st4(o.cinr_rot + 4 * B.l + (env * nl + l) * 4, orr);
     }
   }
   if (o.con_jac != nullptr || o.con_diag != nullptr || o.con_aref != nullptr) {
@@ -116,13 +117,13 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const int* mw, Ws 
       for (long long idx = tm.lane; idx < (long long)m * nv; idx += T) {
         int r = (int)(idx / nv), d = (int)(idx - (long long)r * nv);
         int c = inv[r];
-        o.con_jac[env * m * nv + idx] = c >= 0 ? w.at(L.J)[c * L.ldj + d] : 0.f;
+        o.con_jac[B.mv + env * m * nv + idx] = c >= 0 ? w.jrow(c)[d] : 0.f;
       }
     }
     for (int r = tm.lane; r < m; r += T) {
       int c = inv[r];
-      if (o.con_diag != nullptr) o.con_diag[env * m + r] = c >= 0 ? w.at(L.rdiag)[c] : 0.f;
-      if (o.con_aref != nullptr) o.con_aref[env * m + r] = c >= 0 ? w.at(L.raref)[c] : 0.f;
+      if (o.con_diag != nullptr) o.con_diag[B.m + env * m + r] = c >= 0 ? w.at(L.rdiag)[c] : 0.f;
+      if (o.con_aref != nullptr) o.con_aref[B.m + env * m + r] = c >= 0 ? w.at(L.raref)[c] : 0.f;
     }
   }
   if (o.status != nullptr) {
@@ -130,48 +131,41 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const int* mw, Ws 
     for (int i = tm.lane; i < nq; i += T) fin = fin && isfinite(w.at(L.q)[i]);
     for (int i = tm.lane; i < nv; i += T) fin = fin && isfinite(w.at(L.qd)[i]);
     fin = tm.all(fin);
-    if (tm.lane == 0) o.status[env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
+    if (tm.lane == 0) o.status[B.env + env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
   }
 }
 
+// One env per team for n_steps x n_frames pipeline steps: load, step, write.
+// `arena` is the first per-env shared-memory arena of the CTA; B offsets the
+// env's rows in the (flat) global arrays.  Teams without an env (`active`
+// false) still take every CTA barrier and return before the outputs.
 template <int T, int NVB>
-__global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
-  extern __shared__ __align__(16) int smem[];
-  for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
-  Layout* shared_layout = reinterpret_cast<Layout*>(smem + al4(a.model_words));
-  if (threadIdx.x == 0) {
-    const int* w0 = a.model;
-    *shared_layout = make_layout(w0[BXM_H_NL], w0[BXM_H_NQ], w0[BXM_H_NV], w0[BXM_H_NU], w0[BXM_H_NCON],
-                                 w0[BXM_H_NLIM]);
-  }
-  __syncthreads();
+__device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, const int* smem, const Layout* sl,
+                                         float* arena, int team, long long env, bool active, int n_frames) {
   const Model md(smem);
   const Team<T> tm;
-  const int team = threadIdx.x / T;
-  long long env = (long long)blockIdx.x * a.envs_per_cta + team;
-  // teams past the batch keep hitting the CTA barriers but do no work
-  const bool active = team < a.envs_per_cta && env < a.n_env;
-  if (!active) env = 0;
   Ws w;
-  w.L = shared_layout;
-  w.b = reinterpret_cast<float*>(smem + al4(a.model_words) + kLayoutWords) + (size_t)team * w.L->total;
+  w.L = sl;
+  w.b = arena + (size_t)team * w.L->total;
   const Layout& L = *w.L;
-  const int nq = md.nq, nv = md.nv, nl = md.nl, nu = md.nu, ld = L.ldm;
+  const int nq = md.nq, nv = md.nv, nu = md.nu, ld = L.ldm;
   Prof pf(a.prof, active && tm.lane == 0);
 
   const bool exact = a.exact_inverse || a.init || md.ns_iters == 0;
   if (active) {
-    load_vec<T>(tm, w.at(L.q), a.q_in + env * nq, nq);
-    load_vec<T>(tm, w.at(L.qd), a.qd_in + env * nv, nv);
+    load_vec<T>(tm, w.at(L.q), a.q_in + B.q + env * nq, nq);
+    load_vec<T>(tm, w.at(L.qd), a.qd_in + B.v + env * nv, nv);
   }
   if (active && !exact) {
-    const float* src = a.minv_in + env * nv * nv;
+    const float* src = a.minv_in + B.vv + env * nv * nv;
     for (int idx = tm.lane; idx < nv * nv; idx += T) {
       int i = idx / nv, j = idx - i * nv;
       w.at(L.Minv)[i * ld + j] = src[idx];
     }
   }
-  if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] = 0;
+  // teams without an env may have no arena slot (batch items narrower than
+  // the block): every arena access below is behind `active`
+  if (active && tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] = 0;
   tm.sync();
   pf.mark(BRAXG_PROF_IO);
   bool ok = position_stage<T, NVB>(smem, w, active, exact, 0, pf);
@@ -185,9 +179,9 @@ __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   } else {
     for (int s = 0; s < a.n_steps; ++s) {
       const bool has_act = a.act != nullptr && nu > 0;
-      if (has_act && active) load_vec<T>(tm, w.at(L.act), a.act + s * a.act_step_stride + env * nu, nu);
+      if (has_act && active) load_vec<T>(tm, w.at(L.act), a.act + s * a.act_step_stride + B.u + env * nu, nu);
       tm.sync();
-      for (int f = 0; f < a.n_frames; ++f) {
+      for (int f = 0; f < n_frames; ++f) {
         if (active) stage_smooth<T>(smem, w, has_act);
         __syncthreads();
         pf.mark(BRAXG_PROF_SMOOTH);
@@ -202,18 +196,37 @@ __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
         ok = position_stage<T, NVB>(smem, w, active, a.exact_inverse || md.ns_iters == 0, md.ns_iters, pf) && ok;
         pf.count(BRAXG_PROF_SUBSTEPS, 1ull);
       }
-      if (active && a.traj_q != nullptr) store_vec<T>(tm, a.traj_q + ((long long)s * a.n_env + env) * nq, w.at(L.q), nq);
+      if (active && a.traj_q != nullptr)
+        store_vec<T>(tm, a.traj_q + s * a.traj_q_stride + B.q + env * nq, w.at(L.q), nq);
       if (active && a.traj_qd != nullptr)
-        store_vec<T>(tm, a.traj_qd + ((long long)s * a.n_env + env) * nv, w.at(L.qd), nv);
+        store_vec<T>(tm, a.traj_qd + s * a.traj_qd_stride + B.v + env * nv, w.at(L.qd), nv);
     }
   }
   if (!active) return;  // no CTA barrier follows
-  write_outputs<T>(a, smem, w, env, ok);
+  write_outputs<T>(a, B, smem, w, env, ok);
   pf.mark(BRAXG_PROF_IO);
   pf.count(BRAXG_PROF_NS_RESETS, (unsigned long long)reinterpret_cast<const int*>(w.at(L.misc))[1]);
-
 }
 
+template <int T, int NVB>
+__global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) int smem[];
+  for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
+  Layout* shared_layout = reinterpret_cast<Layout*>(smem + al4(a.model_words));
+  if (threadIdx.x == 0) {
+    const int* w0 = a.model;
+    *shared_layout = layout_of(w0);
+  }
+  __syncthreads();
+  const int team = threadIdx.x / T;
+  long long env = (long long)blockIdx.x * a.envs_per_cta + team;
+  // teams past the batch keep hitting the CTA barriers but do no work
+  const bool active = team < a.envs_per_cta && env < a.n_env;
+  if (!active) env = 0;
+  const EnvBase B{};
+  float* arena = reinterpret_cast<float*>(smem + al4(a.model_words) + kLayoutWords);
+  run_team<T, NVB>(a, B, smem, shared_layout, arena, team, env, active, a.n_frames);
+}
 
 constexpr int kMaxSmemBytes = 227 * 1024;
 

@@ -7,6 +7,13 @@
 
 namespace braxg {
 
+// Element offsets of a model group's first env inside flat (concatenated)
+// batch arrays, one per per-env size class (q: nq, v: nv, vv: nv^2, l: nl,
+// u: nu, m: constraint rows, mv: rows x nv); all zero for a single model.
+struct EnvBase {
+  long long env, q, v, vv, l, u, m, mv;
+};
+
 struct StepArgs {
   const int* model;
   int model_words;
@@ -24,7 +31,33 @@ struct StepArgs {
   braxg_state out;
   float* traj_q;
   float* traj_qd;
+  long long traj_q_stride;   // elements between env steps of traj_q
+  long long traj_qd_stride;  // and of traj_qd
   unsigned long long* prof;
+};
+
+// One model group of an uneven batch.
+struct BatchGroup {
+  const int* model;  // device descriptor
+  int model_words;
+  int threads_per_env;  // 16 or 32
+  int nvb;              // matmul tile bucket: 16, 32 or 64
+  int n_frames;         // pipeline steps per env step for this model
+  EnvBase base;
+};
+
+// A CTA's worth of envs of one group.
+struct BatchItem {
+  int group, env0, count, pad;
+};
+
+struct BatchArgs {
+  StepArgs s;  // flat state arrays, flags and strides (model fields unused)
+  const BatchGroup* groups;
+  const BatchItem* items;
+  int n_items;
+  int* counter;    // next item; zeroed before each launch
+  int smem_bytes;  // dynamic shared memory of the launch
 };
 
 struct VjpArgs {
@@ -40,10 +73,13 @@ struct VjpArgs {
   float* q0_bar;        // [n, nq]
   float* qd0_bar;       // [n, nv]
   float* ckpt;          // [n_ckpt, n, nq + nv]
-  float* seg;           // [ckpt_every * n_frames, n, nq + nv]
+  float* seg;           // [ckpt_every * n_frames, n, nq + nv] frame input states
+  float* snap;          // [ckpt_every * n_frames, n, snap_words] frame snapshots
+  int snap_words;       // forward arena + PG tape words (multiple of 4)
   float* traj_q;        // optional forward trajectory [n_steps, n, nq]
   float* traj_qd;       // [n_steps, n, nv]
   int* status;          // [n]
+  unsigned long long* prof;  // optional per-phase cycle counters
 };
 
 // Launches vjp_kernel<T, NVB> (defined in braxg_vjp_kernel.cuh, instantiated
@@ -55,5 +91,11 @@ cudaError_t launch_vjp(const VjpArgs& a, int grid, int smem, cudaStream_t st);
 // inst_*.cu).
 template <int T, int NVB>
 cudaError_t launch_step(const StepArgs& a, int grid, int smem, cudaStream_t st);
+
+// Launches the persistent batch_kernel (instantiated in inst_batch.cu) after
+// zeroing the item counter on the same stream.
+cudaError_t launch_batch_kernel(const BatchArgs& a, int grid, int block, int smem, cudaStream_t st);
+// Occupancy of batch_kernel: CTAs per SM at this block size and shared memory.
+cudaError_t batch_kernel_occupancy(int block, int smem, int* ctas_per_sm);
 
 }  // namespace braxg

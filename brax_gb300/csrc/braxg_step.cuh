@@ -49,21 +49,28 @@ struct Layout {
   int q, qd, act, qfs, qfc, qdd, tau, v1, v2, misc;
   int xp, xr, xa, xv, rc, ci, cp, cd, cdof, cdofd;
   int M, Minv;
-  int J, rdiag, raref, rmap;
-  int scr, scr_words;
+  int J, jcap, jovf, rdiag, raref, rmap;
+  int scr, scr_words, itmp;
   int total;
 };
 
 __host__ __device__ inline int al4(int x) { return (x + 3) & ~3; }
+__host__ __device__ inline int imax(int a, int b) { return a > b ? a : b; }
 // words reserved after the model descriptor for the shared Layout
 constexpr int kLayoutWords = 64;
 // the projected-gradient solve forms A explicitly while at most this many
 // constraint rows are active (else it applies A = J Minv J^T + diag implicitly)
 constexpr int kMaxExplicitRows = 32;
 
-__host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim) {
+// Per-env shared-memory arena.  The constraint Jacobian keeps its first
+// kMaxExplicitRows active rows in their own slot (all the explicit solve and
+// the adjoint ever see); rows beyond that exist only on the implicit path and
+// sit at the end of the scratch region, which that path leaves free.  The mass
+// matrix lives in scratch too (from CRBA to the inverse, and to the outputs),
+// except for models whose integrator solves with M itself (ns_iters == 0).
+__host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim, int ns_iters) {
   Layout L;
-  int m = 4 * ncon + nlim;
+  const int m = 4 * ncon + nlim;
   L.ldm = nv | 1;  // odd leading dimension: conflict-free strided lane access
   L.ldj = nv | 1;
   int o = 0;
@@ -92,28 +99,60 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.cd = take(6 * nl);
   L.cdof = take(6 * nv);
   L.cdofd = take(6 * nv);
-  L.M = take(nv * L.ldm);
+  const bool own_m = ns_iters == 0;
+  L.M = own_m ? take(nv * L.ldm) : -1;
   L.Minv = take(nv * L.ldm);
-  L.J = take(m * L.ldj);
+  L.jcap = m < kMaxExplicitRows ? m : kMaxExplicitRows;
+  L.J = take(L.jcap * L.ldj);
   L.rdiag = take(m);
   L.raref = take(m);
   L.rmap = take(m);
-  int s = 14 * nl;                                   // FK / com temporaries
-  s = s > 13 * nl + 0 ? s : 13 * nl;                 // crb
-  s = s > 12 * nl + nu ? s : 12 * nl + nu;           // RNE
-  s = s > 2 * nv * L.ldm + 4 ? s : 2 * nv * L.ldm + 4;  // inverse temporaries
-  s = s > 14 * ncon + 16 ? s : 14 * ncon + 16;       // contacts
-  s = s > 8 * m + 4 * nv + 40 ? s : 8 * m + 4 * nv + 40;  // projected gradient (implicit A)
+  const int ovf = (m - L.jcap) * L.ldj;  // overflow Jacobian rows at the scratch end
+  const int nn = nv * L.ldm;
+  // Scratch users, each with the regions it needs at once.  The mass matrix
+  // (when it lives in scratch) must survive from CRBA to the inverse and to
+  // the outputs, past the contacts of the Jacobian stage; two placements are
+  // tried: after the inverse temporaries, or before them.
+  const int head = imax(imax(13 * nl, 14 * ncon + 16), m + 4);  // CRBA, contacts, output row map
+  int common = 14 * nl;                                     // FK / com temporaries
+  common = imax(common, 12 * nl + nu + ovf);                // RNE
+  common = imax(common, 14 * ncon + 16 + ovf);              // contacts + Jacobian rows
+  common = imax(common, 8 * al4(m) + 2 * al4(nv) + 16 + ovf);  // projected gradient (implicit A)
   {
-    const int na = m < kMaxExplicitRows ? m : kMaxExplicitRows;  // explicit A = (J Minv) J^T + diag
-    const int pg = na * (na | 1) + na * L.ldm + 8 * al4(na) + 2 * al4(nv) + 16;
-    s = s > pg ? s : pg;
+    const int na = L.jcap;  // explicit A = (J Minv) J^T + diag; W shares its words with the PG vectors
+    common = imax(common, na * (na | 1) + al4(na) + imax(na * L.ldm, 7 * al4(na)) + 16);
   }
-  s = s > m + 4 ? s : m + 4;                         // output row map
+  common = imax(common, m + 4 + ovf);                       // output row map
+  int m_off = 0, inv_off = 0, s;
+  if (own_m) {
+    s = imax(common, imax(head, 2 * nn + 4));               // inverse temporaries; integrator factor
+  } else {
+    const int ma = al4(imax(head, 2 * nn + 4));             // A: M after the inverse temporaries
+    const int sa = imax(common, ma + nn + ovf);
+    const int mb = al4(head), ib = al4(mb + nn);            // B: M, then the inverse temporaries
+    const int sb = imax(common, imax(mb + nn + ovf, ib + 2 * nn + 4));
+    if (sa <= sb) {
+      m_off = ma;
+      s = sa;
+    } else {
+      m_off = mb;
+      inv_off = ib;
+      s = sb;
+    }
+  }
   L.scr_words = al4(s);
   L.scr = take(L.scr_words);
+  if (!own_m) L.M = L.scr + m_off;
+  L.itmp = L.scr + inv_off;
+  L.jovf = L.scr + L.scr_words - ovf;
   L.total = al4(o);
   return L;
+}
+
+// Layout of a packed model descriptor (header words).
+__host__ __device__ inline Layout layout_of(const int* w) {
+  return make_layout(w[BXM_H_NL], w[BXM_H_NQ], w[BXM_H_NV], w[BXM_H_NU], w[BXM_H_NCON], w[BXM_H_NLIM],
+                     w[BXM_H_NS_ITERS]);
 }
 static_assert(sizeof(Layout) <= kLayoutWords * 4, "Layout must fit its shared slot");
 
@@ -151,6 +190,11 @@ struct Ws {
   float* b;
   const Layout* L;
   __device__ __forceinline__ float* at(int off) const { return b + off; }
+  // active constraint row r of the Jacobian (first jcap rows in their slot,
+  // the rest at the end of scratch)
+  __device__ __forceinline__ float* jrow(int r) const {
+    return b + (r < L->jcap ? L->J + r * L->ldj : L->jovf + (r - L->jcap) * L->ldj);
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -666,7 +710,7 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   const int n = md.nv, ld = L.ldm;
   float* M = w.at(L.M);
   float* P = w.at(L.Minv);
-  float* S1 = w.at(L.scr);
+  float* S1 = w.at(L.itmp);
   float* S2 = S1 + n * ld;
   if (n == 0) return true;
   if (exact) {
@@ -886,13 +930,12 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
-  const int nv = md.nv, ldj = L.ldj, ncon = md.ncon;
+  const int nv = md.nv, ncon = md.ncon;
   float* dist = w.at(L.scr);
   float* cpos = dist + al4(ncon);
   float* frame = cpos + al4(3 * ncon);
   int* rcon = reinterpret_cast<int*>(frame + al4(9 * ncon));
   int* rmap = reinterpret_cast<int*>(w.at(L.rmap));
-  float* J = w.at(L.J);
   float* rdiag = w.at(L.rdiag);
   float* raref = w.at(L.raref);
   const float* qd = w.at(L.qd);
@@ -923,15 +966,19 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
       f3 n = ld3(frame + 9 * k), t1 = ld3(frame + 9 * k + 3), t2 = ld3(frame + 9 * k + 6);
       float mu = fric[k];
       f3 v0 = (-t1) * (-mu) + n, v1 = (-t1) * mu + n, v2 = (-t2) * (-mu) + n, v3 = (-t2) * mu + n;
+      float* j0 = w.jrow(4 * c);
+      float* j1 = w.jrow(4 * c + 1);
+      float* j2 = w.jrow(4 * c + 2);
+      float* j3 = w.jrow(4 * c + 3);
       for (int d = tm.lane; d < nv; d += T) {
         f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
         f3 jb = ((mb >> d) & 1ull) ? cv - cross3(offb, ca) : mk3(0.f, 0.f, 0.f);
         f3 ja = ((ma >> d) & 1ull) ? cv - cross3(offa, ca) : mk3(0.f, 0.f, 0.f);
         f3 diff = jb - ja;
-        J[(4 * c + 0) * ldj + d] = dot3(diff, v0);
-        J[(4 * c + 1) * ldj + d] = dot3(diff, v1);
-        J[(4 * c + 2) * ldj + d] = dot3(diff, v2);
-        J[(4 * c + 3) * ldj + d] = dot3(diff, v3);
+        j0[d] = dot3(diff, v0);
+        j1[d] = dot3(diff, v1);
+        j2[d] = dot3(diff, v2);
+        j3[d] = dot3(diff, v3);
       }
       if (tm.lane < 4) rmap[4 * c + tm.lane] = 4 * k + tm.lane;
     }
@@ -957,7 +1004,8 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
       if (a) {
         int r = nrow + __popc(bal & ((1u << tm.lane) - 1u));
         rmap[r] = 4 * ncon + i;
-        for (int d = 0; d < nv; ++d) J[r * ldj + d] = (d == ldof[i]) ? side : 0.f;
+        float* jr = w.jrow(r);
+        for (int d = 0; d < nv; ++d) jr[d] = (d == ldof[i]) ? side : 0.f;
       }
       nrow += __popc(bal);
     }
@@ -970,7 +1018,8 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
   for (int r = tm.lane; r < nrow; r += T) {
     int orig = rmap[r];
     float vel = 0.f;
-    for (int d = 0; d < nv; ++d) vel += J[r * ldj + d] * qd[d];
+    const float* jr = w.jrow(r);
+    for (int d = 0; d < nv; ++d) vel += jr[d] * qd[d];
     float imp, aref, diag;
     if (orig < 4 * ncon) {  // constraint.py:167-174
       int k = orig >> 2;
@@ -1111,20 +1160,19 @@ __device__ __noinline__ void matvec_A(const int* mw, Ws w, int nrow, const float
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
-  const int nv = md.nv, ldj = L.ldj, ld = L.ldm;
-  const float* J = w.at(L.J);
+  const int nv = md.nv, ld = L.ldm;
   const float* Minv = w.at(L.Minv);
   const float* rdiag = w.at(L.rdiag);
   for (int d = tm.lane; d < nv; d += T) {  // t1 = J^T v
     float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
     int r = 0;
     for (; r + 3 < nrow; r += 4) {
-      s0 = fmaf(J[r * ldj + d], v[r], s0);
-      s1 = fmaf(J[(r + 1) * ldj + d], v[r + 1], s1);
-      s2 = fmaf(J[(r + 2) * ldj + d], v[r + 2], s2);
-      s3 = fmaf(J[(r + 3) * ldj + d], v[r + 3], s3);
+      s0 = fmaf(w.jrow(r)[d], v[r], s0);
+      s1 = fmaf(w.jrow(r + 1)[d], v[r + 1], s1);
+      s2 = fmaf(w.jrow(r + 2)[d], v[r + 2], s2);
+      s3 = fmaf(w.jrow(r + 3)[d], v[r + 3], s3);
     }
-    for (; r < nrow; ++r) s0 = fmaf(J[r * ldj + d], v[r], s0);
+    for (; r < nrow; ++r) s0 = fmaf(w.jrow(r)[d], v[r], s0);
     t1[d] = (s0 + s1) + (s2 + s3);
   }
   tm.sync();
@@ -1141,12 +1189,13 @@ __device__ __noinline__ void matvec_A(const int* mw, Ws w, int nrow, const float
   tm.sync();
   for (int r = tm.lane; r < nrow; r += T) {  // out = J t2 + diag v
     float s0 = 0.f, s1 = 0.f;
+    const float* jr = w.jrow(r);
     int k = 0;
     for (; k + 1 < nv; k += 2) {
-      s0 = fmaf(J[r * ldj + k], t2[k], s0);
-      s1 = fmaf(J[r * ldj + k + 1], t2[k + 1], s1);
+      s0 = fmaf(jr[k], t2[k], s0);
+      s1 = fmaf(jr[k + 1], t2[k + 1], s1);
     }
-    if (k < nv) s0 = fmaf(J[r * ldj + k], t2[k], s0);
+    if (k < nv) s0 = fmaf(jr[k], t2[k], s0);
     out[r] = (s0 + s1) + rdiag[r] * v[r];
   }
   tm.sync();
@@ -1168,9 +1217,9 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   const Layout& L = *w.L;
   const int nv = md.nv, ldj = L.ldj, ld = L.ldm, la = nrow | 1;
   float* A = w.at(L.scr);
-  float* W = A + nrow * la;
-  float* b = W + nrow * ld;
-  float* x = b + al4(nrow);
+  float* b = A + nrow * la;
+  float* W = b + al4(nrow);  // J Minv, dead once A and b are formed
+  float* x = W;
   float* y = x + al4(nrow);
   float* gy = y + al4(nrow);
   float* r = gy + al4(nrow);
@@ -1214,6 +1263,9 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     }
     if (k < nv) s0 = fmaf(W[c * ld + k], qfs[k], s0);
     b[c] = (s0 + s1) - raref[c];
+  }
+  tm.sync();
+  for (int c = tm.lane; c < nrow; c += T) {  // W is dead: its words become x, y, ...
     x[c] = 0.f;
     y[c] = 0.f;
   }
@@ -1333,7 +1385,7 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
-  const int nv = md.nv, ldj = L.ldj, ld = L.ldm;
+  const int nv = md.nv, ld = L.ldm;
   const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
   float* qfc = w.at(L.qfc);
   if (nrow == 0) {
@@ -1358,7 +1410,6 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
   float* ny = gx + al4(m);
   float* t1 = ny + al4(m);
   float* t2 = t1 + al4(nv);
-  const float* J = w.at(L.J);
   const float* Minv = w.at(L.Minv);
   const float* raref = w.at(L.raref);
   const float* qfs = w.at(L.qfs);
@@ -1371,7 +1422,8 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
   tm.sync();
   for (int i = tm.lane; i < nrow; i += T) {
     float s = 0.f;
-    for (int k = 0; k < nv; ++k) s = fmaf(J[i * ldj + k], t2[k], s);
+    const float* ji = w.jrow(i);
+    for (int k = 0; k < nv; ++k) s = fmaf(ji[k], t2[k], s);
     b[i] = s - raref[i];
     x[i] = 0.f;
     y[i] = 0.f;
@@ -1441,7 +1493,7 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
   // qf_constraint = J^T x
   for (int d = tm.lane; d < nv; d += T) {
     float s = 0.f;
-    for (int i = 0; i < nrow; ++i) s = fmaf(J[i * ldj + d], x[i], s);
+    for (int i = 0; i < nrow; ++i) s = fmaf(w.jrow(i)[d], x[i], s);
     qfc[d] = s;
   }
   tm.sync();

@@ -41,6 +41,30 @@ __device__ __forceinline__ void copy_vec(const Team<T>& tm, float* dst, const fl
   for (int i = tm.lane; i < n; i += T) dst[i] = src[i];
 }
 
+// A frame snapshot is the env's whole forward arena (every stage's values
+// after the frame's smooth, constraint and integrate stages) followed by the
+// projected-gradient tape; the reverse of that frame restores it instead of
+// recomputing the frame.  Both parts are whole float4s (al4 sizes, 16-byte
+// aligned arenas and slots).
+template <int T>
+__device__ __forceinline__ void snap_save(const Team<T>& tm, float* slot, const float* arena, int arena_words,
+                                          const float* tape, int tape_words) {
+  float4* d = reinterpret_cast<float4*>(slot);
+  const float4* x = reinterpret_cast<const float4*>(arena);
+  const float4* t = reinterpret_cast<const float4*>(tape);
+  for (int i = tm.lane; i < arena_words / 4; i += T) d[i] = x[i];
+  for (int i = tm.lane; i < tape_words / 4; i += T) d[arena_words / 4 + i] = t[i];
+}
+template <int T>
+__device__ __forceinline__ void snap_load(const Team<T>& tm, const float* slot, float* arena, int arena_words,
+                                          float* tape, int tape_words) {
+  const float4* d = reinterpret_cast<const float4*>(slot);
+  float4* x = reinterpret_cast<float4*>(arena);
+  float4* t = reinterpret_cast<float4*>(tape);
+  for (int i = tm.lane; i < arena_words / 4; i += T) x[i] = d[i];
+  for (int i = tm.lane; i < tape_words / 4; i += T) t[i] = d[arena_words / 4 + i];
+}
+
 template <int T, int NVB>
 __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   extern __shared__ __align__(16) int smem[];
@@ -49,7 +73,7 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   AdjLayout* sal = reinterpret_cast<AdjLayout*>(smem + al4(a.model_words) + kLayoutWords);
   if (threadIdx.x == 0) {
     const int* w0 = a.model;
-    *sl = make_layout(w0[BXM_H_NL], w0[BXM_H_NQ], w0[BXM_H_NV], w0[BXM_H_NU], w0[BXM_H_NCON], w0[BXM_H_NLIM]);
+    *sl = layout_of(w0);
     *sal = make_adj_layout(w0[BXM_H_NL], w0[BXM_H_NQ], w0[BXM_H_NV], w0[BXM_H_NU], w0[BXM_H_NCON], w0[BXM_H_NLIM],
                            w0[BXM_H_PG_ITERS]);
   }
@@ -75,6 +99,11 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   const long long n = a.n_env;
   const bool has_act = a.act != nullptr && nu > 0;
   bool ok = true, taped = true;
+  Prof pf(a.prof, active && tm.lane == 0);
+  const int n_ckpt = (a.n_steps + a.ckpt_every - 1) / a.ckpt_every;
+  const int last_s0 = (n_ckpt - 1) * a.ckpt_every;
+  float* tape = aw.at(A.tape);
+  const int tape_words = a.snap_words - L.total;
   // ---- forward with checkpoints ----
   if (active) {
     copy_vec<T>(tm, w.at(L.q), a.q0 + env * nq, nq);
@@ -91,13 +120,23 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
     }
     if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
     tm.sync();
+    // the last segment is taped and snapshotted here, so it needs no recompute
+    const bool snap = s >= last_s0;
     for (int f = 0; f < a.n_frames; ++f) {
-      fwd_frame<T, NVB>(mw, w, active, has_act, nullptr, ok);
+      const long long slot = (long long)((s - last_s0) * a.n_frames + f) * n + env;
+      if (active && snap) {
+        copy_vec<T>(tm, a.seg + slot * S, w.at(L.q), nq);
+        copy_vec<T>(tm, a.seg + slot * S + nq, w.at(L.qd), nv);
+      }
+      tm.sync();
+      fwd_frame<T, NVB>(mw, w, active, has_act, snap ? tape : nullptr, ok);
+      if (active && snap) snap_save<T>(tm, a.snap + slot * a.snap_words, w.b, L.total, tape, tape_words);
       ok = pos_stage<T, NVB>(mw, w, active) && ok;
     }
     if (active && a.traj_q != nullptr) copy_vec<T>(tm, a.traj_q + ((long long)s * n + env) * nq, w.at(L.q), nq);
     if (active && a.traj_qd != nullptr) copy_vec<T>(tm, a.traj_qd + ((long long)s * n + env) * nv, w.at(L.qd), nv);
   }
+  pf.mark(BRAXG_PROF_VJP_CHECKPOINT);
   // ---- backward ----
   float* qbo = aw.at(A.qbo);
   float* qdbo = aw.at(A.qdbo);
@@ -108,32 +147,35 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
       qdbo[i] = a.qd_bar ? a.qd_bar[((long long)(a.n_steps - 1) * n + env) * nv + i] : 0.f;
   }
   tm.sync();
-  const int n_ckpt = (a.n_steps + a.ckpt_every - 1) / a.ckpt_every;
   for (int sg = n_ckpt - 1; sg >= 0; --sg) {
     const int s0 = sg * a.ckpt_every;
     const int s1 = min(s0 + a.ckpt_every, a.n_steps);
-    if (active) {
-      const float* c = a.ckpt + ((long long)sg * n + env) * S;
-      copy_vec<T>(tm, w.at(L.q), c, nq);
-      copy_vec<T>(tm, w.at(L.qd), c + nq, nv);
-    }
-    tm.sync();
-    __syncthreads();
-    pos_stage<T, NVB>(mw, w, active);
-    for (int s = s0; s < s1; ++s) {  // recompute the segment, keeping every frame's input state
-      if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
-      for (int f = 0; f < a.n_frames; ++f) {
-        if (active) {
-          float* sp = a.seg + ((long long)((s - s0) * a.n_frames + f) * n + env) * S;
-          copy_vec<T>(tm, sp, w.at(L.q), nq);
-          copy_vec<T>(tm, sp + nq, w.at(L.qd), nv);
+    if (sg != n_ckpt - 1) {  // recompute the segment, taping and snapshotting every frame
+      if (active) {
+        const float* c = a.ckpt + ((long long)sg * n + env) * S;
+        copy_vec<T>(tm, w.at(L.q), c, nq);
+        copy_vec<T>(tm, w.at(L.qd), c + nq, nv);
+      }
+      tm.sync();
+      __syncthreads();
+      pos_stage<T, NVB>(mw, w, active);
+      for (int s = s0; s < s1; ++s) {
+        if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
+        for (int f = 0; f < a.n_frames; ++f) {
+          const long long slot = (long long)((s - s0) * a.n_frames + f) * n + env;
+          if (active) {
+            copy_vec<T>(tm, a.seg + slot * S, w.at(L.q), nq);
+            copy_vec<T>(tm, a.seg + slot * S + nq, w.at(L.qd), nv);
+          }
+          tm.sync();
+          bool dummy = true;
+          fwd_frame<T, NVB>(mw, w, active, has_act, tape, dummy);
+          if (active) snap_save<T>(tm, a.snap + slot * a.snap_words, w.b, L.total, tape, tape_words);
+          pos_stage<T, NVB>(mw, w, active);
         }
-        tm.sync();
-        bool dummy = true;
-        fwd_frame<T, NVB>(mw, w, active, has_act, nullptr, dummy);
-        pos_stage<T, NVB>(mw, w, active);
       }
     }
+    pf.mark(BRAXG_PROF_VJP_RECOMPUTE);
     for (int s = s1 - 1; s >= s0; --s) {
       if (active) {
         if (has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
@@ -142,9 +184,9 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
       tm.sync();
       for (int f = a.n_frames - 1; f >= 0; --f) {
         if (active) {
-          const float* sp = a.seg + ((long long)((s - s0) * a.n_frames + f) * n + env) * S;
-          copy_vec<T>(tm, w.at(L.q), sp, nq);
-          copy_vec<T>(tm, w.at(L.qd), sp + nq, nv);
+          const long long slot = (long long)((s - s0) * a.n_frames + f) * n + env;
+          const float* sp = a.seg + slot * S;
+          snap_load<T>(tm, a.snap + slot * a.snap_words, w.b, L.total, tape, tape_words);
           copy_vec<T>(tm, aw.at(A.q0), sp, nq);
           copy_vec<T>(tm, aw.at(A.qd0), sp + nq, nv);
           // zero the accumulated adjoints of this step
@@ -165,27 +207,34 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
         }
         tm.sync();
         __syncthreads();
-        pos_stage<T, NVB>(mw, w, active);
-        bool dummy = true;
-        fwd_frame<T, NVB>(mw, w, active, has_act, aw.at(A.tape), dummy);
+        pf.mark(BRAXG_PROF_VJP_RESTORE);
         if (active) rev_integrate<T>(mw, w, aw);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_INTEGRATE);
         if (active) rev_qdd<T>(mw, w, aw);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_QDD);
         if (active) taped = rev_constraint<T>(mw, w, aw) && taped;
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_CONSTRAINT);
         if (active) rev_smooth<T>(mw, w, aw, has_act);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_SMOOTH);
         if (active) rev_inverse<T, NVB>(mw, w, aw);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_INVERSE);
         if (active) rev_crba<T>(mw, w, aw);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_CRBA);
         if (active) rev_rows<T>(mw, w, aw);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_ROWS);
         if (active) rev_com<T>(mw, w, aw);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_COM);
         if (active) rev_fk<T>(mw, w, aw);
         __syncthreads();
+        pf.mark(BRAXG_PROF_REV_FK);
         if (active) {
           copy_vec<T>(tm, qbo, aw.at(A.qb), nq);
           copy_vec<T>(tm, qdbo, aw.at(A.qdb), nv);

@@ -163,7 +163,9 @@ def profile_buffer(device=None) -> torch.Tensor:
 
 def profile_report(buf: torch.Tensor) -> dict:
   v = buf.cpu().tolist()
-  return {k: v[i] for i, k in enumerate(N.PROFILE_SLOTS)}
+  out = {k: v[i] for i, k in enumerate(N.PROFILE_SLOTS)}
+  out.update({k: v[i] for i, k in N.VJP_PROFILE_SLOTS.items() if v[i]})
+  return out
 
 
 def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
@@ -240,7 +242,8 @@ def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = N
 
 
 def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int = 1,
-                 ckpt_every: int = 16, trajectory: bool = False):
+                 ckpt_every: int = 16, trajectory: bool = False,
+                 profile: Optional[torch.Tensor] = None):
   """Reverse-mode gradient of a rollout through the hand-written adjoint.
 
   Replaces ``jax.grad`` through ``lax.scan`` of ``pipeline_step``
@@ -276,7 +279,7 @@ def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int =
       act_seq.data_ptr() if m.nu else None, q0.data_ptr(), qd0.data_ptr(), _ptr(qb), _ptr(qdb),
       act_bar.data_ptr() if m.nu else None, q0_bar.data_ptr(), qd0_bar.data_ptr(), _ptr(tq),
       _ptr(tqd), ws.data_ptr(), nbytes.value, status.data_ptr(),
-      ctypes.byref(_opts(CHOLESKY, 0, 0))), 'braxg_rollout_vjp')
+      ctypes.byref(_opts(CHOLESKY, 0, 0, profile))), 'braxg_rollout_vjp')
   return act_bar, q0_bar, qd0_bar, status, (tq, tqd)
 
 

@@ -50,7 +50,8 @@ enum braxg_inverse_mode {
 enum braxg_env_flags {
   BRAXG_ENV_NONFINITE = 1,   /* q or qd not finite after the call */
   BRAXG_ENV_NOT_SPD = 2,     /* a Cholesky pivot was <= 0 */
-  BRAXG_ENV_NO_GRADIENT = 4  /* a step ran more than 32 active constraint rows: no gradient */
+  BRAXG_ENV_NO_GRADIENT = 4, /* a step ran more than 32 active constraint rows: no gradient */
+  BRAXG_ENV_SKIPPED = 8      /* not stepped: its batch work item did not fit the launch */
 };
 
 typedef struct {
@@ -91,7 +92,14 @@ enum braxg_profile_slot {
   BRAXG_PROF_FK = 0, BRAXG_PROF_COM, BRAXG_PROF_CRBA, BRAXG_PROF_INVERSE,
   BRAXG_PROF_JACOBIAN, BRAXG_PROF_SMOOTH, BRAXG_PROF_CONSTRAINT, BRAXG_PROF_INTEGRATE,
   BRAXG_PROF_IO, BRAXG_PROF_MATVECS, BRAXG_PROF_ROWS, BRAXG_PROF_NS_RESETS,
-  BRAXG_PROF_SUBSTEPS, BRAXG_PROF_SLOTS = 16
+  BRAXG_PROF_SUBSTEPS,
+  /* braxg_rollout_vjp phases: checkpoint pass, segment recompute, per-frame
+   * restore, and the reverse stages */
+  BRAXG_PROF_VJP_CHECKPOINT = 16, BRAXG_PROF_VJP_RECOMPUTE, BRAXG_PROF_VJP_RESTORE,
+  BRAXG_PROF_REV_INTEGRATE, BRAXG_PROF_REV_QDD, BRAXG_PROF_REV_CONSTRAINT, BRAXG_PROF_REV_SMOOTH,
+  BRAXG_PROF_REV_INVERSE, BRAXG_PROF_REV_CRBA, BRAXG_PROF_REV_ROWS, BRAXG_PROF_REV_COM,
+  BRAXG_PROF_REV_FK,
+  BRAXG_PROF_SLOTS = 32
 };
 
 typedef struct {
@@ -174,6 +182,69 @@ int braxg_rollout_vjp_noalloc(const braxg_model* model, void* stream, int n_env,
                               const float* qd0, const float* q_bar, const float* qd_bar,
                               float* act_bar, float* q0_bar, float* qd0_bar, float* traj_q,
                               float* traj_qd, int32_t* status, const braxg_options* opt);
+
+/* ---- Uneven batches --------------------------------------------------------
+ * Envs of several models (different nv, link counts and contact sets) stepped
+ * by ONE persistent launch.  The reference steps one System per jitted
+ * function (jax.vmap over envs of the same System, brax/envs/wrappers/
+ * training.py:66-72); a batch of different Systems has no counterpart there
+ * and would be one jitted step per System.  Each model keeps the meaning of
+ * braxg_step/braxg_rollout for its own envs.
+ *
+ * State arrays are flat: model g's envs occupy one contiguous run of every
+ * field, starting at braxg_batch_get_offsets(batch, g) in units of that field's
+ * per-env size class; the offsets of index n_models are the totals. */
+typedef struct braxg_batch braxg_batch;
+
+/* Launch shape for the models with nv <= nv_max (the first matching entry
+ * applies; models matching none get 32 lanes and envs_per_cta 0). */
+typedef struct {
+  int32_t nv_max;
+  int32_t threads_per_env;  /* 16 or 32 */
+  int32_t envs_per_cta;     /* envs of one model per CTA work item; 0 = as many as fit */
+  int32_t reserved;
+} braxg_bucket_shape;
+
+typedef struct {
+  int64_t env;      /* status; env index */
+  int64_t q;        /* q, traj_q (x1) */
+  int64_t qd;       /* qd, qf_smooth, qf_constraint, qdd, traj_qd (x1); cdof, cdofd (x6) */
+  int64_t mass_mx;  /* mass_mx, mass_mx_inv (x1) */
+  int64_t link;     /* x_pos, xd_ang, xd_vel, root_com, cinr_pos (x3); x_rot, cinr_rot (x4);
+                       cd (x6); cinr_i (x9) */
+  int64_t act;      /* act (x1) */
+  int64_t row;      /* con_diag, con_aref (x1) */
+  int64_t jac;      /* con_jac (x1) */
+} braxg_batch_offsets;
+
+/* Builds the work list of a batch: n_env[g] envs of models[g] (all on one
+ * device), n_frames[g] pipeline steps per env step (NULL = 1 each).  Work items
+ * are CTA-sized groups of envs of one model, ordered by decreasing estimated
+ * cost and taken from a device counter by a grid of (SMs x resident CTAs)
+ * persistent CTAs.  smem_per_cta = 0 picks 113 KB, two CTAs per SM (grown to
+ * fit the largest single env or explicit envs_per_cta); a non-zero value is a
+ * limit, and a shape that does not fit it is BRAXG_ERR_INVALID.  Allocates the device work list; later calls allocate
+ * nothing. */
+int braxg_batch_create(const braxg_model* const* models, const int32_t* n_env,
+                       const int32_t* n_frames, int n_models,
+                       const braxg_bucket_shape* shapes, int n_shapes,
+                       int32_t smem_per_cta, braxg_batch** out);
+int braxg_batch_destroy(braxg_batch* batch);
+int braxg_batch_get_offsets(const braxg_batch* batch, int index, braxg_batch_offsets* out);
+int braxg_batch_launch_info(const braxg_batch* batch, int32_t* grid, int32_t* block,
+                            int32_t* smem_bytes, int32_t* n_items);
+
+/* braxg_init for every env of the batch (flat q, qd and out fields). */
+int braxg_batch_init(const braxg_batch* batch, void* stream, const float* q,
+                     const float* qd, braxg_state* out, const braxg_options* opt);
+
+/* braxg_rollout for every env of the batch: act_seq [n_steps, total act],
+ * traj_q [n_steps, total q], traj_qd [n_steps, total qd] (optional).  One
+ * kernel launch plus one 4-byte memset of the work counter on `stream`; both
+ * are stream-ordered, so the call can be captured into a CUDA graph. */
+int braxg_batch_rollout(const braxg_batch* batch, void* stream, int n_steps,
+                        const float* act_seq, const braxg_state* in, braxg_state* out,
+                        float* traj_q, float* traj_qd, const braxg_options* opt);
 
 /* Launch shape the tuner picks for this model: lanes per env, envs per CTA,
  * dynamic shared memory bytes per CTA. */

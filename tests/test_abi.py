@@ -91,3 +91,32 @@ def test_pack_roundtrip(name):
   for k, v in H.items():
     if k.startswith('BXM_O_'):
       assert d[v] % 4 == 0
+
+
+def test_batch_argument_validation_without_gpu(lib):
+  from brax_gb300 import _native as N
+  h = ctypes.c_void_p()
+  assert lib.braxg_batch_create(None, None, None, 0, None, 0, 0, ctypes.byref(h)) == N.ERR_INVALID
+  assert b'n_models' in lib.braxg_last_error()
+  ne = (ctypes.c_int32 * 1)(4)
+  models = (ctypes.c_void_p * 1)(None)
+  assert lib.braxg_batch_create(models, ne, None, 1, None, 0, 0, ctypes.byref(h)) == N.ERR_INVALID
+  assert b'NULL' in lib.braxg_last_error()
+  assert lib.braxg_batch_rollout(None, None, 1, None, None, None, None, None, None) == N.ERR_INVALID
+  assert lib.braxg_batch_init(None, None, None, None, None, None) == N.ERR_INVALID
+
+
+def test_chain_workloads_and_uneven_mix():
+  from brax_gb300 import workloads as W
+  for k in (2, 9, 32):
+    s = W.chain(k)
+    assert (s.num_links(), s.q_size(), s.qd_size(), s.act_size()) == (k, k, k, k)
+    assert s.contacts.n == 2  # the last capsule against the plane: two end points
+  mix = W.uneven_mix(8192, 0)
+  assert sum(n for _, n, _ in mix) == 8192
+  names = [s.name for s, _, _ in mix]
+  assert names[-2:] == ['quadruped', 'humanoid_like']
+  n_chain = sum(n for s, n, _ in mix if s.name.startswith('chain'))
+  assert abs(n_chain - 0.6 * 8192) <= 1
+  assert max(s.qd_size() for s, _, _ in mix) == 32 and min(s.qd_size() for s, _, _ in mix) == 2
+

@@ -1,0 +1,185 @@
+"""Uneven batches (several models in one persistent launch) on the GPU.
+
+* every model's envs in a batch give the same state as the same envs stepped
+  by the single-model launch (same lanes per env: identical code per env, so
+  the results agree to the last bit; 1e-6 relative is asserted);
+* chain models with a plane contact match the oracle in one step (q / qd
+  relative error <= 1e-5 for 99 % of envs against the FP32 oracle);
+* a 16-lane shape gives the 32-lane result within FP32 summation-order noise;
+* n steps captured as one CUDA graph of per-step launches reproduce the
+  single-launch rollout;
+* the autotuner returns one valid shape per nv bucket and caches it.
+"""
+
+import numpy as np
+import pytest
+
+from tests.parity_util import rel_err
+
+torch = pytest.importorskip('torch')
+pytestmark = pytest.mark.gpu
+
+
+def _setup():
+  if not torch.cuda.is_available():
+    pytest.skip('no CUDA device')
+  from brax_gb300 import batch as B
+  from brax_gb300 import pipeline as P
+  from brax_gb300 import workloads as W
+  return B, P, W
+
+
+def _mix(W):
+  return [(W.chain(2), 5, 1), (W.chain(7), 9, 1), (W.asset('quadruped'), 13, 5),
+          (W.asset('humanoid_like'), 6, 5), (W.chain(32), 4, 1), (W.chain(3), 0, 1)]
+
+
+def _inputs(W, mix, n_steps, seed):
+  rng = np.random.default_rng(seed)
+  qs, qds, acts = [], [], []
+  for s, n, _ in mix:
+    q, qd = W.reset(s, n, rng)
+    qs.append(q.astype(np.float32))
+    qds.append(qd.astype(np.float32))
+    acts.append(np.stack([W.actions(s, n, rng) for _ in range(n_steps)]).astype(np.float32))
+  return qs, qds, acts
+
+
+@pytest.mark.parametrize('mode', ['chol', 'ns'])
+def test_batch_matches_single_model_launches(mode):
+  B, P, W = _setup()
+  mix = _mix(W)
+  n_steps = 3
+  inv = P.CHOLESKY if mode == 'chol' else P.NEWTON_SCHULZ
+  qs, qds, acts = _inputs(W, mix, n_steps, 1)
+  b = B.Batch([m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix])
+  st = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
+  out, (tq, tqd) = b.rollout(st, b.concat_steps(acts, 'act'), inverse_mode=inv, trajectory=True)
+  torch.cuda.synchronize()
+  assert int((out.status != 0).sum()) == 0
+  got_q, got_qd = b.split(out.q, 'q'), b.split(out.qd, 'qd')
+  got_minv = b.split(out.mass_mx_inv, 'mass_mx_inv')
+  widths = [n * s.q_size() for s, n, _ in mix]
+  tq_parts = torch.split(tq, widths, dim=1)
+  for g, (s, n, nf) in enumerate(mix):
+    if n == 0:
+      assert got_q[g].numel() == 0
+      continue
+    dev = b.device
+    s0 = P.init(s, torch.tensor(qs[g], device=dev), torch.tensor(qds[g], device=dev))
+    ref, (rq, _) = P.rollout(s, s0, torch.tensor(acts[g], device=dev), n_frames=nf, inverse_mode=inv,
+                             trajectory=True, threads_per_env=32)
+    torch.cuda.synchronize()
+    pairs = (('q', got_q[g], ref.q), ('qd', got_qd[g], ref.qd), ('minv', got_minv[g], ref.mass_mx_inv),
+             ('traj_q', tq_parts[g].reshape(n_steps * n, -1), rq.reshape(n_steps * n, -1)))
+    for name, a, r in pairs:
+      e = rel_err(a.cpu().numpy(), r.cpu().numpy())
+      print(f'{s.name} {mode} {name}: max {e.max():.2e}')
+      assert e.max() <= 1e-6, (s.name, name, e.max())
+
+
+def test_chain_contact_step_matches_oracle():
+  """One step of chains of 2..32 links whose last link is in contact with the
+  plane: q / qd against the FP32 oracle on the same inputs (<= 1e-5 for 99 %
+  of envs, <= 1e-3 for all) and against the FP64 oracle within 3x the FP32
+  oracle's own FP64 error."""
+  B, P, W = _setup()
+  from oracle.pipeline import Oracle
+  chains = [W.chain(k) for k in (2, 5, 12, 32)]
+  n = 64
+  rng = np.random.default_rng(7)
+  b = B.Batch(chains, [n] * len(chains))
+  qs, qds, acts, r32s, r64s = [], [], [], [], []
+  touching = 0
+  for s in chains:
+    o64 = Oracle(s, np.float64, exact_inverse=True)
+    o32 = Oracle(s, np.float32, exact_inverse=True)
+    q, qd = W.reset(s, n, rng)
+    st = o64.init(q, qd)
+    for _ in range(30):  # let the chains swing into the plane
+      st = o64.step(st, W.actions(s, n, rng))
+    q, qd = st.q.astype(np.float32), st.qd.astype(np.float32)
+    a = W.actions(s, n, rng).astype(np.float32)
+    r64 = o64.step(o64.init(q.astype(np.float64), qd.astype(np.float64)), a.astype(np.float64))
+    r32 = o32.step(o32.init(q, qd), a)
+    touching += int((np.abs(r64.con_diag) > 0).any(-1).sum()) if getattr(r64, 'con_diag', None) is not None else 0
+    qs.append(q)
+    qds.append(qd)
+    acts.append(a[None])
+    r32s.append(r32)
+    r64s.append(r64)
+  st = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
+  out, _ = b.rollout(st, b.concat_steps(acts, 'act'), inverse_mode=P.CHOLESKY)
+  torch.cuda.synchronize()
+  assert int((out.status != 0).sum()) == 0
+  gq, gqd = b.split(out.q, 'q'), b.split(out.qd, 'qd')
+  for g, s in enumerate(chains):
+    for name, a in (('q', gq[g]), ('qd', gqd[g])):
+      a = a.cpu().numpy()
+      e32 = rel_err(a, getattr(r32s[g], name))
+      e64 = rel_err(a, getattr(r64s[g], name))
+      eo = rel_err(getattr(r32s[g], name), getattr(r64s[g], name))
+      print(f'{s.name} {name}: vs fp32 p99 {np.quantile(e32, 0.99):.2e} max {e32.max():.2e} | vs fp64 '
+            f'p99 {np.quantile(e64, 0.99):.2e} | fp32 oracle vs fp64 p99 {np.quantile(eo, 0.99):.2e}')
+      assert np.quantile(e32, 0.99) <= 1e-5, (s.name, name)
+      assert e32.max() <= 1e-3, (s.name, name)
+      assert np.quantile(e64, 0.99) <= max(1e-5, 3 * np.quantile(eo, 0.99)), (s.name, name)
+  print('envs with an active constraint row:', touching)
+
+
+def test_sixteen_lane_shape_matches_thirty_two():
+  B, P, W = _setup()
+  mix = _mix(W)[:3]
+  qs, qds, acts = _inputs(W, mix, 2, 3)
+  res = []
+  for shapes in ([(64, 32, 0)], [(16, 16, 8), (64, 32, 3)]):
+    b = B.Batch([m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix], shapes=shapes)
+    st = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
+    out, _ = b.rollout(st, b.concat_steps(acts, 'act'))
+    torch.cuda.synchronize()
+    res.append((b.split(out.q, 'q'), b.launch_info()))
+  for g in range(len(mix)):
+    e = rel_err(res[1][0][g].cpu().numpy(), res[0][0][g].cpu().numpy())
+    assert e.max() <= 1e-4, (mix[g][0].name, e.max())
+  assert res[1][1]['block'] >= 128
+
+
+def test_graph_rollout_matches_single_launch():
+  B, P, W = _setup()
+  mix = _mix(W)
+  n_steps = 6
+  qs, qds, acts = _inputs(W, mix, n_steps, 5)
+  b = B.Batch([m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix])
+  table = b.concat_steps(acts, 'act')
+  st = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
+  ref, _ = b.rollout(st, table)
+
+  def policy(k, state, act):
+    act.copy_(table[k])
+
+  g = B.GraphRollout(b, st, n_steps, policy)
+  final = g.replay()
+  torch.cuda.synchronize()
+  for f in ('q', 'qd'):
+    e = rel_err(getattr(final, f).cpu().numpy()[None], getattr(ref, f).cpu().numpy()[None])
+    assert e.max() <= 1e-6, (f, e.max())
+  # a second replay starts from the state the first one left
+  again = g.replay()
+  torch.cuda.synchronize()
+  assert torch.isfinite(again.q).all()
+
+
+def test_autotuner_picks_one_shape_per_bucket(tmp_path, monkeypatch):
+  B, P, W = _setup()
+  from brax_gb300 import autotune
+  monkeypatch.setenv('BRAXG_TUNE_CACHE', str(tmp_path / 'tune.json'))
+  mix = _mix(W)
+  systems, n_env, n_frames = [m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix]
+  shapes = autotune.tune_batch(systems, n_env, n_frames, n_steps=1, reps=1)
+  assert [s[0] for s in shapes] == [8, 16, 32]
+  for _, t, e in shapes:
+    assert t in (16, 32) and 0 <= e <= 256 // t
+  assert (tmp_path / 'tune.json').exists()
+  assert autotune.tune_batch(systems, n_env, n_frames) == shapes  # from the cache
+  b = B.Batch(systems, n_env, n_frames, shapes=shapes)
+  assert b.launch_info()['n_items'] >= 1
