@@ -95,6 +95,23 @@ def profiled_traffic(kernel: str):
   return None
 
 
+def max_over_ranks(seconds: float, device) -> float:
+  """The slowest rank's time (one all-reduce MAX); the value itself on one rank."""
+  import torch
+  import torch.distributed as dist
+  if not dist.is_available() or not dist.is_initialized() or dist.get_world_size() == 1:
+    return seconds
+  t = torch.tensor([seconds], dtype=torch.float64, device=device)
+  dist.all_reduce(t, op=dist.ReduceOp.MAX)
+  return float(t.item())
+
+
+def whole_job_rate(units_per_rank: int, world: int, seconds: float) -> float:
+  """Units all ranks processed (each rank a replica of the same size) over the
+  slowest rank's time."""
+  return units_per_rank * world / seconds
+
+
 def workload_config(n: int, world: int):
   return {'workload': f'{WORKLOAD} nq 15 nv 14 nu 8, 9 geoms vs plane (17 contact slots), '
                       f'{n} envs per GPU, env step = {N_FRAMES} x 0.01 s',
@@ -266,13 +283,9 @@ def run_braxg(args):
     dist.barrier()
   torch.cuda.synchronize()
   times = [a.elapsed_time(b) for a, b in ev]
-  t_total = sum(times) / 1e3
-  if world > 1:
-    t = torch.tensor([t_total], device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    t_total = float(t.item())
+  t_total = max_over_ranks(sum(times) / 1e3, dev)
   status = a_state.status.cpu().numpy()
-  value = args.steps * n * world / t_total
+  value = whole_job_rate(args.steps * n, world, t_total)
   ms_per_step = 1e3 * t_total / args.steps
 
   # ---- e2e through the public API with host buffers ----------------------
@@ -307,13 +320,9 @@ def run_braxg(args):
     h_obs.copy_(obs, non_blocking=True)
     e_ev[k][1].record(stream)
     stream.synchronize()
-  t_e2e = time.perf_counter() - t0
-  if world > 1:
-    t = torch.tensor([t_e2e], device=dev)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    t_e2e = float(t.item())
+  t_e2e = max_over_ranks(time.perf_counter() - t0, dev)
   gpu_e2e = sum(a.elapsed_time(b) for a, b in e_ev) / 1e3
-  e2e = {'value': args.steps * n * world / t_e2e, 'unit': 'env-steps/s',
+  e2e = {'value': whole_job_rate(args.steps * n, world, t_e2e), 'unit': 'env-steps/s',
          'ms_per_step_wall': round(1e3 * t_e2e / args.steps, 4),
          'ms_per_step_gpu': round(1e3 * gpu_e2e / args.steps, 4),
          'ms_per_step_api_call': round(1e3 * api_s / args.steps, 4),

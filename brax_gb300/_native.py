@@ -24,6 +24,7 @@ EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims',
            'braxg_rollout_vjp_noalloc_capacity', 'braxg_launch_shape',
            'braxg_batch_create', 'braxg_batch_destroy', 'braxg_batch_get_offsets',
            'braxg_batch_launch_info', 'braxg_batch_init', 'braxg_batch_rollout',
+           'braxg_env_rollout',
            'braxg_last_launch_count', 'braxg_last_error')
 
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED = 0, 1, 2, 3
@@ -55,6 +56,27 @@ OFFSET_FIELDS = ('env', 'q', 'qd', 'mass_mx', 'link', 'act', 'row', 'jac')
 
 class BatchOffsets(ctypes.Structure):
   _fields_ = [(n, ctypes.c_int64) for n in OFFSET_FIELDS]
+
+
+class Task(ctypes.Structure):
+  _fields_ = [('ctrl_cost_weight', ctypes.c_float), ('healthy_reward', ctypes.c_float),
+              ('healthy_z_min', ctypes.c_float), ('healthy_z_max', ctypes.c_float),
+              ('terminate_when_unhealthy', ctypes.c_int32),
+              ('exclude_current_positions', ctypes.c_int32), ('episode_length', ctypes.c_int32),
+              ('action_repeat', ctypes.c_int32), ('auto_reset', ctypes.c_int32),
+              ('reserved', ctypes.c_int32 * 3)]
+
+
+ENV_IO_FIELDS = ('obs', 'reward', 'done', 'metrics', 'steps', 'truncation', 'last_done',
+                 'first_q', 'first_qd', 'first_mass_mx_inv')
+
+
+class EnvIO(ctypes.Structure):
+  _fields_ = [(n, ctypes.c_void_p) for n in ENV_IO_FIELDS]
+
+
+METRICS = ('reward_forward', 'reward_survive', 'reward_ctrl', 'reward_contact', 'x_position',
+           'y_position', 'distance_from_origin', 'x_velocity', 'y_velocity', 'forward_reward')
 
 
 PROFILE_SLOTS = ('fk', 'com', 'crba', 'inverse', 'jacobian', 'smooth', 'constraint',
@@ -105,6 +127,8 @@ def lib() -> ctypes.CDLL:
                                           P(ctypes.c_int32), P(ctypes.c_int32)]
     l.braxg_batch_init.argtypes = [vp, vp, vp, vp, P(State), P(Options)]
     l.braxg_batch_rollout.argtypes = [vp, vp, i32, vp, P(State), P(State), vp, vp, P(Options)]
+    l.braxg_env_rollout.argtypes = [vp, vp, i32, i32, i32, vp, P(State), P(State), P(Task),
+                                    P(EnvIO), P(Options)]
     l.braxg_last_error.restype = ctypes.c_char_p
     l.braxg_last_launch_count.restype = ctypes.c_int
     for n in EXPORTS:

@@ -212,7 +212,8 @@ int braxg_init(const braxg_model* m, void* stream, int n_env, const float* q, co
 
 static int run_steps(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, const float* act,
                      long long act_stride, const braxg_state* in, braxg_state* out, float* tq, float* tqd,
-                     const braxg_options* opt) {
+                     const braxg_options* opt, const braxg_task* task = nullptr,
+                     const braxg_env_io* io = nullptr) {
   int rc = check_common(m, n_env, opt);
   if (rc) return rc;
   if (in == nullptr || out == nullptr) return fail(BRAXG_ERR_INVALID, "in and out states are required");
@@ -238,6 +239,12 @@ static int run_steps(const braxg_model* m, void* stream, int n_env, int n_steps,
   a.traj_qd = tqd;
   a.traj_q_stride = (long long)n_env * m->dims.nq;
   a.traj_qd_stride = (long long)n_env * m->dims.nv;
+  a.env_step_stride = n_env;
+  if (task != nullptr) {
+    a.has_task = 1;
+    a.task = *task;
+    a.io = *io;
+  }
   return launch(m, opt, a, static_cast<cudaStream_t>(stream));
 }
 
@@ -620,6 +627,25 @@ int braxg_batch_rollout(const braxg_batch* b, void* stream, int n_steps, const f
   s.traj_q_stride = tot.q;
   s.traj_qd_stride = tot.qd;
   return batch_launch(b, stream, s, opt);
+}
+
+int braxg_env_rollout(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, const float* act_seq,
+                      const braxg_state* in, braxg_state* out, const braxg_task* task, const braxg_env_io* io,
+                      const braxg_options* opt) {
+  if (m == nullptr || task == nullptr || io == nullptr) return fail(BRAXG_ERR_INVALID, "model, task and io are required");
+  if (task->episode_length < 1 || task->action_repeat < 1)
+    return fail(BRAXG_ERR_INVALID, "episode_length and action_repeat must be >= 1");
+  if (task->exclude_current_positions && m->dims.nq < 2)
+    return fail(BRAXG_ERR_INVALID, "exclude_current_positions needs nq >= 2");
+  const bool ns = !(opt && opt->inverse_mode == BRAXG_INV_CHOLESKY) && m->ns_iters > 0;
+  if (n_env > 0 && (io->obs == nullptr || io->reward == nullptr || io->steps == nullptr || io->truncation == nullptr ||
+                    io->last_done == nullptr || io->first_q == nullptr || io->first_qd == nullptr ||
+                    (ns && task->auto_reset && io->first_mass_mx_inv == nullptr)))
+    return fail(BRAXG_ERR_INVALID,
+                "io.obs, reward, steps, truncation, last_done, first_q, first_qd (and, Newton-Schulz mode with "
+                "auto_reset, first_mass_mx_inv) are required");
+  long long stride = (long long)n_env * m->dims.nu;
+  return run_steps(m, stream, n_env, n_steps, n_frames, act_seq, stride, in, out, nullptr, nullptr, opt, task, io);
 }
 
 int braxg_step(const braxg_model* m, void* stream, int n_env, int n_frames, const float* act, const braxg_state* in,

@@ -135,11 +135,142 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const EnvBase& B, 
   }
 }
 
+// The locomotion task after one env step (brax/envs/ant.py:233-279): every
+// lane of the team computes the same scalars from shared memory, so the
+// results are team-uniform.  pos0 is the torso (link 0) position before the
+// env step, dt the env step's duration (PipelineEnv.dt = n_frames x timestep).
+struct TaskOut {
+  float reward, done, met[BRAXG_M_COUNT];
+};
+
+template <int T>
+__device__ __forceinline__ TaskOut task_reward(const braxg_task& k, const Model& md, Ws w, f3 pos0, float dt,
+                                               bool has_act) {
+  const Layout& L = *w.L;
+  const f3 p = ld3(w.at(L.xp));
+  const f3 vel = mk3((p.x - pos0.x) / dt, (p.y - pos0.y) / dt, (p.z - pos0.z) / dt);
+  float healthy = p.z < k.healthy_z_min ? 0.f : 1.f;
+  healthy = p.z > k.healthy_z_max ? 0.f : healthy;
+  const float survive = k.terminate_when_unhealthy ? k.healthy_reward : k.healthy_reward * healthy;
+  float sq = 0.f;
+  if (has_act)
+    for (int i = 0; i < md.nu; ++i) sq += w.at(L.act)[i] * w.at(L.act)[i];
+  const float ctrl = k.ctrl_cost_weight * sq;
+  TaskOut o;
+  o.reward = vel.x + survive - ctrl - 0.f;
+  o.done = k.terminate_when_unhealthy ? 1.f - healthy : 0.f;
+  const float dist2 = dot3(p, p);
+  o.met[BRAXG_M_REWARD_FORWARD] = vel.x;
+  o.met[BRAXG_M_REWARD_SURVIVE] = survive;
+  o.met[BRAXG_M_REWARD_CTRL] = -ctrl;
+  o.met[BRAXG_M_REWARD_CONTACT] = -0.f;
+  o.met[BRAXG_M_X_POSITION] = p.x;
+  o.met[BRAXG_M_Y_POSITION] = p.y;
+  o.met[BRAXG_M_DISTANCE_FROM_ORIGIN] = dist2 > 0.f ? sqrtf(dist2) : 0.f;  // math.safe_norm
+  o.met[BRAXG_M_X_VELOCITY] = vel.x;
+  o.met[BRAXG_M_Y_VELOCITY] = vel.y;
+  o.met[BRAXG_M_FORWARD_REWARD] = vel.x;
+  return o;
+}
+
+// The fused env step's per-env bookkeeping, out of line so that the step
+// loop's register allocation does not carry it.  State in the arena's misc
+// words: [2..4] torso position before the env step, [5] reward sum, [6]
+// episode steps, [7] done of the previous env step, [8] the task's done.
+template <int T>
+__device__ __noinline__ void task_begin(const StepArgs& a, Ws w, long long ei, bool first) {
+  float* misc = w.at(w.L->misc);
+  if (Team<T>().lane == 0) {
+    if (first) {
+      misc[6] = a.io.steps[ei];
+      misc[7] = a.io.last_done[ei];
+    }
+    if (misc[7] != 0.f) misc[6] = 0.f;  // AutoResetWrapper: a new episode
+    misc[5] = 0.f;
+  }
+}
+
+template <int T>
+__device__ __noinline__ void task_mark(Ws w) {  // torso position before the env step
+  float* misc = w.at(w.L->misc);
+  if (Team<T>().lane == 0) st3(misc + 2, ld3(w.at(w.L->xp)));
+}
+
+template <int T>
+__device__ __noinline__ void task_after_rep(const StepArgs& a, const int* mw, Ws w, long long ei, bool last,
+                                            float env_dt, bool has_act) {
+  float* misc = w.at(w.L->misc);
+  if (Team<T>().lane != 0) return;
+  const Model md(mw);
+  const TaskOut t = task_reward<T>(a.task, md, w, ld3(misc + 2), env_dt, has_act);
+  misc[5] += t.reward;
+  misc[8] = t.done;
+  if (last && a.io.metrics != nullptr) {
+#pragma unroll
+    for (int i = 0; i < BRAXG_M_COUNT; ++i) a.io.metrics[ei * BRAXG_M_COUNT + i] = t.met[i];
+  }
+}
+
+// EpisodeWrapper's step count and truncation, the outputs of the env step and
+// AutoResetWrapper's return to the episode's first state; true if reset.
+template <int T>
+__device__ __noinline__ bool task_end(const StepArgs& a, const int* mw, Ws w, const EnvBase& B, long long env,
+                                      int s, int reps, bool exact_mode) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  float* misc = w.at(L.misc);
+  const long long ei = B.env + env;
+  if (tm.lane == 0) {
+    const float ep = misc[6] + (float)reps;
+    const bool over = ep >= (float)a.task.episode_length;
+    const float done = over ? 1.f : misc[8];
+    a.io.reward[s * a.env_step_stride + ei] = misc[5];
+    if (a.io.done != nullptr) a.io.done[s * a.env_step_stride + ei] = done;
+    if (s == a.n_steps - 1) a.io.truncation[ei] = over ? 1.f - misc[8] : 0.f;
+    misc[6] = ep;
+    misc[7] = done;
+  }
+  tm.sync();
+  const bool reset = a.task.auto_reset && misc[7] != 0.f;
+  if (reset) {  // back to the episode's first state
+    const int nq = md.nq, nv = md.nv, ld = L.ldm;
+    load_vec<T>(tm, w.at(L.q), a.io.first_q + B.q + env * nq, nq);
+    load_vec<T>(tm, w.at(L.qd), a.io.first_qd + B.v + env * nv, nv);
+    if (!exact_mode) {
+      const float* src = a.io.first_mass_mx_inv + B.vv + env * nv * nv;
+      for (int idx = tm.lane; idx < nv * nv; idx += T) {
+        int i = idx / nv, j = idx - i * nv;
+        w.at(L.Minv)[i * ld + j] = src[idx];
+      }
+    }
+  }
+  tm.sync();
+  return reset;
+}
+
+// obs of the (post-reset) final state and the wrappers' carried state.
+template <int T>
+__device__ __noinline__ void task_outputs(const StepArgs& a, const int* mw, Ws w, long long ei) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  const int nq = md.nq, nv = md.nv;
+  const int ox = a.task.exclude_current_positions ? 2 : 0, osz = nq - ox + nv;
+  float* obs = a.io.obs + ei * osz;
+  for (int i = tm.lane; i < nq - ox; i += T) obs[i] = w.at(L.q)[ox + i];
+  for (int i = tm.lane; i < nv; i += T) obs[nq - ox + i] = w.at(L.qd)[i];
+  if (tm.lane == 0) {
+    a.io.steps[ei] = w.at(L.misc)[6];
+    a.io.last_done[ei] = w.at(L.misc)[7];
+  }
+}
+
 // One env per team for n_steps x n_frames pipeline steps: load, step, write.
 // `arena` is the first per-env shared-memory arena of the CTA; B offsets the
 // env's rows in the (flat) global arrays.  Teams without an env (`active`
 // false) still take every CTA barrier and return before the outputs.
-template <int T, int NVB>
+template <int T, int NVB, bool TASK = false>
 __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, const int* smem, const Layout* sl,
                                          float* arena, int team, long long env, bool active, int n_frames) {
   const Model md(smem);
@@ -169,6 +300,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   tm.sync();
   pf.mark(BRAXG_PROF_IO);
   bool ok = position_stage<T, NVB>(smem, w, active, exact, 0, pf);
+  const long long ei = B.env + env;
   if (a.init) {
     for (int d = tm.lane; active && d < nv; d += T) {
       w.at(L.qfs)[d] = 0.f;
@@ -177,24 +309,38 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
     }
     tm.sync();
   } else {
+    const bool exact_mode = a.exact_inverse || md.ns_iters == 0;
+    const int reps = TASK ? max(1, a.task.action_repeat) : 1;
+    const float env_dt = (float)n_frames * md.dt;
     for (int s = 0; s < a.n_steps; ++s) {
       const bool has_act = a.act != nullptr && nu > 0;
       if (has_act && active) load_vec<T>(tm, w.at(L.act), a.act + s * a.act_step_stride + B.u + env * nu, nu);
+      if (TASK && active) task_begin<T>(a, w, ei, s == 0);
       tm.sync();
-      for (int f = 0; f < n_frames; ++f) {
-        if (active) stage_smooth<T>(smem, w, has_act);
-        __syncthreads();
-        pf.mark(BRAXG_PROF_SMOOTH);
-        int mvs = 0;
-        if (active) mvs = stage_constraint<T>(smem, w);
-        __syncthreads();
-        pf.count(BRAXG_PROF_MATVECS, (unsigned long long)mvs);
-        pf.mark(BRAXG_PROF_CONSTRAINT);
-        if (active) ok = stage_integrate<T>(smem, w) && ok;
-        __syncthreads();
-        pf.mark(BRAXG_PROF_INTEGRATE);
-        ok = position_stage<T, NVB>(smem, w, active, a.exact_inverse || md.ns_iters == 0, md.ns_iters, pf) && ok;
-        pf.count(BRAXG_PROF_SUBSTEPS, 1ull);
+      for (int r = 0; r < reps; ++r) {  // EpisodeWrapper's action repeat
+        if (TASK && active) task_mark<T>(w);
+        for (int f = 0; f < n_frames; ++f) {
+          if (active) stage_smooth<T>(smem, w, has_act);
+          __syncthreads();
+          pf.mark(BRAXG_PROF_SMOOTH);
+          int mvs = 0;
+          if (active) mvs = stage_constraint<T>(smem, w);
+          __syncthreads();
+          pf.count(BRAXG_PROF_MATVECS, (unsigned long long)mvs);
+          pf.mark(BRAXG_PROF_CONSTRAINT);
+          if (active) ok = stage_integrate<T>(smem, w) && ok;
+          __syncthreads();
+          pf.mark(BRAXG_PROF_INTEGRATE);
+          ok = position_stage<T, NVB>(smem, w, active, exact_mode, md.ns_iters, pf) && ok;
+          pf.count(BRAXG_PROF_SUBSTEPS, 1ull);
+        }
+        if (TASK && active)
+          task_after_rep<T>(a, smem, w, ei, r == reps - 1 && s == a.n_steps - 1, env_dt, has_act);
+      }
+      if (TASK) {
+        const bool reset = active && task_end<T>(a, smem, w, B, env, s, reps, exact_mode);
+        // the reset envs' position terms (CTA-uniform: only when some env reset)
+        if (__syncthreads_or(reset)) ok = position_stage<T, NVB>(smem, w, active && reset, exact_mode, 0, pf) && ok;
       }
       if (active && a.traj_q != nullptr)
         store_vec<T>(tm, a.traj_q + s * a.traj_q_stride + B.q + env * nq, w.at(L.q), nq);
@@ -203,12 +349,15 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
     }
   }
   if (!active) return;  // no CTA barrier follows
+  if (TASK && a.n_steps > 0 && !a.init) task_outputs<T>(a, smem, w, ei);
   write_outputs<T>(a, B, smem, w, env, ok);
   pf.mark(BRAXG_PROF_IO);
   pf.count(BRAXG_PROF_NS_RESETS, (unsigned long long)reinterpret_cast<const int*>(w.at(L.misc))[1]);
 }
 
-template <int T, int NVB>
+// TASK: the fused env step variant (braxg_env_rollout); the plain pipeline
+// kernel compiles without any of its code.
+template <int T, int NVB, bool TASK>
 __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   extern __shared__ __align__(16) int smem[];
   for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
@@ -225,14 +374,17 @@ __global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
   if (!active) env = 0;
   const EnvBase B{};
   float* arena = reinterpret_cast<float*>(smem + al4(a.model_words) + kLayoutWords);
-  run_team<T, NVB>(a, B, smem, shared_layout, arena, team, env, active, a.n_frames);
+  run_team<T, NVB, TASK>(a, B, smem, shared_layout, arena, team, env, active, a.n_frames);
 }
 
 constexpr int kMaxSmemBytes = 227 * 1024;
 
-template <int T, int NVB>
-cudaError_t launch_step(const StepArgs& a, int grid, int smem, cudaStream_t st) {
-  auto k = step_kernel<T, NVB>;
+// One launch of a step-kernel variant; the first launch on a device opts the
+// kernel into the large dynamic shared memory (the flag is per template
+// instance, so per kernel).
+template <int T, int NVB, bool TASK>
+cudaError_t launch_step_variant(const StepArgs& a, int grid, int smem, cudaStream_t st) {
+  auto k = step_kernel<T, NVB, TASK>;
   static bool attr_set[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
@@ -243,6 +395,12 @@ cudaError_t launch_step(const StepArgs& a, int grid, int smem, cudaStream_t st) 
   }
   k<<<grid, a.envs_per_cta * T, smem, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int T, int NVB>
+cudaError_t launch_step(const StepArgs& a, int grid, int smem, cudaStream_t st) {
+  if (a.has_task) return launch_step_variant<T, NVB, true>(a, grid, smem, st);
+  return launch_step_variant<T, NVB, false>(a, grid, smem, st);
 }
 
 }  // namespace braxg

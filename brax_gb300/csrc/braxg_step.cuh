@@ -88,7 +88,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.tau = take(nv);
   L.v1 = take(nv);
   L.v2 = take(nv);
-  L.misc = take(8);
+  L.misc = take(12);  // [0] active rows, [1] NS resets, [2..8] env-step task state
   L.xp = take(3 * nl);
   L.xr = take(4 * nl);
   L.xa = take(3 * nl);
@@ -697,6 +697,89 @@ __device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc,
   return ok;
 }
 
+// spd_inverse with the work spread over the entries: every lane owns fixed
+// entries of the packed lower triangle (entry e = i(i+1)/2 + j, e = lane,
+// lane + T, ...), kept as (i, j) in registers, and each step of the
+// factorisation / elimination updates all live entries at once instead of
+// one column per lane.  Each entry sees the same operations in the same order
+// as in spd_inverse.  E bounds the entries per lane for matrices up to NVB.
+template <int T, int NVB>
+__device__ bool spd_inverse_owned(const Team<T>& tm, int n, int ld, const float* Msrc, float* Lw, float* X,
+                                  float* Minv) {
+  constexpr int E = (NVB * (NVB + 1) / 2 + T - 1) / T;
+  int oi[E], oj[E];
+  {
+    const int cnt = n * (n + 1) / 2;
+    int e = tm.lane, i = 0, j = tm.lane;
+    while (j > i) {
+      j -= i + 1;
+      ++i;
+    }
+#pragma unroll
+    for (int t = 0; t < E; ++t) {
+      const bool v = e < cnt;
+      oi[t] = v ? i : -1;
+      oj[t] = v ? j : 0;
+      e += T;
+      j += T;
+      while (j > i) {
+        j -= i + 1;
+        ++i;
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < E; ++t)
+    if (oi[t] >= 0) {
+      Lw[oi[t] * ld + oj[t]] = Msrc[oi[t] * ld + oj[t]];
+      X[oi[t] * ld + oj[t]] = (oi[t] == oj[t]) ? 1.f : 0.f;
+    }
+  tm.sync();
+  bool ok = true;
+  for (int k = 0; k < n; ++k) {  // right-looking Cholesky
+    const float piv = Lw[k * ld + k];
+    ok = ok && (piv > 0.f);
+    const float d = sqrtf(fmaxf(piv, 1e-30f));
+#pragma unroll
+    for (int t = 0; t < E; ++t)
+      if (oj[t] == k && oi[t] > k) Lw[oi[t] * ld + k] = Lw[oi[t] * ld + k] / d;
+    tm.sync();
+    if (tm.lane == 0) Lw[k * ld + k] = d;
+#pragma unroll
+    for (int t = 0; t < E; ++t)
+      if (oj[t] > k) Lw[oi[t] * ld + oj[t]] = Lw[oi[t] * ld + oj[t]] - Lw[oi[t] * ld + k] * Lw[oj[t] * ld + k];
+    tm.sync();
+  }
+  for (int k = 0; k < n; ++k) {  // X = L^-1, right-looking forward elimination
+    const float lkk = Lw[k * ld + k];
+#pragma unroll
+    for (int t = 0; t < E; ++t)
+      if (oi[t] == k) X[k * ld + oj[t]] = X[k * ld + oj[t]] / lkk;
+    tm.sync();
+#pragma unroll
+    for (int t = 0; t < E; ++t)
+      if (oi[t] > k && oj[t] <= k) X[oi[t] * ld + oj[t]] = X[oi[t] * ld + oj[t]] - Lw[oi[t] * ld + k] * X[k * ld + oj[t]];
+    tm.sync();
+  }
+#pragma unroll
+  for (int t = 0; t < E; ++t) {  // Minv = X^T X, entry (i, j), i >= j
+    if (oi[t] < 0) continue;
+    const int i = oi[t], j = oj[t];
+    float s0 = 0.f, s1 = 0.f;
+    int m = i;
+    for (; m + 1 < n; m += 2) {
+      s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
+      s1 = fmaf(X[(m + 1) * ld + i], X[(m + 1) * ld + j], s1);
+    }
+    if (m < n) s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
+    const float v = s0 + s1;
+    Minv[i * ld + j] = v;
+    Minv[j * ld + i] = v;
+  }
+  tm.sync();
+  return ok;
+}
+
 // ---------------------------------------------------------------------------
 // mass.matrix_inv: brax/generalized/mass.py:86-106 + brax/math.py:278-305
 // mode 0 keeps/updates Minv by Newton-Schulz (num_iter iterations; 0 keeps
@@ -714,7 +797,9 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   float* S2 = S1 + n * ld;
   if (n == 0) return true;
   if (exact) {
-    return spd_inverse<T>(tm, n, ld, M, S1, S2, P);
+    // entry ownership while the owned (i, j) pairs fit a few registers
+    if constexpr ((NVB * (NVB + 1) / 2 + T - 1) / T <= 17) return spd_inverse_owned<T, NVB>(tm, n, ld, M, S1, S2, P);
+    else return spd_inverse<T>(tm, n, ld, M, S1, S2, P);
   }
   if (num_iter <= 0) return true;
   float* cur = P;

@@ -101,13 +101,17 @@ def uneven_mix(total: int = 8192, seed: int = 0):
   return out
 
 
-def reset(sys: System, n: int, rng: np.random.Generator):
-  """Seeded (q, qd) for n envs: chains q ~ U(-pi/4, pi/4), qd ~ N(0, 0.1);
-  models with a free root init_q + U(-0.1, 0.1) jitter, qd ~ 0.1 N(0, 1)
-  (brax/envs/ant.py:209-213)."""
+def reset(sys: System, n: int, rng: np.random.Generator, chain_spread: float = 0.1):
+  """Seeded (q, qd) for n envs.  Chains hang close to straight with the last
+  link on the plane: q ~ U(-chain_spread, chain_spread) per joint, qd ~
+  N(0, 0.1) (the 3-link chain workload spreads its 3 joints over
+  U(-pi/4, pi/4); spread that wide, chains of 20+ links whip their free end
+  past what the semi-implicit integrator holds at dt 0.01, in the FP64
+  restatement as well).  Models with a free root: init_q + U(-0.1, 0.1)
+  jitter, qd ~ 0.1 N(0, 1) (brax/envs/ant.py:209-213)."""
   nq, nv = sys.q_size(), sys.qd_size()
   if family(sys) == 'chain':
-    q = rng.uniform(-np.pi / 4, np.pi / 4, (n, nq))
+    q = rng.uniform(-chain_spread, chain_spread, (n, nq))
     qd = rng.normal(0.0, 0.1, (n, nv))
   else:
     q = sys.init_q[None] + rng.uniform(-0.1, 0.1, (n, nq))
@@ -116,9 +120,12 @@ def reset(sys: System, n: int, rng: np.random.Generator):
 
 
 def actions(sys: System, n: int, rng: np.random.Generator):
-  """Actions in the control range: humanoid-like N(0, 0.3) clipped to [-1, 1],
-  the others U(-1, 1)."""
+  """Actions in the control range: chains zero (the plain 3-link chain
+  workload's zero actions: gravity and the plane only), humanoid-like
+  N(0, 0.3) clipped to [-1, 1], the others U(-1, 1)."""
   nu = sys.act_size()
+  if family(sys) == 'chain':
+    return np.zeros((n, nu))
   if family(sys) == 'humanoid_like':
     return np.clip(rng.normal(0.0, 0.3, (n, nu)), -1.0, 1.0)
   return rng.uniform(-1.0, 1.0, (n, nu))

@@ -139,6 +139,56 @@ int braxg_rollout(const braxg_model* model, void* stream, int n_env, int n_steps
                   braxg_state* out, float* traj_q, float* traj_qd,
                   const braxg_options* opt);
 
+/* ---- Fused env step ---------------------------------------------------------
+ * The locomotion task of brax/envs/ant.py:233-279 (forward reward, healthy
+ * reward, control cost, healthy-z termination, obs = q[2:] ++ qd) wrapped by
+ * EpisodeWrapper and AutoResetWrapper (brax/envs/wrappers/training.py:75-158),
+ * computed in the same launch as the physics: per env step, the n_frames
+ * pipeline steps, then reward / done / metrics, then (done envs) the reset to
+ * the episode's first state. */
+typedef struct {
+  float ctrl_cost_weight;            /* 0.5 */
+  float healthy_reward;              /* 1.0 */
+  float healthy_z_min, healthy_z_max;  /* 0.2, 1.0: torso (link 0) height range */
+  int32_t terminate_when_unhealthy;  /* 1 */
+  int32_t exclude_current_positions; /* 1: obs = q[2:] ++ qd, else q ++ qd */
+  int32_t episode_length;            /* 1000 env steps (EpisodeWrapper) */
+  int32_t action_repeat;             /* 1 */
+  int32_t auto_reset;                /* 1 (AutoResetWrapper) */
+  int32_t reserved[3];
+} braxg_task;
+
+/* Metric columns of braxg_env_io.metrics (ant.py:256-267 order). */
+enum braxg_env_metric {
+  BRAXG_M_REWARD_FORWARD = 0, BRAXG_M_REWARD_SURVIVE, BRAXG_M_REWARD_CTRL,
+  BRAXG_M_REWARD_CONTACT, BRAXG_M_X_POSITION, BRAXG_M_Y_POSITION,
+  BRAXG_M_DISTANCE_FROM_ORIGIN, BRAXG_M_X_VELOCITY, BRAXG_M_Y_VELOCITY,
+  BRAXG_M_FORWARD_REWARD, BRAXG_M_COUNT = 10
+};
+
+/* Per-env task buffers (device pointers).  steps, truncation and done carry the
+ * wrappers' state between calls (read and written); first_* is the state an
+ * auto-reset returns to (the episode's first pipeline state). */
+typedef struct {
+  float* obs;          /* [n, obs_size] after the last env step (post-reset) */
+  float* reward;       /* [n_steps, n] */
+  float* done;         /* [n_steps, n] (optional) */
+  float* metrics;      /* [n, BRAXG_M_COUNT] of the last env step (optional) */
+  float* steps;        /* [n] episode step counter */
+  float* truncation;   /* [n] */
+  float* last_done;    /* [n] done of the previous env step (in) / last (out) */
+  const float* first_q;            /* [n, nq] */
+  const float* first_qd;           /* [n, nv] */
+  const float* first_mass_mx_inv;  /* [n, nv, nv] (Newton-Schulz mode) */
+} braxg_env_io;
+
+/* n_steps env steps (env.step of AutoResetWrapper(EpisodeWrapper(task))) with
+ * act_seq [n_steps, n, nu]; the pipeline state in/out as braxg_rollout. */
+int braxg_env_rollout(const braxg_model* model, void* stream, int n_env, int n_steps,
+                      int n_frames, const float* act_seq, const braxg_state* in,
+                      braxg_state* out, const braxg_task* task, const braxg_env_io* io,
+                      const braxg_options* opt);
+
 /* Device workspace braxg_rollout_vjp needs: the checkpoints (every
  * ckpt_every env steps) and the per-frame states of one recomputed segment. */
 int braxg_rollout_vjp_workspace(const braxg_model* model, int n_env, int n_steps, int n_frames,
