@@ -112,6 +112,11 @@ def whole_job_rate(units_per_rank: int, world: int, seconds: float) -> float:
   return units_per_rank * world / seconds
 
 
+def WORKLOAD_SYS():
+  from brax_gb300 import mjcf
+  return mjcf.load_asset(WORKLOAD)
+
+
 def workload_config(n: int, world: int):
   return {'workload': f'{WORKLOAD} nq 15 nv 14 nu 8, 9 geoms vs plane (17 contact slots), '
                       f'{n} envs per GPU, env step = {N_FRAMES} x 0.01 s',
@@ -359,6 +364,7 @@ def run_braxg(args):
   clocks = clk.summary()
   adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank)
   uneven = None if args.no_uneven else bench_uneven(torch, dev, rank)
+  env_step = bench_env(torch, dev, rank)
   out = {
       'metric': METRIC, 'value': round(value, 1), 'unit': 'env-steps/s', 'n_gpus': world,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
@@ -371,7 +377,7 @@ def run_braxg(args):
                                           model.launch_shape(mode, args.threads_per_env,
                                                              args.envs_per_cta)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
-      'adjoint': adjoint, 'uneven': uneven,
+      'adjoint': adjoint, 'uneven': uneven, 'env_step': env_step,
       'env_status_nonzero': int((status != 0).sum()),
   }
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -426,6 +432,38 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
           'fwd_ms': round(1e3 * t_f, 3), 'fwd_adj_ms': round(1e3 * t_b, 3),
           'cost_ratio_fwd_adj_over_fwd': round(t_b / t_f, 3),
           'envs_without_gradient': bad, 'gpu_launches_fwd_adj': 1}
+
+
+def bench_env(torch, dev, rank, n=4096, steps=50, warmup=3):
+  """The fused env step (locomotion task + EpisodeWrapper + AutoResetWrapper in
+  the physics launch) on the headline workload: one launch per env step, L2
+  flushed between steps like the pipeline measurement."""
+  from brax_gb300 import envs as E
+  env = E.Locomotion(WORKLOAD_SYS(), device=dev)
+  gen = torch.Generator(device=dev)
+  gen.manual_seed(500 + rank)
+  st = env.reset(n, generator=gen)
+  acts = torch.rand(warmup + steps, n, env.action_size, device=dev, generator=gen) * 2 - 1
+  for k in range(warmup):
+    st = env.step(st, acts[k])
+  flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+  stream = torch.cuda.current_stream(dev)
+  torch.cuda.synchronize()
+  t = 0.0
+  dones = 0.0
+  for k in range(steps):
+    flush.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    st = env.step(st, acts[warmup + k])
+    e1.record(stream)
+    e1.synchronize()
+    t += e0.elapsed_time(e1) / 1e3
+    dones += float(st.done.sum().item())
+  bad = int((st.pipeline_state.status != 0).sum().item())
+  return {'workload': f'quadruped locomotion task, {n} envs, auto-reset, episode_length 1000, 5 frames',
+          'env_steps_per_s': round(steps * n / t, 1), 'ms_per_step': round(1e3 * t / steps, 4),
+          'resets_per_env_step': round(dones / steps, 2), 'env_status_nonzero': bad, 'gpu_launches_per_step': 1}
 
 
 def bench_uneven(torch, dev, rank, total=8192, n_steps=256):

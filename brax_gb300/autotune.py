@@ -81,10 +81,15 @@ def _store(table: Dict):
 
 
 def _time_shape(systems, n_env, n_frames, shape, device, n_steps: int, reps: int, smem: int) -> float:
+  return _time_batch(systems, n_env, n_frames, [(BUCKETS[-1], shape[0], shape[1])], device, n_steps, reps,
+                     smem)
+
+
+def _time_batch(systems, n_env, n_frames, shapes, device, n_steps: int, reps: int, smem: int = 0) -> float:
+  """Median CUDA-event time (ms) of an n_steps rollout of the batch."""
   from brax_gb300.batch import Batch
   from brax_gb300 import workloads as W
-  b = Batch(systems, n_env, n_frames, shapes=[(BUCKETS[-1], shape[0], shape[1])], smem_per_cta=smem,
-            device=device)
+  b = Batch(systems, n_env, n_frames, shapes=shapes, smem_per_cta=smem, device=device)
   rng = np.random.default_rng(0)
   qs, qds, acts = [], [], []
   for s, n in zip(systems, n_env):
@@ -109,11 +114,13 @@ def _time_shape(systems, n_env, n_frames, shape, device, n_steps: int, reps: int
 
 
 def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Sequence[int]] = None,
-               device=None, n_steps: int = 2, reps: int = 3, use_cache: bool = True,
+               device=None, n_steps: int = 8, reps: int = 5, use_cache: bool = True,
                verbose: bool = False) -> List[Tuple[int, int, int]]:
   """Shapes [(nv_max, threads_per_env, envs_per_cta)] for ``Batch(shapes=...)``,
   one per nv bucket present, each the fastest candidate for that bucket's
-  models timed alone."""
+  models timed alone; the combination is then timed on the whole batch
+  against the default shape (32 lanes, envs per CTA filling 113 KB) and the
+  faster of the two is returned (an empty list for the default)."""
   device = torch.device('cuda') if device is None else torch.device(device)
   if device.index is None:
     device = torch.device('cuda', torch.cuda.current_device())
@@ -153,6 +160,23 @@ def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Seque
       table[key] = hit
       dirty = True
     shapes.append((bucket, hit['threads_per_env'], hit['envs_per_cta']))
+  if len(groups) > 0:  # the combination against the default on the whole batch
+    all_idx = [g for idx in groups.values() for g in idx]
+    key = _key(device, 0, [systems[g] for g in all_idx], [n_env[g] for g in all_idx],
+               [n_frames[g] for g in all_idx]) + '|' + repr(shapes)
+    hit = table.get(key)
+    if hit is None:
+      live = [g for g in range(len(systems)) if n_env[g] > 0]
+      args = ([systems[g] for g in live], [n_env[g] for g in live], [n_frames[g] for g in live])
+      tuned = _time_batch(*args, shapes, device, n_steps, reps)
+      default = _time_batch(*args, [], device, n_steps, reps)
+      hit = {'use_tuned': tuned <= default, 'tuned_ms': tuned, 'default_ms': default}
+      table[key] = hit
+      dirty = True
+      if verbose:
+        print(f'whole batch: tuned {tuned:.3f} ms, default {default:.3f} ms')
+    if not hit['use_tuned']:
+      shapes = []
   if dirty and use_cache:
     with _lock:
       merged = _load()

@@ -25,6 +25,7 @@ struct braxg_model {
   std::vector<int> h;
   braxg_dims dims;
   int ns_iters;
+  int sms;  // multiprocessors of the model's device
   braxg::Layout L;
 };
 
@@ -55,7 +56,7 @@ constexpr int kMaxSmem = 227 * 1024;
 // per-CTA budget of the default launch shape: two CTAs fit one SM
 constexpr int kHalfSmem = 113 * 1024;
 
-int choose_shape(const braxg_model* m, const braxg_options* opt, Shape* s) {
+int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shape* s) {
   int nv = m->dims.nv;
   s->NVB = nv <= 16 ? 16 : (nv <= 32 ? 32 : 64);
   int T = (opt && opt->threads_per_env) ? opt->threads_per_env : 32;
@@ -71,8 +72,11 @@ int choose_shape(const braxg_model* m, const braxg_options* opt, Shape* s) {
                 env_bytes, kMaxSmem - model_bytes);
   int epc = (opt && opt->envs_per_cta) ? opt->envs_per_cta : 0;
   if (epc == 0) {
-    // default: up to half the SM's shared memory per CTA, so two CTAs share an SM
+    // default: up to half the SM's shared memory per CTA, so two CTAs share an
+    // SM; a batch too small to fill every SM that way is spread over all of
+    // them instead (latency-bound envs run faster with fewer per SM)
     epc = (kHalfSmem - model_bytes) / env_bytes;
+    if (n_env > 0 && m->sms > 0) epc = std::min(epc, (n_env + m->sms - 1) / m->sms);
     if (epc < 1) epc = 1;
     if (epc > max_epc) epc = max_epc;
   }
@@ -86,7 +90,7 @@ int choose_shape(const braxg_model* m, const braxg_options* opt, Shape* s) {
 int launch(const braxg_model* m, const braxg_options* opt, braxg::StepArgs& a, cudaStream_t st) {
   g_launches = 0;
   Shape s;
-  int rc = choose_shape(m, opt, &s);
+  int rc = choose_shape(m, opt, a.n_env, &s);
   if (rc) return rc;
   if (a.n_env == 0) return BRAXG_OK;
   a.envs_per_cta = s.epc;
@@ -151,6 +155,7 @@ int braxg_model_create(const void* desc, size_t desc_bytes, int device, braxg_mo
   int cur = 0;
   cudaGetDevice(&cur);
   cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, device);
   if (e == cudaSuccess) e = cudaMalloc(&m->d_desc, (size_t)words * 4);
   if (e == cudaSuccess) e = cudaMemcpy(m->d_desc, w, (size_t)words * 4, cudaMemcpyHostToDevice);
   cudaSetDevice(cur);
@@ -182,7 +187,7 @@ int braxg_model_dims(const braxg_model* m, braxg_dims* out) {
 int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int32_t* tpe, int32_t* epc, int32_t* smem) {
   if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model is NULL");
   Shape s;
-  int rc = choose_shape(m, opt, &s);
+  int rc = choose_shape(m, opt, 0, &s);
   if (rc) return rc;
   if (tpe) *tpe = s.T;
   if (epc) *epc = s.epc;
@@ -331,6 +336,7 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
   int epc = (kMaxSmem - head) / env_bytes;
   if (epc < 1) return fail(BRAXG_ERR_UNSUPPORTED, "model too large for the gradient kernel's shared memory");
   if (epc > 8) epc = 8;
+  if (m->sms > 0) epc = std::max(1, std::min(epc, (n_env + m->sms - 1) / m->sms));  // spread over every SM
   a.envs_per_cta = epc;
   int smem = head + epc * env_bytes;
   int grid = (n_env + epc - 1) / epc;

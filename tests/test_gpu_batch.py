@@ -8,7 +8,8 @@
 * a 16-lane shape gives the 32-lane result within FP32 summation-order noise;
 * n steps captured as one CUDA graph of per-step launches reproduce the
   single-launch rollout;
-* the autotuner returns one valid shape per nv bucket and caches it.
+* the autotuner returns one valid shape per nv bucket (or the default when
+  that is faster on the whole batch) and caches its choice.
 """
 
 import numpy as np
@@ -182,7 +183,8 @@ def test_autotuner_picks_one_shape_per_bucket(tmp_path, monkeypatch):
   mix = _mix(W)
   systems, n_env, n_frames = [m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix]
   shapes = autotune.tune_batch(systems, n_env, n_frames, n_steps=1, reps=1)
-  assert [s[0] for s in shapes] == [8, 16, 32]
+  # one shape per bucket, or none when the default shape was faster on the whole batch
+  assert [s[0] for s in shapes] in ([8, 16, 32], [])
   for _, t, e in shapes:
     assert t in (16, 32) and 0 <= e <= 256 // t
   assert (tmp_path / 'tune.json').exists()
