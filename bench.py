@@ -391,7 +391,10 @@ def run_braxg(args):
 def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16, reps=3):
   """Forward rollout vs fused forward + adjoint (the APG workload): quadruped,
   512 envs, 128 env steps of 5 frames, loss -mean(torso x-velocity) +
-  1e-3 sum |u|^2, gradients w.r.t. the actions and qd0, checkpoint every 16."""
+  1e-3 sum |u|^2, gradients w.r.t. the actions and qd0, checkpoint every 16.
+  Timed with every segment's frame snapshots resident (the default when they
+  fit: no recompute) and with the smallest workspace (recompute of all but
+  the last segment)."""
   rng = np.random.default_rng(55 + rank)
   q0 = torch.tensor((sys_.init_q + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))).astype(np.float32), device=dev)
   qd0 = torch.tensor((0.1 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32), device=dev)
@@ -419,18 +422,22 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
 
   status = [None]
 
-  def fwd_adj():
-    r = pipeline.rollout_grad(sys_, q0, qd0, u, None, qd_bar, n_frames=N_FRAMES, ckpt_every=ckpt)
+  def fwd_adj(resident=None):
+    r = pipeline.rollout_grad(sys_, q0, qd0, u, None, qd_bar, n_frames=N_FRAMES, ckpt_every=ckpt,
+                              resident_segments=resident)
     status[0] = r[3]
 
   t_f = timed(fwd)
-  t_b = timed(fwd_adj)
+  t_b = timed(fwd_adj)  # every segment's snapshots resident (they fit): no recompute
+  t_m = timed(lambda: fwd_adj(1))  # smallest workspace: all but the last segment recomputed
   bad = int((status[0] != 0).sum().item())
   return {'workload': f'quadruped, {n} envs, {horizon} env steps x {N_FRAMES} frames, checkpoint every {ckpt}',
           'fwd_env_steps_per_s': round(n * horizon / t_f, 1),
           'fwd_adj_env_steps_per_s': round(n * horizon / t_b, 1),
           'fwd_ms': round(1e3 * t_f, 3), 'fwd_adj_ms': round(1e3 * t_b, 3),
           'cost_ratio_fwd_adj_over_fwd': round(t_b / t_f, 3),
+          'fwd_adj_ms_smallest_workspace': round(1e3 * t_m, 3),
+          'cost_ratio_smallest_workspace': round(t_m / t_f, 3),
           'envs_without_gradient': bad, 'gpu_launches_fwd_adj': 1}
 
 

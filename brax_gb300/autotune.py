@@ -168,8 +168,8 @@ def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Seque
     if hit is None:
       live = [g for g in range(len(systems)) if n_env[g] > 0]
       args = ([systems[g] for g in live], [n_env[g] for g in live], [n_frames[g] for g in live])
-      tuned = _time_batch(*args, shapes, device, n_steps, reps)
-      default = _time_batch(*args, [], device, n_steps, reps)
+      tuned = _time_batch(*args, shapes, device, 4 * n_steps, reps)
+      default = _time_batch(*args, [], device, 4 * n_steps, reps)
       hit = {'use_tuned': tuned <= default, 'tuned_ms': tuned, 'default_ms': default}
       table[key] = hit
       dirty = True

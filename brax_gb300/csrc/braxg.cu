@@ -258,29 +258,45 @@ static int vjp_snap_words(const braxg_model* m) {
   return m->L.total + braxg::al4(braxg::kTapeHeadWords + m->h[BXM_H_PG_ITERS] * braxg::kTapeIterWords);
 }
 
-// Workspace of braxg_rollout_vjp: checkpoints [n_ckpt, n, nq + nv], one
-// segment's frame input states [ckpt_every * n_frames, n, nq + nv] and its
-// frame snapshots [ckpt_every * n_frames, n, snap_words]; each part starts on
-// a 256-byte boundary.
-static void vjp_sizes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, size_t* ckpt_floats,
-                      size_t* seg_floats, size_t* snap_floats) {
+// Workspace of braxg_rollout_vjp: checkpoints [n_ckpt, n, nq + nv], then the
+// frame input states [frames, n, nq + nv] and frame snapshots
+// [frames, n, snap_words] of the snapshot blocks: the last `resident` segments
+// as the checkpoint pass leaves them, and the first block reused by every
+// recomputed segment; each part starts on a 256-byte boundary.
+static int vjp_n_ckpt(int n_steps, int ckpt_every) { return (n_steps + ckpt_every - 1) / ckpt_every; }
+
+static void vjp_sizes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, int resident,
+                      size_t* ckpt_floats, size_t* seg_floats, size_t* snap_floats) {
   size_t S = (size_t)m->dims.nq + m->dims.nv;
-  size_t n_ckpt = (size_t)(n_steps + ckpt_every - 1) / ckpt_every;
-  size_t seg_frames = (size_t)std::min(ckpt_every, n_steps) * n_frames;
-  *ckpt_floats = (n_ckpt * n_env * S + 63) / 64 * 64;
-  *seg_floats = (seg_frames * n_env * S + 63) / 64 * 64;
-  *snap_floats = seg_frames * n_env * (size_t)vjp_snap_words(m);
+  const int n_ckpt = vjp_n_ckpt(n_steps, ckpt_every);
+  const int first_res = n_ckpt - resident;
+  const int steps = std::max(n_steps - first_res * ckpt_every, first_res > 0 ? ckpt_every : 0);
+  size_t frames = (size_t)steps * n_frames;
+  *ckpt_floats = ((size_t)n_ckpt * n_env * S + 63) / 64 * 64;
+  *seg_floats = (frames * n_env * S + 63) / 64 * 64;
+  *snap_floats = frames * n_env * (size_t)vjp_snap_words(m);
+}
+
+static size_t vjp_bytes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, int resident) {
+  size_t c, sg, sn;
+  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, resident, &c, &sg, &sn);
+  return (c + sg + sn) * sizeof(float);
+}
+
+int braxg_rollout_vjp_workspace_resident(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every,
+                                         int resident, size_t* bytes) {
+  if (m == nullptr || bytes == nullptr) return fail(BRAXG_ERR_INVALID, "NULL argument");
+  if (n_env < 0 || n_steps < 1 || n_frames < 1 || ckpt_every < 1)
+    return fail(BRAXG_ERR_INVALID, "n_env >= 0, n_steps, n_frames and ckpt_every >= 1 required");
+  const int n_ckpt = vjp_n_ckpt(n_steps, ckpt_every);
+  if (resident <= 0 || resident > n_ckpt) resident = n_ckpt;
+  *bytes = vjp_bytes(m, n_env, n_steps, n_frames, ckpt_every, resident);
+  return BRAXG_OK;
 }
 
 int braxg_rollout_vjp_workspace(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every,
                                 size_t* bytes) {
-  if (m == nullptr || bytes == nullptr) return fail(BRAXG_ERR_INVALID, "NULL argument");
-  if (n_env < 0 || n_steps < 1 || n_frames < 1 || ckpt_every < 1)
-    return fail(BRAXG_ERR_INVALID, "n_env >= 0, n_steps, n_frames and ckpt_every >= 1 required");
-  size_t c, sg, sn;
-  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, &c, &sg, &sn);
-  *bytes = (c + sg + sn) * sizeof(float);
-  return BRAXG_OK;
+  return braxg_rollout_vjp_workspace_resident(m, n_env, n_steps, n_frames, ckpt_every, 1, bytes);
 }
 
 int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, int ckpt_every,
@@ -302,8 +318,14 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
     if ((kind != BXM_CON_PLANE_SPHERE && kind != BXM_CON_PLANE_CAPSULE) || la >= 0)
       return fail(BRAXG_ERR_UNSUPPORTED, "gradients support world-plane sphere/capsule contacts only");
   }
+  // as many trailing segments resident as the workspace holds
+  const int n_ckpt = vjp_n_ckpt(n_steps, ckpt_every);
+  int resident = 1;
+  while (resident < n_ckpt &&
+         vjp_bytes(m, n_env, n_steps, n_frames, ckpt_every, resident + 1) <= workspace_bytes)
+    ++resident;
   size_t c, sg, sn;
-  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, &c, &sg, &sn);
+  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, resident, &c, &sg, &sn);
   if (reinterpret_cast<uintptr_t>(workspace) % 16 != 0)
     return fail(BRAXG_ERR_INVALID, "workspace must be 16-byte aligned");
   braxg::VjpArgs a{};
@@ -325,6 +347,7 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
   a.seg = static_cast<float*>(workspace) + c;
   a.snap = static_cast<float*>(workspace) + c + sg;
   a.snap_words = vjp_snap_words(m);
+  a.resident = resident;
   a.traj_q = traj_q;
   a.traj_qd = traj_qd;
   a.status = status;

@@ -80,6 +80,7 @@ struct VjpArgs {
   float* seg;           // [ckpt_every * n_frames, n, nq + nv] frame input states
   float* snap;          // [ckpt_every * n_frames, n, snap_words] frame snapshots
   int snap_words;       // forward arena + PG tape words (multiple of 4)
+  int resident;         // trailing segments snapshotted by the checkpoint pass (>= 1)
   float* traj_q;        // optional forward trajectory [n_steps, n, nq]
   float* traj_qd;       // [n_steps, n, nv]
   int* status;          // [n]

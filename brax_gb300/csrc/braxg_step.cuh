@@ -1404,6 +1404,7 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     float cur = ss;
     for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
     tm.sync();
+    bool accepted = false;  // r = A nx + b for the accepted trial point
     for (int ls = 0; ls < md.pg_maxls; ++ls) {
       resid(nx, r);
       matvecs += 1;
@@ -1417,7 +1418,10 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
       fn = tm.sum(fn);
       dv = tm.sum(dv);
       sq = tm.sum(sq);
-      if (!(cur * (fn - fy) > cur * dv + 0.5f * sq)) break;
+      if (!(cur * (fn - fy) > cur * dv + 0.5f * sq)) {
+        accepted = true;
+        break;
+      }
       cur = cur * 0.5f;
       for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
       tm.sync();
@@ -1434,9 +1438,12 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
       }
     }
     iters = it + 1;
-    resid(nx, r);
+    if (!accepted) {  // an accepted trial already left A nx + b in r (same inputs, same bits)
+      resid(nx, r);
+      matvecs += 1;
+    }
     grad(r, gx);
-    matvecs += 2;
+    matvecs += 1;
     float es = 0.f;
     for (int i = tm.lane; i < nrow; i += T) {
       float e = fmaxf(nx[i] + (-1.f) * gx[i], 0.f) - nx[i];
@@ -1532,6 +1539,7 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
     float cur = ss;
     for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
     tm.sync();
+    bool accepted = false;  // r = A nx for the accepted trial point
     for (int ls = 0; ls < md.pg_maxls; ++ls) {
       matvec_A<T>(md.w, w, nrow, nx, r, t1, t2);
       matvecs += 1;
@@ -1547,7 +1555,10 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
       dv = tm.sum(dv);
       sq = tm.sum(sq);
       bool cond = cur * (fn - fy) > cur * dv + 0.5f * sq;
-      if (!cond) break;
+      if (!cond) {
+        accepted = true;
+        break;
+      }
       cur = cur * 0.5f;
       for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
       tm.sync();
@@ -1558,11 +1569,14 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
     for (int i = tm.lane; i < nrow; i += T) ny[i] = nx[i] + beta * (nx[i] - x[i]);
     tm.sync();
     // gradient at the new iterate and the stopping error
-    matvec_A<T>(md.w, w, nrow, nx, r, t1, t2);
+    if (!accepted) {  // an accepted trial already left A nx in r
+      matvec_A<T>(md.w, w, nrow, nx, r, t1, t2);
+      matvecs += 1;
+    }
     for (int i = tm.lane; i < nrow; i += T) r[i] = r[i] + b[i];
     tm.sync();
     matvec_A<T>(md.w, w, nrow, r, gx, t1, t2);
-    matvecs += 2;
+    matvecs += 1;
     float es = 0.f;
     for (int i = tm.lane; i < nrow; i += T) {
       float e = fmaxf(nx[i] + (-1.f) * gx[i], 0.f) - nx[i];

@@ -101,7 +101,10 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   bool ok = true, taped = true;
   Prof pf(a.prof, active && tm.lane == 0);
   const int n_ckpt = (a.n_steps + a.ckpt_every - 1) / a.ckpt_every;
-  const int last_s0 = (n_ckpt - 1) * a.ckpt_every;
+  // the last `resident` segments are taped and snapshotted by the checkpoint
+  // pass itself; earlier segments are recomputed into the first block
+  const int first_res = n_ckpt - a.resident;
+  const int res_s0 = first_res * a.ckpt_every;
   float* tape = aw.at(A.tape);
   const int tape_words = a.snap_words - L.total;
   // ---- forward with checkpoints ----
@@ -120,10 +123,10 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
     }
     if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
     tm.sync();
-    // the last segment is taped and snapshotted here, so it needs no recompute
-    const bool snap = s >= last_s0;
+    // resident segments are taped and snapshotted here, so they need no recompute
+    const bool snap = s >= res_s0;
     for (int f = 0; f < a.n_frames; ++f) {
-      const long long slot = (long long)((s - last_s0) * a.n_frames + f) * n + env;
+      const long long slot = (long long)((s - res_s0) * a.n_frames + f) * n + env;
       if (active && snap) {
         copy_vec<T>(tm, a.seg + slot * S, w.at(L.q), nq);
         copy_vec<T>(tm, a.seg + slot * S + nq, w.at(L.qd), nv);
@@ -150,7 +153,10 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   for (int sg = n_ckpt - 1; sg >= 0; --sg) {
     const int s0 = sg * a.ckpt_every;
     const int s1 = min(s0 + a.ckpt_every, a.n_steps);
-    if (sg != n_ckpt - 1) {  // recompute the segment, taping and snapshotting every frame
+    // frame slots of this segment: resident segments where the checkpoint
+    // pass put them, recomputed ones from the first block
+    const int base_s = sg >= first_res ? res_s0 : s0;
+    if (sg < first_res) {  // recompute the segment, taping and snapshotting every frame
       if (active) {
         const float* c = a.ckpt + ((long long)sg * n + env) * S;
         copy_vec<T>(tm, w.at(L.q), c, nq);
@@ -162,7 +168,7 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
       for (int s = s0; s < s1; ++s) {
         if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
         for (int f = 0; f < a.n_frames; ++f) {
-          const long long slot = (long long)((s - s0) * a.n_frames + f) * n + env;
+          const long long slot = (long long)((s - base_s) * a.n_frames + f) * n + env;
           if (active) {
             copy_vec<T>(tm, a.seg + slot * S, w.at(L.q), nq);
             copy_vec<T>(tm, a.seg + slot * S + nq, w.at(L.qd), nv);
@@ -184,7 +190,7 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
       tm.sync();
       for (int f = a.n_frames - 1; f >= 0; --f) {
         if (active) {
-          const long long slot = (long long)((s - s0) * a.n_frames + f) * n + env;
+          const long long slot = (long long)((s - base_s) * a.n_frames + f) * n + env;
           const float* sp = a.seg + slot * S;
           snap_load<T>(tm, a.snap + slot * a.snap_words, w.b, L.total, tape, tape_words);
           copy_vec<T>(tm, aw.at(A.q0), sp, nq);

@@ -243,12 +243,15 @@ def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = N
 
 def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int = 1,
                  ckpt_every: int = 16, trajectory: bool = False,
-                 profile: Optional[torch.Tensor] = None):
+                 profile: Optional[torch.Tensor] = None, resident_segments: Optional[int] = None):
   """Reverse-mode gradient of a rollout through the hand-written adjoint.
 
   Replaces ``jax.grad`` through ``lax.scan`` of ``pipeline_step``
   (brax/training/agents/apg/train.py:188-198).  ``q_bar`` / ``qd_bar``
   [n_steps, n, nq|nv] are the loss cotangents of the state after every env step.
+  ``resident_segments``: checkpoint segments whose frame snapshots stay
+  resident from the checkpoint pass (the others are recomputed); None keeps
+  as many as fit a quarter of the free device memory.
   Returns (act_bar, q0_bar, qd0_bar, status, (traj_q, traj_qd)).
   """
   m = model_for(sys, q0.device)
@@ -270,8 +273,20 @@ def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int =
   status = torch.zeros(n, dtype=torch.int32, device=dev)
   nbytes = ctypes.c_size_t()
   lib = N.lib()
-  N.check(lib.braxg_rollout_vjp_workspace(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
-                                          ctypes.byref(nbytes)), 'braxg_rollout_vjp_workspace')
+  n_ckpt = (n_steps + int(ckpt_every) - 1) // int(ckpt_every)
+  if resident_segments is None:
+    # as many segments resident as fit a quarter of the free device memory
+    free = torch.cuda.mem_get_info(dev)[0]
+    resident_segments = 1
+    for r in range(n_ckpt, 0, -1):
+      N.check(lib.braxg_rollout_vjp_workspace_resident(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
+                                                       r, ctypes.byref(nbytes)), 'workspace')
+      if nbytes.value <= free // 4:
+        resident_segments = r
+        break
+  N.check(lib.braxg_rollout_vjp_workspace_resident(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
+                                                   int(resident_segments), ctypes.byref(nbytes)),
+          'braxg_rollout_vjp_workspace_resident')
   ws = torch.empty(max(nbytes.value, 4), dtype=torch.uint8, device=dev)
   stream = torch.cuda.current_stream(dev).cuda_stream
   N.check(lib.braxg_rollout_vjp(

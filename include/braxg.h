@@ -189,16 +189,27 @@ int braxg_env_rollout(const braxg_model* model, void* stream, int n_env, int n_s
                       braxg_state* out, const braxg_task* task, const braxg_env_io* io,
                       const braxg_options* opt);
 
-/* Device workspace braxg_rollout_vjp needs: the checkpoints (every
- * ckpt_every env steps) and the per-frame states of one recomputed segment. */
+/* Smallest device workspace braxg_rollout_vjp accepts: the checkpoints (every
+ * ckpt_every env steps) and the frame states and frame snapshots of one
+ * segment; every segment but the last is then recomputed. */
 int braxg_rollout_vjp_workspace(const braxg_model* model, int n_env, int n_steps, int n_frames,
                                 int ckpt_every, size_t* bytes);
+
+/* Workspace that keeps the last `resident` segments' frame snapshots from the
+ * checkpoint pass (resident <= 0: all segments, no recompute at all).
+ * braxg_rollout_vjp keeps as many trailing segments resident as the
+ * workspace it is given holds, so more memory means less recompute; the
+ * gradient is the same either way. */
+int braxg_rollout_vjp_workspace_resident(const braxg_model* model, int n_env, int n_steps,
+                                         int n_frames, int ckpt_every, int resident,
+                                         size_t* bytes);
 
 /* Gradient of a rollout (the reverse of braxg_rollout), the replacement for
  * jax.grad through lax.scan of pipeline_step (brax/training/agents/apg/
  * train.py:188-198).  Runs the forward from (q0, qd0) with act_seq
  * [n_steps, n, nu], checkpointing every ckpt_every env steps, then the
- * hand-written reverse of every pipeline step with recompute.  q_bar / qd_bar
+ * hand-written reverse of every pipeline step, recomputing the segments whose
+ * frame snapshots the workspace cannot hold.  q_bar / qd_bar
  * [n_steps, n, nq|nv] are the loss cotangents of the state after each env step
  * (NULL = zero); outputs are act_bar [n_steps, n, nu], q0_bar [n, nq],
  * qd0_bar [n, nv] and, optionally, the forward trajectory traj_q / traj_qd.

@@ -130,3 +130,21 @@ def test_torch_autograd_function():
   assert u.grad is not None and torch.isfinite(u.grad).all()
   assert qd0t.grad is not None and torch.isfinite(qd0t.grad).all()
   assert u.grad.abs().sum() > 0
+
+
+def test_gradient_independent_of_resident_segments():
+  """Checkpoint segments either stay resident from the checkpoint pass or are
+  recomputed; both give the same frame snapshots, so the same gradient bits."""
+  P = _P()
+  sys_ = load('quadruped')
+  n, H, k = 24, 8, 2  # four checkpoint segments
+  q0, qd0 = seeded_inputs(sys_, n, 33)
+  rng = np.random.default_rng(34)
+  u = _t(rng.uniform(-1, 1, (H, n, sys_.act_size())))
+  qdb = _t(rng.normal(size=(H, n, sys_.qd_size())))
+  res = [P.rollout_grad(sys_, _t(q0), _t(qd0), u, None, qdb, n_frames=5, ckpt_every=k,
+                        resident_segments=r) for r in (1, 2, 4, None)]
+  torch.cuda.synchronize()
+  for r in res[1:]:
+    for a, b in zip(r[:4], res[0][:4]):
+      torch.testing.assert_close(a, b, rtol=0, atol=0)
