@@ -622,7 +622,7 @@ def loads(xml: str, name: str = '') -> S.System:
 
   # --- geoms ------------------------------------------------------------
   g_type, g_body, g_pos, g_quat, g_size = [], [], [], [], []
-  g_fric, g_sr, g_si, g_ct, g_ca, g_names = [], [], [], [], [], []
+  g_fric, g_sr, g_si, g_ct, g_ca, g_names, g_rgba = [], [], [], [], [], [], []
   for bi, b in enumerate(bodies):
     for g in b.geoms:
       gt = _GEOM_TYPES[g.get('type', 'sphere')]
@@ -646,6 +646,7 @@ def loads(xml: str, name: str = '') -> S.System:
       g_ct.append(int(g.get('contype', 1)))
       g_ca.append(int(g.get('conaffinity', 1)))
       g_names.append(g.get('name', ''))
+      g_rgba.append(_vec(g.get('rgba'), 4, [0.5, 0.5, 0.5, 1.0]))
       if float(g.get('solmix', 1.0)) != 1.0:
         raise NotImplementedError('geom_solmix parameter not supported.')
       if int(g.get('priority', 0)) != 0:
@@ -798,7 +799,8 @@ def loads(xml: str, name: str = '') -> S.System:
       geom_size=g_size, geom_friction=g_fric, geom_solref=g_sr, geom_solimp=g_si,
       geom_contype=g_ct, geom_conaffinity=g_ca, elasticity=elasticity,
       contacts=contacts, viscosity=viscosity, density=density,
-      name=name or root.attrib.get('model', ''))
+      name=name or root.attrib.get('model', ''),
+      geom_rgba=np.array(g_rgba, dtype=np.float64).reshape(ngeom, 4))
   _set_invweights(sys, q0)
   return sys
 

@@ -150,6 +150,7 @@ class System:
   viscosity: float = 0.0
   density: float = 0.0
   name: str = ''
+  geom_rgba: Optional[np.ndarray] = None  # (ngeom, 4), MJCF rgba (default 0.5 0.5 0.5 1)
 
   @property
   def enable_fluid(self) -> bool:
