@@ -84,7 +84,8 @@ PROFILE_SLOTS = ('fk', 'com', 'crba', 'inverse', 'jacobian', 'smooth', 'constrai
                  'integrate', 'io', 'matvecs', 'rows', 'ns_resets', 'substeps')
 VJP_PROFILE_SLOTS = {16: 'checkpoint_pass', 17: 'segment_recompute', 18: 'restore',
                      19: 'rev_integrate', 20: 'rev_qdd', 21: 'rev_constraint', 22: 'rev_smooth',
-                     23: 'rev_inverse', 24: 'rev_crba', 25: 'rev_rows', 26: 'rev_com', 27: 'rev_fk'}
+                     23: 'rev_inverse', 24: 'rev_crba', 25: 'rev_rows', 26: 'rev_com', 27: 'rev_fk',
+                     28: 'pg_build', 29: 'pg_iterate'}
 N_PROFILE_SLOTS = 32
 
 

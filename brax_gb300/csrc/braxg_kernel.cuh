@@ -296,7 +296,10 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   }
   // teams without an env may have no arena slot (batch items narrower than
   // the block): every arena access below is behind `active`
-  if (active && tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] = 0;
+  if (active && tm.lane == 0) {
+    int* mi = reinterpret_cast<int*>(w.at(L.misc));
+    mi[1] = mi[9] = mi[10] = 0;
+  }
   tm.sync();
   pf.mark(BRAXG_PROF_IO);
   bool ok = position_stage<T, NVB>(smem, w, active, exact, 0, pf);
@@ -353,6 +356,8 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   write_outputs<T>(a, B, smem, w, env, ok);
   pf.mark(BRAXG_PROF_IO);
   pf.count(BRAXG_PROF_NS_RESETS, (unsigned long long)reinterpret_cast<const int*>(w.at(L.misc))[1]);
+  pf.count(BRAXG_PROF_PG_BUILD, (unsigned long long)reinterpret_cast<const unsigned*>(w.at(L.misc))[9]);
+  pf.count(BRAXG_PROF_PG_ITERATE, (unsigned long long)reinterpret_cast<const unsigned*>(w.at(L.misc))[10]);
 }
 
 // TASK: the fused env step variant (braxg_env_rollout); the plain pipeline

@@ -88,7 +88,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.tau = take(nv);
   L.v1 = take(nv);
   L.v2 = take(nv);
-  L.misc = take(12);  // [0] active rows, [1] NS resets, [2..8] env-step task state
+  L.misc = take(12);  // [0] active rows, [1] NS resets, [2..8] env-step task state, [9..10] PG cycles
   L.xp = take(3 * nl);
   L.xr = take(4 * nl);
   L.xa = take(3 * nl);
@@ -1317,6 +1317,9 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   const float* raref = w.at(L.raref);
   const float* qfs = w.at(L.qfs);
   float* qfc = w.at(L.qfc);
+  // cycles spent forming W, A, b and iterating, for the stage profile
+  unsigned* pg_cycles = reinterpret_cast<unsigned*>(w.at(L.misc)) + 9;
+  const long long t_build = clock64();
   for (int k = tm.lane; k < nv; k += T)  // W = J Minv (lanes over columns)
     for (int i = 0; i < nrow; ++i) {
       float s0 = 0.f, s1 = 0.f;
@@ -1355,6 +1358,8 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     y[c] = 0.f;
   }
   tm.sync();
+  const long long t_iter = clock64();
+  if (tm.lane == 0) pg_cycles[0] += (unsigned)(t_iter - t_build);
   // out = A v + b (lanes over rows)
   auto resid = [&](const float* v, float* out) {
     for (int i = tm.lane; i < nrow; i += T) {
@@ -1468,6 +1473,7 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
       tape[1] = (float)nrow;
     }
   }
+  if (tm.lane == 0) pg_cycles[1] += (unsigned)(clock64() - t_iter);
   tm.sync();
   return matvecs;
 }

@@ -99,6 +99,8 @@ enum braxg_profile_slot {
   BRAXG_PROF_REV_INTEGRATE, BRAXG_PROF_REV_QDD, BRAXG_PROF_REV_CONSTRAINT, BRAXG_PROF_REV_SMOOTH,
   BRAXG_PROF_REV_INVERSE, BRAXG_PROF_REV_CRBA, BRAXG_PROF_REV_ROWS, BRAXG_PROF_REV_COM,
   BRAXG_PROF_REV_FK,
+  /* explicit projected-gradient solve: forming W, A, b / iterating */
+  BRAXG_PROF_PG_BUILD = 28, BRAXG_PROF_PG_ITERATE,
   BRAXG_PROF_SLOTS = 32
 };
 
