@@ -26,10 +26,10 @@ from brax_gb300 import model_pack
 from brax_gb300 import pipeline as P
 
 BUCKETS = (8, 16, 32, 64)
-# per-CTA shared memory of the tuned launch: two CTAs per SM, as the batch
-# default; shapes are timed under the same limit so that the combined launch
-# (which takes the largest group's CTA size) keeps two CTAs per SM
-SMEM_PER_CTA = 113 * 1024
+# per-CTA shared memory of the tuned launch: one CTA per SM (all of an SM's
+# warps then run the same stage's code), as the batch default; shapes are
+# timed under the same limit as the combined launch that uses them
+SMEM_PER_CTA = 227 * 1024 - 16
 _lock = threading.Lock()
 
 
@@ -45,11 +45,12 @@ def bucket_of(nv: int) -> int:
 
 
 def candidates(bucket: int) -> List[Tuple[int, int]]:
-  """(threads_per_env, envs_per_cta) pairs; envs_per_cta 0 = fit 113 KB per CTA."""
+  """(threads_per_env, envs_per_cta) pairs; envs_per_cta 0 = as many as the
+  CTA's shared memory and 512 threads hold."""
   out = []
   lanes = (16, 32) if bucket <= 32 else (32,)
   for t in lanes:
-    for e in (0, 2, 4, 6, 8) if t == 32 else (0, 4, 8, 12, 16):
+    for e in (0, 4, 8, 12, 16) if t == 32 else (0, 8, 16, 24, 32):
       out.append((t, e))
   return out
 
@@ -119,7 +120,7 @@ def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Seque
   """Shapes [(nv_max, threads_per_env, envs_per_cta)] for ``Batch(shapes=...)``,
   one per nv bucket present, each the fastest candidate for that bucket's
   models timed alone; the combination is then timed on the whole batch
-  against the default shape (32 lanes, envs per CTA filling 113 KB) and the
+  against the default shape (32 lanes, envs per CTA filling the CTA) and the
   faster of the two is returned (an empty list for the default)."""
   device = torch.device('cuda') if device is None else torch.device(device)
   if device.index is None:

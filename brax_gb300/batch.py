@@ -48,8 +48,8 @@ class Batch:
   env step, on one device (braxg_batch_create).
 
   ``shapes``: [(nv_max, threads_per_env, envs_per_cta)], first match per model
-  (``brax_gb300.autotune.tune_batch`` picks them); ``smem_per_cta`` 0 = 113 KB
-  per CTA (two CTAs per SM).
+  (``brax_gb300.autotune.tune_batch`` picks them); ``smem_per_cta`` 0 = up to
+  227 KB per CTA (one CTA per SM).
   """
 
   def __init__(self, systems: Sequence, n_env: Sequence[int], n_frames: Optional[Sequence[int]] = None,

@@ -53,29 +53,32 @@ struct Shape {
 };
 
 constexpr int kMaxSmem = 227 * 1024;
-// per-CTA budget of the default launch shape: two CTAs fit one SM
-constexpr int kHalfSmem = 113 * 1024;
+// threads per CTA of the step kernels (launch bound 512 x 1: 128 registers)
+constexpr int kMaxBlock = 512;
 
 int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shape* s) {
   int nv = m->dims.nv;
   s->NVB = nv <= 16 ? 16 : (nv <= 32 ? 32 : 64);
-  int T = (opt && opt->threads_per_env) ? opt->threads_per_env : 32;
+  // default lanes per env: 16 for small models (nv <= 8: two envs per warp),
+  // else 32 (measured on the packaged models, one CTA per SM)
+  int T = (opt && opt->threads_per_env) ? opt->threads_per_env : (nv <= 8 ? 16 : 32);
   if (T != 16 && T != 32) return fail(BRAXG_ERR_INVALID, "threads_per_env must be 0, 16 or 32 (got %d)", T);
   if (T == 16 && s->NVB == 64) T = 32;
   s->T = T;
   int model_bytes = (braxg::al4(m->words) + braxg::kLayoutWords) * 4;
   int env_bytes = m->L.total * 4;
-  int max_epc = 256 / T;
+  int max_epc = kMaxBlock / T;
   int fit = (kMaxSmem - model_bytes) / env_bytes;
   if (fit < 1)
     return fail(BRAXG_ERR_UNSUPPORTED, "model needs %d bytes of shared memory per env; at most %d fit",
                 env_bytes, kMaxSmem - model_bytes);
   int epc = (opt && opt->envs_per_cta) ? opt->envs_per_cta : 0;
   if (epc == 0) {
-    // default: up to half the SM's shared memory per CTA, so two CTAs share an
-    // SM; a batch too small to fill every SM that way is spread over all of
-    // them instead (latency-bound envs run faster with fewer per SM)
-    epc = (kHalfSmem - model_bytes) / env_bytes;
+    // default: one CTA per SM holding as many envs as its shared memory and
+    // 512 threads allow, so that every warp of the SM runs the same stage's
+    // code (the instruction working set of one stage); a batch too small to
+    // fill every SM that way is spread over all of them instead
+    epc = (kMaxSmem - model_bytes) / env_bytes;
     if (n_env > 0 && m->sms > 0) epc = std::min(epc, (n_env + m->sms - 1) / m->sms);
     if (epc < 1) epc = 1;
     if (epc > max_epc) epc = max_epc;
@@ -468,7 +471,7 @@ int braxg_batch_create(const braxg_model* const* models, const int32_t* n_env, c
     double cost;
   };
   std::vector<Plan> plan(n_models);
-  int budget = smem_per_cta > 0 ? smem_per_cta : kHalfSmem;
+  int budget = smem_per_cta > 0 ? smem_per_cta : max_smem;
   for (int g = 0; g < n_models; ++g) {
     const braxg_model* m = models[g];
     if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model %d is NULL", g);
@@ -476,7 +479,7 @@ int braxg_batch_create(const braxg_model* const* models, const int32_t* n_env, c
     if (n_env[g] < 0) return fail(BRAXG_ERR_INVALID, "n_env[%d] = %d < 0", g, n_env[g]);
     if (n_frames != nullptr && n_frames[g] < 1) return fail(BRAXG_ERR_INVALID, "n_frames[%d] must be >= 1", g);
     const int nv = m->dims.nv;
-    int T = 32, epc = 0;
+    int T = nv <= 8 ? 16 : 32, epc = 0;  // as the single-model default
     for (int k = 0; k < n_shapes; ++k) {
       if (nv <= shapes[k].nv_max) {
         T = shapes[k].threads_per_env;
@@ -486,7 +489,8 @@ int braxg_batch_create(const braxg_model* const* models, const int32_t* n_env, c
     }
     if (T != 16 && T != 32) return fail(BRAXG_ERR_INVALID, "threads_per_env must be 16 or 32 (got %d)", T);
     if (T == 16 && nv > 32) return fail(BRAXG_ERR_INVALID, "16 lanes per env support nv <= 32 (model %d has %d)", g, nv);
-    if (epc < 0 || epc > 256 / T) return fail(BRAXG_ERR_INVALID, "envs_per_cta %d out of range [0, %d]", epc, 256 / T);
+    if (epc < 0 || epc > kMaxBlock / T)
+      return fail(BRAXG_ERR_INVALID, "envs_per_cta %d out of range [0, %d]", epc, kMaxBlock / T);
     Plan& p = plan[g];
     p.T = T;
     p.epc = epc;
@@ -515,7 +519,7 @@ int braxg_batch_create(const braxg_model* const* models, const int32_t* n_env, c
   for (int g = 0; g < n_models; ++g) {
     const braxg_model* m = models[g];
     Plan& p = plan[g];
-    if (p.epc == 0) p.epc = std::max(1, std::min(256 / p.T, (budget - p.head) / p.env_bytes));
+    if (p.epc == 0) p.epc = std::max(1, std::min(kMaxBlock / p.T, (budget - p.head) / p.env_bytes));
     block = std::max(block, (p.epc * p.T + 31) / 32 * 32);
     smem = std::max(smem, p.head + p.epc * p.env_bytes);
     braxg::BatchGroup& G = b->groups[g];

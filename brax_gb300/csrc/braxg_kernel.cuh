@@ -363,7 +363,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
 // TASK: the fused env step variant (braxg_env_rollout); the plain pipeline
 // kernel compiles without any of its code.
 template <int T, int NVB, bool TASK>
-__global__ void __launch_bounds__(256, 2) step_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(512, 1) step_kernel(const StepArgs a) {
   extern __shared__ __align__(16) int smem[];
   for (int i = threadIdx.x; i < a.model_words; i += blockDim.x) smem[i] = a.model[i];
   Layout* shared_layout = reinterpret_cast<Layout*>(smem + al4(a.model_words));

@@ -42,7 +42,7 @@ __device__ __forceinline__ void batch_item(const BatchArgs& ba, const BatchItem&
   }
 }
 
-__global__ void __launch_bounds__(256, 2) batch_kernel(const BatchArgs ba) {
+__global__ void __launch_bounds__(512, 1) batch_kernel(const BatchArgs ba) {
   extern __shared__ __align__(16) int smem[];
   __shared__ int next;
   for (;;) {

@@ -260,7 +260,8 @@ int braxg_rollout_vjp_noalloc(const braxg_model* model, void* stream, int n_env,
 typedef struct braxg_batch braxg_batch;
 
 /* Launch shape for the models with nv <= nv_max (the first matching entry
- * applies; models matching none get 32 lanes and envs_per_cta 0). */
+ * applies; models matching none get the single-model default: 16 lanes for
+ * nv <= 8, else 32, and envs_per_cta 0). */
 typedef struct {
   int32_t nv_max;
   int32_t threads_per_env;  /* 16 or 32 */
@@ -284,9 +285,9 @@ typedef struct {
  * device), n_frames[g] pipeline steps per env step (NULL = 1 each).  Work items
  * are CTA-sized groups of envs of one model, ordered by decreasing estimated
  * cost and taken from a device counter by a grid of (SMs x resident CTAs)
- * persistent CTAs.  smem_per_cta = 0 picks 113 KB, two CTAs per SM (grown to
- * fit the largest single env or explicit envs_per_cta); a non-zero value is a
- * limit, and a shape that does not fit it is BRAXG_ERR_INVALID.  Allocates the device work list; later calls allocate
+ * persistent CTAs.  smem_per_cta = 0 allows the whole 227 KB (one CTA per
+ * SM, all its warps on the same stage's code); a non-zero value is a limit,
+ * and a shape that does not fit it is BRAXG_ERR_INVALID.  Allocates the device work list; later calls allocate
  * nothing. */
 int braxg_batch_create(const braxg_model* const* models, const int32_t* n_env,
                        const int32_t* n_frames, int n_models,
