@@ -143,16 +143,13 @@ def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Seque
     hit = table.get(key)
     if hit is None:
       results = {}
-      for smem in (SMEM_PER_CTA, 0):  # 0: models too large for two CTAs per SM
-        for shape in candidates(bucket):
-          try:
-            results[shape] = _time_shape(sys_b, ne_b, nf_b, shape, device, n_steps, reps, smem)
-          except (ValueError, NotImplementedError):
-            continue  # shape does not fit this bucket's models
-          if verbose:
-            print(f'nv<={bucket} threads {shape[0]} envs/cta {shape[1]}: {results[shape]:.3f} ms')
-        if results:
-          break
+      for shape in candidates(bucket):
+        try:
+          results[shape] = _time_shape(sys_b, ne_b, nf_b, shape, device, n_steps, reps, SMEM_PER_CTA)
+        except (ValueError, NotImplementedError):
+          continue  # shape does not fit this bucket's models
+        if verbose:
+          print(f'nv<={bucket} threads {shape[0]} envs/cta {shape[1]}: {results[shape]:.3f} ms')
       if not results:
         raise NotImplementedError(f'no launch shape fits the nv<={bucket} models')
       best = min(results, key=results.get)
