@@ -290,6 +290,30 @@ def run_braxg(args):
   times = [a.elapsed_time(b) for a, b in ev]
   t_total = max_over_ranks(sum(times) / 1e3, dev)
   status = a_state.status.cpu().numpy()
+
+  # the same timed loop with the reference's inverse (Newton-Schulz, K = 10)
+  other = pipeline.NEWTON_SCHULZ if mode == pipeline.CHOLESKY else pipeline.CHOLESKY
+  kw_o = dict(kw, inverse_mode=other)
+  c_state = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
+  d_state = pipeline._alloc(model, n, False, dev)
+  for i in range(args.warmup):
+    pipeline.step(sys_, c_state, acts[i], n_frames=N_FRAMES, out=d_state, **kw_o)
+    c_state, d_state = d_state, c_state
+  torch.cuda.synchronize()
+  t_other = 0.0
+  for k in range(args.steps):
+    flush.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    pipeline.step(sys_, c_state, acts[args.warmup + k], n_frames=N_FRAMES, out=d_state, **kw_o)
+    e1.record(stream)
+    c_state, d_state = d_state, c_state
+    e1.synchronize()
+    t_other += e0.elapsed_time(e1) / 1e3
+  t_other = max_over_ranks(t_other, dev)
+  other_mode = {'inverse_mode': 'newton_schulz' if other == pipeline.NEWTON_SCHULZ else 'cholesky',
+                'value': round(whole_job_rate(args.steps * n, world, t_other), 1),
+                'ms_per_step': round(1e3 * t_other / args.steps, 4)}
   value = whole_job_rate(args.steps * n, world, t_total)
   ms_per_step = 1e3 * t_total / args.steps
 
@@ -377,6 +401,7 @@ def run_braxg(args):
                                           model.launch_shape(mode, args.threads_per_env,
                                                              args.envs_per_cta)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
+      'other_inverse_mode': other_mode,
       'adjoint': adjoint, 'uneven': uneven, 'env_step': env_step,
       'env_status_nonzero': int((status != 0).sum()),
   }
