@@ -780,6 +780,78 @@ __device__ bool spd_inverse_owned(const Team<T>& tm, int n, int ld, const float*
   return ok;
 }
 
+// Exact SPD inverse by the symmetric sweep operator (Gauss-Jordan elimination
+// kept symmetric): for k = 0..n-1, with d = B[k][k],
+//   B[i][j] -= B[i][k] B[k][j] / d   (i, j != k),
+//   B[i][k] /= d                      (i != k),
+//   B[k][k]  = -1 / d,
+// after which B = -M^-1.  Only the lower triangle is stored; each lane owns
+// fixed entries (as spd_inverse_owned) and every step reads the old column k,
+// then writes, so one elimination pass replaces the Cholesky factorisation,
+// the triangular inverse and X^T X.  The pivots are the Cholesky pivots
+// squared, so a pivot <= 0 flags a matrix that is not positive definite.
+template <int T, int NVB>
+__device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float* Msrc, float* B, float* Minv) {
+  constexpr int E = (NVB * (NVB + 1) / 2 + T - 1) / T;
+  int oi[E], oj[E];
+  {
+    const int cnt = n * (n + 1) / 2;
+    int e = tm.lane, i = 0, j = tm.lane;
+    while (j > i) {
+      j -= i + 1;
+      ++i;
+    }
+#pragma unroll
+    for (int t = 0; t < E; ++t) {
+      const bool v = e < cnt;
+      oi[t] = v ? i : -1;
+      oj[t] = v ? j : 0;
+      e += T;
+      j += T;
+      while (j > i) {
+        j -= i + 1;
+        ++i;
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < E; ++t)
+    if (oi[t] >= 0) B[oi[t] * ld + oj[t]] = Msrc[oi[t] * ld + oj[t]];
+  tm.sync();
+  bool ok = true;
+  for (int k = 0; k < n; ++k) {
+    const float d = B[k * ld + k];
+    ok = ok && (d > 0.f);
+    const float r = 1.f / d;
+    float nv[E];
+#pragma unroll
+    for (int t = 0; t < E; ++t) {
+      const int i = oi[t], j = oj[t];
+      if (i < 0) continue;
+      // column k of the (symmetric) matrix from the lower triangle
+      const float bik = i >= k ? B[i * ld + k] : B[k * ld + i];
+      const float bjk = j >= k ? B[j * ld + k] : B[k * ld + j];
+      if (i != k && j != k) nv[t] = B[i * ld + j] - bik * (bjk * r);
+      else if (i == k && j == k) nv[t] = -r;
+      else nv[t] = (i == k ? bjk : bik) * r;
+    }
+    tm.sync();  // every read of the old column k is done
+#pragma unroll
+    for (int t = 0; t < E; ++t)
+      if (oi[t] >= 0) B[oi[t] * ld + oj[t]] = nv[t];
+    tm.sync();
+  }
+#pragma unroll
+  for (int t = 0; t < E; ++t)
+    if (oi[t] >= 0) {
+      const float v = -B[oi[t] * ld + oj[t]];
+      Minv[oi[t] * ld + oj[t]] = v;
+      Minv[oj[t] * ld + oi[t]] = v;
+    }
+  tm.sync();
+  return ok;
+}
+
 // ---------------------------------------------------------------------------
 // mass.matrix_inv: brax/generalized/mass.py:86-106 + brax/math.py:278-305
 // mode 0 keeps/updates Minv by Newton-Schulz (num_iter iterations; 0 keeps
@@ -798,7 +870,7 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   if (n == 0) return true;
   if (exact) {
     // entry ownership while the owned (i, j) pairs fit a few registers
-    if constexpr ((NVB * (NVB + 1) / 2 + T - 1) / T <= 17) return spd_inverse_owned<T, NVB>(tm, n, ld, M, S1, S2, P);
+    if constexpr ((NVB * (NVB + 1) / 2 + T - 1) / T <= 17) return spd_inverse_sweep<T, NVB>(tm, n, ld, M, S1, P);
     else return spd_inverse<T>(tm, n, ld, M, S1, S2, P);
   }
   if (num_iter <= 0) return true;
