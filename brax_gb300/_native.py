@@ -43,7 +43,7 @@ class Dims(ctypes.Structure):
 
 class Options(ctypes.Structure):
   _fields_ = [('inverse_mode', ctypes.c_int32), ('threads_per_env', ctypes.c_int32),
-              ('envs_per_cta', ctypes.c_int32), ('reserved', ctypes.c_int32),
+              ('envs_per_cta', ctypes.c_int32), ('relax_barriers', ctypes.c_int32),
               ('stage_cycles', ctypes.c_void_p)]
 
 

@@ -98,6 +98,7 @@ int launch(const braxg_model* m, const braxg_options* opt, braxg::StepArgs& a, c
   if (a.n_env == 0) return BRAXG_OK;
   a.envs_per_cta = s.epc;
   a.prof = opt ? opt->stage_cycles : nullptr;
+  a.relax = opt ? opt->relax_barriers : 0;
   int grid = (a.n_env + s.epc - 1) / s.epc;
   int cur = 0;
   cudaGetDevice(&cur);
@@ -601,6 +602,7 @@ static int batch_launch(const braxg_batch* b, void* stream, braxg::StepArgs& s, 
   if (b->items.empty()) return BRAXG_OK;
   braxg::BatchArgs ba{};
   s.prof = opt ? opt->stage_cycles : nullptr;
+  s.relax = opt ? opt->relax_barriers : 0;
   ba.s = s;
   ba.groups = b->d_groups;
   ba.items = b->d_items;

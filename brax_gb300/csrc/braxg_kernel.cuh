@@ -328,11 +328,11 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
           pf.mark(BRAXG_PROF_SMOOTH);
           int mvs = 0;
           if (active) mvs = stage_constraint<T>(smem, w);
-          __syncthreads();
+          if (!(a.relax & 1)) __syncthreads();  // launch-uniform condition
           pf.count(BRAXG_PROF_MATVECS, (unsigned long long)mvs);
           pf.mark(BRAXG_PROF_CONSTRAINT);
           if (active) ok = stage_integrate<T>(smem, w) && ok;
-          __syncthreads();
+          if (!(a.relax & 2)) __syncthreads();
           pf.mark(BRAXG_PROF_INTEGRATE);
           ok = position_stage<T, NVB>(smem, w, active, exact_mode, md.ns_iters, pf) && ok;
           pf.count(BRAXG_PROF_SUBSTEPS, 1ull);

@@ -697,96 +697,14 @@ __device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc,
   return ok;
 }
 
-// spd_inverse with the work spread over the entries: every lane owns fixed
-// entries of the packed lower triangle (entry e = i(i+1)/2 + j, e = lane,
-// lane + T, ...), kept as (i, j) in registers, and each step of the
-// factorisation / elimination updates all live entries at once instead of
-// one column per lane.  Each entry sees the same operations in the same order
-// as in spd_inverse.  E bounds the entries per lane for matrices up to NVB.
-template <int T, int NVB>
-__device__ bool spd_inverse_owned(const Team<T>& tm, int n, int ld, const float* Msrc, float* Lw, float* X,
-                                  float* Minv) {
-  constexpr int E = (NVB * (NVB + 1) / 2 + T - 1) / T;
-  int oi[E], oj[E];
-  {
-    const int cnt = n * (n + 1) / 2;
-    int e = tm.lane, i = 0, j = tm.lane;
-    while (j > i) {
-      j -= i + 1;
-      ++i;
-    }
-#pragma unroll
-    for (int t = 0; t < E; ++t) {
-      const bool v = e < cnt;
-      oi[t] = v ? i : -1;
-      oj[t] = v ? j : 0;
-      e += T;
-      j += T;
-      while (j > i) {
-        j -= i + 1;
-        ++i;
-      }
-    }
-  }
-#pragma unroll
-  for (int t = 0; t < E; ++t)
-    if (oi[t] >= 0) {
-      Lw[oi[t] * ld + oj[t]] = Msrc[oi[t] * ld + oj[t]];
-      X[oi[t] * ld + oj[t]] = (oi[t] == oj[t]) ? 1.f : 0.f;
-    }
-  tm.sync();
-  bool ok = true;
-  for (int k = 0; k < n; ++k) {  // right-looking Cholesky
-    const float piv = Lw[k * ld + k];
-    ok = ok && (piv > 0.f);
-    const float d = sqrtf(fmaxf(piv, 1e-30f));
-#pragma unroll
-    for (int t = 0; t < E; ++t)
-      if (oj[t] == k && oi[t] > k) Lw[oi[t] * ld + k] = Lw[oi[t] * ld + k] / d;
-    tm.sync();
-    if (tm.lane == 0) Lw[k * ld + k] = d;
-#pragma unroll
-    for (int t = 0; t < E; ++t)
-      if (oj[t] > k) Lw[oi[t] * ld + oj[t]] = Lw[oi[t] * ld + oj[t]] - Lw[oi[t] * ld + k] * Lw[oj[t] * ld + k];
-    tm.sync();
-  }
-  for (int k = 0; k < n; ++k) {  // X = L^-1, right-looking forward elimination
-    const float lkk = Lw[k * ld + k];
-#pragma unroll
-    for (int t = 0; t < E; ++t)
-      if (oi[t] == k) X[k * ld + oj[t]] = X[k * ld + oj[t]] / lkk;
-    tm.sync();
-#pragma unroll
-    for (int t = 0; t < E; ++t)
-      if (oi[t] > k && oj[t] <= k) X[oi[t] * ld + oj[t]] = X[oi[t] * ld + oj[t]] - Lw[oi[t] * ld + k] * X[k * ld + oj[t]];
-    tm.sync();
-  }
-#pragma unroll
-  for (int t = 0; t < E; ++t) {  // Minv = X^T X, entry (i, j), i >= j
-    if (oi[t] < 0) continue;
-    const int i = oi[t], j = oj[t];
-    float s0 = 0.f, s1 = 0.f;
-    int m = i;
-    for (; m + 1 < n; m += 2) {
-      s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
-      s1 = fmaf(X[(m + 1) * ld + i], X[(m + 1) * ld + j], s1);
-    }
-    if (m < n) s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
-    const float v = s0 + s1;
-    Minv[i * ld + j] = v;
-    Minv[j * ld + i] = v;
-  }
-  tm.sync();
-  return ok;
-}
-
 // Exact SPD inverse by the symmetric sweep operator (Gauss-Jordan elimination
 // kept symmetric): for k = 0..n-1, with d = B[k][k],
 //   B[i][j] -= B[i][k] B[k][j] / d   (i, j != k),
 //   B[i][k] /= d                      (i != k),
 //   B[k][k]  = -1 / d,
 // after which B = -M^-1.  Only the lower triangle is stored; each lane owns
-// fixed entries (as spd_inverse_owned) and every step reads the old column k,
+// fixed entries of the packed lower triangle, (i, j) kept in registers, and
+// every step reads the old column k,
 // then writes, so one elimination pass replaces the Cholesky factorisation,
 // the triangular inverse and X^T X.  The pivots are the Cholesky pivots
 // squared, so a pivot <= 0 flags a matrix that is not positive definite.
@@ -1392,8 +1310,16 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   // cycles spent forming W, A, b and iterating, for the stage profile
   unsigned* pg_cycles = reinterpret_cast<unsigned*>(w.at(L.misc)) + 9;
   const long long t_build = clock64();
-  for (int k = tm.lane; k < nv; k += T)  // W = J Minv (lanes over columns)
-    for (int i = 0; i < nrow; ++i) {
+  // W = J Minv, lanes over the nrow x nv entries (entry e: row e / nv, column
+  // e % nv, walked incrementally); each entry's sum is the same two-chain
+  // dot product in the same order as with one lane per column
+  {
+    int i = 0, k = tm.lane;
+    while (k >= nv) {
+      k -= nv;
+      ++i;
+    }
+    for (; i < nrow;) {
       float s0 = 0.f, s1 = 0.f;
       int d = 0;
       for (; d + 1 < nv; d += 2) {
@@ -1402,10 +1328,21 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
       }
       if (d < nv) s0 = fmaf(J[i * ldj + d], Minv[d * ld + k], s0);
       W[i * ld + k] = s0 + s1;
+      k += T;
+      while (k >= nv) {
+        k -= nv;
+        ++i;
+      }
     }
+  }
   tm.sync();
-  for (int c = tm.lane; c < nrow; c += T) {  // A[:, c] = W J[c]^T (+ diag)
-    for (int i = 0; i < nrow; ++i) {
+  {  // A = W J^T + diag, lanes over the nrow x nrow entries (row i, column c)
+    int i = 0, c = tm.lane;
+    while (c >= nrow) {
+      c -= nrow;
+      ++i;
+    }
+    for (; i < nrow;) {
       float s0 = 0.f, s1 = 0.f;
       int k = 0;
       for (; k + 1 < nv; k += 2) {
@@ -1414,8 +1351,15 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
       }
       if (k < nv) s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
       A[i * la + c] = (s0 + s1) + (i == c ? rdiag[i] : 0.f);
+      c += T;
+      while (c >= nrow) {
+        c -= nrow;
+        ++i;
+      }
     }
-    float s0 = 0.f, s1 = 0.f;  // b[c] = W[c] qf_smooth - aref[c]
+  }
+  for (int c = tm.lane; c < nrow; c += T) {  // b[c] = W[c] qf_smooth - aref[c]
+    float s0 = 0.f, s1 = 0.f;
     int k = 0;
     for (; k + 1 < nv; k += 2) {
       s0 = fmaf(W[c * ld + k], qfs[k], s0);

@@ -150,8 +150,8 @@ def _as_batch(x: torch.Tensor, width: int, name: str, dev) -> torch.Tensor:
   return x.to(torch.float32).contiguous()
 
 
-def _opts(inverse_mode, threads_per_env, envs_per_cta, profile=None):
-  return N.Options(int(inverse_mode), int(threads_per_env), int(envs_per_cta), 0,
+def _opts(inverse_mode, threads_per_env, envs_per_cta, profile=None, relax_barriers=0):
+  return N.Options(int(inverse_mode), int(threads_per_env), int(envs_per_cta), int(relax_barriers),
                    None if profile is None else profile.data_ptr())
 
 
@@ -191,7 +191,7 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
 def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
          full: bool = False, inverse_mode: int = NEWTON_SCHULZ, out: Optional[State] = None,
          threads_per_env: int = 0, envs_per_cta: int = 0,
-         profile: Optional[torch.Tensor] = None) -> State:
+         profile: Optional[torch.Tensor] = None, relax_barriers: int = 0) -> State:
   """brax/generalized/pipeline.py:64-94; n_frames > 1 repeats it with the same
   action (PipelineEnv.pipeline_step, brax/envs/base.py:128-137)."""
   if debug:
@@ -212,7 +212,7 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
   N.check(N.lib().braxg_step(m.handle, ctypes.c_void_p(stream), n, int(n_frames), act_p,
                              ctypes.byref(cin), ctypes.byref(cout),
                              ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta,
-                                                profile))),
+                                                profile, relax_barriers))),
           'braxg_step')
   return out
 

@@ -108,7 +108,11 @@ typedef struct {
   int32_t inverse_mode;     /* braxg_inverse_mode */
   int32_t threads_per_env;  /* 0 = tuned, else 16 or 32 lanes per env */
   int32_t envs_per_cta;     /* 0 = tuned */
-  int32_t reserved;
+  /* CTA barriers skipped between stages (bit 0: after the constraint solve,
+   * bit 1: after the integrator).  Teams never share data, so this changes
+   * no result, only how far the envs of a CTA may drift apart: 0 keeps
+   * every stage in lockstep. */
+  int32_t relax_barriers;
   /* Optional device buffer of BRAXG_PROF_SLOTS uint64 counters the kernel
    * adds its per-stage cycle counts into (NULL = no profiling). */
   unsigned long long* stage_cycles;

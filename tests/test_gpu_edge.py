@@ -127,3 +127,18 @@ def test_widest_tile_chain48():
     eo = rel_err(getattr(r32, f), getattr(r64, f))
     print(f'chain48 {f}: vs fp64 p99 {np.quantile(e64, 0.99):.2e} | fp32 oracle vs fp64 p99 {np.quantile(eo, 0.99):.2e}')
     assert np.quantile(e64, 0.99) <= max(1e-5, 3 * np.quantile(eo, 0.99)), f
+
+
+@pytest.mark.parametrize('relax', [1, 2, 3])
+def test_relaxed_barriers_change_no_result(relax):
+  P, _ = _P()
+  sys_ = load('quadruped')
+  n = 64
+  q, qd = seeded_inputs(sys_, n, 58)
+  act = _t(actions(sys_, n, np.random.default_rng(59)))
+  s = P.init(sys_, _t(q), _t(qd))
+  a = P.step(sys_, s, act, n_frames=5, inverse_mode=P.CHOLESKY)
+  b = P.step(sys_, s, act, n_frames=5, inverse_mode=P.CHOLESKY, relax_barriers=relax)
+  torch.cuda.synchronize()
+  for f in ('q', 'qd', 'mass_mx_inv', 'x_pos'):
+    torch.testing.assert_close(getattr(a, f), getattr(b, f), rtol=0, atol=0)
