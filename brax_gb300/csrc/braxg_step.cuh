@@ -709,7 +709,8 @@ __device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc,
 // the triangular inverse and X^T X.  The pivots are the Cholesky pivots
 // squared, so a pivot <= 0 flags a matrix that is not positive definite.
 template <int T, int NVB>
-__device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float* Msrc, float* B, float* Minv) {
+__device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float* Msrc, float* B0, float* B1,
+                                  float* Minv) {
   constexpr int E = (NVB * (NVB + 1) / 2 + T - 1) / T;
   int oi[E], oj[E];
   {
@@ -734,14 +735,17 @@ __device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float*
   }
 #pragma unroll
   for (int t = 0; t < E; ++t)
-    if (oi[t] >= 0) B[oi[t] * ld + oj[t]] = Msrc[oi[t] * ld + oj[t]];
+    if (oi[t] >= 0) B0[oi[t] * ld + oj[t]] = Msrc[oi[t] * ld + oj[t]];
   tm.sync();
   bool ok = true;
+  // step k reads one buffer and writes every entry of the other, so one team
+  // barrier per step suffices (the buffer written next was last read before it)
+  const float* B = B0;
+  float* Bn = B1;
   for (int k = 0; k < n; ++k) {
     const float d = B[k * ld + k];
     ok = ok && (d > 0.f);
     const float r = 1.f / d;
-    float nv[E];
 #pragma unroll
     for (int t = 0; t < E; ++t) {
       const int i = oi[t], j = oj[t];
@@ -749,15 +753,16 @@ __device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float*
       // column k of the (symmetric) matrix from the lower triangle
       const float bik = i >= k ? B[i * ld + k] : B[k * ld + i];
       const float bjk = j >= k ? B[j * ld + k] : B[k * ld + j];
-      if (i != k && j != k) nv[t] = B[i * ld + j] - bik * (bjk * r);
-      else if (i == k && j == k) nv[t] = -r;
-      else nv[t] = (i == k ? bjk : bik) * r;
+      float v;
+      if (i != k && j != k) v = B[i * ld + j] - bik * (bjk * r);
+      else if (i == k && j == k) v = -r;
+      else v = (i == k ? bjk : bik) * r;
+      Bn[i * ld + j] = v;
     }
-    tm.sync();  // every read of the old column k is done
-#pragma unroll
-    for (int t = 0; t < E; ++t)
-      if (oi[t] >= 0) B[oi[t] * ld + oj[t]] = nv[t];
     tm.sync();
+    float* t_ = const_cast<float*>(B);
+    B = Bn;
+    Bn = t_;
   }
 #pragma unroll
   for (int t = 0; t < E; ++t)
@@ -788,7 +793,7 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   if (n == 0) return true;
   if (exact) {
     // entry ownership while the owned (i, j) pairs fit a few registers
-    if constexpr ((NVB * (NVB + 1) / 2 + T - 1) / T <= 17) return spd_inverse_sweep<T, NVB>(tm, n, ld, M, S1, P);
+    if constexpr ((NVB * (NVB + 1) / 2 + T - 1) / T <= 17) return spd_inverse_sweep<T, NVB>(tm, n, ld, M, S1, S2, P);
     else return spd_inverse<T>(tm, n, ld, M, S1, S2, P);
   }
   if (num_iter <= 0) return true;
@@ -1031,32 +1036,39 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
     const float* fric = md.F(BXM_O_CON_FRIC);
     const float* rc = w.at(L.rc);
     const float* cdof = w.at(L.cdof);
-    for (int c = 0; c < nact; ++c) {  // constraint.py:154-164
-      int k = rcon[c];
-      int a = la[k], b = lb[k];
-      uint64_t ma = a >= 0 ? md.anc(a) : 0ull, mb = md.anc(b);
-      f3 p = ld3(cpos + 3 * k);
-      f3 offa = a >= 0 ? p - ld3(rc + 3 * a) : mk3(0.f, 0.f, 0.f);
-      f3 offb = p - ld3(rc + 3 * b);
-      f3 n = ld3(frame + 9 * k), t1 = ld3(frame + 9 * k + 3), t2 = ld3(frame + 9 * k + 6);
-      float mu = fric[k];
-      f3 v0 = (-t1) * (-mu) + n, v1 = (-t1) * mu + n, v2 = (-t2) * (-mu) + n, v3 = (-t2) * mu + n;
-      float* j0 = w.jrow(4 * c);
-      float* j1 = w.jrow(4 * c + 1);
-      float* j2 = w.jrow(4 * c + 2);
-      float* j3 = w.jrow(4 * c + 3);
-      for (int d = tm.lane; d < nv; d += T) {
-        f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
-        f3 jb = ((mb >> d) & 1ull) ? cv - cross3(offb, ca) : mk3(0.f, 0.f, 0.f);
-        f3 ja = ((ma >> d) & 1ull) ? cv - cross3(offa, ca) : mk3(0.f, 0.f, 0.f);
-        f3 diff = jb - ja;
-        j0[d] = dot3(diff, v0);
-        j1[d] = dot3(diff, v1);
-        j2[d] = dot3(diff, v2);
-        j3[d] = dot3(diff, v3);
-      }
-      if (tm.lane < 4) rmap[4 * c + tm.lane] = 4 * k + tm.lane;
+    // constraint.py:154-164: lanes over the (active contact, dof) pairs, all
+    // active contacts' 4 pyramid rows in one pass (pair e: contact e / nv,
+    // dof e % nv, walked incrementally)
+    int c = 0, d = tm.lane;
+    while (d >= nv) {
+      d -= nv;
+      ++c;
     }
+    for (; c < nact;) {
+      const int k = rcon[c];
+      const int a = la[k], b = lb[k];
+      const uint64_t ma = a >= 0 ? md.anc(a) : 0ull, mb = md.anc(b);
+      const f3 p = ld3(cpos + 3 * k);
+      const f3 offa = a >= 0 ? p - ld3(rc + 3 * a) : mk3(0.f, 0.f, 0.f);
+      const f3 offb = p - ld3(rc + 3 * b);
+      const f3 n = ld3(frame + 9 * k), t1 = ld3(frame + 9 * k + 3), t2 = ld3(frame + 9 * k + 6);
+      const float mu = fric[k];
+      const f3 v0 = (-t1) * (-mu) + n, v1 = (-t1) * mu + n, v2 = (-t2) * (-mu) + n, v3 = (-t2) * mu + n;
+      const f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
+      const f3 jb = ((mb >> d) & 1ull) ? cv - cross3(offb, ca) : mk3(0.f, 0.f, 0.f);
+      const f3 ja = ((ma >> d) & 1ull) ? cv - cross3(offa, ca) : mk3(0.f, 0.f, 0.f);
+      const f3 diff = jb - ja;
+      w.jrow(4 * c)[d] = dot3(diff, v0);
+      w.jrow(4 * c + 1)[d] = dot3(diff, v1);
+      w.jrow(4 * c + 2)[d] = dot3(diff, v2);
+      w.jrow(4 * c + 3)[d] = dot3(diff, v3);
+      d += T;
+      while (d >= nv) {
+        d -= nv;
+        ++c;
+      }
+    }
+    for (int r = tm.lane; r < 4 * nact; r += T) rmap[r] = 4 * rcon[r >> 2] + (r & 3);
   }
   int nrow = 4 * nact;
   if (md.nlim > 0) {  // constraint.py:101-132
