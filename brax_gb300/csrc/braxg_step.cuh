@@ -113,7 +113,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   // (when it lives in scratch) must survive from CRBA to the inverse and to
   // the outputs, past the contacts of the Jacobian stage; two placements are
   // tried: after the inverse temporaries, or before them.
-  const int head = imax(imax(13 * nl, 14 * ncon + 16), m + 4);  // CRBA, contacts, output row map
+  const int head = imax(imax(13 * nl + 6 * nv, 14 * ncon + 16), m + 4);  // CRBA, contacts, output row map
   int common = 14 * nl;                                     // FK / com temporaries
   common = imax(common, 12 * nl + nu + ovf);                // RNE
   common = imax(common, 14 * ncon + 16 + ovf);              // contacts + Jacobian rows
@@ -516,17 +516,33 @@ __device__ __noinline__ void stage_crba(const int* mw, Ws w) {
   const float* cdof = w.at(L.cdof);
   const float* arm = md.F(BXM_O_D_ARM);
   float* M = w.at(L.M);
+  float* F = crbm + nl;  // per dof: crb[link] * cdof (the row's force), after crb's words
   for (int r = tm.lane; r < nv; r += T) {
     int l = dlink[r];
     f3 fa, fv;
     inertia_mul(crbi + 9 * l, ld3(crbp + 3 * l), crbm[l], ld3(cdof + 6 * r), ld3(cdof + 6 * r + 3), fa, fv);
-    uint64_t anc = md.anc(l);
-    for (int c = 0; c <= r; ++c) {
-      float v = 0.f;
-      if ((anc >> c) & 1ull) v = dot3(ld3(cdof + 6 * c + 3), fv) + dot3(ld3(cdof + 6 * c), fa);
-      if (c == r) v = v + arm[r];
-      M[r * ld + c] = v;
-      M[c * ld + r] = v;
+    st3(F + 6 * r, fa);
+    st3(F + 6 * r + 3, fv);
+  }
+  tm.sync();
+  // lower-triangle entries (r >= c) over the lanes, entry e = r(r+1)/2 + c
+  // walked incrementally; M[r][c] = cdof[c] . F[r] for ancestor dofs
+  int r = 0, c = tm.lane;
+  while (c > r) {
+    c -= r + 1;
+    ++r;
+  }
+  while (r < nv) {
+    const int l = dlink[r];
+    float v = 0.f;
+    if ((md.anc(l) >> c) & 1ull) v = dot3(ld3(cdof + 6 * c + 3), ld3(F + 6 * r + 3)) + dot3(ld3(cdof + 6 * c), ld3(F + 6 * r));
+    if (c == r) v = v + arm[r];
+    M[r * ld + c] = v;
+    M[c * ld + r] = v;
+    c += T;
+    while (c > r) {
+      c -= r + 1;
+      ++r;
     }
   }
   tm.sync();
