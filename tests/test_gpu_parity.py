@@ -186,3 +186,41 @@ def test_multi_frame_step_matches_oracle_rollout(name):
   e = rel_err(_np(got.q), ref.q)
   print(f'2 env steps x 5 frames q: p50 {np.median(e):.2e} p90 {np.quantile(e, 0.9):.2e} max {e.max():.2e}')
   assert np.median(e) <= 1e-4
+
+
+def test_implicit_solve_path_lying_humanoid():
+  """Humanoid-like models lying on the ground (torso turned 90 degrees about
+  x, 0.05-0.2 m high): most envs have more than 32 active constraint rows, so
+  the step takes the implicit projected-gradient path with Jacobian rows
+  beyond the first 32 at the end of scratch.  One step against the FP64
+  oracle within 3x the FP32 oracle's own error (the humanoid bar)."""
+  P = _pipeline()
+  from oracle.pipeline import Oracle
+  sys = load('humanoid_like')
+  n = 64
+  rng = np.random.default_rng(61)
+  q = sys.init_q[None] + rng.uniform(-0.1, 0.1, (n, sys.q_size()))
+  qd = 0.1 * rng.normal(size=(n, sys.qd_size()))
+  q[:, 3:7] = [np.cos(np.pi / 4), np.sin(np.pi / 4), 0.0, 0.0]
+  q[:, 2] = rng.uniform(0.05, 0.2, n)
+  q, qd = q.astype(np.float32), qd.astype(np.float32)
+  act = np.clip(rng.normal(0.0, 0.3, (n, sys.act_size())), -1, 1)
+  full = P.init(sys, _t(q), _t(qd), full=True)
+  torch.cuda.synchronize()
+  rows = (np.abs(_np(full.con_diag)) > 0).sum(-1)
+  assert (rows > 32).mean() >= 0.5, rows
+  o32 = Oracle(sys, np.float32, exact_inverse=True)
+  o64 = Oracle(sys, np.float64, exact_inverse=True)
+  r32 = o32.step(o32.init(q, qd), act.astype(np.float32))
+  r64 = o64.step(o64.init(q.astype(np.float64), qd.astype(np.float64)), act)
+  got = P.step(sys, P.init(sys, _t(q), _t(qd)), _t(act), inverse_mode=P.CHOLESKY)
+  torch.cuda.synchronize()
+  assert (_np(got.status) == 0).all()
+  for field in ('q', 'qd'):
+    g = _np(getattr(got, field))
+    e64 = rel_err(g, getattr(r64, field))
+    eo = rel_err(getattr(r32, field), getattr(r64, field))
+    print(f'lying humanoid {field}: vs fp64 p99 {np.quantile(e64, 0.99):.2e} max {e64.max():.2e} | '
+          f'fp32 oracle vs fp64 p99 {np.quantile(eo, 0.99):.2e}; rows > 32 in {(rows > 32).sum()} of {n}')
+    assert np.quantile(e64, 0.99) <= max(1e-5, 3 * np.quantile(eo, 0.99)), field
+    assert (e64 > max(1e-3, 3 * eo.max())).mean() <= 0.01, field
