@@ -11,9 +11,10 @@ value  : env-steps/s with state and actions resident in HBM; each timed step
          is one braxg_step launch (5 frames x 4096 envs) timed with CUDA
          events on the launching stream; the L2 is flushed (a 256 MB write)
          before every timed step, outside the events.
-e2e    : the same metric through the public API with host buffers: per step
-         the actions are copied from pinned host memory, the step runs, and
-         the observation (q, qd) is copied back and waited for.
+e2e    : the same metric through the C ABI (braxg_step via ctypes) with host
+         buffers: per step the actions are copied from pinned host memory,
+         the step runs, and the observation (q, qd) is copied back to pinned
+         host memory and waited for; wall-clock time.
 --impl reference: the CPU baseline (the numpy restatement of the reference
          path, see oracle/) on all host cores.
 """
@@ -317,12 +318,18 @@ def run_braxg(args):
   value = whole_job_rate(args.steps * n, world, t_total)
   ms_per_step = 1e3 * t_total / args.steps
 
-  # ---- e2e through the public API with host buffers ----------------------
-  h_act = torch.empty(args.steps, n, sys_.act_size(), dtype=torch.float32).pin_memory()
+  # ---- e2e through the C ABI with host buffers ------------------------------
+  # Per step: the actions are copied from pinned host memory, braxg_step runs
+  # (called through ctypes with its argument structs built once), and the
+  # observation (q, qd) is copied back to pinned host memory and waited for.
+  import ctypes
+  lib = _native.lib()
+  nq_, nv_, nu_ = sys_.q_size(), sys_.qd_size(), sys_.act_size()
+  h_act = torch.empty(args.steps, n, nu_, dtype=torch.float32).pin_memory()
   h_act.copy_(acts[args.warmup:].cpu())
-  h_obs = torch.empty(n, sys_.q_size() + sys_.qd_size(), dtype=torch.float32).pin_memory()
-  d_act = torch.empty(n, sys_.act_size(), dtype=torch.float32, device=dev)
-  obs = torch.empty(n, sys_.q_size() + sys_.qd_size(), dtype=torch.float32, device=dev)
+  h_q = torch.empty(n, nq_, dtype=torch.float32).pin_memory()
+  h_qd = torch.empty(n, nv_, dtype=torch.float32).pin_memory()
+  d_act = torch.empty(n, nu_, dtype=torch.float32, device=dev)
   # the same trajectory segment as the device-timed loop: a fresh reset, the
   # same warm-up steps, then the timed steps with the actions read from host
   st = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
@@ -330,6 +337,10 @@ def run_braxg(args):
   for k in range(args.warmup):
     pipeline.step(sys_, st, acts[k], n_frames=N_FRAMES, out=st2, **kw)
     st, st2 = st2, st
+  cs = [pipeline._cstate(st), pipeline._cstate(st2)]  # ping-pong: in = cs[k % 2], out = the other
+  states = [st, st2]
+  c_opt = pipeline._opts(mode, args.threads_per_env, args.envs_per_cta)
+  c_stream = ctypes.c_void_p(stream.cuda_stream)
   torch.cuda.synchronize()
   if world > 1:
     dist.barrier()
@@ -341,12 +352,14 @@ def run_braxg(args):
     e_ev[k][0].record(stream)
     d_act.copy_(h_act[k], non_blocking=True)
     ta = time.perf_counter()
-    pipeline.step(sys_, st, d_act, n_frames=N_FRAMES, out=st2, **kw)
+    rc = lib.braxg_step(model.handle, c_stream, n, N_FRAMES, d_act.data_ptr(), ctypes.byref(cs[k % 2]),
+                        ctypes.byref(cs[1 - k % 2]), ctypes.byref(c_opt))
     api_s += time.perf_counter() - ta
-    st, st2 = st2, st
-    obs[:, :sys_.q_size()].copy_(st.q)
-    obs[:, sys_.q_size():].copy_(st.qd)
-    h_obs.copy_(obs, non_blocking=True)
+    if rc != 0:
+      _native.check(rc, 'braxg_step')
+    out_s = states[1 - k % 2]
+    h_q.copy_(out_s.q, non_blocking=True)
+    h_qd.copy_(out_s.qd, non_blocking=True)
     e_ev[k][1].record(stream)
     stream.synchronize()
   t_e2e = max_over_ranks(time.perf_counter() - t0, dev)
@@ -355,8 +368,9 @@ def run_braxg(args):
          'ms_per_step_wall': round(1e3 * t_e2e / args.steps, 4),
          'ms_per_step_gpu': round(1e3 * gpu_e2e / args.steps, 4),
          'ms_per_step_api_call': round(1e3 * api_s / args.steps, 4),
-         'h2d_bytes_per_step': n * sys_.act_size() * 4,
-         'd2h_bytes_per_step': n * (sys_.q_size() + sys_.qd_size()) * 4}
+         'path': 'braxg_step through ctypes; actions H2D from pinned memory, q and qd D2H to pinned memory',
+         'h2d_bytes_per_step': n * nu_ * 4,
+         'd2h_bytes_per_step': n * (nq_ + nv_) * 4}
 
   # ---- roofline -----------------------------------------------------------
   nmv = load_nmv()[WORKLOAD]
