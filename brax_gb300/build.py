@@ -14,7 +14,7 @@ BUILD_DIR = os.path.join(ROOT, 'brax_gb300', '_lib', 'obj')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # one translation unit per group of kernel instantiations so they compile in
 # parallel; braxg.cu holds the C ABI
-UNITS = ['braxg.cu', 'inst_t32_nv16.cu', 'inst_t32_nv32.cu', 'inst_t32_nv64.cu',
+UNITS = ['braxg.cu', 'braxg_grad.cu', 'braxg_batch.cu', 'inst_t32_nv16.cu', 'inst_t32_nv32.cu', 'inst_t32_nv64.cu',
          'inst_t16.cu', 'inst_vjp_nv16.cu', 'inst_vjp_nv32.cu', 'inst_batch.cu']
 
 
