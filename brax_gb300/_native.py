@@ -41,10 +41,14 @@ class Dims(ctypes.Structure):
   _fields_ = [(n, ctypes.c_int32) for n in ('nl', 'nq', 'nv', 'nu', 'ncon', 'nlim', 'm')]
 
 
+class Randomization(ctypes.Structure):
+  _fields_ = [(n, ctypes.c_void_p) for n in ('friction', 'act_gain', 'act_bias_q', 'act_bias_qd')]
+
+
 class Options(ctypes.Structure):
   _fields_ = [('inverse_mode', ctypes.c_int32), ('threads_per_env', ctypes.c_int32),
               ('envs_per_cta', ctypes.c_int32), ('relax_barriers', ctypes.c_int32),
-              ('stage_cycles', ctypes.c_void_p)]
+              ('stage_cycles', ctypes.c_void_p), ('randomization', ctypes.POINTER(Randomization))]
 
 
 class BucketShape(ctypes.Structure):

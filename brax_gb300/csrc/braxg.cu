@@ -101,6 +101,7 @@ int launch(const braxg_model* m, const braxg_options* opt, braxg::StepArgs& a, c
   a.envs_per_cta = s.epc;
   a.prof = opt ? opt->stage_cycles : nullptr;
   a.relax = opt ? opt->relax_barriers : 0;
+  if (opt && opt->randomization) a.dr = *opt->randomization;
   int grid = (a.n_env + s.epc - 1) / s.epc;
   int cur = 0;
   cudaGetDevice(&cur);

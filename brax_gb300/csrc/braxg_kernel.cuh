@@ -24,6 +24,22 @@ __device__ void store_mat(const Team<T>& tm, float* dst, const float* src, int n
   }
 }
 
+// The env's copy of the parameters per-env randomisation may override
+// (contact friction, actuator gain / bias_q / bias_qd): the [n, k] rows of the
+// randomisation arrays where given, else the model's values.
+template <int T>
+__device__ __forceinline__ void load_params(const Team<T>& tm, const braxg_randomization& dr, const Model& md, Ws w,
+                                            long long env) {
+  float* p = w.at(w.L->prm);
+  const int nc = md.ncon, nu = md.nu;
+  for (int i = tm.lane; i < nc; i += T) p[i] = dr.friction ? dr.friction[env * nc + i] : md.F(BXM_O_CON_FRIC)[i];
+  for (int i = tm.lane; i < nu; i += T) {
+    p[nc + i] = dr.act_gain ? dr.act_gain[env * nu + i] : md.F(BXM_O_ACT_GAIN)[i];
+    p[nc + nu + i] = dr.act_bias_q ? dr.act_bias_q[env * nu + i] : md.F(BXM_O_ACT_BQ)[i];
+    p[nc + 2 * nu + i] = dr.act_bias_qd ? dr.act_bias_qd[env * nu + i] : md.F(BXM_O_ACT_BQD)[i];
+  }
+}
+
 // Per-stage cycle accumulation (only when a profile buffer is passed): lane 0
 // of each team adds the clock64 delta of every stage straight into the buffer.
 struct Prof {
@@ -286,6 +302,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   if (active) {
     load_vec<T>(tm, w.at(L.q), a.q_in + B.q + env * nq, nq);
     load_vec<T>(tm, w.at(L.qd), a.qd_in + B.v + env * nv, nv);
+    load_params<T>(tm, a.dr, md, w, env);
   }
   if (active && !exact) {
     const float* src = a.minv_in + B.vv + env * nv * nv;

@@ -35,6 +35,7 @@ struct StepArgs {
   long long traj_qd_stride;  // and of traj_qd
   unsigned long long* prof;
   int relax;                 // braxg_options.relax_barriers
+  braxg_randomization dr;    // per-env System parameters (NULL fields: the model's)
   int has_task;              // fused env step (task, io) after every env step
   long long env_step_stride; // envs between env steps of io.reward / io.done
   braxg_task task;

@@ -50,6 +50,7 @@ struct Layout {
   int xp, xr, xa, xv, rc, ci, cp, cd, cdof, cdofd;
   int M, Minv;
   int J, jcap, jovf, rdiag, raref, rmap;
+  int prm;  // per-env parameters: friction [ncon], actuator gain, bias_q, bias_qd [nu each]
   int scr, scr_words, itmp;
   int total;
 };
@@ -107,6 +108,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.rdiag = take(m);
   L.raref = take(m);
   L.rmap = take(m);
+  L.prm = take(ncon + 3 * nu);
   const int ovf = (m - L.jcap) * L.ldj;  // overflow Jacobian rows at the scratch end
   const int nn = nv * L.ldm;
   // Scratch users, each with the regions it needs at once.  The mass matrix
@@ -1049,7 +1051,7 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
     tm.sync();
     const int* la = md.I(BXM_O_CON_LA);
     const int* lb = md.I(BXM_O_CON_LB);
-    const float* fric = md.F(BXM_O_CON_FRIC);
+    const float* fric = w.at(L.prm);  // per-env sliding friction
     const float* rc = w.at(L.rc);
     const float* cdof = w.at(L.cdof);
     // constraint.py:154-164: lanes over the (active contact, dof) pairs, all
@@ -1117,7 +1119,7 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
   // per-row impedance, reference acceleration and A diagonal
   const float* csolp = md.F(BXM_O_CON_SOLP);
   const float* cinvw = md.F(BXM_O_CON_INVW);
-  const float* fric = md.F(BXM_O_CON_FRIC);
+  const float* fric = w.at(L.prm);
   for (int r = tm.lane; r < nrow; r += T) {
     int orig = rmap[r];
     float vel = 0.f;
@@ -1168,8 +1170,9 @@ __device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
       const float* fr = md.F(BXM_O_ACT_FR) + 2 * a;
       float gear = md.F(BXM_O_ACT_GEAR)[a];
       float u = fminf(fmaxf(act[a], cr[0]), cr[1]);
-      float bias = gear * (q[aqid[a]] * md.F(BXM_O_ACT_BQ)[a] + qd[aqdid[a]] * md.F(BXM_O_ACT_BQD)[a]);
-      float f = md.F(BXM_O_ACT_GAIN)[a] * u + bias;
+      const float* prm = w.at(L.prm) + md.ncon;  // per-env gain, bias_q, bias_qd
+      float bias = gear * (q[aqid[a]] * prm[md.nu + a] + qd[aqdid[a]] * prm[2 * md.nu + a]);
+      float f = prm[a] * u + bias;
       f = fminf(fmaxf(f, fr[0]), fr[1]);
       force[a] = f * gear;
     }

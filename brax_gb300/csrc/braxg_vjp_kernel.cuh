@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   if (active) {
     copy_vec<T>(tm, w.at(L.q), a.q0 + env * nq, nq);
     copy_vec<T>(tm, w.at(L.qd), a.qd0 + env * nv, nv);
+    load_params<T>(tm, braxg_randomization{}, md, w, env);  // the model's parameters
   }
   tm.sync();
   __syncthreads();

@@ -44,13 +44,16 @@ class Locomotion:
                reset_noise_scale: float = 0.1,
                exclude_current_positions_from_observation: bool = True, n_frames: int = 5,
                episode_length: int = 1000, action_repeat: int = 1, auto_reset: bool = True,
-               inverse_mode: int = P.CHOLESKY, device=None):
+               inverse_mode: int = P.CHOLESKY, randomization: Optional[dict] = None, device=None):
     self.sys = sys
     self.model = P.model_for(sys, device)
     self.device = self.model.device
     self.n_frames = int(n_frames)
     self.reset_noise_scale = float(reset_noise_scale)
     self.inverse_mode = int(inverse_mode)
+    # per-env System parameters (DomainRandomizationVmapWrapper,
+    # brax/envs/wrappers/training.py:223-260): pipeline.randomize(...)
+    self.randomization = randomization
     self.exclude = bool(exclude_current_positions_from_observation)
     self.task = N.Task(float(ctrl_cost_weight), float(healthy_reward), float(healthy_z_range[0]),
                        float(healthy_z_range[1]), int(terminate_when_unhealthy), int(self.exclude),
@@ -81,7 +84,8 @@ class Locomotion:
       q = init_q + (torch.rand(n_env, m.nq, device=self.device, generator=generator) * 2 - 1) * s
     if qd is None:
       qd = s * torch.randn(n_env, m.nv, device=self.device, generator=generator)
-    ps = P.init(self.sys, q.to(self.device, torch.float32), qd.to(self.device, torch.float32))
+    ps = P.init(self.sys, q.to(self.device, torch.float32), qd.to(self.device, torch.float32),
+                randomization=self.randomization)
     z = lambda: torch.zeros(n_env, dtype=torch.float32, device=self.device)
     info = {'steps': z(), 'truncation': z(), 'first_q': ps.q.clone(), 'first_qd': ps.qd.clone(),
             'first_mass_mx_inv': ps.mass_mx_inv.clone(), 'first_obs': self._obs(ps)}
@@ -110,11 +114,12 @@ class Locomotion:
                  trunc.data_ptr(), last_done.data_ptr(), state.info['first_q'].data_ptr(),
                  state.info['first_qd'].data_ptr(), state.info['first_mass_mx_inv'].data_ptr())
     cin, cout = P._cstate(ps), P._cstate(out)
+    dr, _keep = P._randomization(m, n, self.randomization)
     stream = torch.cuda.current_stream(self.device).cuda_stream
     N.check(N.lib().braxg_env_rollout(m.handle, ctypes.c_void_p(stream), n, n_steps, self.n_frames,
                                       act_seq.data_ptr() if m.nu else None, ctypes.byref(cin),
                                       ctypes.byref(cout), ctypes.byref(self.task), ctypes.byref(io),
-                                      ctypes.byref(P._opts(self.inverse_mode, 0, 0))),
+                                      ctypes.byref(P._opts(self.inverse_mode, 0, 0, dr=dr))),
             'braxg_env_rollout')
     info = dict(state.info, steps=steps, truncation=trunc)
     metrics = {k: met[:, i] for i, k in enumerate(N.METRICS)}

@@ -150,9 +150,51 @@ def _as_batch(x: torch.Tensor, width: int, name: str, dev) -> torch.Tensor:
   return x.to(torch.float32).contiguous()
 
 
-def _opts(inverse_mode, threads_per_env, envs_per_cta, profile=None, relax_barriers=0):
-  return N.Options(int(inverse_mode), int(threads_per_env), int(envs_per_cta), int(relax_barriers),
-                   None if profile is None else profile.data_ptr())
+_DR_FIELDS = ('friction', 'act_gain', 'act_bias_q', 'act_bias_qd')
+
+
+def _randomization(m: 'Model', n: int, randomization):
+  """A C Randomization struct for a dict of per-env tensors (friction
+  [n, ncon], act_gain / act_bias_q / act_bias_qd [n, nu]), with the tensors it
+  points to (kept alive by the caller for the call)."""
+  if not randomization:
+    return None, []
+  keep = []
+  ptrs = {}
+  for k, v in randomization.items():
+    if k not in _DR_FIELDS:
+      raise ValueError(f'unknown randomization field {k!r}; expected one of {_DR_FIELDS}')
+    width = m.ncon if k == 'friction' else m.nu
+    v = torch.as_tensor(v, dtype=torch.float32, device=m.device).reshape(n, width).contiguous()
+    keep.append(v)
+    ptrs[k] = v.data_ptr()
+  return N.Randomization(*[ptrs.get(k) for k in _DR_FIELDS]), keep
+
+
+def randomize(sys, n: int, generator: Optional[torch.Generator] = None, friction_range=(0.6, 1.4),
+              gain_scale_range=(1.0, 1.0), device=None) -> dict:
+  """Per-env parameters in the manner of brax's domain randomisation
+  examples: one sliding friction per env, uniform in friction_range, for
+  every contact slot (every geom gets it, so every pair's mixed friction is
+  it), and the actuator gains scaled by a per-env factor."""
+  m = model_for(sys, device)
+  f = torch.rand(n, 1, device=m.device, generator=generator)
+  f = friction_range[0] + (friction_range[1] - friction_range[0]) * f
+  out = {'friction': f.expand(n, m.ncon).contiguous()}
+  if m.nu and gain_scale_range != (1.0, 1.0):
+    g = torch.rand(n, 1, device=m.device, generator=generator)
+    g = gain_scale_range[0] + (gain_scale_range[1] - gain_scale_range[0]) * g
+    gain = torch.tensor(sys.actuator.gain, dtype=torch.float32, device=m.device)[None]
+    out['act_gain'] = (gain * g).contiguous()
+  return out
+
+
+def _opts(inverse_mode, threads_per_env, envs_per_cta, profile=None, relax_barriers=0, dr=None):
+  o = N.Options(int(inverse_mode), int(threads_per_env), int(envs_per_cta), int(relax_barriers),
+                None if profile is None else profile.data_ptr())
+  if dr is not None:
+    o.randomization = ctypes.pointer(dr)
+  return o
 
 
 def profile_buffer(device=None) -> torch.Tensor:
@@ -169,7 +211,8 @@ def profile_report(buf: torch.Tensor) -> dict:
 
 
 def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
-         full: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0) -> State:
+         full: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0,
+         randomization: Optional[dict] = None) -> State:
   """brax/generalized/pipeline.py:32-61 for a batch of envs."""
   if debug:
     raise NotImplementedError('debug contacts are not materialised')
@@ -180,10 +223,11 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
     raise ValueError('q and qd batch sizes differ')
   out = _alloc(m, q.shape[0], full, m.device)
   cs = _cstate(out)
+  dr, _keep = _randomization(m, q.shape[0], randomization)
   stream = torch.cuda.current_stream(m.device).cuda_stream
   N.check(N.lib().braxg_init(m.handle, ctypes.c_void_p(stream), q.shape[0], q.data_ptr(),
                              qd.data_ptr(), ctypes.byref(cs),
-                             ctypes.byref(_opts(NEWTON_SCHULZ, threads_per_env, envs_per_cta))),
+                             ctypes.byref(_opts(NEWTON_SCHULZ, threads_per_env, envs_per_cta, dr=dr))),
           'braxg_init')
   return out
 
@@ -191,7 +235,8 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
 def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
          full: bool = False, inverse_mode: int = NEWTON_SCHULZ, out: Optional[State] = None,
          threads_per_env: int = 0, envs_per_cta: int = 0,
-         profile: Optional[torch.Tensor] = None, relax_barriers: int = 0) -> State:
+         profile: Optional[torch.Tensor] = None, relax_barriers: int = 0,
+         randomization: Optional[dict] = None) -> State:
   """brax/generalized/pipeline.py:64-94; n_frames > 1 repeats it with the same
   action (PipelineEnv.pipeline_step, brax/envs/base.py:128-137)."""
   if debug:
@@ -208,17 +253,19 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
     out = _alloc(m, n, full, m.device)
   cin = _cstate(state)
   cout = _cstate(out)
+  dr, _keep = _randomization(m, n, randomization)
   stream = torch.cuda.current_stream(m.device).cuda_stream
   N.check(N.lib().braxg_step(m.handle, ctypes.c_void_p(stream), n, int(n_frames), act_p,
                              ctypes.byref(cin), ctypes.byref(cout),
                              ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta,
-                                                profile, relax_barriers))),
+                                                profile, relax_barriers, dr))),
           'braxg_step')
   return out
 
 
 def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = NEWTON_SCHULZ,
-            trajectory: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0):
+            trajectory: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0,
+            randomization: Optional[dict] = None):
   """len(act_seq) env steps in one launch; returns (final State, (traj_q, traj_qd))."""
   m = model_for(sys, state.q.device)
   n = state.q.shape[0]
@@ -232,11 +279,13 @@ def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = N
     tq = torch.empty(n_steps, n, m.nq, dtype=torch.float32, device=m.device)
     tqd = torch.empty(n_steps, n, m.nv, dtype=torch.float32, device=m.device)
   cin, cout = _cstate(state), _cstate(out)
+  dr, _keep = _randomization(m, n, randomization)
   stream = torch.cuda.current_stream(m.device).cuda_stream
   N.check(N.lib().braxg_rollout(m.handle, ctypes.c_void_p(stream), n, n_steps, int(n_frames),
                                 act_seq.data_ptr() if m.nu else None, ctypes.byref(cin),
                                 ctypes.byref(cout), _ptr(tq), _ptr(tqd),
-                                ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta))),
+                                ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta,
+                                                   dr=dr))),
           'braxg_rollout')
   return out, (tq, tqd)
 

@@ -104,6 +104,18 @@ enum braxg_profile_slot {
   BRAXG_PROF_SLOTS = 32
 };
 
+/* Per-env System parameters (the fields brax's DomainRandomizationVmapWrapper,
+ * brax/envs/wrappers/training.py:223-260, is used to randomise): each pointer
+ * is [n, k] device memory overriding the model's value for every env, or
+ * NULL to keep the model's.  Forward paths only (step, rollout, env
+ * rollout); gradients use the model's values. */
+typedef struct {
+  const float* friction;     /* [n, ncon] sliding friction of every contact slot */
+  const float* act_gain;     /* [n, nu] actuator gain */
+  const float* act_bias_q;   /* [n, nu] actuator bias on q */
+  const float* act_bias_qd;  /* [n, nu] actuator bias on qd */
+} braxg_randomization;
+
 typedef struct {
   int32_t inverse_mode;     /* braxg_inverse_mode */
   int32_t threads_per_env;  /* 0 = tuned, else 16 or 32 lanes per env */
@@ -116,6 +128,8 @@ typedef struct {
   /* Optional device buffer of BRAXG_PROF_SLOTS uint64 counters the kernel
    * adds its per-stage cycle counts into (NULL = no profiling). */
   unsigned long long* stage_cycles;
+  /* Optional per-env System parameters (NULL = the model's for every env). */
+  const braxg_randomization* randomization;
 } braxg_options;
 
 /* Copies a packed System descriptor to `device`.  Replaces tracing the
