@@ -42,7 +42,8 @@ enum braxg_inverse_mode {
   /* Newton-Schulz warm start from the previous inverse with the reference's
    * iteration count and best-iterate acceptance (brax/math.py:278-305). */
   BRAXG_INV_NEWTON_SCHULZ = 0,
-  /* Exact SPD inverse from a per-env Cholesky factorisation. */
+  /* Exact SPD inverse (per-env symmetric Gauss-Jordan sweep; its pivots are
+   * a Cholesky factorisation's, so a non-positive one flags the env). */
   BRAXG_INV_CHOLESKY = 1
 };
 
