@@ -52,6 +52,8 @@ def parse():
   p.add_argument('--inverse', default='cholesky', choices=['newton_schulz', 'cholesky'])
   p.add_argument('--threads-per-env', type=int, default=0)
   p.add_argument('--envs-per-cta', type=int, default=0)
+  p.add_argument('--no-state-cache', dest='state_cache', action='store_false',
+                 help='states carry no position-term cache (every step recomputes them)')
   p.add_argument('--cpu-sample-envs', type=int, default=256)
   p.add_argument('--no-cpu-baseline', action='store_true')
   p.add_argument('--no-adjoint', action='store_true')
@@ -257,9 +259,10 @@ def run_braxg(args):
   gen.manual_seed(77 + rank)
   acts = torch.rand(total, n, sys_.act_size(), device=dev, generator=gen) * 2 - 1
   model = pipeline.model_for(sys_, dev)
-  s0 = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
+  s0 = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev),
+                      cache=args.state_cache)
   a_state = s0
-  b_state = pipeline._alloc(model, n, False, dev)
+  b_state = pipeline._alloc(model, n, False, dev, cache=args.state_cache)
   flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
   stream = torch.cuda.current_stream(dev)
 
@@ -295,8 +298,9 @@ def run_braxg(args):
   # the same timed loop with the reference's inverse (Newton-Schulz, K = 10)
   other = pipeline.NEWTON_SCHULZ if mode == pipeline.CHOLESKY else pipeline.CHOLESKY
   kw_o = dict(kw, inverse_mode=other)
-  c_state = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
-  d_state = pipeline._alloc(model, n, False, dev)
+  c_state = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev),
+                      cache=args.state_cache)
+  d_state = pipeline._alloc(model, n, False, dev, cache=args.state_cache)
   for i in range(args.warmup):
     pipeline.step(sys_, c_state, acts[i], n_frames=N_FRAMES, out=d_state, **kw_o)
     c_state, d_state = d_state, c_state
@@ -332,8 +336,9 @@ def run_braxg(args):
   d_act = torch.empty(n, nu_, dtype=torch.float32, device=dev)
   # the same trajectory segment as the device-timed loop: a fresh reset, the
   # same warm-up steps, then the timed steps with the actions read from host
-  st = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
-  st2 = pipeline._alloc(model, n, False, dev)
+  st = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev),
+                      cache=args.state_cache)
+  st2 = pipeline._alloc(model, n, False, dev, cache=args.state_cache)
   for k in range(args.warmup):
     pipeline.step(sys_, st, acts[k], n_frames=N_FRAMES, out=st2, **kw)
     st, st2 = st2, st
@@ -410,6 +415,7 @@ def run_braxg(args):
       'data': 'synthetic (seeded resets and U(-1,1) actions)',
       'config': {**workload_config(n, world),
                  'inverse_mode': args.inverse,
+                 'state_cache': bool(args.state_cache),
                  'l2': 'flushed (256 MB write) before every timed step',
                  'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
                                           model.launch_shape(mode, args.threads_per_env,

@@ -191,6 +191,12 @@ int braxg_model_dims(const braxg_model* m, braxg_dims* out) {
   return BRAXG_OK;
 }
 
+int braxg_model_cache_words(const braxg_model* m, int32_t* words) {
+  if (m == nullptr || words == nullptr) return fail(BRAXG_ERR_INVALID, "NULL argument");
+  *words = m->L.total;  // the env's whole shared-memory arena
+  return BRAXG_OK;
+}
+
 int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int32_t* tpe, int32_t* epc, int32_t* smem) {
   if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model is NULL");
   Shape s;
@@ -202,12 +208,21 @@ int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int32_t* 
   return BRAXG_OK;
 }
 
+// The caches are read and written with 16-byte vector accesses.
+static int check_caches(const braxg_state* in, const braxg_state* out) {
+  auto misaligned = [](const float* p) { return p != nullptr && (reinterpret_cast<uintptr_t>(p) & 15) != 0; };
+  if ((in && misaligned(in->cache)) || (out && misaligned(out->cache)))
+    return fail(BRAXG_ERR_INVALID, "state cache must be 16-byte aligned");
+  return BRAXG_OK;
+}
+
 int braxg_init(const braxg_model* m, void* stream, int n_env, const float* q, const float* qd, braxg_state* out,
                const braxg_options* opt) {
   int rc = check_common(m, n_env, opt);
   if (rc) return rc;
   if (out == nullptr || (n_env > 0 && (q == nullptr || qd == nullptr)))
     return fail(BRAXG_ERR_INVALID, "q, qd and out are required");
+  if ((rc = check_caches(nullptr, out))) return rc;
   braxg::StepArgs a{};
   a.model = m->d_desc;
   a.model_words = m->words;
@@ -230,6 +245,7 @@ static int run_steps(const braxg_model* m, void* stream, int n_env, int n_steps,
   if (rc) return rc;
   if (in == nullptr || out == nullptr) return fail(BRAXG_ERR_INVALID, "in and out states are required");
   if (n_frames < 1 || n_steps < 0) return fail(BRAXG_ERR_INVALID, "n_frames must be >= 1 and n_steps >= 0");
+  if ((rc = check_caches(in, out))) return rc;
   bool ns = !(opt && opt->inverse_mode == BRAXG_INV_CHOLESKY) && m->ns_iters > 0;
   if (n_env > 0 && (in->q == nullptr || in->qd == nullptr || (ns && in->mass_mx_inv == nullptr)))
     return fail(BRAXG_ERR_INVALID, "in->q, in->qd and (Newton-Schulz mode) in->mass_mx_inv are required");
@@ -244,6 +260,7 @@ static int run_steps(const braxg_model* m, void* stream, int n_env, int n_steps,
   a.q_in = in->q;
   a.qd_in = in->qd;
   a.minv_in = in->mass_mx_inv;
+  a.cache_in = in->cache;
   a.act = act;
   a.act_step_stride = act_stride;
   a.out = *out;

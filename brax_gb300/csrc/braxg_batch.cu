@@ -221,6 +221,7 @@ int braxg_batch_init(const braxg_batch* b, void* stream, const float* q, const f
   s.q_in = q;
   s.qd_in = qd;
   s.out = *out;
+  s.out.cache = nullptr;  // per-model arena sizes differ: batches keep no cache
   return batch_launch(b, stream, s, opt);
 }
 
@@ -246,6 +247,7 @@ int braxg_batch_rollout(const braxg_batch* b, void* stream, int n_steps, const f
   s.act = act_seq;
   s.act_step_stride = tot.act;
   s.out = *out;
+  s.out.cache = nullptr;
   s.traj_q = traj_q;
   s.traj_qd = traj_qd;
   s.traj_q_stride = tot.q;

@@ -40,6 +40,77 @@ __device__ __forceinline__ void load_params(const Team<T>& tm, const braxg_rando
   }
 }
 
+// Whether an env's arena, just restored from the input state's cache, holds
+// the position terms of exactly this call's input: q, qd (and, when the
+// inverse is carried, mass_mx_inv) and the per-env parameters equal the cached
+// ones bit for bit (team-uniform).
+template <int T>
+__device__ __forceinline__ bool cache_matches(const StepArgs& a, const EnvBase& B, const int* mw, Ws w, long long env,
+                                           bool carried_minv) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  const int nq = md.nq, nv = md.nv, nc = md.ncon, nu = md.nu, ld = L.ldm;
+  auto same = [](float x, float y) { return __float_as_uint(x) == __float_as_uint(y); };
+  bool eq = true;
+  for (int i = tm.lane; i < nq; i += T) eq = eq && same(w.at(L.q)[i], a.q_in[B.q + env * nq + i]);
+  for (int i = tm.lane; i < nv; i += T) eq = eq && same(w.at(L.qd)[i], a.qd_in[B.v + env * nv + i]);
+  if (carried_minv)
+    for (int idx = tm.lane; idx < nv * nv; idx += T) {
+      int i = idx / nv, j = idx - i * nv;
+      eq = eq && same(w.at(L.Minv)[i * ld + j], a.minv_in[B.vv + env * nv * nv + idx]);
+    }
+  const float* p = w.at(L.prm);
+  const braxg_randomization& dr = a.dr;
+  for (int i = tm.lane; i < nc; i += T)
+    eq = eq && same(p[i], dr.friction ? dr.friction[env * nc + i] : md.F(BXM_O_CON_FRIC)[i]);
+  for (int i = tm.lane; i < nu; i += T) {
+    eq = eq && same(p[nc + i], dr.act_gain ? dr.act_gain[env * nu + i] : md.F(BXM_O_ACT_GAIN)[i]);
+    eq = eq && same(p[nc + nu + i], dr.act_bias_q ? dr.act_bias_q[env * nu + i] : md.F(BXM_O_ACT_BQ)[i]);
+    eq = eq && same(p[nc + 2 * nu + i], dr.act_bias_qd ? dr.act_bias_qd[env * nu + i] : md.F(BXM_O_ACT_BQD)[i]);
+  }
+  return tm.all(eq);
+}
+
+template <int T>
+__device__ __forceinline__ void copy_arena(const Team<T>& tm, float* dst, const float* src, int words) {
+  float4* d = reinterpret_cast<float4*>(dst);
+  const float4* s = reinterpret_cast<const float4*>(src);
+  for (int i = tm.lane; i < words / 4; i += T) d[i] = s[i];
+}
+
+// Tag of a cached arena (misc[11]): the team width that computed it (lane
+// reductions make the terms depend on it bit for bit) and whether its
+// mass_mx_inv is the exact inverse of its mass matrix.  An env whose launch
+// flagged a non-finite value stores tag 0, which no launch accepts.
+template <int T>
+__device__ __forceinline__ int cache_tag(bool exact_minv) { return 2 * T + (exact_minv ? 1 : 0); }
+
+// Restores the env's arena from the input state's cache; true if it applies.
+// In exact-inverse mode the cached mass_mx_inv must be exact; in
+// Newton-Schulz mode it must equal the carried one.
+template <int T>
+__device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, const int* mw, Ws w, long long env,
+                                           bool exact) {
+  const Team<T> tm;
+  copy_arena<T>(tm, w.b, a.cache_in + (B.env + env) * w.L->total, w.L->total);
+  tm.sync();
+  const int tag = reinterpret_cast<const int*>(w.at(w.L->misc))[11];
+  const bool tag_ok = exact ? tag == cache_tag<T>(true) : (tag >> 1) == T;
+  return cache_matches<T>(a, B, mw, w, env, !exact) && tag_ok;
+}
+
+// Stores the env's arena (the output state's position terms) into its cache.
+template <int T>
+__device__ __noinline__ void store_cache(const StepArgs& a, const EnvBase& B, Ws w, long long env, bool exact,
+                                        bool ok) {
+  const Team<T> tm;
+  tm.sync();
+  if (tm.lane == 0) reinterpret_cast<int*>(w.at(w.L->misc))[11] = ok ? cache_tag<T>(exact) : 0;
+  tm.sync();
+  copy_arena<T>(tm, a.out.cache + (B.env + env) * w.L->total, w.b, w.L->total);
+}
+
 // Per-stage cycle accumulation (only when a profile buffer is passed): lane 0
 // of each team adds the clock64 delta of every stage straight into the buffer.
 struct Prof {
@@ -299,6 +370,9 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   Prof pf(a.prof, active && tm.lane == 0);
 
   const bool exact = a.exact_inverse || a.init || md.ns_iters == 0;
+  // the input state's cached position terms, where they still apply
+  bool cached = false;
+  if (active && !a.init && a.cache_in != nullptr) cached = restore_cache<T>(a, B, smem, w, env, exact);
   if (active) {
     load_vec<T>(tm, w.at(L.q), a.q_in + B.q + env * nq, nq);
     load_vec<T>(tm, w.at(L.qd), a.qd_in + B.v + env * nv, nv);
@@ -319,7 +393,10 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   }
   tm.sync();
   pf.mark(BRAXG_PROF_IO);
-  bool ok = position_stage<T, NVB>(smem, w, active, exact, 0, pf);
+  // position terms of the input state (CTA-uniform: skipped when every env of
+  // the CTA restored them from the cache)
+  bool ok = true;
+  if (__syncthreads_or(active && !cached)) ok = position_stage<T, NVB>(smem, w, active && !cached, exact, 0, pf);
   const long long ei = B.env + env;
   if (a.init) {
     for (int d = tm.lane; active && d < nv; d += T) {
@@ -369,6 +446,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
     }
   }
   if (!active) return;  // no CTA barrier follows
+  if (a.out.cache != nullptr) store_cache<T>(a, B, w, env, exact, ok);  // before the outputs touch scratch
   if (TASK && a.n_steps > 0 && !a.init) task_outputs<T>(a, smem, w, ei);
   write_outputs<T>(a, B, smem, w, env, ok);
   pf.mark(BRAXG_PROF_IO);

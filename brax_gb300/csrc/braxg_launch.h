@@ -26,6 +26,7 @@ struct StepArgs {
   const float* q_in;
   const float* qd_in;
   const float* minv_in;
+  const float* cache_in;   // position-level cache of the input state (or null)
   const float* act;
   long long act_step_stride;
   braxg_state out;

@@ -104,7 +104,7 @@ class Locomotion:
     if act_seq.shape[1:] != (n, m.nu):
       raise ValueError(f'act_seq must be (n_steps, {n}, {m.nu})')
     n_steps = act_seq.shape[0]
-    out = ps if donate else P._alloc(m, n, False, self.device)
+    out = ps if donate else P._alloc(m, n, False, self.device, ps.cache is not None)
     f = lambda *sh: torch.empty(*sh, dtype=torch.float32, device=self.device)
     obs, rewards, dones, met = f(n, self.observation_size), f(n_steps, n), f(n_steps, n), f(n, len(N.METRICS))
     steps = state.info['steps'].clone()

@@ -46,6 +46,9 @@ class Model:
     N.check(lib.braxg_model_dims(h, ctypes.byref(d)), 'braxg_model_dims')
     self.nl, self.nq, self.nv, self.nu = d.nl, d.nq, d.nv, d.nu
     self.ncon, self.nlim, self.m = d.ncon, d.nlim, d.m
+    w = ctypes.c_int32()
+    N.check(lib.braxg_model_cache_words(h, ctypes.byref(w)), 'braxg_model_cache_words')
+    self.cache_words = w.value
 
   @property
   def handle(self):
@@ -111,17 +114,23 @@ class State:
   con_diag: Optional[torch.Tensor] = None
   con_aref: Optional[torch.Tensor] = None
   contact: None = None
+  # [n, Model.cache_words] position-level terms of this state, computed by
+  # the call that made it; a step from this state reuses them for every env
+  # whose q / qd / parameters are unchanged (bit for bit) instead of
+  # recomputing them.  Not part of brax's State.
+  cache: Optional[torch.Tensor] = None
 
   def replace(self, **kw) -> 'State':
     return dataclasses.replace(self, **kw)
 
 
-def _alloc(m: Model, n: int, full: bool, dev) -> State:
+def _alloc(m: Model, n: int, full: bool, dev, cache: bool = False) -> State:
   f = lambda *s: torch.empty(*s, dtype=torch.float32, device=dev)
   s = State(q=f(n, m.nq), qd=f(n, m.nv), x_pos=f(n, m.nl, 3), x_rot=f(n, m.nl, 4),
             xd_ang=f(n, m.nl, 3), xd_vel=f(n, m.nl, 3), mass_mx_inv=f(n, m.nv, m.nv),
             qf_smooth=f(n, m.nv), qf_constraint=f(n, m.nv), qdd=f(n, m.nv),
-            status=torch.empty(n, dtype=torch.int32, device=dev))
+            status=torch.empty(n, dtype=torch.int32, device=dev),
+            cache=f(n, m.cache_words) if cache else None)
   if full:
     s = s.replace(root_com=f(n, m.nl, 3), cinr_pos=f(n, m.nl, 3), cinr_rot=f(n, m.nl, 4),
                   cinr_i=f(n, m.nl, 3, 3), cd=f(n, m.nl, 6), cdof=f(n, m.nv, 6),
@@ -212,8 +221,9 @@ def profile_report(buf: torch.Tensor) -> dict:
 
 def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
          full: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0,
-         randomization: Optional[dict] = None) -> State:
-  """brax/generalized/pipeline.py:32-61 for a batch of envs."""
+         randomization: Optional[dict] = None, cache: bool = True) -> State:
+  """brax/generalized/pipeline.py:32-61 for a batch of envs.  ``cache``
+  gives the state (and the states stepped from it) a position-term cache."""
   if debug:
     raise NotImplementedError('debug contacts are not materialised')
   m = model_for(sys, q.device if isinstance(q, torch.Tensor) else None)
@@ -221,7 +231,7 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
   qd = _as_batch(qd, m.nv, 'qd', m.device)
   if q.shape[0] != qd.shape[0]:
     raise ValueError('q and qd batch sizes differ')
-  out = _alloc(m, q.shape[0], full, m.device)
+  out = _alloc(m, q.shape[0], full, m.device, cache)
   cs = _cstate(out)
   dr, _keep = _randomization(m, q.shape[0], randomization)
   stream = torch.cuda.current_stream(m.device).cuda_stream
@@ -250,7 +260,7 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
       raise ValueError(f'act batch {act.shape[0]} != state batch {n}')
     act_p = act.data_ptr()
   if out is None:
-    out = _alloc(m, n, full, m.device)
+    out = _alloc(m, n, full, m.device, state.cache is not None)
   cin = _cstate(state)
   cout = _cstate(out)
   dr, _keep = _randomization(m, n, randomization)
@@ -273,7 +283,7 @@ def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = N
   if act_seq.dim() != 3 or act_seq.shape[1] != n or act_seq.shape[2] != m.nu:
     raise ValueError(f'act_seq must be (n_steps, {n}, {m.nu})')
   n_steps = act_seq.shape[0]
-  out = _alloc(m, n, False, m.device)
+  out = _alloc(m, n, False, m.device, state.cache is not None)
   tq = tqd = None
   if trajectory:
     tq = torch.empty(n_steps, n, m.nq, dtype=torch.float32, device=m.device)

@@ -85,6 +85,17 @@ typedef struct {
   float* con_diag;      /* [n, m] */
   float* con_aref;      /* [n, m] */
   int32_t* status;      /* [n] braxg_env_flags */
+  /* Optional [n, braxg_model_cache_words] cache (16-byte aligned) of every
+   * position-level term of the state (the lagged terms the reference State
+   * carries, brax/generalized/pipeline.py:79-92), written by the call that
+   * produces the state.  A call whose input state carries it skips
+   * recomputing those terms for every env whose q, qd (Newton-Schulz mode:
+   * and mass_mx_inv) and per-env parameters equal the cached ones bit for bit
+   * and whose cache was computed with the same threads_per_env (exact-inverse
+   * mode: and an exact mass_mx_inv); other envs recompute them, so the result
+   * is the same either way.  The cache belongs to the model that wrote it.
+   * The braxg_batch_* calls neither read nor write it. */
+  float* cache;
 } braxg_state;
 
 /* Per-stage profile slots of braxg_options.stage_cycles (sums over envs of
@@ -138,6 +149,8 @@ typedef struct {
 int braxg_model_create(const void* desc, size_t desc_bytes, int device, braxg_model** out);
 int braxg_model_destroy(braxg_model* model);
 int braxg_model_dims(const braxg_model* model, braxg_dims* out);
+/* Floats per env of braxg_state.cache for this model. */
+int braxg_model_cache_words(const braxg_model* model, int32_t* words);
 
 /* brax/generalized/pipeline.py:32-61.  Reads q [n, nq], qd [n, nv]; writes the
  * State fields of `out` (mass_mx_inv is the exact SPD inverse, the forces are
