@@ -79,6 +79,26 @@ __device__ __forceinline__ void copy_arena(const Team<T>& tm, float* dst, const 
   for (int i = tm.lane; i < words / 4; i += T) d[i] = s[i];
 }
 
+// Copies the words of an arena that hold position-level terms: everything
+// before the scratch region, the mass matrix (in scratch unless the
+// integrator owns it) and the active overflow Jacobian rows at the scratch
+// end.  The active row count is read from `arena` (the destination on a
+// restore, the source on a store) once the part before scratch is there, and
+// clamped to the model's row count.
+template <int T>
+__device__ __forceinline__ void copy_position_terms(const Team<T>& tm, float* dst, const float* src, const Layout& L,
+                                                    int nv, int m, const float* arena) {
+  copy_arena<T>(tm, dst, src, L.scr);
+  tm.sync();
+  const int nrow = min(max(reinterpret_cast<const int*>(arena + L.misc)[0], 0), m);
+  if (L.M >= L.scr) copy_arena<T>(tm, dst + L.M, src + L.M, al4(nv * L.ldm));
+  const int novf = nrow - L.jcap;
+  if (novf > 0) {
+    const int o0 = L.jovf & ~3, o1 = al4(L.jovf + novf * L.ldj);
+    copy_arena<T>(tm, dst + o0, src + o0, o1 - o0);
+  }
+}
+
 // Tag of a cached arena (misc[11]): the team width that computed it (lane
 // reductions make the terms depend on it bit for bit) and whether its
 // mass_mx_inv is the exact inverse of its mass matrix.  An env whose launch
@@ -93,7 +113,8 @@ template <int T>
 __device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, const int* mw, Ws w, long long env,
                                            bool exact) {
   const Team<T> tm;
-  copy_arena<T>(tm, w.b, a.cache_in + (B.env + env) * w.L->total, w.L->total);
+  const Model md(mw);
+  copy_position_terms<T>(tm, w.b, a.cache_in + (B.env + env) * w.L->total, *w.L, md.nv, md.m, w.b);
   tm.sync();
   const int tag = reinterpret_cast<const int*>(w.at(w.L->misc))[11];
   const bool tag_ok = exact ? tag == cache_tag<T>(true) : (tag >> 1) == T;
@@ -102,13 +123,14 @@ __device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, 
 
 // Stores the env's arena (the output state's position terms) into its cache.
 template <int T>
-__device__ __noinline__ void store_cache(const StepArgs& a, const EnvBase& B, Ws w, long long env, bool exact,
-                                        bool ok) {
+__device__ __noinline__ void store_cache(const StepArgs& a, const EnvBase& B, const int* mw, Ws w, long long env,
+                                        bool exact, bool ok) {
   const Team<T> tm;
+  const Model md(mw);
   tm.sync();
   if (tm.lane == 0) reinterpret_cast<int*>(w.at(w.L->misc))[11] = ok ? cache_tag<T>(exact) : 0;
   tm.sync();
-  copy_arena<T>(tm, a.out.cache + (B.env + env) * w.L->total, w.b, w.L->total);
+  copy_position_terms<T>(tm, a.out.cache + (B.env + env) * w.L->total, w.b, *w.L, md.nv, md.m, w.b);
 }
 
 // Per-stage cycle accumulation (only when a profile buffer is passed): lane 0
@@ -393,10 +415,9 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   }
   tm.sync();
   pf.mark(BRAXG_PROF_IO);
-  // position terms of the input state (CTA-uniform: skipped when every env of
-  // the CTA restored them from the cache)
-  bool ok = true;
-  if (__syncthreads_or(active && !cached)) ok = position_stage<T, NVB>(smem, w, active && !cached, exact, 0, pf);
+  // position terms of the input state (envs that restored them from the
+  // cache only take the stage's CTA barriers)
+  bool ok = position_stage<T, NVB>(smem, w, active && !cached, exact, 0, pf);
   const long long ei = B.env + env;
   if (a.init) {
     for (int d = tm.lane; active && d < nv; d += T) {
@@ -446,7 +467,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
     }
   }
   if (!active) return;  // no CTA barrier follows
-  if (a.out.cache != nullptr) store_cache<T>(a, B, w, env, exact, ok);  // before the outputs touch scratch
+  if (a.out.cache != nullptr) store_cache<T>(a, B, smem, w, env, exact, ok);  // before the outputs touch scratch
   if (TASK && a.n_steps > 0 && !a.init) task_outputs<T>(a, smem, w, ei);
   write_outputs<T>(a, B, smem, w, env, ok);
   pf.mark(BRAXG_PROF_IO);
