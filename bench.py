@@ -380,6 +380,10 @@ def run_braxg(args):
   # ---- roofline -----------------------------------------------------------
   nmv = load_nmv()[WORKLOAD]
   f_step, b_step = algorithmic(sys_, nmv['mean_matvecs_per_step'], args.inverse == 'newton_schulz')
+  # the state cache: its position-term spans read at the launch start and
+  # written at its end (active constraint rows past the first 32 not counted)
+  b_cache = 2 * 4 * model.cache_span[0] if args.state_cache else 0
+  b_launch = (b_step + b_cache) * n
   launch_s = t_total / args.steps
   flops_launch = f_step * N_FRAMES * n
   achieved = flops_launch / launch_s / 1e12
@@ -400,9 +404,10 @@ def run_braxg(args):
       'peak_source': (f'nominal FP32 CUDA-core peak ({props.multi_processor_count} SMs x 128 '
                       f'FMA/clk x 2 x {sm_max:.0f} MHz); MEASURED_PEAKS.json has no FP32 figure'),
       'flops_per_launch': flops_launch,
-      'hbm': {'achieved_gbs': round(b_step * n / launch_s / 1e9, 2), 'peak_gbs': hbm_peak,
-              'frac': round(b_step * n / launch_s / 1e9 / hbm_peak, 5),
-              'bytes_per_launch': b_step * n, 'peak_source': 'MEASURED_PEAKS.json hbm_gbs (of measured)'},
+      'hbm': {'achieved_gbs': round(b_launch / launch_s / 1e9, 2), 'peak_gbs': hbm_peak,
+              'frac': round(b_launch / launch_s / 1e9 / hbm_peak, 5),
+              'bytes_per_launch': b_launch, 'state_bytes_per_env': b_step, 'cache_bytes_per_env': b_cache,
+              'peak_source': 'MEASURED_PEAKS.json hbm_gbs (of measured)'},
   }
   clocks = clk.summary()
   adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank)

@@ -18,7 +18,7 @@ STATE_FIELDS = (
     'qf_constraint', 'qdd', 'root_com', 'cinr_pos', 'cinr_rot', 'cinr_i', 'cd',
     'cdof', 'cdofd', 'mass_mx', 'con_jac', 'con_diag', 'con_aref', 'status', 'cache')
 
-EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims', 'braxg_model_cache_words',
+EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims', 'braxg_model_cache_words', 'braxg_model_cache_span',
            'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_rollout_vjp_workspace',
            'braxg_rollout_vjp_workspace_resident',
            'braxg_rollout_vjp', 'braxg_rollout_vjp_noalloc',
@@ -113,6 +113,7 @@ def lib() -> ctypes.CDLL:
     l.braxg_model_destroy.argtypes = [vp]
     l.braxg_model_dims.argtypes = [vp, P(Dims)]
     l.braxg_model_cache_words.argtypes = [vp, P(ctypes.c_int32)]
+    l.braxg_model_cache_span.argtypes = [vp, P(ctypes.c_int32), P(ctypes.c_int32), P(ctypes.c_int32)]
     l.braxg_init.argtypes = [vp, vp, i32, vp, vp, P(State), P(Options)]
     l.braxg_step.argtypes = [vp, vp, i32, i32, vp, P(State), P(State), P(Options)]
     l.braxg_rollout.argtypes = [vp, vp, i32, i32, i32, vp, P(State), P(State), vp, vp,

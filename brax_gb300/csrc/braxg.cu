@@ -197,6 +197,16 @@ int braxg_model_cache_words(const braxg_model* m, int32_t* words) {
   return BRAXG_OK;
 }
 
+int braxg_model_cache_span(const braxg_model* m, int32_t* fixed_words, int32_t* row_words, int32_t* rows_in_fixed) {
+  if (m == nullptr || fixed_words == nullptr || row_words == nullptr || rows_in_fixed == nullptr)
+    return fail(BRAXG_ERR_INVALID, "NULL argument");
+  const braxg::Layout& L = m->L;  // the spans copy_position_terms copies
+  *fixed_words = L.scr + (L.M >= L.scr ? braxg::al4(m->dims.nv * L.ldm) : 0);
+  *row_words = L.ldj;
+  *rows_in_fixed = L.jcap;
+  return BRAXG_OK;
+}
+
 int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int32_t* tpe, int32_t* epc, int32_t* smem) {
   if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model is NULL");
   Shape s;

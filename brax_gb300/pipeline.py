@@ -49,6 +49,11 @@ class Model:
     w = ctypes.c_int32()
     N.check(lib.braxg_model_cache_words(h, ctypes.byref(w)), 'braxg_model_cache_words')
     self.cache_words = w.value
+    fw, rw, rf = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    N.check(lib.braxg_model_cache_span(h, ctypes.byref(fw), ctypes.byref(rw), ctypes.byref(rf)),
+            'braxg_model_cache_span')
+    # floats per env a call copies each way: fixed + row_words per active row past rows_in_fixed
+    self.cache_span = (fw.value, rw.value, rf.value)
 
   @property
   def handle(self):

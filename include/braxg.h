@@ -152,6 +152,12 @@ int braxg_model_dims(const braxg_model* model, braxg_dims* out);
 /* Floats per env of braxg_state.cache for this model. */
 int braxg_model_cache_words(const braxg_model* model, int32_t* words);
 
+/* Floats per env that a call actually reads from and writes to the caches:
+ * `fixed_words`, plus `row_words` for every active constraint row beyond the
+ * first `rows_in_fixed`. */
+int braxg_model_cache_span(const braxg_model* model, int32_t* fixed_words, int32_t* row_words,
+                           int32_t* rows_in_fixed);
+
 /* brax/generalized/pipeline.py:32-61.  Reads q [n, nq], qd [n, nv]; writes the
  * State fields of `out` (mass_mx_inv is the exact SPD inverse, the forces are
  * zero). */
