@@ -151,12 +151,17 @@ class ClockSampler:
     try:
       self.proc = subprocess.Popen(
           ['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.Q}',
-           '--format=csv,noheader,nounits', '-lms', '200'],
+           '--format=csv,noheader,nounits', '-lms', '50'],
           stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
       self.t = threading.Thread(target=self._read, daemon=True)
       self.t.start()
+      # the timed region starts once the sampler is producing samples
+      deadline = time.perf_counter() + 5.0
+      while not self.lines and time.perf_counter() < deadline and self.proc.poll() is None:
+        time.sleep(0.01)
     except (OSError, FileNotFoundError):
       self.proc = None
+    self.first = len(self.lines)
     return self
 
   def _read(self):
@@ -175,7 +180,9 @@ class ClockSampler:
   def summary(self):
     sm, mx, reasons = [], None, set()
     names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
-    for line in self.lines:
+    # samples taken during the timed region (the last earlier one if none)
+    lines = self.lines[self.first:] or self.lines[-1:]
+    for line in lines:
       f = [x.strip() for x in line.split(',')]
       if len(f) < 9:
         continue
@@ -198,36 +205,75 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 
 
-def _cpu_worker(args):
-  name, n, steps, seed = args
+_CPU = {}
+
+
+def _cpu_init(name, n, seed_base):
+  """Pool initialiser: one oracle and one batch of envs per worker process."""
   os.environ.setdefault('OMP_NUM_THREADS', '1')
   from brax_gb300 import mjcf
   from oracle.pipeline import Oracle
   sys_ = mjcf.load_asset(name)
   o = Oracle(sys_, np.float32)
-  rng = np.random.default_rng(seed)
+  rng = np.random.default_rng(seed_base + os.getpid())
   q = (sys_.init_q + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))).astype(np.float32)
   qd = (0.1 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32)
-  s = o.init(q, qd)
-  t0 = time.perf_counter()
-  for _ in range(steps):
-    s = o.env_step(s, rng.uniform(-1, 1, (n, sys_.act_size())).astype(np.float32), N_FRAMES)
-  return time.perf_counter() - t0, n * steps
+  _CPU.update(sys=sys_, o=o, rng=rng, s=o.init(q, qd), n=n)
 
 
-def cpu_baseline(sample_envs: int, steps: int = 2):
-  cores = os.cpu_count() or 1
-  ctx = mp.get_context('spawn')
+def _cpu_step(_):
+  """One env step (N_FRAMES pipeline steps) of this worker's envs."""
+  c = _CPU
   t0 = time.perf_counter()
-  with ctx.Pool(cores) as pool:
-    res = pool.map(_cpu_worker, [(WORKLOAD, sample_envs, steps, 100 + i) for i in range(cores)])
-  wall = time.perf_counter() - t0
-  busy = max(r[0] for r in res)
-  total = sum(r[1] for r in res)
-  return {'value': total / busy, 'unit': 'env-steps/s', 'cores': cores, 'kind': 'port',
-          'sample': f'{cores} processes x {sample_envs} envs x {steps} env steps '
-                    f'({N_FRAMES} frames each), numpy FP32 restatement of the reference path; '
-                    f'slowest process {busy:.1f} s, pool wall {wall:.1f} s'}
+  c['s'] = c['o'].env_step(c['s'], c['rng'].uniform(-1, 1, (c['n'], c['sys'].act_size())).astype(np.float32),
+                           N_FRAMES)
+  return time.perf_counter() - t0, c['n']
+
+
+class CpuReference:
+  """The numpy FP32 restatement of the reference path (oracle/) on every
+  host core: one spawn-started worker process per core, each stepping its own
+  batch of `sample_envs` envs.  A step is one env step of every worker's
+  batch; its time is the wall time of that pool round."""
+
+  def __init__(self, sample_envs: int):
+    self.cores = os.cpu_count() or 1
+    self.sample_envs = sample_envs
+    self.pool = mp.get_context('spawn').Pool(self.cores, _cpu_init, (WORKLOAD, sample_envs, 100))
+
+  def step(self):
+    t0 = time.perf_counter()
+    res = self.pool.map(_cpu_step, range(self.cores), chunksize=1)
+    return time.perf_counter() - t0, sum(r[1] for r in res)
+
+  def run(self, steps: int, warmup: int):
+    for _ in range(warmup):
+      self.step()
+    wall, units = [], 0
+    for _ in range(steps):
+      t, u = self.step()
+      wall.append(t)
+      units += u
+    return units / sum(wall), wall
+
+  def describe(self, steps: int, wall) -> str:
+    return (f'{self.cores} processes x {self.sample_envs} envs, {steps} timed env steps '
+            f'({N_FRAMES} frames each), numpy FP32 restatement of the reference path; '
+            f'{sum(wall):.1f} s wall, about {self.cores * sum(wall):.0f} core-seconds')
+
+  def close(self):
+    self.pool.terminate()
+    self.pool.join()
+
+
+def cpu_baseline(sample_envs: int, steps: int = 8, warmup: int = 1):
+  ref = CpuReference(sample_envs)
+  try:
+    value, wall = ref.run(steps, warmup)
+  finally:
+    ref.close()
+  return {'value': value, 'unit': 'env-steps/s', 'cores': ref.cores, 'kind': 'port',
+          'sample': ref.describe(steps, wall)}
 
 
 # ---------------------------------------------------------------------------
@@ -595,17 +641,17 @@ def run_reference(args):
   world = int(os.environ.get('WORLD_SIZE', '1'))
   if rank != 0:
     return
-  vals = []
-  cb = None
-  for _ in range(max(1, min(args.steps, 3))):
-    cb = cpu_baseline(args.cpu_sample_envs, steps=1)
-    vals.append(cb['value'])
-  value = statistics.median(vals)
-  cb['value'] = value
+  ref = CpuReference(args.cpu_sample_envs)
+  try:
+    value, wall = ref.run(args.steps, args.warmup)
+  finally:
+    ref.close()
+  cb = {'value': value, 'unit': 'env-steps/s', 'cores': ref.cores, 'kind': 'port',
+        'sample': ref.describe(args.steps, wall)}
   out = {
       'metric': METRIC, 'value': round(value, 2), 'unit': 'env-steps/s', 'n_gpus': world,
-      'steps': len(vals), 'warmup': 0, 'ms_per_step': None, 'higher_is_better': True,
-      'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+      'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(1e3 * sum(wall) / len(wall), 3),
+      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
       'impl': 'reference',
       'config': {**workload_config(args.envs, world), 'inverse_mode': 'newton_schulz (the reference algorithm)',
                  'sample': cb['sample']},
@@ -613,7 +659,8 @@ def run_reference(args):
       'e2e': {'value': round(value, 2), 'unit': 'env-steps/s', 'h2d_bytes_per_step': 0,
               'd2h_bytes_per_step': 0},
       'note': ('the reference is pure Python/JAX and jax/jaxlib/mujoco are not installable here; '
-               'this arm times the numpy restatement of the same path (oracle/), kind "port"'),
+               'this arm times the numpy restatement of the same path (oracle/), kind "port"; '
+               'a step is one env step of cores x cpu_sample_envs envs'),
   }
   print(json.dumps(out))
 
