@@ -225,21 +225,36 @@ def _parse_body(elem: ElementTree.Element, ctx: _Ctx, cls: str) -> _Elem:
   return _Elem('body', attrib, children)
 
 
+def _fuse_frame(attrib: Dict[str, str], ctx: _Ctx):
+  """An element's frame as body fusing reads it: a `quat` attribute as
+  written (not normalised: rotating by it scales by its squared norm, as the
+  reference's fusing does), other orientation forms as unit quaternions."""
+  if 'quat' in attrib:
+    return _vec(attrib.get('pos'), 3, [0, 0, 0]), _vec(attrib['quat'])
+  return _frame(attrib, ctx)
+
+
+def _fmt(v) -> str:
+  """The fused attributes are written with 6 decimals, as the reference's
+  fusing writes them ('%f')."""
+  return ' '.join('%f' % float(x) for x in v)
+
+
 def _offset(e: _Elem, ppos, pquat, ctx: _Ctx):
   """Moves an element into its grandparent's frame (brax/io/mjcf.py:47-73)."""
   if 'fromto' in e.attrib:
     ft = _vec(e.attrib['fromto'])
     a = ppos + _qrot(ft[0:3], pquat)
     b = ppos + _qrot(ft[3:6], pquat)
-    e.attrib['fromto'] = ' '.join(repr(float(v)) for v in np.concatenate([a, b]))
+    e.attrib['fromto'] = _fmt(np.concatenate([a, b]))
     return
-  pos, quat = _frame(e.attrib, ctx)
+  pos, quat = _fuse_frame(e.attrib, ctx)
   pos = ppos + _qrot(pos, pquat)
   quat = _qmul(pquat, quat)
   for k in ('euler', 'axisangle', 'zaxis'):
     e.attrib.pop(k, None)
-  e.attrib['pos'] = ' '.join(repr(float(v)) for v in pos)
-  e.attrib['quat'] = ' '.join(repr(float(v)) for v in quat)
+  e.attrib['pos'] = _fmt(pos)
+  e.attrib['quat'] = _fmt(quat)
 
 
 def _fuse(elem: _Elem, ctx: _Ctx):
@@ -250,7 +265,7 @@ def _fuse(elem: _Elem, ctx: _Ctx):
       continue
     if any(c.tag in ('joint', 'freejoint') for c in child.children):
       continue
-    cpos, cquat = _frame(child.attrib, ctx)
+    cpos, cquat = _fuse_frame(child.attrib, ctx)
     for gc in child.children:
       if gc.tag in ('body', 'geom', 'site') and (cpos != 0).any():
         _offset(gc, cpos, cquat, ctx)
@@ -363,7 +378,7 @@ def _flatten(world: _Elem, ctx: _Ctx) -> List[_Body]:
           joints.append(j.attrib)
       inertial = next((j.attrib for j in c.children if j.tag == 'inertial'), None)
       idx = len(bodies)
-      bodies.append(_Body(c.attrib.get('name', f'body{idx}'), parent, pos, quat,
+      bodies.append(_Body(c.attrib.get('name', ''), parent, pos, quat,
                           joints, [g.attrib for g in c.children if g.tag == 'geom'],
                           inertial))
       walk(c, idx)
@@ -510,6 +525,11 @@ def loads(xml: str, name: str = '') -> S.System:
 
   # --- joints -> link types, dofs -----------------------------------------
   link_types, jnts = '', []
+  # qpos0 of the non-free joints (brax/io/mjcf.py:266-271 checks it before
+  # the joint stacks)
+  if any(j.get('type', 'hinge') != 'free' and float(j.get('ref', 0.0)) != 0.0
+         for b in bodies[1:] for j in b.joints):
+    raise NotImplementedError('The `ref` attribute on joint types is not supported.')
   for bi, b in enumerate(bodies[1:], start=1):
     types = [j.get('type', 'hinge') for j in b.joints]
     if not types:
@@ -582,8 +602,6 @@ def loads(xml: str, name: str = '') -> S.System:
       motions_vel.append(axis[None])
     else:
       raise RuntimeError(f'invalid joint type: {typ}')
-    if float(j.get('ref', 0.0)) != 0.0:
-      raise NotImplementedError('The `ref` attribute on joint types is not supported.')
     any_limited |= limited
     armature.append(arm)
     stiffness.append(stiff)
@@ -625,6 +643,8 @@ def loads(xml: str, name: str = '') -> S.System:
   g_fric, g_sr, g_si, g_ct, g_ca, g_names, g_rgba = [], [], [], [], [], [], []
   for bi, b in enumerate(bodies):
     for g in b.geoms:
+      if g.get('fluidshape', 'none') == 'ellipsoid':  # geom_fluid != 0, brax/io/mjcf.py:242-243
+        raise NotImplementedError('Ellipsoid fluid model not implemented.')
       gt = _GEOM_TYPES[g.get('type', 'sphere')]
       if gt in (S.GEOM_HFIELD, S.GEOM_MESH, S.GEOM_ELLIPSOID):
         if int(g.get('contype', 1)) | int(g.get('conaffinity', 1)):
@@ -725,7 +745,7 @@ def loads(xml: str, name: str = '') -> S.System:
   excludes = set()
   con = root.find('contact')
   if con is not None:
-    names = {b.name: i for i, b in enumerate(bodies)}
+    names = {b.name: i for i, b in enumerate(bodies) if b.name}
     for ex in con.findall('exclude'):
       b1, b2 = names[ex.attrib['body1']], names[ex.attrib['body2']]
       excludes.add((min(b1, b2), max(b1, b2)))
