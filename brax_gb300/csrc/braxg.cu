@@ -146,7 +146,7 @@ int braxg_model_create(const void* desc, size_t desc_bytes, int device, braxg_mo
     return fail(BRAXG_ERR_INVALID, "bad descriptor magic/version");
   int words = w[BXM_H_WORDS];
   if ((size_t)words * 4 != desc_bytes) return fail(BRAXG_ERR_INVALID, "descriptor length mismatch");
-  for (int k = BXM_O_LINK_PARENT; k <= BXM_O_CON_SOLP; ++k)
+  for (int k = BXM_O_LINK_PARENT; k <= BXM_O_LI_BOX; ++k)
     if (w[k] < BXM_HEADER_WORDS || w[k] > words) return fail(BRAXG_ERR_INVALID, "descriptor offset %d out of range", k);
   braxg_dims d{w[BXM_H_NL], w[BXM_H_NQ], w[BXM_H_NV], w[BXM_H_NU], w[BXM_H_NCON], w[BXM_H_NLIM], w[BXM_H_M]};
   if (d.nl < 1 || d.nv < 1 || d.nv > 64 || d.nq < 1 || d.nu < 0 || d.ncon < 0 || d.nlim < 0 || d.nl > 64)

@@ -78,6 +78,7 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
   if (workspace == nullptr || workspace_bytes < need)
     return fail(BRAXG_ERR_INVALID, "workspace of %zu bytes required (got %zu)", need, workspace_bytes);
   if (m->dims.nv > 32) return fail(BRAXG_ERR_UNSUPPORTED, "gradients support nv <= 32");
+  if (m->h[BXM_H_FLUID]) return fail(BRAXG_ERR_UNSUPPORTED, "gradients do not cover fluid forces");
   for (int k = 0; k < m->dims.ncon; ++k) {
     int kind = m->h[m->h[BXM_O_CON_KIND] + k], la = m->h[m->h[BXM_O_CON_LA] + k];
     if ((kind != BXM_CON_PLANE_SPHERE && kind != BXM_CON_PLANE_CAPSULE) || la >= 0)

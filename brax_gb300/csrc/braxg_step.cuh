@@ -12,8 +12,8 @@ namespace braxg {
 // ---------------------------------------------------------------------------
 struct Model {
   const int* w;
-  int nl, nq, nv, nu, ncon, nlim, m, nlevel, ns_iters, pg_iters, pg_maxls;
-  float dt, pg_tol;
+  int nl, nq, nv, nu, ncon, nlim, m, nlevel, ns_iters, pg_iters, pg_maxls, fluid;
+  float dt, pg_tol, visc, dens;
   f3 g;
   __device__ explicit Model(const int* w_) : w(w_) {
     nl = w[BXM_H_NL];
@@ -29,6 +29,9 @@ struct Model {
     pg_maxls = w[BXM_H_PG_MAXLS];
     dt = __int_as_float(w[BXM_H_DT]);
     pg_tol = __int_as_float(w[BXM_H_PG_TOL]);
+    fluid = w[BXM_H_FLUID];
+    visc = __int_as_float(w[BXM_H_VISC]);
+    dens = __int_as_float(w[BXM_H_DENS]);
     g = mk3(__int_as_float(w[BXM_H_GX]), __int_as_float(w[BXM_H_GY]), __int_as_float(w[BXM_H_GZ]));
   }
   __device__ __forceinline__ const int* I(int k) const { return w + w[k]; }
@@ -69,7 +72,8 @@ constexpr int kMaxExplicitRows = 32;
 // sit at the end of the scratch region, which that path leaves free.  The mass
 // matrix lives in scratch too (from CRBA to the inverse, and to the outputs),
 // except for models whose integrator solves with M itself (ns_iters == 0).
-__host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim, int ns_iters) {
+__host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim, int ns_iters,
+                                              int fluid = 0) {
   Layout L;
   const int m = 4 * ncon + nlim;
   L.ldm = nv | 1;  // odd leading dimension: conflict-free strided lane access
@@ -117,7 +121,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   // tried: after the inverse temporaries, or before them.
   const int head = imax(imax(13 * nl + 6 * nv, 14 * ncon + 16), m + 4);  // CRBA, contacts, output row map
   int common = 14 * nl;                                     // FK / com temporaries
-  common = imax(common, 12 * nl + nu + ovf);                // RNE
+  common = imax(common, (fluid ? 21 : 12) * nl + al4(nu) + ovf);  // RNE (+ fluid forces)
   common = imax(common, 14 * ncon + 16 + ovf);              // contacts + Jacobian rows
   common = imax(common, 8 * al4(m) + 2 * al4(nv) + 16 + ovf);  // projected gradient (implicit A)
   {
@@ -154,7 +158,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
 // Layout of a packed model descriptor (header words).
 __host__ __device__ inline Layout layout_of(const int* w) {
   return make_layout(w[BXM_H_NL], w[BXM_H_NQ], w[BXM_H_NV], w[BXM_H_NU], w[BXM_H_NCON], w[BXM_H_NLIM],
-                     w[BXM_H_NS_ITERS]);
+                     w[BXM_H_NS_ITERS], w[BXM_H_FLUID]);
 }
 static_assert(sizeof(Layout) <= kLayoutWords * 4, "Layout must fit its shared slot");
 
@@ -1234,6 +1238,46 @@ __device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
     }
     tm.sync();
   }
+  // fluid forces (dynamics.py:198-211 with fluid.py:53-82): per link, the
+  // inertia-box drag of its com point's velocity in the inertia frame,
+  // rotated back to world, stored with the point's offset from the tree's com
+  float* ff = force + al4(md.nu);  // [nl][9]: force ang, force vel, offset
+  if (md.fluid) {
+    const float* xp = w.at(L.xp);
+    const float* xr = w.at(L.xr);
+    const float* rc = w.at(L.rc);
+    const float* lip = md.F(BXM_O_LI_POS);
+    const float* lir = md.F(BXM_O_LI_ROT);
+    const float* box = md.F(BXM_O_LI_BOX);
+    for (int l = tm.lane; l < nl; l += T) {
+      f3 ip;
+      q4 ir;
+      tf_do(ld3(xp + 3 * l), ld4(xr + 4 * l), ld3(lip + 3 * l), ld4(lir + 4 * l), ip, ir);
+      const f3 off = ip - ld3(rc + 3 * l);
+      const q4 rt = q4{ir.w, -ir.x, -ir.y, -ir.z};  // quat_inv
+      const f3 ca = ld3(cd + 6 * l), cv = ld3(cd + 6 * l + 3);
+      const f3 wa = rotate(ca, rt);
+      const f3 wv = rotate(cv - cross3(off, ca), rt);
+      const f3 b = ld3(box + 3 * l);
+      const float diam = (b.x + b.y + b.z) / 3.f;
+      const float ang_scale = -kPi * (diam * diam * diam) * md.visc;  // fluid.py:26-34
+      const float vel_scale = -3.f * kPi * diam * md.visc;
+      f3 fa = ang_scale * wa, fv = vel_scale * wv;
+      const float dv = -0.5f * md.dens;  // fluid.py:37-50
+      fv = fv + mk3(dv * (b.y * b.z) * fabsf(wv.x) * wv.x, dv * (b.x * b.z) * fabsf(wv.y) * wv.y,
+                    dv * (b.x * b.y) * fabsf(wv.z) * wv.z);
+      const float b4x = (b.x * b.x) * (b.x * b.x), b4y = (b.y * b.y) * (b.y * b.y),
+                  b4z = (b.z * b.z) * (b.z * b.z);
+      const float da = -1.f * md.dens;
+      fa = fa + mk3(da * (b.x * (b4y + b4z)) * fabsf(wa.x) * wa.x / 64.f,
+                    da * (b.y * (b4x + b4z)) * fabsf(wa.y) * wa.y / 64.f,
+                    da * (b.z * (b4x + b4y)) * fabsf(wa.z) * wa.z / 64.f);
+      st3(ff + 9 * l, rotate(fa, ir));  // fluid.py:80
+      st3(ff + 9 * l + 3, rotate(fv, ir));
+      st3(ff + 9 * l + 6, off);
+    }
+    tm.sync();
+  }
   // qf_smooth = passive - bias + tau: dynamics.py:182, 190-196, 232-234
   const int* dlink = md.I(BXM_O_DOF_LINK);
   const float* cdof = w.at(L.cdof);
@@ -1247,6 +1291,16 @@ __device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
     float pas = 0.f;
     if (ltype[l] != 0) pas = -q[qadr[l] + (d - dadr[l])] * stiff[d];
     pas = pas - damp[d] * qd[d];
+    if (md.fluid) {  // sum over links of point_jacobian(x_i.pos) . force (dynamics.py:206-211)
+      const f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
+      float fl = 0.f;
+      for (int k = 0; k < nl; ++k) {
+        if (!((md.anc(k) >> d) & 1ull)) continue;  // dof d does not move link k
+        const f3 jv = cv - cross3(ld3(ff + 9 * k + 6), ca);
+        fl = fl + (dot3(jv, ld3(ff + 9 * k + 3)) + dot3(ca, ld3(ff + 9 * k)));
+      }
+      pas = pas + fl;
+    }
     float tau = 0.f;
     if (has_act)
       for (int a = 0; a < md.nu; ++a)

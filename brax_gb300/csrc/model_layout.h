@@ -29,6 +29,9 @@ enum BxmHeader {
   BXM_H_GY,
   BXM_H_GZ,
   BXM_H_PG_TOL,       // float (jaxopt default 1e-3)
+  BXM_H_FLUID,        // 1 when viscosity or density is nonzero (System.enable_fluid)
+  BXM_H_VISC,         // float fluid viscosity
+  BXM_H_DENS,         // float fluid density
   // int arrays
   BXM_O_LINK_PARENT,  // [nl]
   BXM_O_LINK_TYPE,    // [nl] 0 = free, 1/2/3 = stacked hinge/slide dofs
@@ -84,6 +87,7 @@ enum BxmHeader {
   BXM_O_CON_FRIC,     // [ncon] sliding friction
   BXM_O_CON_INVW,     // [ncon] invweight[la]*(la>-1) + invweight[lb]
   BXM_O_CON_SOLP,     // [ncon*7] solref + solimp
+  BXM_O_LI_BOX,       // [nl*3] inertia-equivalent box of each link (brax/fluid.py:71-76)
   BXM_HEADER_WORDS = 128
 };
 

@@ -125,6 +125,7 @@ def pack(sys: S.System) -> np.ndarray:
       'BXM_O_CON_INVW': con_invw,
       'BXM_O_CON_SOLP': (np.concatenate([cs.solref, cs.solimp], axis=1)
                          if ncon else np.zeros((0, 7))),
+      'BXM_O_LI_BOX': fluid_box(sys),
   }
   words = [np.zeros(H['BXM_HEADER_WORDS'], np.int32)]
   off = H['BXM_HEADER_WORDS']
@@ -158,6 +159,17 @@ def pack(sys: S.System) -> np.ndarray:
   hdr[H['BXM_H_DT']] = f32(sys.dt)
   hdr[H['BXM_H_GX']], hdr[H['BXM_H_GY']], hdr[H['BXM_H_GZ']] = (f32(g) for g in sys.gravity)
   hdr[H['BXM_H_PG_TOL']] = f32(1e-3)
-  if sys.enable_fluid:
-    raise NotImplementedError('fluid forces (brax/fluid.py) are not supported')
+  hdr[H['BXM_H_FLUID']] = int(sys.enable_fluid)
+  hdr[H['BXM_H_VISC']] = f32(sys.viscosity)
+  hdr[H['BXM_H_DENS']] = f32(sys.density)
   return np.concatenate(words)
+
+
+def fluid_box(sys: S.System) -> np.ndarray:
+  """[nl, 3] edge lengths of the box with each link's mass and principal
+  moments (brax/fluid.py:71-76): sqrt(6 (tr(I) - 2 I_kk) / m), floored at
+  1e-12 before the square root."""
+  i = np.asarray(sys.link.inertia.i, np.float64).reshape(-1, 3, 3)
+  d = np.diagonal(i, axis1=-2, axis2=-1)
+  v = 6.0 * np.maximum(d.sum(-1, keepdims=True) - 2.0 * d, 1e-12)
+  return np.sqrt(v / np.asarray(sys.link.inertia.mass, np.float64)[:, None])

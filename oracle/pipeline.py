@@ -243,7 +243,8 @@ class Oracle:
         c_solimp=f(sys.contacts.solimp),
         a_cr=f(sys.actuator.ctrl_range), a_fr=f(sys.actuator.force_range),
         a_gain=f(sys.actuator.gain), a_gear=f(sys.actuator.gear),
-        a_bq=f(sys.actuator.bias_q), a_bqd=f(sys.actuator.bias_qd))
+        a_bq=f(sys.actuator.bias_q), a_bqd=f(sys.actuator.bias_qd),
+        viscosity=self.dt_.type(sys.viscosity), density=self.dt_.type(sys.density))
     self.matvecs = 0
 
   # -------------------------------------------------------------------------
@@ -797,9 +798,37 @@ class Oracle:
         d = st.dadr[i] + k
         frc[:, d] = -s.q[:, st.qadr[i] + k] * c['stiffness'][d]
     frc = frc - c['damping'] * s.qd
-    if self.sys.enable_fluid:
-      raise NotImplementedError('fluid forces (brax/fluid.py) are not restated')
+    if self.sys.enable_fluid:  # :198-211
+      fa, fv, xi_p = self.fluid_force(s)
+      for i in range(st.nl):
+        ja, jv = self.point_jacobian(s, xi_p[:, i], i)
+        frc = frc + (dot(jv, fv[:, None, i]) + dot(ja, fa[:, None, i]))
     return frc
+
+  def fluid_force(self, s: State):
+    """fluid.force, brax/fluid.py:53-82: (force ang, force vel) per link in
+    world orientation, and the links' com positions x_i.pos."""
+    c, dt = self.c, self.dt_
+    xi_p, xi_r = tf_do_tf(s.x_pos, s.x_rot, c['li_pos'], c['li_rot'])  # :64
+    off = xi_p - s.root_com  # :66
+    rt = quat_inv(xi_r)  # :67, Transform.do(Motion), base.py:573-578
+    wa = rotate(s.cd_ang, rt)
+    wv = rotate(s.cd_vel - cross(off, s.cd_ang), rt)
+    diag = np.diagonal(c['li_i'], axis1=-2, axis2=-1)  # :71-76
+    sign = np.ones((3, 3), dt) - 2 * np.eye(3, dtype=dt)
+    box = np.sum(diag[:, None, :] * sign, axis=-1)
+    box = dt.type(6.0) * np.maximum(box, dt.type(1e-12))
+    box = np.sqrt(box / c['li_mass'][:, None])
+    pi = dt.type(np.pi)
+    diam = np.mean(box, axis=-1)  # _box_viscosity, :24-33
+    fa = (-pi * diam ** 3 * c['viscosity'])[:, None] * wa
+    fv = (dt.type(-3.0) * pi * diam * c['viscosity'])[:, None] * wv
+    b0, b1, b2 = box[:, 0], box[:, 1], box[:, 2]  # _box_density, :36-50
+    bv = np.stack([b1 * b2, b0 * b2, b0 * b1], axis=-1)
+    fv = fv + dt.type(-0.5) * c['density'] * bv * np.abs(wv) * wv
+    ba = np.stack([b0 * (b1 ** 4 + b2 ** 4), b1 * (b0 ** 4 + b2 ** 4), b2 * (b0 ** 4 + b1 ** 4)], axis=-1)
+    fa = fa + dt.type(-1.0) * c['density'] * ba * np.abs(wa) * wa / dt.type(64.0)
+    return rotate(fa, xi_r), rotate(fv, xi_r), xi_p  # :80, Transform.do(Force) with pos 0
 
   def forward(self, s: State, tau):
     return self.passive(s) - self.inverse(s) + tau
