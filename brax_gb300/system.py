@@ -242,3 +242,49 @@ class System:
 
   def n_constraint_rows(self) -> int:
     return 4 * self.contacts.n + self.n_limit_rows()
+
+
+# --------------------------------------------------------------------------
+# JSON round trip of a compiled System (exact: floats are written as the
+# shortest repr that reads back to the same float64)
+# --------------------------------------------------------------------------
+_CLASSES = {c.__name__: c for c in (Transform, Motion, Inertia, Link, DoF, Actuator, ContactSlots, System)}
+
+
+def _enc(v):
+  if dataclasses.is_dataclass(v):
+    return {'__class__': type(v).__name__,
+            **{f.name: _enc(getattr(v, f.name)) for f in dataclasses.fields(v)}}
+  if isinstance(v, np.ndarray):
+    return {'__ndarray__': v.dtype.str, 'shape': list(v.shape), 'data': v.reshape(-1).tolist()}
+  if isinstance(v, tuple):
+    return {'__tuple__': [_enc(x) for x in v]}
+  if isinstance(v, list):
+    return [_enc(x) for x in v]
+  if isinstance(v, np.generic):
+    return v.item()
+  return v
+
+
+def _dec(v):
+  if isinstance(v, dict):
+    if '__ndarray__' in v:
+      return np.array(v['data'], dtype=np.dtype(v['__ndarray__'])).reshape(v['shape'])
+    if '__tuple__' in v:
+      return tuple(_dec(x) for x in v['__tuple__'])
+    cls = _CLASSES[v['__class__']]
+    return cls(**{k: _dec(x) for k, x in v.items() if k != '__class__'})
+  if isinstance(v, list):
+    return [_dec(x) for x in v]
+  return v
+
+
+def to_json(sys: System) -> str:
+  """The System as JSON text (every field, bit-exact on reading back)."""
+  import json
+  return json.dumps(_enc(sys))
+
+
+def from_json(text: str) -> System:
+  import json
+  return _dec(json.loads(text))
