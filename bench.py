@@ -58,6 +58,7 @@ def parse():
   p.add_argument('--no-cpu-baseline', action='store_true')
   p.add_argument('--no-adjoint', action='store_true')
   p.add_argument('--no-uneven', action='store_true')
+  p.add_argument('--no-humanoid', action='store_true')
   return p.parse_args()
 
 
@@ -459,6 +460,7 @@ def run_braxg(args):
   adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank)
   uneven = None if args.no_uneven else bench_uneven(torch, dev, rank)
   env_step = bench_env(torch, dev, rank)
+  humanoid = None if args.no_humanoid else bench_humanoid(torch, pipeline, dev, rank)
   out = {
       'metric': METRIC, 'value': round(value, 1), 'unit': 'env-steps/s', 'n_gpus': world,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
@@ -473,7 +475,7 @@ def run_braxg(args):
                                                              args.envs_per_cta)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
       'other_inverse_mode': other_mode,
-      'adjoint': adjoint, 'uneven': uneven, 'env_step': env_step,
+      'adjoint': adjoint, 'uneven': uneven, 'env_step': env_step, 'humanoid': humanoid,
       'env_status_nonzero': int((status != 0).sum()),
   }
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -567,6 +569,50 @@ def bench_env(torch, dev, rank, n=4096, steps=50, warmup=3):
   return {'workload': f'quadruped locomotion task, {n} envs, auto-reset, episode_length 1000, 5 frames',
           'env_steps_per_s': round(steps * n / t, 1), 'ms_per_step': round(1e3 * t / steps, 4),
           'resets_per_env_step': round(dones / steps, 2), 'env_status_nonzero': bad, 'gpu_launches_per_step': 1}
+
+
+def bench_humanoid(torch, pipeline, dev, rank, n=16384, steps=20, warmup=3):
+  """The humanoid-like workload (nv 27, 17 motors, 27 contact slots): 16384
+  envs, env step = 5 x 0.003 s, actions N(0, 0.3) clipped to [-1, 1], one
+  launch per env step in the bench's default inverse mode, L2 flushed between
+  steps."""
+  from brax_gb300 import mjcf
+  sys_ = mjcf.load_asset('humanoid_like')
+  rng = np.random.default_rng(700 + rank)
+  q0 = (sys_.init_q + rng.uniform(-0.01, 0.01, (n, sys_.q_size()))).astype(np.float32)
+  qa = 3  # the free root's quaternion
+  q0[:, qa:qa + 4] /= np.linalg.norm(q0[:, qa:qa + 4], axis=1, keepdims=True)
+  qd0 = (0.01 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32)
+  gen = torch.Generator(device=dev)
+  gen.manual_seed(701 + rank)
+  acts = (torch.randn(warmup + steps, n, sys_.act_size(), device=dev, generator=gen) * 0.3).clamp_(-1, 1)
+  s = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev))
+  model = pipeline.model_for(sys_, dev)
+  bufs = [s, pipeline._alloc(model, n, False, dev, cache=True)]
+  for k in range(warmup):
+    pipeline.step(sys_, bufs[k % 2], acts[k], n_frames=N_FRAMES, inverse_mode=pipeline.CHOLESKY,
+                  out=bufs[1 - k % 2])
+  flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+  stream = torch.cuda.current_stream(dev)
+  torch.cuda.synchronize()
+  t = 0.0
+  for j in range(steps):
+    k = warmup + j
+    flush.zero_()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    pipeline.step(sys_, bufs[k % 2], acts[k], n_frames=N_FRAMES, inverse_mode=pipeline.CHOLESKY,
+                  out=bufs[1 - k % 2])
+    e1.record(stream)
+    e1.synchronize()
+    t += e0.elapsed_time(e1) / 1e3
+  last = bufs[(warmup + steps) % 2]
+  return {'workload': f'humanoid-like nq 28 nv 27 nu 17, 27 contact slots, {n} envs, env step = '
+                      f'{N_FRAMES} x {sys_.dt} s, actions N(0, 0.3) clipped, Cholesky mode',
+          'env_steps_per_s': round(steps * n / t, 1), 'ms_per_step': round(1e3 * t / steps, 4),
+          'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
+                                   model.launch_shape(pipeline.CHOLESKY))),
+          'env_status_nonzero': int((last.status != 0).sum().item()), 'gpu_launches_per_step': 1}
 
 
 def bench_uneven(torch, dev, rank, total=8192, n_steps=256):
