@@ -59,6 +59,13 @@ struct Layout {
 };
 
 __host__ __device__ inline int al4(int x) { return (x + 3) & ~3; }
+// Row stride of the explicit projected-gradient matrix A: a multiple of 4
+// (16-byte row loads) that is 4 mod 8, so that the 8 lanes of each quarter
+// warp's 16-byte loads of 8 consecutive rows cover all 32 banks once.
+__host__ __device__ inline int explicit_lda(int nrow) {
+  const int la = al4(nrow);
+  return (la & 7) == 0 ? la + 4 : la;
+}
 __host__ __device__ inline int imax(int a, int b) { return a > b ? a : b; }
 // words reserved after the model descriptor for the shared Layout
 constexpr int kLayoutWords = 64;
@@ -126,7 +133,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   common = imax(common, 8 * al4(m) + 2 * al4(nv) + 16 + ovf);  // projected gradient (implicit A)
   {
     const int na = L.jcap;  // explicit A = (J Minv) J^T + diag; W shares its words with the PG vectors
-    common = imax(common, na * (na | 1) + al4(na) + imax(na * L.ldm, 7 * al4(na)) + 16);
+    common = imax(common, na * explicit_lda(na) + al4(na) + imax(na * L.ldm, 7 * al4(na)) + 16);
   }
   common = imax(common, m + 4 + ovf);                       // output row map
   int m_off = 0, inv_off = 0, s;
@@ -1375,7 +1382,7 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
-  const int nv = md.nv, ldj = L.ldj, ld = L.ldm, la = nrow | 1;
+  const int nv = md.nv, ldj = L.ldj, ld = L.ldm, la = explicit_lda(nrow), n4 = al4(nrow) / 4;
   float* A = w.at(L.scr);
   float* b = A + nrow * la;
   float* W = b + al4(nrow);  // J Minv, dead once A and b are formed
@@ -1421,10 +1428,12 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     }
   }
   tm.sync();
-  {  // A = W J^T + diag, lanes over the nrow x nrow entries (row i, column c)
+  {  // A = W J^T + diag: the lower triangle (row i, column c <= i), lanes over
+     // its entries, mirrored into the upper one, so that A is symmetric bit
+     // for bit (J Minv J^T is symmetric) and A^T v is A v
     int i = 0, c = tm.lane;
-    while (c >= nrow) {
-      c -= nrow;
+    while (c > i) {
+      c -= i + 1;
       ++i;
     }
     for (; i < nrow;) {
@@ -1435,12 +1444,19 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
         s1 = fmaf(W[i * ld + k + 1], J[c * ldj + k + 1], s1);
       }
       if (k < nv) s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
-      A[i * la + c] = (s0 + s1) + (i == c ? rdiag[i] : 0.f);
+      const float v = (s0 + s1) + (i == c ? rdiag[i] : 0.f);
+      A[i * la + c] = v;
+      A[c * la + i] = v;
       c += T;
-      while (c >= nrow) {
-        c -= nrow;
+      while (c > i) {
+        c -= i + 1;
         ++i;
       }
+    }
+    // zero padding: columns nrow .. 4 n4 of every row (the float4 matvecs read them)
+    for (int e = tm.lane; e < nrow * (4 * n4 - nrow); e += T) {
+      const int r = e / (4 * n4 - nrow);
+      A[r * la + nrow + (e - r * (4 * n4 - nrow))] = 0.f;
     }
   }
   for (int c = tm.lane; c < nrow; c += T) {  // b[c] = W[c] qf_smooth - aref[c]
@@ -1454,41 +1470,32 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     b[c] = (s0 + s1) - raref[c];
   }
   tm.sync();
-  for (int c = tm.lane; c < nrow; c += T) {  // W is dead: its words become x, y, ...
-    x[c] = 0.f;
-    y[c] = 0.f;
-  }
+  // W is dead: its words become x, y, ...; every vector's padding up to
+  // 4 n4 stays zero (the matvecs read it)
+  for (int c = tm.lane; c < 7 * al4(nrow); c += T) x[c] = 0.f;
   tm.sync();
   const long long t_iter = clock64();
   if (tm.lane == 0) pg_cycles[0] += (unsigned)(t_iter - t_build);
-  // out = A v + b (lanes over rows)
-  auto resid = [&](const float* v, float* out) {
+  // A v (lanes over rows; 16-byte row and vector loads, even and odd
+  // columns in two chains), plus b when `add_b`
+  auto matvec = [&](const float* v, float* out, bool add_b) {
+    const float4* v4 = reinterpret_cast<const float4*>(v);
     for (int i = tm.lane; i < nrow; i += T) {
+      const float4* a4 = reinterpret_cast<const float4*>(A + i * la);
       float s0 = 0.f, s1 = 0.f;
-      int c = 0;
-      for (; c + 1 < nrow; c += 2) {
-        s0 = fmaf(A[i * la + c], v[c], s0);
-        s1 = fmaf(A[i * la + c + 1], v[c + 1], s1);
+      for (int c = 0; c < n4; ++c) {
+        const float4 a = a4[c], u = v4[c];
+        s0 = fmaf(a.x, u.x, s0);
+        s1 = fmaf(a.y, u.y, s1);
+        s0 = fmaf(a.z, u.z, s0);
+        s1 = fmaf(a.w, u.w, s1);
       }
-      if (c < nrow) s0 = fmaf(A[i * la + c], v[c], s0);
-      out[i] = (s0 + s1) + b[i];
+      out[i] = add_b ? (s0 + s1) + b[i] : s0 + s1;
     }
     tm.sync();
   };
-  // out = A^T v (lanes over columns)
-  auto grad = [&](const float* v, float* out) {
-    for (int c = tm.lane; c < nrow; c += T) {
-      float s0 = 0.f, s1 = 0.f;
-      int i = 0;
-      for (; i + 1 < nrow; i += 2) {
-        s0 = fmaf(A[i * la + c], v[i], s0);
-        s1 = fmaf(A[(i + 1) * la + c], v[i + 1], s1);
-      }
-      if (i < nrow) s0 = fmaf(A[i * la + c], v[i], s0);
-      out[c] = s0 + s1;
-    }
-    tm.sync();
-  };
+  auto resid = [&](const float* v, float* out) { matvec(v, out, true); };   // A v + b
+  auto grad = [&](const float* v, float* out) { matvec(v, out, false); };  // A^T v = A v
   float t = 1.f, ss = 1.f, err = INFINITY;
   int matvecs = 0;
   int iters = 0;
