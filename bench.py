@@ -211,7 +211,6 @@ _CPU = {}
 
 def _cpu_init(name, n, seed_base):
   """Pool initialiser: one oracle and one batch of envs per worker process."""
-  os.environ.setdefault('OMP_NUM_THREADS', '1')
   from brax_gb300 import mjcf
   from oracle.pipeline import Oracle
   sys_ = mjcf.load_asset(name)
@@ -222,45 +221,54 @@ def _cpu_init(name, n, seed_base):
   _CPU.update(sys=sys_, o=o, rng=rng, s=o.init(q, qd), n=n)
 
 
-def _cpu_step(_):
-  """One env step (N_FRAMES pipeline steps) of this worker's envs."""
+def _cpu_run(args):
+  """`warmup` untimed then `steps` timed env steps (N_FRAMES pipeline steps
+  each) of this worker's envs; returns the timed steps' durations."""
+  warmup, steps = args
   c = _CPU
-  t0 = time.perf_counter()
-  c['s'] = c['o'].env_step(c['s'], c['rng'].uniform(-1, 1, (c['n'], c['sys'].act_size())).astype(np.float32),
-                           N_FRAMES)
-  return time.perf_counter() - t0, c['n']
+  out = []
+  for k in range(warmup + steps):
+    t0 = time.perf_counter()
+    act = c['rng'].uniform(-1, 1, (c['n'], c['sys'].act_size())).astype(np.float32)
+    c['s'] = c['o'].env_step(c['s'], act, N_FRAMES)
+    if k >= warmup:
+      out.append(time.perf_counter() - t0)
+  return out
 
 
 class CpuReference:
   """The numpy FP32 restatement of the reference path (oracle/) on every
-  host core: one spawn-started worker process per core, each stepping its own
-  batch of `sample_envs` envs.  A step is one env step of every worker's
-  batch; its time is the wall time of that pool round."""
+  host core: one spawn-started worker process per core (one BLAS thread
+  each), each stepping its own batch of `sample_envs` envs through the same
+  number of env steps, all at once.  A step is one env step of every
+  worker's batch; the run's time is the slowest worker's."""
 
   def __init__(self, sample_envs: int):
     self.cores = os.cpu_count() or 1
     self.sample_envs = sample_envs
-    self.pool = mp.get_context('spawn').Pool(self.cores, _cpu_init, (WORKLOAD, sample_envs, 100))
-
-  def step(self):
-    t0 = time.perf_counter()
-    res = self.pool.map(_cpu_step, range(self.cores), chunksize=1)
-    return time.perf_counter() - t0, sum(r[1] for r in res)
+    keys = ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS')
+    old = {k: os.environ.get(k) for k in keys}
+    os.environ.update({k: '1' for k in keys})  # inherited by the workers
+    try:
+      self.pool = mp.get_context('spawn').Pool(self.cores, _cpu_init, (WORKLOAD, sample_envs, 100))
+    finally:
+      for k, v in old.items():
+        if v is None:
+          os.environ.pop(k, None)
+        else:
+          os.environ[k] = v
 
   def run(self, steps: int, warmup: int):
-    for _ in range(warmup):
-      self.step()
-    wall, units = [], 0
-    for _ in range(steps):
-      t, u = self.step()
-      wall.append(t)
-      units += u
-    return units / sum(wall), wall
+    """Returns (env-steps/s, per-step times of the slowest worker)."""
+    res = self.pool.map(_cpu_run, [(warmup, steps)] * self.cores, chunksize=1)
+    slowest = max(res, key=sum)
+    return self.cores * self.sample_envs * steps / sum(slowest), slowest
 
   def describe(self, steps: int, wall) -> str:
     return (f'{self.cores} processes x {self.sample_envs} envs, {steps} timed env steps '
-            f'({N_FRAMES} frames each), numpy FP32 restatement of the reference path; '
-            f'{sum(wall):.1f} s wall, about {self.cores * sum(wall):.0f} core-seconds')
+            f'({N_FRAMES} frames each) in each process at once, numpy FP32 restatement of the '
+            f'reference path; slowest process {sum(wall):.1f} s, about '
+            f'{self.cores * sum(wall):.0f} core-seconds')
 
   def close(self):
     self.pool.terminate()
