@@ -122,6 +122,9 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.prm = take(ncon + 3 * nu);
   const int ovf = (m - L.jcap) * L.ldj;  // overflow Jacobian rows at the scratch end
   const int nn = nv * L.ldm;
+  // inverse temporaries: the sweep's rows (nv x explicit_lda(nv)), the
+  // Newton-Schulz / integrator-factor pair (2 nv x ldm)
+  const int inv_tmp = imax(2 * nn + 4, nv * explicit_lda(nv));
   // Scratch users, each with the regions it needs at once.  The mass matrix
   // (when it lives in scratch) must survive from CRBA to the inverse and to
   // the outputs, past the contacts of the Jacobian stage; two placements are
@@ -138,12 +141,12 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   common = imax(common, m + 4 + ovf);                       // output row map
   int m_off = 0, inv_off = 0, s;
   if (own_m) {
-    s = imax(common, imax(head, 2 * nn + 4));               // inverse temporaries; integrator factor
+    s = imax(common, imax(head, inv_tmp));                  // inverse temporaries; integrator factor
   } else {
-    const int ma = al4(imax(head, 2 * nn + 4));             // A: M after the inverse temporaries
+    const int ma = al4(imax(head, inv_tmp));                // A: M after the inverse temporaries
     const int sa = imax(common, ma + nn + ovf);
     const int mb = al4(head), ib = al4(mb + nn);            // B: M, then the inverse temporaries
-    const int sb = imax(common, imax(mb + nn + ovf, ib + 2 * nn + 4));
+    const int sb = imax(common, imax(mb + nn + ovf, ib + inv_tmp));
     if (sa <= sb) {
       m_off = ma;
       s = sa;
@@ -670,136 +673,57 @@ __device__ bool cholesky(const Team<T>& tm, int n, int ld, float* A) {
   return ok;
 }
 
-// Exact SPD inverse by Cholesky: M = L L^T (right-looking, lanes over the
-// trailing entries), X = L^-1 (right-looking forward elimination, lanes over
-// the updated entries), Minv = X^T X (lanes over the lower triangle, mirrored).
-// Lw and X are n x ld scratch matrices.  Returns false (team-uniform) when a
-// pivot is not positive.
+// Exact SPD inverse by the symmetric sweep operator (Gauss-Jordan
+// elimination kept symmetric), full rows, lanes over rows: for k = 0..n-1,
+// with r = 1 / B[k][k],
+//   B[i][j] -= (B[i][k] B[k][j]) r   (i, j != k),
+//   B[i][k] *= r,  B[k][j] *= r  (i, j != k),   B[k][k] = -r,
+// after which B = -M^-1.  The product B[i][k] B[k][j] is the same for (i, j)
+// and (j, i), so B stays symmetric bit for bit and row k doubles as column k
+// (one broadcast row read per step).  Plain Gauss-Jordan, whose rows drift
+// apart from its columns, loses an order of magnitude of accuracy on the
+// ill-conditioned mass matrices of long hanging chains.  B is n rows of
+// stride explicit_lda(n) (16-byte, conflict-free row loads and stores); the
+// pivots are the Schur-complement pivots that a Cholesky factorisation takes
+// the square roots of, so a pivot <= 0 flags a matrix that is not positive
+// definite.  Returns false (team-uniform) on a non-positive pivot.
 template <int T>
-__device__ bool spd_inverse(const Team<T>& tm, int n, int ld, const float* Msrc, float* Lw, float* X, float* Minv) {
-  // lanes own columns: no integer division in the index arithmetic
-  for (int j = tm.lane; j < n; j += T)
-    for (int i = 0; i < n; ++i) {
-      Lw[i * ld + j] = Msrc[i * ld + j];
-      X[i * ld + j] = (i == j) ? 1.f : 0.f;
-    }
+__device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float* Msrc, float* B, float* Minv) {
+  const int lb = explicit_lda(n), w4 = al4(n);
+  for (int e = tm.lane; e < n * w4; e += T) {
+    const int i = e / w4, j = e - i * w4;
+    B[i * lb + j] = j < n ? Msrc[i * ld + j] : 0.f;
+  }
   tm.sync();
   bool ok = true;
   for (int k = 0; k < n; ++k) {
-    float piv = Lw[k * ld + k];
-    ok = ok && (piv > 0.f);
-    float d = sqrtf(fmaxf(piv, 1e-30f));
-    for (int i = k + 1 + tm.lane; i < n; i += T) Lw[i * ld + k] = Lw[i * ld + k] / d;
-    tm.sync();
-    if (tm.lane == 0) Lw[k * ld + k] = d;
-    for (int j = k + 1 + tm.lane; j < n; j += T) {  // trailing update of column j
-      const float ljk = Lw[j * ld + k];
-      for (int i = j; i < n; ++i) Lw[i * ld + j] = Lw[i * ld + j] - Lw[i * ld + k] * ljk;
-    }
-    tm.sync();
-  }
-  for (int k = 0; k < n; ++k) {
-    const float lkk = Lw[k * ld + k];
-    for (int j = tm.lane; j <= k; j += T) X[k * ld + j] = X[k * ld + j] / lkk;
-    tm.sync();
-    for (int j = tm.lane; j <= k; j += T) {  // eliminate column j below row k
-      const float xkj = X[k * ld + j];
-      for (int i = k + 1; i < n; ++i) X[i * ld + j] = X[i * ld + j] - Lw[i * ld + k] * xkj;
-    }
-    tm.sync();
-  }
-  for (int j = tm.lane; j < n; j += T) {  // Minv = X^T X, column j, rows i >= j
-    for (int i = j; i < n; ++i) {
-      float s0 = 0.f, s1 = 0.f;
-      int m = i;
-      for (; m + 1 < n; m += 2) {
-        s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
-        s1 = fmaf(X[(m + 1) * ld + i], X[(m + 1) * ld + j], s1);
-      }
-      if (m < n) s0 = fmaf(X[m * ld + i], X[m * ld + j], s0);
-      float v = s0 + s1;
-      Minv[i * ld + j] = v;
-      Minv[j * ld + i] = v;
-    }
-  }
-  tm.sync();
-  return ok;
-}
-
-// Exact SPD inverse by the symmetric sweep operator (Gauss-Jordan elimination
-// kept symmetric): for k = 0..n-1, with d = B[k][k],
-//   B[i][j] -= B[i][k] B[k][j] / d   (i, j != k),
-//   B[i][k] /= d                      (i != k),
-//   B[k][k]  = -1 / d,
-// after which B = -M^-1.  Only the lower triangle is stored; each lane owns
-// fixed entries of the packed lower triangle, (i, j) kept in registers, and
-// every step reads the old column k,
-// then writes, so one elimination pass replaces the Cholesky factorisation,
-// the triangular inverse and X^T X.  The pivots are the Cholesky pivots
-// squared, so a pivot <= 0 flags a matrix that is not positive definite.
-template <int T, int NVB>
-__device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float* Msrc, float* B0, float* B1,
-                                  float* Minv) {
-  constexpr int E = (NVB * (NVB + 1) / 2 + T - 1) / T;
-  int oi[E], oj[E];
-  {
-    const int cnt = n * (n + 1) / 2;
-    int e = tm.lane, i = 0, j = tm.lane;
-    while (j > i) {
-      j -= i + 1;
-      ++i;
-    }
-#pragma unroll
-    for (int t = 0; t < E; ++t) {
-      const bool v = e < cnt;
-      oi[t] = v ? i : -1;
-      oj[t] = v ? j : 0;
-      e += T;
-      j += T;
-      while (j > i) {
-        j -= i + 1;
-        ++i;
-      }
-    }
-  }
-#pragma unroll
-  for (int t = 0; t < E; ++t)
-    if (oi[t] >= 0) B0[oi[t] * ld + oj[t]] = Msrc[oi[t] * ld + oj[t]];
-  tm.sync();
-  bool ok = true;
-  // step k reads one buffer and writes every entry of the other, so one team
-  // barrier per step suffices (the buffer written next was last read before it)
-  const float* B = B0;
-  float* Bn = B1;
-  for (int k = 0; k < n; ++k) {
-    const float d = B[k * ld + k];
+    const float d = B[k * lb + k];
     ok = ok && (d > 0.f);
     const float r = 1.f / d;
-#pragma unroll
-    for (int t = 0; t < E; ++t) {
-      const int i = oi[t], j = oj[t];
-      if (i < 0) continue;
-      // column k of the (symmetric) matrix from the lower triangle
-      const float bik = i >= k ? B[i * ld + k] : B[k * ld + i];
-      const float bjk = j >= k ? B[j * ld + k] : B[k * ld + j];
-      float v;
-      if (i != k && j != k) v = B[i * ld + j] - bik * (bjk * r);
-      else if (i == k && j == k) v = -r;
-      else v = (i == k ? bjk : bik) * r;
-      Bn[i * ld + j] = v;
+    const float4* rk = reinterpret_cast<const float4*>(B + k * lb);
+    for (int i = tm.lane; i < n; i += T) {  // every row but k, from the old row k
+      if (i == k) continue;
+      float4* ri = reinterpret_cast<float4*>(B + i * lb);
+      const float bik = B[i * lb + k];
+      for (int c = 0; c < w4 / 4; ++c) {
+        const float4 a = rk[c];
+        float4 v = ri[c];
+        v.x = fmaf(-(bik * a.x), r, v.x);
+        v.y = fmaf(-(bik * a.y), r, v.y);
+        v.z = fmaf(-(bik * a.z), r, v.z);
+        v.w = fmaf(-(bik * a.w), r, v.w);
+        ri[c] = v;
+      }
+      B[i * lb + k] = bik * r;
     }
     tm.sync();
-    float* t_ = const_cast<float*>(B);
-    B = Bn;
-    Bn = t_;
+    for (int j = tm.lane; j < n; j += T) B[k * lb + j] = j == k ? -r : B[k * lb + j] * r;  // row k
+    tm.sync();
   }
-#pragma unroll
-  for (int t = 0; t < E; ++t)
-    if (oi[t] >= 0) {
-      const float v = -B[oi[t] * ld + oj[t]];
-      Minv[oi[t] * ld + oj[t]] = v;
-      Minv[oj[t] * ld + oi[t]] = v;
-    }
+  for (int e = tm.lane; e < n * n; e += T) {  // Minv = -B (symmetric)
+    const int i = e / n, j = e - i * n;
+    Minv[i * ld + j] = -B[i * lb + j];
+  }
   tm.sync();
   return ok;
 }
@@ -820,11 +744,7 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   float* S1 = w.at(L.itmp);
   float* S2 = S1 + n * ld;
   if (n == 0) return true;
-  if (exact) {
-    // entry ownership while the owned (i, j) pairs fit a few registers
-    if constexpr ((NVB * (NVB + 1) / 2 + T - 1) / T <= 17) return spd_inverse_sweep<T, NVB>(tm, n, ld, M, S1, S2, P);
-    else return spd_inverse<T>(tm, n, ld, M, S1, S2, P);
-  }
+  if (exact) return spd_inverse_sweep<T>(tm, n, ld, M, S1, P);
   if (num_iter <= 0) return true;
   float* cur = P;
   float* R = S1;
