@@ -136,7 +136,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   common = imax(common, 8 * al4(m) + 2 * al4(nv) + 16 + ovf);  // projected gradient (implicit A)
   {
     const int na = L.jcap;  // explicit A = (J Minv) J^T + diag; W shares its words with the PG vectors
-    common = imax(common, na * explicit_lda(na) + al4(na) + imax(na * L.ldm, 7 * al4(na)) + 16);
+    common = imax(common, na * explicit_lda(na) + al4(na) + imax(na * L.ldm, 9 * al4(na)) + 16);
   }
   common = imax(common, m + 4 + ovf);                       // output row map
   int m_off = 0, inv_off = 0, s;
@@ -1306,13 +1306,17 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   float* A = w.at(L.scr);
   float* b = A + nrow * la;
   float* W = b + al4(nrow);  // J Minv, dead once A and b are formed
+  // FISTA iterates and, by linearity of A, their residuals A v + b and
+  // gradients A (A v + b): x, y, the trial point nx; rx, ry, rn; gx, gy, gn
   float* x = W;
   float* y = x + al4(nrow);
-  float* gy = y + al4(nrow);
-  float* r = gy + al4(nrow);
-  float* nx = r + al4(nrow);
-  float* ny = nx + al4(nrow);
-  float* gx = ny + al4(nrow);
+  float* nx = y + al4(nrow);
+  float* rx = nx + al4(nrow);
+  float* ry = rx + al4(nrow);
+  float* rn = ry + al4(nrow);
+  float* gx = rn + al4(nrow);
+  float* gy = gx + al4(nrow);
+  float* gn = gy + al4(nrow);
   const float* J = w.at(L.J);
   const float* Minv = w.at(L.Minv);
   const float* rdiag = w.at(L.rdiag);
@@ -1389,10 +1393,11 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     if (k < nv) s0 = fmaf(W[c * ld + k], qfs[k], s0);
     b[c] = (s0 + s1) - raref[c];
   }
+  for (int c = nrow + tm.lane; c < 4 * n4; c += T) b[c] = 0.f;  // padding (b is a matvec input)
   tm.sync();
   // W is dead: its words become x, y, ...; every vector's padding up to
   // 4 n4 stays zero (the matvecs read it)
-  for (int c = tm.lane; c < 7 * al4(nrow); c += T) x[c] = 0.f;
+  for (int c = tm.lane; c < 9 * al4(nrow); c += T) x[c] = 0.f;
   tm.sync();
   const long long t_iter = clock64();
   if (tm.lane == 0) pg_cycles[0] += (unsigned)(t_iter - t_build);
@@ -1420,30 +1425,36 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   int matvecs = 0;
   int iters = 0;
   constexpr int kA = (kMaxExplicitRows + 3) & ~3;
+  // x = y = 0: residual b, gradient A b
+  for (int i = tm.lane; i < nrow; i += T) {
+    rx[i] = b[i];
+    ry[i] = b[i];
+  }
+  tm.sync();
+  grad(b, gy);
+  matvecs += 1;
+  for (int i = tm.lane; i < nrow; i += T) gx[i] = gy[i];
   for (int it = 0; it < md.pg_iters; ++it) {
     if (it > 0 && !(err > md.pg_tol)) break;
-    resid(y, r);
     float* rec = tape != nullptr ? tape + kTapeHeadWords + it * kTapeIterWords : nullptr;
     if (rec != nullptr)
       for (int i = tm.lane; i < nrow; i += T) {
         rec[4 + i] = y[i];
-        rec[4 + kA + i] = r[i];
+        rec[4 + kA + i] = ry[i];
       }
     float fs = 0.f;
-    for (int i = tm.lane; i < nrow; i += T) fs += 0.5f * r[i] * r[i];
+    for (int i = tm.lane; i < nrow; i += T) fs += 0.5f * ry[i] * ry[i];
     const float fy = tm.sum(fs);
-    grad(r, gy);
-    matvecs += 2;
     float cur = ss;
     for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
     tm.sync();
-    bool accepted = false;  // r = A nx + b for the accepted trial point
+    bool accepted = false;  // rn = A nx + b for the accepted trial point
     for (int ls = 0; ls < md.pg_maxls; ++ls) {
-      resid(nx, r);
+      resid(nx, rn);
       matvecs += 1;
       float fn = 0.f, dv = 0.f, sq = 0.f;
       for (int i = tm.lane; i < nrow; i += T) {
-        fn += 0.5f * r[i] * r[i];
+        fn += 0.5f * rn[i] * rn[i];
         float dx = nx[i] - y[i];
         dv += dx * gy[i];
         sq += dx * dx;
@@ -1462,7 +1473,6 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     const float nss = cur <= 1e-6f ? 1.f : cur / 0.5f;
     const float nt = 0.5f * (1.f + sqrtf(1.f + 4.f * t * t));
     const float beta = (t - 1.f) / nt;
-    for (int i = tm.lane; i < nrow; i += T) ny[i] = nx[i] + beta * (nx[i] - x[i]);
     if (rec != nullptr) {
       for (int i = tm.lane; i < nrow; i += T) rec[4 + 2 * kA + i] = (y[i] + (-cur) * gy[i]) > 0.f ? 1.f : 0.f;
       if (tm.lane == 0) {
@@ -1471,18 +1481,26 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
       }
     }
     iters = it + 1;
-    if (!accepted) {  // an accepted trial already left A nx + b in r (same inputs, same bits)
-      resid(nx, r);
+    if (!accepted) {  // the last halving's point has not been evaluated
+      resid(nx, rn);
       matvecs += 1;
     }
-    grad(r, gx);
+    grad(rn, gn);
     matvecs += 1;
+    // stopping error at nx; then the momentum step, applied to the point, its
+    // residual and its gradient alike (A is linear), so that y's residual and
+    // gradient cost no matvec
     float es = 0.f;
     for (int i = tm.lane; i < nrow; i += T) {
-      float e = fmaxf(nx[i] + (-1.f) * gx[i], 0.f) - nx[i];
+      const float xn = nx[i], r1 = rn[i], g1 = gn[i];
+      const float e = fmaxf(xn + (-1.f) * g1, 0.f) - xn;
       es += e * e;
-      x[i] = nx[i];
-      y[i] = ny[i];
+      y[i] = xn + beta * (xn - x[i]);
+      ry[i] = r1 + beta * (r1 - rx[i]);
+      gy[i] = g1 + beta * (g1 - gx[i]);
+      x[i] = xn;
+      rx[i] = r1;
+      gx[i] = g1;
     }
     err = sqrtf(tm.sum(es));
     tm.sync();
