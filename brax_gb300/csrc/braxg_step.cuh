@@ -130,7 +130,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   // the outputs, past the contacts of the Jacobian stage; two placements are
   // tried: after the inverse temporaries, or before them.
   const int head = imax(imax(13 * nl + 6 * nv, 14 * ncon + 16), m + 4);  // CRBA, contacts, output row map
-  int common = 14 * nl;                                     // FK / com temporaries
+  int common = al4(14 * nl) + 4 * nv;                       // FK / com temporaries, joint quaternions
   common = imax(common, (fluid ? 21 : 12) * nl + al4(nu) + ovf);  // RNE (+ fluid forces)
   common = imax(common, 14 * ncon + 16 + ovf);              // contacts + Jacobian rows
   common = imax(common, 8 * al4(m) + 2 * al4(nv) + 16 + ovf);  // projected gradient (implicit A)
@@ -227,6 +227,7 @@ __device__ __noinline__ void stage_fk(const int* mw, Ws w) {
   float* jr_ = jp_ + 3 * md.nl;
   float* ja_ = jr_ + 4 * md.nl;
   float* jv_ = ja_ + 3 * md.nl;
+  float* jq_ = w.at(L.scr) + al4(14 * md.nl);  // [nv][4] joint rotation of each stacked dof
   const int* ltype = md.I(BXM_O_LINK_TYPE);
   const int* qadr = md.I(BXM_O_LINK_QADR);
   const int* dadr = md.I(BXM_O_LINK_DADR);
@@ -247,6 +248,7 @@ __device__ __noinline__ void stage_fk(const int* mw, Ws w) {
         f3 ang = ld3(dang + 3 * d), vel = ld3(dvel + 3 * d);
         float qk = q[qa + k], qdk = qd[d];
         q4 rk = qnormalize(quat_rot_axis(ang, qk));
+        st4(jq_ + 4 * d, rk);  // reused by transform_com's cdof
         f3 pk = vel * qk;
         f3 dak = ang * qdk, dvk = vel * qdk;
         if (k == 0) {
@@ -399,6 +401,7 @@ __device__ __noinline__ void stage_com(const int* mw, Ws w) {
   const float* dvel = md.F(BXM_O_D_VEL);
   const float* q = w.at(L.q);
   const float* qd = w.at(L.qd);
+  const float* jq = w.at(L.scr) + al4(14 * nl);
   float* cdof = w.at(L.cdof);
   for (int l = tm.lane; l < nl; l += T) {
     int typ = ltype[l], da = dadr[l], qa = qadr[l];
@@ -418,7 +421,7 @@ __device__ __noinline__ void stage_com(const int* mw, Ws w) {
         ca = rotate(ang, ar);
         cv = rotate(vel, ar) + cross3(ap, ca);
         float qk = q[qa + k];
-        q4 rk = qnormalize(quat_rot_axis(ang, qk));
+        const q4 rk = ld4(jq + 4 * d);  // forward kinematics' joint rotation of this dof
         f3 np_;
         q4 nr;
         tf_do(ap, ar, vel * qk, rk, np_, nr);
