@@ -69,7 +69,8 @@ __host__ __device__ inline AdjLayout make_adj_layout(int nl, int nq, int nv, int
   t = t > 20 * nl ? t : 20 * nl;                           // com: per-link gathers
   t = t > nv * ldm ? t : nv * ldm;                         // inverse: Minv_bar Minv
   const int kA = (kMaxExplicitRows + 3) & ~3;
-  t = t > na * la + na * ldm + 4 * kA ? t : na * la + na * ldm + 4 * kA;  // constraint: A, W, vectors
+  const int lae = explicit_lda(na);
+  t = t > na * lae + na * ldm + 4 * kA ? t : na * lae + na * ldm + 4 * kA;  // constraint: A, W, vectors
   t += 16;
   A.tmp_words = al4(t);
   A.tmp = take(A.tmp_words);
@@ -191,7 +192,8 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
   const int nrow = (int)tape[1];
   if (iters < 0) return false;
   if (nrow == 0) return true;
-  const int la = nrow | 1;
+  const int lab = nrow | 1;  // Ab rows
+  const int la = explicit_lda(nrow), n4 = al4(nrow) / 4;  // Am rows (16-byte matvecs, as the forward)
   constexpr int kA = (kMaxExplicitRows + 3) & ~3;
   const float* J = w.at(L.J);
   const float* Minv = w.at(L.Minv);
@@ -204,37 +206,81 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
   float* xbar = a.at(A.xb);
   float* Am = a.at(A.tmp);
   float* W = Am + nrow * la;
-  float* ybar = W + nrow * ld;
+  float* ybar = W + al4(nrow * ld);  // 16-byte aligned: gb and rb are float4 matvec inputs
   float* vv = ybar + kA;   // scratch vectors of length nrow
   float* gb = vv + kA;
   float* rb = gb + kA;
-  // W = J Minv, A = W J^T + diag (as the forward formed them)
-  for (int k = tm.lane; k < nv; k += T)
-    for (int i = 0; i < nrow; ++i) {
-      float s = 0.f;
-      for (int d = 0; d < nv; ++d) s = fmaf(J[i * ldj + d], Minv[d * ld + k], s);
-      W[i * ld + k] = s;
+  // W = J Minv (lanes over its entries), then A = W J^T + diag as the forward
+  // formed it: the lower triangle mirrored, zero padding columns
+  for (int e = tm.lane; e < nrow * nv; e += T) {
+    const int i = e / nv, k = e - i * nv;
+    float s0 = 0.f, s1 = 0.f;
+    int d = 0;
+    for (; d + 1 < nv; d += 2) {
+      s0 = fmaf(J[i * ldj + d], Minv[d * ld + k], s0);
+      s1 = fmaf(J[i * ldj + d + 1], Minv[(d + 1) * ld + k], s1);
     }
+    if (d < nv) s0 = fmaf(J[i * ldj + d], Minv[d * ld + k], s0);
+    W[i * ld + k] = s0 + s1;
+  }
+  for (int e = tm.lane; e < 4 * kA; e += T) ybar[e] = 0.f;  // ybar, vv, gb, rb with their padding
+  for (int e = tm.lane; e < nrow * lab; e += T) Ab[e] = 0.f;
   tm.sync();
-  for (int c = tm.lane; c < nrow; c += T)
-    for (int i = 0; i < nrow; ++i) {
-      float s = 0.f;
-      for (int k = 0; k < nv; ++k) s = fmaf(W[i * ld + k], J[c * ldj + k], s);
-      Am[i * la + c] = s + (i == c ? rdiag[i] : 0.f);
-      Ab[i * la + c] = 0.f;
+  {
+    int i = 0, c = tm.lane;
+    while (c > i) {
+      c -= i + 1;
+      ++i;
     }
+    for (; i < nrow;) {
+      float s0 = 0.f, s1 = 0.f;
+      int k = 0;
+      for (; k + 1 < nv; k += 2) {
+        s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+        s1 = fmaf(W[i * ld + k + 1], J[c * ldj + k + 1], s1);
+      }
+      if (k < nv) s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+      const float v = (s0 + s1) + (i == c ? rdiag[i] : 0.f);
+      Am[i * la + c] = v;
+      Am[c * la + i] = v;
+      c += T;
+      while (c > i) {
+        c -= i + 1;
+        ++i;
+      }
+    }
+    for (int e = tm.lane; e < nrow * (4 * n4 - nrow); e += T) {
+      const int r = e / (4 * n4 - nrow);
+      Am[r * la + nrow + (e - r * (4 * n4 - nrow))] = 0.f;
+    }
+  }
   // qfc = J^T x*: Jb = x* qfcb^T, xbar = J qfcb
   const float* xs = tape + 4;
-  for (int d = tm.lane; d < nv; d += T)
-    for (int i = 0; i < nrow; ++i) Jb[i * ldj + d] = xs[i] * qfcb[d];
+  for (int e = tm.lane; e < nrow * nv; e += T) {
+    const int i = e / nv, d = e - i * nv;
+    Jb[i * ldj + d] = xs[i] * qfcb[d];
+  }
   for (int i = tm.lane; i < nrow; i += T) {
     float s = 0.f;
     for (int d = 0; d < nv; ++d) s = fmaf(J[i * ldj + d], qfcb[d], s);
     xbar[i] = s;
-    ybar[i] = 0.f;
     bb[i] = 0.f;
   }
   tm.sync();
+  // A v for v with zero padding (A is symmetric: also A^T v)
+  auto matvec = [&](const float* v, int i) {
+    const float4* a4 = reinterpret_cast<const float4*>(Am + i * la);
+    const float4* v4 = reinterpret_cast<const float4*>(v);
+    float s0 = 0.f, s1 = 0.f;
+    for (int c = 0; c < n4; ++c) {
+      const float4 x = a4[c], u = v4[c];
+      s0 = fmaf(x.x, u.x, s0);
+      s1 = fmaf(x.y, u.y, s1);
+      s0 = fmaf(x.z, u.z, s0);
+      s1 = fmaf(x.w, u.w, s1);
+    }
+    return s0 + s1;
+  };
   for (int k = iters - 1; k >= 0; --k) {
     const float* rec = tape + kTapeHeadWords + k * kTapeIterWords;
     const float step = rec[0], beta = rec[1];
@@ -250,48 +296,42 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
     }
     tm.sync();
     for (int i = tm.lane; i < nrow; i += T) {  // rb = A gb
-      float s = 0.f;
-      for (int c = 0; c < nrow; ++c) s = fmaf(Am[i * la + c], gb[c], s);
+      const float s = matvec(gb, i);
       rb[i] = s;
       bb[i] += s;
     }
     tm.sync();
-    for (int c = tm.lane; c < nrow; c += T) {  // Ab += ry gb^T + rb y^T ; ybar = zb + A^T rb
-      float s = 0.f;
-      for (int i = 0; i < nrow; ++i) {
-        Ab[i * la + c] += ry[i] * gb[c] + rb[i] * y[c];
-        s = fmaf(Am[i * la + c], rb[i], s);
-      }
-      ybar[c] = vv[c] + s;
-    }
+    for (int c = tm.lane; c < nrow; c += T)  // Ab += ry gb^T + rb y^T
+      for (int i = 0; i < nrow; ++i) Ab[i * lab + c] += ry[i] * gb[c] + rb[i] * y[c];
+    for (int i = tm.lane; i < nrow; i += T) ybar[i] = vv[i] + matvec(rb, i);  // ybar = zb + A^T rb
     tm.sync();
   }
-  // A = (J Minv) J^T + diag: Jb += Ab W'^T... (Minv symmetric): Jb += (Ab + Ab^T) W
+  // A = (J Minv) J^T + diag: Jb += (Ab + Ab^T) W (Minv symmetric), lanes over Jb's entries
   float* diagb = a.at(A.diagb);
-  for (int d = tm.lane; d < nv; d += T)
-    for (int i = 0; i < nrow; ++i) {
-      float s = 0.f;
-      for (int c = 0; c < nrow; ++c) s = fmaf(Ab[i * la + c] + Ab[c * la + i], W[c * ld + d], s);
-      Jb[i * ldj + d] += s;
-    }
-  for (int i = tm.lane; i < nrow; i += T) diagb[i] = Ab[i * la + i];
+  for (int e = tm.lane; e < nrow * nv; e += T) {
+    const int i = e / nv, d = e - i * nv;
+    float s = 0.f;
+    for (int c = 0; c < nrow; ++c) s = fmaf(Ab[i * lab + c] + Ab[c * lab + i], W[c * ld + d], s);
+    Jb[i * ldj + d] += s;
+  }
+  for (int i = tm.lane; i < nrow; i += T) diagb[i] = Ab[i * lab + i];
   tm.sync();
   // Minvb += J^T Ab J via Z = Ab J (reuses W's rows as Z)
   float* Z = W;
-  for (int d = tm.lane; d < nv; d += T)
-    for (int i = 0; i < nrow; ++i) {
-      float s = 0.f;
-      for (int c = 0; c < nrow; ++c) s = fmaf(Ab[i * la + c], J[c * ldj + d], s);
-      Z[i * ld + d] = s;
-    }
+  for (int e = tm.lane; e < nrow * nv; e += T) {
+    const int i = e / nv, d = e - i * nv;
+    float s = 0.f;
+    for (int c = 0; c < nrow; ++c) s = fmaf(Ab[i * lab + c], J[c * ldj + d], s);
+    Z[i * ld + d] = s;
+  }
   tm.sync();
   float* Minvb = a.at(A.Minvb);
-  for (int j = tm.lane; j < nv; j += T)
-    for (int i2 = 0; i2 < nv; ++i2) {
-      float s = 0.f;
-      for (int r = 0; r < nrow; ++r) s = fmaf(J[r * ldj + i2], Z[r * ld + j], s);
-      Minvb[i2 * ld + j] += s;
-    }
+  for (int e = tm.lane; e < nv * nv; e += T) {
+    const int i2 = e / nv, j = e - i2 * nv;
+    float s = 0.f;
+    for (int r = 0; r < nrow; ++r) s = fmaf(J[r * ldj + i2], Z[r * ld + j], s);
+    Minvb[i2 * ld + j] += s;
+  }
   tm.sync();
   // b = J (Minv qfs) - aref
   float* u = a.at(A.u);
