@@ -172,3 +172,23 @@ def test_misaligned_cache_raises():
   buf = torch.empty(n * m.cache_words + 4, dtype=torch.float32, device='cuda')
   with pytest.raises(ValueError):
     P.step(sys_, s.replace(cache=buf[1:1 + n * m.cache_words].view(n, m.cache_words)), None)
+
+
+def test_cache_skips_the_launch_start_position_stage():
+  """With every env's cache valid, the per-stage cycle counters show the
+  launch-start position stage gone: n_frames position stages per launch
+  instead of n_frames + 1."""
+  P = _P()
+  sys_ = load('quadruped')
+  n = 256
+  q, qd = seeded_inputs(sys_, n, 106)
+  act = _t(actions(sys_, n, np.random.default_rng(107)))
+  s = P.step(sys_, P.init(sys_, _t(q), _t(qd)), act, n_frames=2, inverse_mode=P.CHOLESKY)
+  fk = []
+  for st in (s, s.replace(cache=None)):
+    buf = P.profile_buffer()
+    P.step(sys_, st, act, n_frames=2, inverse_mode=P.CHOLESKY, profile=buf)
+    torch.cuda.synchronize()
+    fk.append(P.profile_report(buf)['fk'])
+  # 2 forward-kinematics passes with the cache, 3 without
+  assert fk[0] < 0.85 * fk[1], fk
