@@ -481,7 +481,7 @@ def run_braxg(args):
                  'l2': 'flushed (256 MB write) before every timed step',
                  'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
                                           model.launch_shape(mode, args.threads_per_env,
-                                                             args.envs_per_cta)))},
+                                                             args.envs_per_cta, n_env=n)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
       'other_inverse_mode': other_mode,
       'adjoint': adjoint, 'uneven': uneven, 'env_step': env_step, 'humanoid': humanoid,
@@ -620,7 +620,7 @@ def bench_humanoid(torch, pipeline, dev, rank, n=16384, steps=20, warmup=3):
                       f'{N_FRAMES} x {sys_.dt} s, actions N(0, 0.3) clipped, Cholesky mode',
           'env_steps_per_s': round(steps * n / t, 1), 'ms_per_step': round(1e3 * t / steps, 4),
           'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
-                                   model.launch_shape(pipeline.CHOLESKY))),
+                                   model.launch_shape(pipeline.CHOLESKY, n_env=n))),
           'env_status_nonzero': int((last.status != 0).sum().item()), 'gpu_launches_per_step': 1}
 
 

@@ -127,7 +127,7 @@ def lib() -> ctypes.CDLL:
                                             vp, vp, vp, vp, vp, P(Options)]
     l.braxg_rollout_vjp_noalloc_capacity.restype = ctypes.c_size_t
     l.braxg_rollout_vjp_noalloc_capacity.argtypes = []
-    l.braxg_launch_shape.argtypes = [vp, P(Options), P(ctypes.c_int32), P(ctypes.c_int32),
+    l.braxg_launch_shape.argtypes = [vp, P(Options), i32, P(ctypes.c_int32), P(ctypes.c_int32),
                                      P(ctypes.c_int32)]
     l.braxg_batch_create.argtypes = [P(vp), P(ctypes.c_int32), P(ctypes.c_int32), i32,
                                      P(BucketShape), i32, ctypes.c_int32, P(vp)]

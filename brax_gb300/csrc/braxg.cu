@@ -78,12 +78,18 @@ int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shap
   if (epc == 0) {
     // default: one CTA per SM holding as many envs as its shared memory and
     // 512 threads allow, so that every warp of the SM runs the same stage's
-    // code (the instruction working set of one stage); a batch too small to
-    // fill every SM that way is spread over all of them instead
-    epc = (kMaxSmem - model_bytes) / env_bytes;
-    if (n_env > 0 && m->sms > 0) epc = std::min(epc, (n_env + m->sms - 1) / m->sms);
+    // code (the instruction working set of one stage); the batch then takes
+    // the fewest waves of such CTAs with its envs spread evenly over every
+    // SM of each wave (4096 quadrupeds: 2 waves of 152 CTAs of at most 14
+    // envs, not 256 CTAs of 16 whose second wave leaves 48 SMs idle; a batch
+    // smaller than one wave is spread over all SMs)
+    epc = std::min(fit, max_epc);
+    if (n_env > 0 && m->sms > 0) {
+      const long long per_wave = (long long)m->sms * epc;
+      const long long waves = (n_env + per_wave - 1) / per_wave;
+      epc = (int)((n_env + (long long)m->sms * waves - 1) / ((long long)m->sms * waves));
+    }
     if (epc < 1) epc = 1;
-    if (epc > max_epc) epc = max_epc;
   }
   if (epc > max_epc || epc > fit || epc < 1)
     return fail(BRAXG_ERR_INVALID, "envs_per_cta %d out of range [1, %d]", epc, fit < max_epc ? fit : max_epc);
@@ -207,10 +213,12 @@ int braxg_model_cache_span(const braxg_model* m, int32_t* fixed_words, int32_t* 
   return BRAXG_OK;
 }
 
-int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int32_t* tpe, int32_t* epc, int32_t* smem) {
+int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int n_env, int32_t* tpe, int32_t* epc,
+                       int32_t* smem) {
   if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model is NULL");
+  if (n_env < 0) return fail(BRAXG_ERR_INVALID, "n_env must be >= 0");
   Shape s;
-  int rc = choose_shape(m, opt, 0, &s);
+  int rc = choose_shape(m, opt, n_env, &s);
   if (rc) return rc;
   if (tpe) *tpe = s.T;
   if (epc) *epc = s.epc;

@@ -68,10 +68,12 @@ class Model:
         pass
       self._h = None
 
-  def launch_shape(self, inverse_mode=NEWTON_SCHULZ, threads_per_env=0, envs_per_cta=0):
+  def launch_shape(self, inverse_mode=NEWTON_SCHULZ, threads_per_env=0, envs_per_cta=0, n_env=0):
+    """(threads_per_env, envs_per_cta, smem_bytes) of a call on n_env envs
+    (0: the largest CTA)."""
     t, e, s = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
     opt = N.Options(inverse_mode, threads_per_env, envs_per_cta)
-    N.check(N.lib().braxg_launch_shape(self._h, ctypes.byref(opt), ctypes.byref(t),
+    N.check(N.lib().braxg_launch_shape(self._h, ctypes.byref(opt), int(n_env), ctypes.byref(t),
                                        ctypes.byref(e), ctypes.byref(s)), 'braxg_launch_shape')
     return t.value, e.value, s.value
 

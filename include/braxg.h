@@ -348,9 +348,10 @@ int braxg_batch_rollout(const braxg_batch* batch, void* stream, int n_steps,
                         const float* act_seq, const braxg_state* in, braxg_state* out,
                         float* traj_q, float* traj_qd, const braxg_options* opt);
 
-/* Launch shape the tuner picks for this model: lanes per env, envs per CTA,
- * dynamic shared memory bytes per CTA. */
-int braxg_launch_shape(const braxg_model* model, const braxg_options* opt,
+/* Launch shape a braxg_init / braxg_step / braxg_rollout / braxg_env_rollout
+ * call of n_env envs takes for this model (n_env 0: the largest CTA): lanes
+ * per env, envs per CTA, dynamic shared memory bytes per CTA. */
+int braxg_launch_shape(const braxg_model* model, const braxg_options* opt, int n_env,
                        int32_t* threads_per_env, int32_t* envs_per_cta,
                        int32_t* smem_bytes);
 

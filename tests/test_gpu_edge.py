@@ -142,3 +142,19 @@ def test_relaxed_barriers_change_no_result(relax):
   torch.cuda.synchronize()
   for f in ('q', 'qd', 'mass_mx_inv', 'x_pos'):
     torch.testing.assert_close(getattr(a, f), getattr(b, f), rtol=0, atol=0)
+
+
+def test_default_shape_balances_waves():
+  """The default envs per CTA: the fewest waves of one full CTA per SM, the
+  envs spread evenly over every SM of each wave."""
+  P, _ = _P()
+  sys_ = load('quadruped')
+  m = P.model_for(sys_)
+  sms = torch.cuda.get_device_properties(0).multi_processor_count
+  full = m.launch_shape(P.CHOLESKY)[1]  # the largest CTA
+  for n in (1, sms, sms * full, sms * full + 1, 4096, 3 * sms * full - 5):
+    waves = -(-n // (sms * full))
+    expect = -(-n // (sms * waves))
+    t, e, _ = m.launch_shape(P.CHOLESKY, n_env=n)
+    assert (t, e) == (32, expect), (n, e, expect)
+    assert -(-n // e) <= waves * sms
