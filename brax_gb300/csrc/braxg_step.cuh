@@ -66,6 +66,12 @@ __host__ __device__ inline int explicit_lda(int nrow) {
   const int la = al4(nrow);
   return (la & 7) == 0 ? la + 4 : la;
 }
+// Row stride of the Newton-Schulz iterates: covers the register tile's
+// columns (up to the dof bucket 16 / 32 / 64) with 16-byte aligned rows.
+__host__ __device__ inline int ns_ldb(int nv) {
+  const int nvb = nv <= 16 ? 16 : (nv <= 32 ? 32 : 64);
+  return explicit_lda(nv > nvb ? nv : nvb);
+}
 __host__ __device__ inline int imax(int a, int b) { return a > b ? a : b; }
 // words reserved after the model descriptor for the shared Layout
 constexpr int kLayoutWords = 64;
@@ -123,8 +129,9 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   const int ovf = (m - L.jcap) * L.ldj;  // overflow Jacobian rows at the scratch end
   const int nn = nv * L.ldm;
   // inverse temporaries: the sweep's rows (nv x explicit_lda(nv)), the
-  // Newton-Schulz / integrator-factor pair (2 nv x ldm)
-  const int inv_tmp = imax(2 * nn + 4, nv * explicit_lda(nv));
+  // Newton-Schulz iterates and residual (3 nv x ns_ldb(nv)), the integrator's
+  // factor pair (2 nv x ldm)
+  const int inv_tmp = imax(imax(2 * nn + 4, nv * explicit_lda(nv)), 3 * nv * ns_ldb(nv));
   // Scratch users, each with the regions it needs at once.  The mass matrix
   // (when it lives in scratch) must survive from CRBA to the inverse and to
   // the outputs, past the contacts of the Jacobian stage; two placements are
@@ -573,7 +580,9 @@ __device__ __noinline__ void stage_crba(const int* mw, Ws w) {
 // op 0: C = A B;  op 1: C = I - A B;  op 2: C = A (I + B)
 // Register-tiled: the lanes form an RB x CB grid, each lane owns a TR x TC
 // block of C (TR = NVB / RB, TC = NVB / CB).  Shapes whose tile would hold
-// more than 32 accumulators use one column per lane instead.
+// more than 32 accumulators use one column per lane instead.  `rows4`: B's
+// rows are 16-byte aligned and zero from column n up to NVB, so a tile's
+// row of B is read with 16-byte loads (the same values, the same sums).
 template <int T, int NVB>
 struct MMTile {
   static constexpr int RB = (T == 32) ? 8 : 4;
@@ -584,7 +593,8 @@ struct MMTile {
 };
 
 template <int T, int NVB>
-__device__ void matmul(const Team<T>& tm, int n, int ld, const float* A, const float* B, float* C, int op) {
+__device__ void matmul(const Team<T>& tm, int n, const float* A, int lda, const float* B, int ldb, float* C,
+                       int ldc, int op, bool rows4 = false) {
   using G = MMTile<T, NVB>;
   if constexpr (G::tiled) {
     const int rb = tm.lane / G::CB, cb = tm.lane - (tm.lane / G::CB) * G::CB;
@@ -598,12 +608,30 @@ __device__ void matmul(const Team<T>& tm, int n, int ld, const float* A, const f
       for (int k = 0; k < n; ++k) {
         float a[G::TR], b[G::TC];
 #pragma unroll
-        for (int r = 0; r < G::TR; ++r) a[r] = (i0 + r < n) ? A[(i0 + r) * ld + k] : 0.f;
+        for (int r = 0; r < G::TR; ++r) a[r] = (i0 + r < n) ? A[(i0 + r) * lda + k] : 0.f;
+        if constexpr (G::TC % 4 == 0) {
+          if (rows4) {
+            const float4* b4 = reinterpret_cast<const float4*>(B + k * ldb + j0);
 #pragma unroll
-        for (int c = 0; c < G::TC; ++c) {
-          float v = (j0 + c < n) ? B[k * ld + j0 + c] : 0.f;
-          if (op == 2 && k == j0 + c) v = v + 1.f;
-          b[c] = v;
+            for (int c = 0; c < G::TC / 4; ++c) {
+              const float4 v = b4[c];
+              b[4 * c] = v.x;
+              b[4 * c + 1] = v.y;
+              b[4 * c + 2] = v.z;
+              b[4 * c + 3] = v.w;
+            }
+          } else {
+#pragma unroll
+            for (int c = 0; c < G::TC; ++c) b[c] = (j0 + c < n) ? B[k * ldb + j0 + c] : 0.f;
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < G::TC; ++c) b[c] = (j0 + c < n) ? B[k * ldb + j0 + c] : 0.f;
+        }
+        if (op == 2) {
+#pragma unroll
+          for (int c = 0; c < G::TC; ++c)
+            if (k == j0 + c) b[c] = b[c] + 1.f;
         }
 #pragma unroll
         for (int r = 0; r < G::TR; ++r)
@@ -615,7 +643,7 @@ __device__ void matmul(const Team<T>& tm, int n, int ld, const float* A, const f
 #pragma unroll
         for (int c = 0; c < G::TC; ++c) {
           int i = i0 + r, j = j0 + c;
-          if (i < n && j < n) C[i * ld + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[r][c]) : acc[r][c];
+          if (i < n && j < n) C[i * ldc + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[r][c]) : acc[r][c];
         }
     }
   } else {
@@ -624,18 +652,23 @@ __device__ void matmul(const Team<T>& tm, int n, int ld, const float* A, const f
 #pragma unroll
       for (int i = 0; i < NVB; ++i) acc[i] = 0.f;
       for (int k = 0; k < n; ++k) {
-        float b = B[k * ld + j];
+        float b = B[k * ldb + j];
         if (op == 2 && k == j) b = b + 1.f;
 #pragma unroll
         for (int i = 0; i < NVB; ++i)
-          if (i < n) acc[i] = fmaf(A[i * ld + k], b, acc[i]);
+          if (i < n) acc[i] = fmaf(A[i * lda + k], b, acc[i]);
       }
 #pragma unroll
       for (int i = 0; i < NVB; ++i)
-        if (i < n) C[i * ld + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[i]) : acc[i];
+        if (i < n) C[i * ldc + j] = (op == 1) ? ((i == j ? 1.f : 0.f) - acc[i]) : acc[i];
     }
   }
   tm.sync();
+}
+
+template <int T, int NVB>
+__device__ void matmul(const Team<T>& tm, int n, int ld, const float* A, const float* B, float* C, int op) {
+  matmul<T, NVB>(tm, n, A, ld, B, ld, C, ld, op);
 }
 
 // safe_norm (brax/math.py:308-328) of an n x n matrix
@@ -749,11 +782,20 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   if (n == 0) return true;
   if (exact) return spd_inverse_sweep<T>(tm, n, ld, M, S1, P);
   if (num_iter <= 0) return true;
-  float* cur = P;
-  float* R = S1;
-  float* nxt = S2;
-  matmul<T, NVB>(tm, n, ld, M, cur, R, 1);  // r0 = I - A A_inv
-  float nr0 = safe_norm_mat<T>(tm, n, ld, R);
+  // the iterates and residuals live in rows of stride lb (16-byte loads of
+  // every product's right-hand operand; columns n .. lb zero); M stays in
+  // place as the left-hand operand
+  const int lb = ns_ldb(n);
+  float* cur = S1;
+  float* nxt = S1 + n * lb;
+  float* R = S1 + 2 * n * lb;
+  for (int e = tm.lane; e < 3 * n * lb; e += T) {
+    const int i = e / lb, j = e - i * lb;  // rows of the three buffers in turn
+    S1[e] = (j < n && i < n) ? P[i * ld + j] : 0.f;
+  }
+  tm.sync();
+  matmul<T, NVB>(tm, n, M, ld, cur, lb, R, lb, 1, true);  // r0 = I - A A_inv
+  float nr0 = safe_norm_mat<T>(tm, n, lb, R);
   if (nr0 > 1.f) {  // reset to 0.5 A^T / tr(A A^T) (r0 is kept, as the reference does)
     if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] += 1;
     float s = 0.f;
@@ -764,14 +806,14 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
       }
     s = tm.sum(s);
     for (int j = tm.lane; j < n; j += T)
-      for (int i = 0; i < n; ++i) cur[i * ld + j] = 0.5f * M[j * ld + i] / s;
+      for (int i = 0; i < n; ++i) cur[i * lb + j] = 0.5f * M[j * ld + i] / s;
     tm.sync();
   }
   float err = 1.f;
   for (int it = 0; it < num_iter; ++it) {
-    matmul<T, NVB>(tm, n, ld, cur, R, nxt, 2);  // a_inv (I + r)
-    matmul<T, NVB>(tm, n, ld, M, nxt, R, 1);    // I - a a_inv_next
-    float e = safe_norm_mat<T>(tm, n, ld, R);
+    matmul<T, NVB>(tm, n, cur, lb, R, lb, nxt, lb, 2, true);  // a_inv (I + r)
+    matmul<T, NVB>(tm, n, M, ld, nxt, lb, R, lb, 1, true);    // I - a a_inv_next
+    float e = safe_norm_mat<T>(tm, n, lb, R);
     if (e < err) {
       float* t = cur;
       cur = nxt;
@@ -779,11 +821,9 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
     }
     err = e;
   }
-  if (cur != P) {
-    for (int j = tm.lane; j < n; j += T)
-      for (int i = 0; i < n; ++i) P[i * ld + j] = cur[i * ld + j];
-    tm.sync();
-  }
+  for (int j = tm.lane; j < n; j += T)
+    for (int i = 0; i < n; ++i) P[i * ld + j] = cur[i * lb + j];
+  tm.sync();
   return true;
 }
 
