@@ -41,7 +41,7 @@ WORKLOAD = 'quadruped'
 N_FRAMES = 5
 
 
-def parse():
+def parse(argv=None):
   p = argparse.ArgumentParser()
   p.add_argument('--gpus', type=int, default=1)
   p.add_argument('--steps', type=int, default=200)
@@ -58,7 +58,7 @@ def parse():
   p.add_argument('--no-adjoint', action='store_true')
   p.add_argument('--no-uneven', action='store_true')
   p.add_argument('--no-humanoid', action='store_true')
-  return p.parse_args()
+  return p.parse_args(argv)
 
 
 # ---------------------------------------------------------------------------

@@ -50,3 +50,46 @@ def test_two_gloo_ranks_report_the_slowest_rank():
 def test_single_rank_needs_no_process_group():
   import bench
   assert bench.max_over_ranks(3.5, 'cpu') == 3.5
+
+
+def test_reference_arm_runs_on_rank_0_only(monkeypatch, capsys):
+  """Under torchrun the reference arm's other ranks exit without work: no
+  worker pool, no output line."""
+  import bench
+  monkeypatch.setenv('RANK', '1')
+  monkeypatch.setenv('WORLD_SIZE', '2')
+  monkeypatch.setattr(bench, 'CpuReference', lambda *a, **k: pytest.fail('rank 1 started the CPU pool'))
+  bench.run_reference(bench.parse(['--impl', 'reference', '--steps', '1', '--warmup', '0']))
+  assert capsys.readouterr().out == ''
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+  """Rank 0's reference line: the contract's keys, e2e with no host-device
+  bytes, and a cpu_baseline describing this run (a stub pool)."""
+  import json
+  import bench
+
+  class Stub:
+    cores = 4
+
+    def __init__(self, n):
+      self.sample_envs = n
+
+    def run(self, steps, warmup):
+      return 1234.5, [0.1] * steps
+
+    def describe(self, steps, wall):
+      return f'stub {steps}'
+
+    def close(self):
+      pass
+
+  monkeypatch.setenv('RANK', '0')
+  monkeypatch.setenv('WORLD_SIZE', '1')
+  monkeypatch.setattr(bench, 'CpuReference', Stub)
+  bench.run_reference(bench.parse(['--impl', 'reference', '--steps', '3', '--warmup', '1']))
+  d = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+  assert d['impl'] == 'reference' and d['value'] == 1234.5 and d['steps'] == 3 and d['warmup'] == 1
+  assert d['e2e'] == {'value': 1234.5, 'unit': 'env-steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}
+  assert d['cpu_baseline']['kind'] == 'port' and d['cpu_baseline']['cores'] == 4
+  assert d['higher_is_better'] is True and d['unit'] == 'env-steps/s'
