@@ -192,3 +192,46 @@ def test_cache_skips_the_launch_start_position_stage():
     fk.append(P.profile_report(buf)['fk'])
   # 2 forward-kinematics passes with the cache, 3 without
   assert fk[0] < 0.85 * fk[1], fk
+
+
+def test_cache_with_overflow_rows_and_implicit_solve():
+  """Lying humanoid-like models (most envs with more than 32 active rows:
+  the Jacobian rows beyond 32 live at the end of scratch and the cache copies
+  them): cached steps equal uncached ones bit for bit."""
+  P = _P()
+  sys_ = load('humanoid_like')
+  n = 48
+  rng = np.random.default_rng(108)
+  q = sys_.init_q[None] + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))
+  qd = 0.1 * rng.normal(size=(n, sys_.qd_size()))
+  q[:, 3:7] = [np.cos(np.pi / 4), np.sin(np.pi / 4), 0.0, 0.0]
+  q[:, 2] = rng.uniform(0.05, 0.2, n)
+  act = _t(np.clip(rng.normal(0.0, 0.3, (n, sys_.act_size())), -1, 1))
+  full = P.init(sys_, _t(q), _t(qd), full=True)
+  torch.cuda.synchronize()
+  assert ((full.con_diag.abs() > 0).sum(-1) > 32).float().mean().item() >= 0.5
+  c = P.init(sys_, _t(q), _t(qd))
+  u = P.init(sys_, _t(q), _t(qd), cache=False)
+  for _ in range(3):
+    c = P.step(sys_, c, act, n_frames=2, inverse_mode=P.CHOLESKY)
+    u = P.step(sys_, u, act, n_frames=2, inverse_mode=P.CHOLESKY)
+    torch.cuda.synchronize()
+    _same(c, u)
+
+
+@pytest.mark.parametrize('tpe', [16, 32])
+def test_cache_chain_both_team_widths(tpe):
+  P = _P()
+  sys_ = load('chain3')
+  n = 40
+  q, qd = seeded_inputs(sys_, n, 109)
+  rng = np.random.default_rng(110)
+  c = P.init(sys_, _t(q), _t(qd), threads_per_env=tpe)
+  u = P.init(sys_, _t(q), _t(qd), cache=False, threads_per_env=tpe)
+  for _ in range(3):
+    act = _t(actions(sys_, n, rng))
+    for mode in (P.CHOLESKY, P.NEWTON_SCHULZ):
+      c = P.step(sys_, c, act, n_frames=2, inverse_mode=mode, threads_per_env=tpe)
+      u = P.step(sys_, u, act, n_frames=2, inverse_mode=mode, threads_per_env=tpe)
+      torch.cuda.synchronize()
+      _same(c, u)
