@@ -58,7 +58,7 @@ struct Shape {
 };
 
 
-int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shape* s) {
+int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shape* s, bool ovf_global = false) {
   int nv = m->dims.nv;
   s->NVB = nv <= 16 ? 16 : (nv <= 32 ? 32 : 64);
   // default lanes per env: 16 for small models (nv <= 8: two envs per warp),
@@ -68,7 +68,7 @@ int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shap
   if (T == 16 && s->NVB == 64) T = 32;
   s->T = T;
   int model_bytes = (braxg::al4(m->words) + braxg::kLayoutWords) * 4;
-  int env_bytes = m->L.total * 4;
+  int env_bytes = (ovf_global ? m->Lg.total : m->L.total) * 4;
   int max_epc = kMaxBlock / T;
   int fit = (kMaxSmem - model_bytes) / env_bytes;
   if (fit < 1)
@@ -101,7 +101,11 @@ int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shap
 int launch(const braxg_model* m, const braxg_options* opt, braxg::StepArgs& a, cudaStream_t st) {
   g_launches = 0;
   Shape s;
-  int rc = choose_shape(m, opt, a.n_env, &s);
+  // Jacobian rows beyond the first 32 go to the output state's cache slots
+  // when it has them and that layout fits more envs per CTA
+  a.ovf_global = (m->ovf_ok && a.out.cache != nullptr) ? 1 : 0;
+  a.cache_stride = m->cache_words;
+  int rc = choose_shape(m, opt, a.n_env, &s, a.ovf_global != 0);
   if (rc) return rc;
   if (a.n_env == 0) return BRAXG_OK;
   a.envs_per_cta = s.epc;
@@ -165,6 +169,15 @@ int braxg_model_create(const void* desc, size_t desc_bytes, int device, braxg_mo
   m->dims = d;
   m->ns_iters = w[BXM_H_NS_ITERS];
   m->L = braxg::layout_of(w);
+  m->Lg = braxg::layout_of(w, 1);
+  {
+    const int model_bytes = (braxg::al4(words) + braxg::kLayoutWords) * 4;
+    const int fit_s = (kMaxSmem - model_bytes) / (m->L.total * 4);
+    const int fit_g = (kMaxSmem - model_bytes) / (m->Lg.total * 4);
+    m->ovf_ok = fit_g > fit_s && m->Lg.total < m->L.total;
+    const int ovf_words = (d.m - m->L.jcap) * m->L.ldj;
+    m->cache_words = m->ovf_ok ? std::max(m->L.total, braxg::al4(m->Lg.total + ovf_words)) : m->L.total;
+  }
   int cur = 0;
   cudaGetDevice(&cur);
   cudaError_t e = cudaSetDevice(device);
@@ -199,14 +212,14 @@ int braxg_model_dims(const braxg_model* m, braxg_dims* out) {
 
 int braxg_model_cache_words(const braxg_model* m, int32_t* words) {
   if (m == nullptr || words == nullptr) return fail(BRAXG_ERR_INVALID, "NULL argument");
-  *words = m->L.total;  // the env's whole shared-memory arena
+  *words = m->cache_words;  // the env's arena (and its overflow Jacobian rows)
   return BRAXG_OK;
 }
 
 int braxg_model_cache_span(const braxg_model* m, int32_t* fixed_words, int32_t* row_words, int32_t* rows_in_fixed) {
   if (m == nullptr || fixed_words == nullptr || row_words == nullptr || rows_in_fixed == nullptr)
     return fail(BRAXG_ERR_INVALID, "NULL argument");
-  const braxg::Layout& L = m->L;  // the spans copy_position_terms copies
+  const braxg::Layout& L = m->ovf_ok ? m->Lg : m->L;  // the spans copy_position_terms copies (cached calls)
   *fixed_words = L.scr + (L.M >= L.scr ? braxg::al4(m->dims.nv * L.ldm) : 0);
   *row_words = L.ldj;
   *rows_in_fixed = L.jcap;
@@ -218,7 +231,7 @@ int braxg_launch_shape(const braxg_model* m, const braxg_options* opt, int n_env
   if (m == nullptr) return fail(BRAXG_ERR_INVALID, "model is NULL");
   if (n_env < 0) return fail(BRAXG_ERR_INVALID, "n_env must be >= 0");
   Shape s;
-  int rc = choose_shape(m, opt, n_env, &s);
+  int rc = choose_shape(m, opt, n_env, &s, m->ovf_ok);  // as for output states with a cache
   if (rc) return rc;
   if (tpe) *tpe = s.T;
   if (epc) *epc = s.epc;

@@ -17,7 +17,13 @@ struct braxg_model {
   braxg_dims dims;
   int ns_iters;
   int sms;  // multiprocessors of the model's device
-  braxg::Layout L;
+  braxg::Layout L;   // arena with every Jacobian row in shared memory
+  // arena whose Jacobian rows beyond the first 32 live in the output state's
+  // cache slot; used by the single-model calls whose output carries a cache
+  // when it fits more envs per CTA than L (ovf_ok)
+  braxg::Layout Lg;
+  bool ovf_ok;
+  int cache_words;   // floats per env of a cache buffer (either layout)
 };
 
 namespace braxg {

@@ -81,30 +81,36 @@ __device__ __forceinline__ void copy_arena(const Team<T>& tm, float* dst, const 
 
 // Copies the words of an arena that hold position-level terms: everything
 // before the scratch region, the mass matrix (in scratch unless the
-// integrator owns it) and the active overflow Jacobian rows at the scratch
-// end.  The active row count is read from `arena` (the destination on a
-// restore, the source on a store) once the part before scratch is there, and
-// clamped to the model's row count.
+// integrator owns it) and the active overflow Jacobian rows.  Those rows are
+// copied from `ovf_src` to `ovf_dst` (the arena's scratch end, or the env's
+// cache slots when they live there; no copy when the two are the same).
+// The active row count is read from `arena` (the destination on a restore,
+// the source on a store) once the part before scratch is there, and clamped
+// to the model's row count.
 template <int T>
 __device__ __forceinline__ void copy_position_terms(const Team<T>& tm, float* dst, const float* src, const Layout& L,
-                                                    int nv, int m, const float* arena) {
+                                                    int nv, int m, const float* arena, float* ovf_dst,
+                                                    const float* ovf_src) {
   copy_arena<T>(tm, dst, src, L.scr);
   tm.sync();
   const int nrow = min(max(reinterpret_cast<const int*>(arena + L.misc)[0], 0), m);
   if (L.M >= L.scr) copy_arena<T>(tm, dst + L.M, src + L.M, al4(nv * L.ldm));
   const int novf = nrow - L.jcap;
-  if (novf > 0) {
+  if (novf > 0 && ovf_dst != ovf_src) {
     const int o0 = L.jovf & ~3, o1 = al4(L.jovf + novf * L.ldj);
-    copy_arena<T>(tm, dst + o0, src + o0, o1 - o0);
+    copy_arena<T>(tm, ovf_dst + o0, ovf_src + o0, o1 - o0);
   }
 }
 
 // Tag of a cached arena (misc[11]): the team width that computed it (lane
-// reductions make the terms depend on it bit for bit) and whether its
-// mass_mx_inv is the exact inverse of its mass matrix.  An env whose launch
-// flagged a non-finite value stores tag 0, which no launch accepts.
+// reductions make the terms depend on it bit for bit), where its overflow
+// Jacobian rows live (the arena layout), and whether its mass_mx_inv is the
+// exact inverse of its mass matrix.  An env whose launch flagged a
+// non-finite value stores tag 0, which no launch accepts.
 template <int T>
-__device__ __forceinline__ int cache_tag(bool exact_minv) { return 2 * T + (exact_minv ? 1 : 0); }
+__device__ __forceinline__ int cache_tag(bool ovf_g, bool exact_minv) {
+  return 4 * T + (ovf_g ? 2 : 0) + (exact_minv ? 1 : 0);
+}
 
 // Restores the env's arena from the input state's cache; true if it applies.
 // In exact-inverse mode the cached mass_mx_inv must be exact; in
@@ -114,10 +120,13 @@ __device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, 
                                            bool exact) {
   const Team<T> tm;
   const Model md(mw);
-  copy_position_terms<T>(tm, w.b, a.cache_in + (B.env + env) * w.L->total, *w.L, md.nv, md.m, w.b);
+  const float* slot = a.cache_in + (B.env + env) * a.cache_stride;
+  // overflow rows: into the arena, or from the input's cache slot to the output's
+  copy_position_terms<T>(tm, w.b, slot, *w.L, md.nv, md.m, w.b, w.L->ovf_g ? w.g : w.b, slot);
   tm.sync();
   const int tag = reinterpret_cast<const int*>(w.at(w.L->misc))[11];
-  const bool tag_ok = exact ? tag == cache_tag<T>(true) : (tag >> 1) == T;
+  const int want = cache_tag<T>(w.L->ovf_g != 0, true);
+  const bool tag_ok = exact ? tag == want : (tag >> 1) == (want >> 1);
   return cache_matches<T>(a, B, mw, w, env, !exact) && tag_ok;
 }
 
@@ -128,9 +137,11 @@ __device__ __noinline__ void store_cache(const StepArgs& a, const EnvBase& B, co
   const Team<T> tm;
   const Model md(mw);
   tm.sync();
-  if (tm.lane == 0) reinterpret_cast<int*>(w.at(w.L->misc))[11] = ok ? cache_tag<T>(exact) : 0;
+  if (tm.lane == 0) reinterpret_cast<int*>(w.at(w.L->misc))[11] = ok ? cache_tag<T>(w.L->ovf_g != 0, exact) : 0;
   tm.sync();
-  copy_position_terms<T>(tm, a.out.cache + (B.env + env) * w.L->total, w.b, *w.L, md.nv, md.m, w.b);
+  float* slot = a.out.cache + (B.env + env) * a.cache_stride;
+  // overflow rows: from the arena's scratch end, or already in this slot
+  copy_position_terms<T>(tm, slot, w.b, *w.L, md.nv, md.m, w.b, slot, w.L->ovf_g ? slot : w.b);
 }
 
 // Per-stage cycle accumulation (only when a profile buffer is passed): lane 0
@@ -387,6 +398,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   Ws w;
   w.L = sl;
   w.b = arena + (size_t)team * w.L->total;
+  if (sl->ovf_g) w.g = a.out.cache + (B.env + env) * a.cache_stride;
   const Layout& L = *w.L;
   const int nq = md.nq, nv = md.nv, nu = md.nu, ld = L.ldm;
   Prof pf(a.prof, active && tm.lane == 0);
@@ -485,7 +497,7 @@ __global__ void __launch_bounds__(512, 1) step_kernel(const StepArgs a) {
   Layout* shared_layout = reinterpret_cast<Layout*>(smem + al4(a.model_words));
   if (threadIdx.x == 0) {
     const int* w0 = a.model;
-    *shared_layout = layout_of(w0);
+    *shared_layout = layout_of(w0, a.ovf_global);
   }
   __syncthreads();
   const int team = threadIdx.x / T;

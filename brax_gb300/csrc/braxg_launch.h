@@ -27,6 +27,8 @@ struct StepArgs {
   const float* qd_in;
   const float* minv_in;
   const float* cache_in;   // position-level cache of the input state (or null)
+  long long cache_stride;  // words per env of the cache buffers
+  int ovf_global;          // Jacobian rows beyond the first 32 in the output cache (Layout::ovf_g)
   const float* act;
   long long act_step_stride;
   braxg_state out;

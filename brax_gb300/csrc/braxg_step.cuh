@@ -56,6 +56,9 @@ struct Layout {
   int prm;  // per-env parameters: friction [ncon], actuator gain, bias_q, bias_qd [nu each]
   int scr, scr_words, itmp;
   int total;
+  // 1: the Jacobian rows beyond jcap live outside the arena, at word jovf of
+  // the env's slot of the output state's cache (global memory)
+  int ovf_g;
 };
 
 __host__ __device__ inline int al4(int x) { return (x + 3) & ~3; }
@@ -86,7 +89,7 @@ constexpr int kMaxExplicitRows = 32;
 // matrix lives in scratch too (from CRBA to the inverse, and to the outputs),
 // except for models whose integrator solves with M itself (ns_iters == 0).
 __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim, int ns_iters,
-                                              int fluid = 0) {
+                                              int fluid = 0, int ovf_global = 0) {
   Layout L;
   const int m = 4 * ncon + nlim;
   L.ldm = nv | 1;  // odd leading dimension: conflict-free strided lane access
@@ -126,12 +129,13 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.raref = take(m);
   L.rmap = take(m);
   L.prm = take(ncon + 3 * nu);
-  const int ovf = (m - L.jcap) * L.ldj;  // overflow Jacobian rows at the scratch end
+  // overflow Jacobian rows: at the scratch end, or outside the arena
+  const int ovf = ovf_global ? 0 : (m - L.jcap) * L.ldj;
   const int nn = nv * L.ldm;
   // inverse temporaries: the sweep's rows (nv x explicit_lda(nv)), the
-  // Newton-Schulz iterates and residual (3 nv x ns_ldb(nv)), the integrator's
-  // factor pair (2 nv x ldm)
-  const int inv_tmp = imax(imax(2 * nn + 4, nv * explicit_lda(nv)), 3 * nv * ns_ldb(nv));
+  // Newton-Schulz iterates and residual (3 nv x ns_ldb(nv) up to 16 dofs,
+  // else 2 nv x ldm), the integrator's factor pair (2 nv x ldm)
+  const int inv_tmp = imax(imax(2 * nn + 4, nv * explicit_lda(nv)), nv <= 16 ? 3 * nv * ns_ldb(nv) : 0);
   // Scratch users, each with the regions it needs at once.  The mass matrix
   // (when it lives in scratch) must survive from CRBA to the inverse and to
   // the outputs, past the contacts of the Jacobian stage; two placements are
@@ -167,15 +171,16 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.scr = take(L.scr_words);
   if (!own_m) L.M = L.scr + m_off;
   L.itmp = L.scr + inv_off;
-  L.jovf = L.scr + L.scr_words - ovf;
   L.total = al4(o);
+  L.ovf_g = ovf_global ? 1 : 0;
+  L.jovf = ovf_global ? L.total : L.scr + L.scr_words - ovf;
   return L;
 }
 
 // Layout of a packed model descriptor (header words).
-__host__ __device__ inline Layout layout_of(const int* w) {
+__host__ __device__ inline Layout layout_of(const int* w, int ovf_global = 0) {
   return make_layout(w[BXM_H_NL], w[BXM_H_NQ], w[BXM_H_NV], w[BXM_H_NU], w[BXM_H_NCON], w[BXM_H_NLIM],
-                     w[BXM_H_NS_ITERS], w[BXM_H_FLUID]);
+                     w[BXM_H_NS_ITERS], w[BXM_H_FLUID], ovf_global);
 }
 static_assert(sizeof(Layout) <= kLayoutWords * 4, "Layout must fit its shared slot");
 
@@ -212,11 +217,13 @@ struct Team {
 struct Ws {
   float* b;
   const Layout* L;
+  float* g = nullptr;  // the env's slot of the output state's cache (overflow rows, L->ovf_g)
   __device__ __forceinline__ float* at(int off) const { return b + off; }
   // active constraint row r of the Jacobian (first jcap rows in their slot,
-  // the rest at the end of scratch)
+  // the rest at the end of scratch or in the env's cache slot)
   __device__ __forceinline__ float* jrow(int r) const {
-    return b + (r < L->jcap ? L->J + r * L->ldj : L->jovf + (r - L->jcap) * L->ldj);
+    if (r < L->jcap) return b + L->J + r * L->ldj;
+    return (L->ovf_g ? g : b) + L->jovf + (r - L->jcap) * L->ldj;
   }
 };
 
@@ -778,23 +785,27 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   float* M = w.at(L.M);
   float* P = w.at(L.Minv);
   float* S1 = w.at(L.itmp);
-  float* S2 = S1 + n * ld;
   if (n == 0) return true;
   if (exact) return spd_inverse_sweep<T>(tm, n, ld, M, S1, P);
   if (num_iter <= 0) return true;
-  // the iterates and residuals live in rows of stride lb (16-byte loads of
-  // every product's right-hand operand; columns n .. lb zero); M stays in
-  // place as the left-hand operand
-  const int lb = ns_ldb(n);
-  float* cur = S1;
-  float* nxt = S1 + n * lb;
-  float* R = S1 + 2 * n * lb;
-  for (int e = tm.lane; e < 3 * n * lb; e += T) {
-    const int i = e / lb, j = e - i * lb;  // rows of the three buffers in turn
-    S1[e] = (j < n && i < n) ? P[i * ld + j] : 0.f;
+  // Up to 16 dofs the iterates and residuals live in rows of stride lb
+  // (16-byte loads of every product's right-hand operand; columns n .. lb
+  // zero; three such n x lb buffers are small there).  Larger models keep
+  // the iterate in place and use the arena's stride (two n x ld buffers).
+  // M stays in place as the left-hand operand.
+  constexpr bool kRows4 = NVB <= 16;
+  const int lb = kRows4 ? ns_ldb(n) : ld;
+  float* cur = kRows4 ? S1 : P;
+  float* nxt = kRows4 ? S1 + n * lb : S1 + n * ld;
+  float* R = kRows4 ? S1 + 2 * n * lb : S1;
+  if (kRows4) {
+    for (int e = tm.lane; e < 3 * n * lb; e += T) {
+      const int i = e / lb, j = e - i * lb;  // rows of the three buffers in turn
+      S1[e] = (j < n && i < n) ? P[i * ld + j] : 0.f;
+    }
+    tm.sync();
   }
-  tm.sync();
-  matmul<T, NVB>(tm, n, M, ld, cur, lb, R, lb, 1, true);  // r0 = I - A A_inv
+  matmul<T, NVB>(tm, n, M, ld, cur, lb, R, lb, 1, kRows4);  // r0 = I - A A_inv
   float nr0 = safe_norm_mat<T>(tm, n, lb, R);
   if (nr0 > 1.f) {  // reset to 0.5 A^T / tr(A A^T) (r0 is kept, as the reference does)
     if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] += 1;
@@ -811,8 +822,8 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   }
   float err = 1.f;
   for (int it = 0; it < num_iter; ++it) {
-    matmul<T, NVB>(tm, n, cur, lb, R, lb, nxt, lb, 2, true);  // a_inv (I + r)
-    matmul<T, NVB>(tm, n, M, ld, nxt, lb, R, lb, 1, true);    // I - a a_inv_next
+    matmul<T, NVB>(tm, n, cur, lb, R, lb, nxt, lb, 2, kRows4);  // a_inv (I + r)
+    matmul<T, NVB>(tm, n, M, ld, nxt, lb, R, lb, 1, kRows4);    // I - a a_inv_next
     float e = safe_norm_mat<T>(tm, n, lb, R);
     if (e < err) {
       float* t = cur;
@@ -821,9 +832,11 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
     }
     err = e;
   }
-  for (int j = tm.lane; j < n; j += T)
-    for (int i = 0; i < n; ++i) P[i * ld + j] = cur[i * lb + j];
-  tm.sync();
+  if (cur != P) {
+    for (int j = tm.lane; j < n; j += T)
+      for (int i = 0; i < n; ++i) P[i * ld + j] = cur[i * lb + j];
+    tm.sync();
+  }
   return true;
 }
 

@@ -94,7 +94,10 @@ typedef struct {
    * and whose cache was computed with the same threads_per_env (exact-inverse
    * mode: and an exact mass_mx_inv); other envs recompute them, so the result
    * is the same either way.  The cache belongs to the model that wrote it.
-   * The braxg_batch_* calls neither read nor write it. */
+   * For models with more than 32 constraint rows whose arena that saves
+   * shared memory, the output's cache also holds the step's Jacobian rows
+   * beyond the first 32 while it runs (so more envs fit per CTA).  The
+   * braxg_batch_* calls neither read nor write it. */
   float* cache;
 } braxg_state;
 
@@ -349,8 +352,9 @@ int braxg_batch_rollout(const braxg_batch* batch, void* stream, int n_steps,
                         float* traj_q, float* traj_qd, const braxg_options* opt);
 
 /* Launch shape a braxg_init / braxg_step / braxg_rollout / braxg_env_rollout
- * call of n_env envs takes for this model (n_env 0: the largest CTA): lanes
- * per env, envs per CTA, dynamic shared memory bytes per CTA. */
+ * call of n_env envs takes for this model (n_env 0: the largest CTA) when its
+ * output state carries a cache (see braxg_state.cache): lanes per env, envs
+ * per CTA, dynamic shared memory bytes per CTA. */
 int braxg_launch_shape(const braxg_model* model, const braxg_options* opt, int n_env,
                        int32_t* threads_per_env, int32_t* envs_per_cta,
                        int32_t* smem_bytes);
