@@ -122,8 +122,7 @@ __device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, 
   const Model md(mw);
   const float* slot = a.cache_in + (B.env + env) * a.cache_stride;
   // overflow rows: into the arena, or from the input's cache slot to the output's
-  float* out_slot = w.L->ovf_g ? a.out.cache + (B.env + env) * a.cache_stride : w.b;
-  copy_position_terms<T>(tm, w.b, slot, *w.L, md.nv, md.m, w.b, out_slot, slot);
+  copy_position_terms<T>(tm, w.b, slot, *w.L, md.nv, md.m, w.b, w.L->ovf_g ? w.g : w.b, slot);
   tm.sync();
   const int tag = reinterpret_cast<const int*>(w.at(w.L->misc))[11];
   const int want = cache_tag<T>(w.L->ovf_g != 0, true);
@@ -393,14 +392,13 @@ __device__ __noinline__ void task_outputs(const StepArgs& a, const int* mw, Ws w
 // false) still take every CTA barrier and return before the outputs.
 template <int T, int NVB, bool TASK = false>
 __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, const int* smem, const Layout* sl,
-                                         float* arena, int team, long long env, bool active, int n_frames,
-                                         float* ovf0, long long ovf_stride, int ovf_off) {
+                                         float* arena, int team, long long env, bool active, int n_frames) {
   const Model md(smem);
   const Team<T> tm;
   Ws w;
   w.L = sl;
   w.b = arena + (size_t)team * w.L->total;
-  if (sl->ovf_g) w.g = ovf0 + env * ovf_stride + ovf_off;  // the env's overflow Jacobian rows (global)
+  if (sl->ovf_g) w.g = a.out.cache + (B.env + env) * a.cache_stride;
   const Layout& L = *w.L;
   const int nq = md.nq, nv = md.nv, nu = md.nu, ld = L.ldm;
   Prof pf(a.prof, active && tm.lane == 0);
@@ -509,9 +507,7 @@ __global__ void __launch_bounds__(512, 1) step_kernel(const StepArgs a) {
   if (!active) env = 0;
   const EnvBase B{};
   float* arena = reinterpret_cast<float*>(smem + al4(a.model_words) + kLayoutWords);
-  // overflow rows (a.ovf_global): in each env's output cache slot, after the arena's copy
-  run_team<T, NVB, TASK>(a, B, smem, shared_layout, arena, team, env, active, a.n_frames, a.out.cache,
-                         a.cache_stride, shared_layout->jovf);
+  run_team<T, NVB, TASK>(a, B, smem, shared_layout, arena, team, env, active, a.n_frames);
 }
 
 constexpr int kMaxSmemBytes = 227 * 1024;

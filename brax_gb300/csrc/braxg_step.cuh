@@ -56,8 +56,8 @@ struct Layout {
   int prm;  // per-env parameters: friction [ncon], actuator gain, bias_q, bias_qd [nu each]
   int scr, scr_words, itmp;
   int total;
-  // 1: the Jacobian rows beyond jcap live outside the arena in global memory
-  // (in a cache slot they sit at word jovf, after the arena's copy)
+  // 1: the Jacobian rows beyond jcap live outside the arena, at word jovf of
+  // the env's slot of the output state's cache (global memory)
   int ovf_g;
 };
 
@@ -217,13 +217,13 @@ struct Team {
 struct Ws {
   float* b;
   const Layout* L;
-  float* g = nullptr;  // the env's overflow Jacobian rows in global memory (L->ovf_g)
+  float* g = nullptr;  // the env's slot of the output state's cache (overflow rows, L->ovf_g)
   __device__ __forceinline__ float* at(int off) const { return b + off; }
   // active constraint row r of the Jacobian (first jcap rows in their slot,
-  // the rest at the end of scratch or in global memory)
+  // the rest at the end of scratch or in the env's cache slot)
   __device__ __forceinline__ float* jrow(int r) const {
     if (r < L->jcap) return b + L->J + r * L->ldj;
-    return (L->ovf_g ? g : b + L->jovf) + (r - L->jcap) * L->ldj;
+    return (L->ovf_g ? g : b) + L->jovf + (r - L->jcap) * L->ldj;
   }
 };
 

@@ -33,12 +33,12 @@ __device__ __forceinline__ void batch_item(const BatchArgs& ba, const BatchItem&
   const long long env = active ? (long long)it.env0 + team : it.env0;
   const int nf = g.n_frames;
   if (T == 16) {
-    if (g.nvb == 16) run_team<16, 16>(ba.s, g.base, smem, sl, arena, team, env, active, nf, nullptr, 0, 0);
-    else run_team<16, 32>(ba.s, g.base, smem, sl, arena, team, env, active, nf, nullptr, 0, 0);
+    if (g.nvb == 16) run_team<16, 16>(ba.s, g.base, smem, sl, arena, team, env, active, nf);
+    else run_team<16, 32>(ba.s, g.base, smem, sl, arena, team, env, active, nf);
   } else {
-    if (g.nvb == 16) run_team<32, 16>(ba.s, g.base, smem, sl, arena, team, env, active, nf, nullptr, 0, 0);
-    else if (g.nvb == 32) run_team<32, 32>(ba.s, g.base, smem, sl, arena, team, env, active, nf, nullptr, 0, 0);
-    else run_team<32, 64>(ba.s, g.base, smem, sl, arena, team, env, active, nf, nullptr, 0, 0);
+    if (g.nvb == 16) run_team<32, 16>(ba.s, g.base, smem, sl, arena, team, env, active, nf);
+    else if (g.nvb == 32) run_team<32, 32>(ba.s, g.base, smem, sl, arena, team, env, active, nf);
+    else run_team<32, 64>(ba.s, g.base, smem, sl, arena, team, env, active, nf);
   }
 }
 
