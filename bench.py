@@ -39,6 +39,9 @@ sys.path.insert(0, ROOT)
 METRIC = 'env-steps/s fwd & fwd+adjoint, 4096-env quadruped, 1 GB300, at 1e-5 rel err'
 WORKLOAD = 'quadruped'
 N_FRAMES = 5
+# what each --inverse choice runs (the bench line names the algorithm)
+INVERSE_NAMES = {'cholesky': 'exact (symmetric sweep inverse; Cholesky pivots)',
+                 'newton_schulz': 'newton_schulz (the reference algorithm, K from the model)'}
 
 
 def parse(argv=None):
@@ -372,7 +375,7 @@ def run_braxg(args):
     e1.synchronize()
     t_other += e0.elapsed_time(e1) / 1e3
   t_other = max_over_ranks(t_other, dev)
-  other_mode = {'inverse_mode': 'newton_schulz' if other == pipeline.NEWTON_SCHULZ else 'cholesky',
+  other_mode = {'inverse_mode': INVERSE_NAMES['newton_schulz' if other == pipeline.NEWTON_SCHULZ else 'cholesky'],
                 'value': round(whole_job_rate(args.steps * n, world, t_other), 1),
                 'ms_per_step': round(1e3 * t_other / args.steps, 4)}
   value = whole_job_rate(args.steps * n, world, t_total)
@@ -437,9 +440,10 @@ def run_braxg(args):
   nmv = load_nmv()[WORKLOAD]
   f_step, b_step = algorithmic(sys_, nmv['mean_matvecs_per_step'], args.inverse == 'newton_schulz')
   # the state cache: its position-term spans read at the launch start and
-  # written at its end (active constraint rows past the first 32 not counted)
+  # written at its end (active constraint rows past the first 32 not counted);
+  # overhead traffic of this implementation, not algorithmic bytes
   b_cache = 2 * 4 * model.cache_span[0] if args.state_cache else 0
-  b_launch = (b_step + b_cache) * n
+  b_launch = b_step * n
   launch_s = t_total / args.steps
   flops_launch = f_step * N_FRAMES * n
   achieved = flops_launch / launch_s / 1e12
@@ -452,7 +456,11 @@ def run_braxg(args):
     pass
   sm_max = peaks.get('sm_max_mhz', 2070.0)
   peak_fp32 = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
-  hbm_peak = peaks.get('hbm_gbs', 6800.0)
+  hbm_peak = peaks.get('hbm_gbs')
+  hbm_src = 'MEASURED_PEAKS.json hbm_gbs (of measured)'
+  if hbm_peak is None:
+    hbm_peak, hbm_src = 6800.0, 'no MEASURED_PEAKS.json: 6.8 TB/s (of fallback, an earlier GB300 copy measurement)'
+  achieved_gbs = b_launch / launch_s / 1e9
   roofline = {
       'bound': 'fp32', 'achieved': round(achieved, 3), 'peak': round(peak_fp32, 1),
       'unit': 'TFLOP/s', 'frac': round(achieved / peak_fp32, 4),
@@ -460,10 +468,13 @@ def run_braxg(args):
       'peak_source': (f'nominal FP32 CUDA-core peak ({props.multi_processor_count} SMs x 128 '
                       f'FMA/clk x 2 x {sm_max:.0f} MHz); MEASURED_PEAKS.json has no FP32 figure'),
       'flops_per_launch': flops_launch,
-      'hbm': {'achieved_gbs': round(b_launch / launch_s / 1e9, 2), 'peak_gbs': hbm_peak,
-              'frac': round(b_launch / launch_s / 1e9 / hbm_peak, 5),
-              'bytes_per_launch': b_launch, 'state_bytes_per_env': b_step, 'cache_bytes_per_env': b_cache,
-              'peak_source': 'MEASURED_PEAKS.json hbm_gbs (of measured)'},
+      'hbm': {'achieved_gbs': round(achieved_gbs, 2), 'peak_gbs': hbm_peak,
+              'frac': round(achieved_gbs / hbm_peak, 5),
+              'algorithmic_bytes_per_launch': b_launch, 'state_bytes_per_env': b_step,
+              'overhead': {'cache_bytes_per_env': b_cache, 'cache_bytes_per_launch': b_cache * n,
+                           'note': 'position-term cache restore + store: traffic of this design, '
+                                   'not algorithmic bytes; included in roofline.traffic'},
+              'peak_source': hbm_src},
   }
   clocks = clk.summary()
   adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank)
@@ -476,7 +487,7 @@ def run_braxg(args):
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded resets and U(-1,1) actions)',
       'config': {**workload_config(n, world),
-                 'inverse_mode': args.inverse,
+                 'inverse_mode': INVERSE_NAMES[args.inverse],
                  'state_cache': bool(args.state_cache),
                  'l2': 'flushed (256 MB write) before every timed step',
                  'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),

@@ -130,12 +130,14 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
   int smem = head + epc * env_bytes;
   int grid = (n_env + epc - 1) / epc;
   int cur = 0;
-  cudaGetDevice(&cur);
-  if (cur != m->device) cudaSetDevice(m->device);
-  cudaError_t e = m->dims.nv <= 16 ? braxg::launch_vjp<32, 16>(a, grid, smem, static_cast<cudaStream_t>(stream))
-                                   : braxg::launch_vjp<32, 32>(a, grid, smem, static_cast<cudaStream_t>(stream));
-  if (cur != m->device) cudaSetDevice(cur);
+  cudaError_t e = cudaGetDevice(&cur);
+  if (e == cudaSuccess && cur != m->device) e = cudaSetDevice(m->device);
+  if (e != cudaSuccess) return cuda_fail(e, "selecting the model's device");
+  e = m->dims.nv <= 16 ? braxg::launch_vjp<32, 16>(a, grid, smem, static_cast<cudaStream_t>(stream))
+                       : braxg::launch_vjp<32, 32>(a, grid, smem, static_cast<cudaStream_t>(stream));
+  const cudaError_t back = cur != m->device ? cudaSetDevice(cur) : cudaSuccess;
   if (e != cudaSuccess) return cuda_fail(e, "gradient kernel launch");
+  if (back != cudaSuccess) return cuda_fail(back, "restoring the current device");
   braxg::host::set_launches(1);
   return BRAXG_OK;
 }
@@ -145,6 +147,9 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
 // braxg_rollout_vjp lives in one fixed device array of this library, so the
 // caller passes only its inputs and outputs and nothing here allocates.  Each
 // device that loads the library holds the array until the process exits.
+// The array's device address is looked up once per device and kept for the
+// process: cudaDeviceReset destroys the context that address belongs to, so
+// after a reset this entry point (like every model handle) must not be used.
 // ---------------------------------------------------------------------------
 static constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB
 static __device__ __align__(256) unsigned char g_vjp_scratch[kNoAllocScratchBytes];
@@ -174,12 +179,14 @@ int braxg_rollout_vjp_noalloc(const braxg_model* m, void* stream, int n_env, int
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (g_scratch_addr[m->device] == nullptr) {
       int cur = 0;
-      cudaGetDevice(&cur);
-      cudaError_t e = cudaSetDevice(m->device);
+      cudaError_t e = cudaGetDevice(&cur);
+      if (e != cudaSuccess) return cuda_fail(e, "braxg_rollout_vjp_noalloc: cudaGetDevice");
+      e = cudaSetDevice(m->device);
       void* addr = nullptr;
       if (e == cudaSuccess) e = cudaGetSymbolAddress(&addr, g_vjp_scratch);
-      cudaSetDevice(cur);
+      const cudaError_t back = cudaSetDevice(cur);
       if (e != cudaSuccess) return cuda_fail(e, "braxg_rollout_vjp_noalloc: cudaGetSymbolAddress");
+      if (back != cudaSuccess) return cuda_fail(back, "braxg_rollout_vjp_noalloc: restoring the current device");
       g_scratch_addr[m->device] = addr;
     }
     scratch = g_scratch_addr[m->device];

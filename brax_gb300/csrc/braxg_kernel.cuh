@@ -518,14 +518,12 @@ constexpr int kMaxSmemBytes = 227 * 1024;
 template <int T, int NVB, bool TASK>
 cudaError_t launch_step_variant(const StepArgs& a, int grid, int smem, cudaStream_t st) {
   auto k = step_kernel<T, NVB, TASK>;
-  static bool attr_set[64] = {false};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 64 && !attr_set[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr_set[dev] = true;
-  }
+  static SmemOptIn opt_in;
+  cudaError_t e = opt_in.ensure(k, [](int* b) {
+    *b = kMaxSmemBytes;
+    return cudaSuccess;
+  });
+  if (e != cudaSuccess) return e;
   k<<<grid, a.envs_per_cta * T, smem, st>>>(a);
   return cudaGetLastError();
 }

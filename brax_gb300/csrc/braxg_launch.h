@@ -3,9 +3,42 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "braxg.h"
 
 namespace braxg {
+
+// Device ordinals a kernel's one-time attribute set-up tracks.
+constexpr int kMaxDevices = 64;
+
+// One kernel's opt-in to more than 48 KB of dynamic shared memory, set once
+// per device (the attribute is per device context) under a lock, so that
+// first launches from several host threads do not race.  A device ordinal at
+// or above kMaxDevices is refused with cudaErrorInvalidDevice rather than
+// launched without the attribute.
+class SmemOptIn {
+ public:
+  // `bytes(int*)` computes the attribute's value (called once per device).
+  template <class K, class F>
+  cudaError_t ensure(K kernel, F bytes) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(mu_);
+    if (done_[dev]) return cudaSuccess;
+    int b = 0;
+    e = bytes(&b);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    if (e == cudaSuccess) done_[dev] = true;
+    return e;
+  }
+
+ private:
+  std::mutex mu_;
+  bool done_[kMaxDevices] = {};
+};
 
 // Element offsets of a model group's first env inside flat (concatenated)
 // batch arrays, one per per-env size class (q: nq, v: nv, vv: nv^2, l: nl,

@@ -270,14 +270,12 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
 template <int T, int NVB>
 cudaError_t launch_vjp(const VjpArgs& a, int grid, int smem, cudaStream_t st) {
   auto k = vjp_kernel<T, NVB>;
-  static bool attr_set[64] = {false};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 64 && !attr_set[dev]) {
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr_set[dev] = true;
-  }
+  static SmemOptIn opt_in;
+  cudaError_t e = opt_in.ensure(k, [](int* b) {
+    *b = kMaxSmemBytes;
+    return cudaSuccess;
+  });
+  if (e != cudaSuccess) return e;
   k<<<grid, a.envs_per_cta * T, smem, st>>>(a);
   return cudaGetLastError();
 }

@@ -66,17 +66,10 @@ static cudaError_t batch_smem_limit(int* limit) {
 }
 
 cudaError_t launch_batch_kernel(const BatchArgs& a, int grid, int block, int smem, cudaStream_t st) {
-  static bool attr_set[64] = {false};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev < 64 && !attr_set[dev]) {
-    int limit = 0;
-    cudaError_t e = batch_smem_limit(&limit);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, limit);
-    if (e != cudaSuccess) return e;
-    attr_set[dev] = true;
-  }
-  cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(int), st);
+  static SmemOptIn opt_in;
+  cudaError_t e = opt_in.ensure(batch_kernel, batch_smem_limit);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(a.counter, 0, sizeof(int), st);
   if (e != cudaSuccess) return e;
   batch_kernel<<<grid, block, smem, st>>>(a);
   return cudaGetLastError();

@@ -276,7 +276,9 @@ int braxg_rollout_vjp(const braxg_model* model, void* stream, int n_env, int n_s
  * (braxg_rollout_vjp_workspace) fail with BRAXG_ERR_INVALID.  Nothing is
  * allocated or freed.  The first call on a device looks up the array's device
  * address with that device current, so make one call on each device before
- * any stream capture.  All calls share the one array: calls that overlap on
+ * any stream capture; the address is kept for the process, so after
+ * cudaDeviceReset (which also invalidates every model handle) the entry point
+ * must not be called again.  All calls share the one array: calls that overlap on
  * the GPU (different streams, or different threads without ordering) race on
  * it and corrupt each other's gradients.  No counterpart in the reference: it
  * exists only for callers that cannot allocate. */
@@ -297,7 +299,14 @@ int braxg_rollout_vjp_noalloc(const braxg_model* model, void* stream, int n_env,
  *
  * State arrays are flat: model g's envs occupy one contiguous run of every
  * field, starting at braxg_batch_get_offsets(batch, g) in units of that field's
- * per-env size class; the offsets of index n_models are the totals. */
+ * per-env size class; the offsets of index n_models are the totals.
+ *
+ * Calls on ONE batch must be stream-ordered (one stream, or streams ordered
+ * by events; a replay of a captured graph counts as a call): every launch
+ * zeroes and then draws work items from the batch's one device counter, so
+ * two launches of the same batch running at the same time skip or repeat
+ * each other's items and give wrong results with no error.  Different
+ * batches are independent. */
 typedef struct braxg_batch braxg_batch;
 
 /* Launch shape for the models with nv <= nv_max (the first matching entry

@@ -7,9 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
   sys.path.insert(0, ROOT)
 
-# Location of the reference checkout; only CPU-side golden tests read its
-# fixture models, and they skip when it is absent.
-REF = os.environ.get('BRAXG_REFERENCE', '/root/reference')
+# Location of the reference checkout (brax 0.14.2): $BRAXG_REFERENCE, else a
+# checkout named `reference` beside this repository.  Only CPU-side golden
+# tests read its fixture models, and they skip when it is absent.
+REF = os.environ.get('BRAXG_REFERENCE') or os.path.join(os.path.dirname(ROOT), 'reference')
 
 
 def pytest_configure(config):

@@ -1,0 +1,241 @@
+"""Parity of the benchmarked launches.
+
+Each workload configuration is stepped by exactly the launch the benchmark
+times: the same env count, frames per env step, default launch shape and
+inverse mode, with the state's position-term cache carried from the previous
+launch.  The input is the state the GPU reached after warm-up env steps from
+the seeded resets (in contact for the legged models).  The test compares
+q / qd after that one env step with the oracle run on the same FP32 inputs
+(q, qd and, in Newton-Schulz mode, the carried mass_mx_inv):
+
+* quadruped: 4096 envs, 5 x 0.01 s, 10 warm-up env steps (the bench's);
+* chain3: 128 envs, 1 x 0.01 s, zero actions;
+* humanoid-like: 16384 envs, 5 x 0.003 s (oracle on every 16th env);
+* the uneven batch: 8192 envs of 33 models in one persistent launch (oracle
+  on every chain env, every 4th quadruped and every 4th humanoid-like env).
+
+The bar, with rel_err per env = max |a - b| / max(max |b|, 1):
+
+* p99 over envs of the GPU's error against the FP32 oracle <= 1e-5 wherever
+  the configuration's FP32 result is well conditioned (the chain, the
+  quadruped, chains up to 12 links);
+* every env: error <= max(1e-5, 10 x s_env).  s_env is the env's FP32
+  sensitivity: the largest change of the FP32 oracle's own result when its
+  FP32 inputs move by one ulp (three random draws).  An env whose FP32 result
+  moves by s_env under a one-ulp change of its inputs cannot be held closer
+  than about s_env by an FP32 evaluation in another operation order (the
+  projected-gradient line search takes accept / reject decisions on nearly
+  equal FP32 values); each env above 1e-5 is printed with its s_env;
+* ill-conditioned configurations (the humanoid-like model, cond(M) ~ 6.5e3,
+  and chains longer than 12 links): p99 of the error <= 3 x p99 of s_env.
+
+The error against the FP64 oracle is printed beside the FP32 oracle's own.
+"""
+
+import numpy as np
+import pytest
+
+from tests.parity_util import load, rel_err
+
+torch = pytest.importorskip('torch')
+pytestmark = pytest.mark.gpu
+
+# the FP32 oracle's one-ulp sensitivity is estimated over this many draws
+SENS_DRAWS = 3
+
+
+def _setup():
+  if not torch.cuda.is_available():
+    pytest.skip('no CUDA device')
+  from brax_gb300 import pipeline
+  return pipeline
+
+
+def _np(x):
+  return x.detach().cpu().numpy()
+
+
+def _nudge(x, rng):
+  """x with every entry moved by -1, 0 or +1 ulp (FP32)."""
+  x = np.asarray(x, np.float32)
+  d = rng.integers(-1, 2, x.shape)
+  up = np.nextafter(x, np.float32(np.inf))
+  dn = np.nextafter(x, np.float32(-np.inf))
+  return np.where(d > 0, up, np.where(d < 0, dn, x)).astype(np.float32)
+
+
+def oracle_check(sys, q, qd, minv, act, n_frames, exact, got_q, got_qd, label, well_conditioned):
+  """One env step of the FP32 and FP64 oracles from the GPU's FP32 inputs;
+  asserts the bar of this module on the GPU's q / qd and returns the stats."""
+  from oracle.pipeline import Oracle
+  o32 = Oracle(sys, np.float32, exact_inverse=exact)
+  o64 = Oracle(sys, np.float64, exact_inverse=exact)
+  mi = None if exact else minv
+  r32 = o32.env_step(o32.restore(q, qd, mi), act.astype(np.float32), n_frames)
+  r64 = o64.env_step(o64.restore(q.astype(np.float64), qd.astype(np.float64),
+                                 None if exact else minv.astype(np.float64)),
+                     act.astype(np.float64), n_frames)
+  rng = np.random.default_rng(12345)
+  sens = {'q': np.zeros(q.shape[0]), 'qd': np.zeros(q.shape[0])}
+  for _ in range(SENS_DRAWS):
+    rp = o32.env_step(o32.restore(_nudge(q, rng), _nudge(qd, rng), mi), act.astype(np.float32), n_frames)
+    for f in sens:
+      sens[f] = np.maximum(sens[f], rel_err(getattr(rp, f), getattr(r32, f)))
+  stats = {}
+  for f, g in (('q', got_q), ('qd', got_qd)):
+    e32 = rel_err(g, getattr(r32, f))
+    e64 = rel_err(g, getattr(r64, f))
+    eo = rel_err(getattr(r32, f), getattr(r64, f))
+    s = sens[f]
+    st = {'gpu_vs_fp32_p50': float(np.median(e32)), 'gpu_vs_fp32_p99': float(np.quantile(e32, 0.99)),
+          'gpu_vs_fp32_max': float(e32.max()), 'gpu_vs_fp64_p99': float(np.quantile(e64, 0.99)),
+          'fp32_oracle_vs_fp64_p99': float(np.quantile(eo, 0.99)),
+          'fp32_sensitivity_p99': float(np.quantile(s, 0.99))}
+    stats[f] = st
+    print(f'{label} {f}: vs fp32 p50 {st["gpu_vs_fp32_p50"]:.2e} p99 {st["gpu_vs_fp32_p99"]:.2e} '
+          f'max {st["gpu_vs_fp32_max"]:.2e} | vs fp64 p99 {st["gpu_vs_fp64_p99"]:.2e} '
+          f'(fp32 oracle {st["fp32_oracle_vs_fp64_p99"]:.2e}) | fp32 one-ulp sensitivity p99 '
+          f'{st["fp32_sensitivity_p99"]:.2e}')
+    out = np.nonzero(e32 > 1e-5)[0]
+    for i in out[np.argsort(-e32[out])][:12]:
+      print(f'  env {i}: vs fp32 {e32[i]:.2e}, fp32 one-ulp sensitivity {s[i]:.2e}, vs fp64 {e64[i]:.2e}, '
+            f'fp32 oracle vs fp64 {eo[i]:.2e}')
+    bad = e32 > np.maximum(1e-5, 10 * s)
+    assert not bad.any(), (label, f, np.nonzero(bad)[0][:10], e32[bad][:10], s[bad][:10])
+    if well_conditioned:
+      assert st['gpu_vs_fp32_p99'] <= 1e-5, (label, f, st)
+    else:
+      assert st['gpu_vs_fp32_p99'] <= max(1e-5, 3 * st['fp32_sensitivity_p99']), (label, f, st)
+  return stats
+
+
+def _single_model(P, name, n, n_frames, warmup, mode, act_fn, reset_fn, sample):
+  """Runs `warmup` env steps then the benched launch; returns the inputs and
+  outputs of that launch (numpy) for the envs in `sample`."""
+  sys = load(name)
+  dev = torch.device('cuda')
+  q0, qd0 = reset_fn(sys, n)
+  rng = np.random.default_rng(77)
+  acts = [act_fn(sys, n, rng).astype(np.float32) for _ in range(warmup + 1)]
+  m = P.model_for(sys, dev)
+  a = P.init(sys, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev), cache=True)
+  b = P._alloc(m, n, False, dev, cache=True)
+  for k in range(warmup):
+    P.step(sys, a, torch.tensor(acts[k], device=dev), n_frames=n_frames, inverse_mode=mode, out=b)
+    a, b = b, a
+  torch.cuda.synchronize()
+  assert (_np(a.status) == 0).mean() > 0.99
+  q, qd, minv = _np(a.q), _np(a.qd), _np(a.mass_mx_inv)
+  # the benched launch: default shape, cache carried from the previous launch
+  P.step(sys, a, torch.tensor(acts[warmup], device=dev), n_frames=n_frames, inverse_mode=mode, out=b)
+  torch.cuda.synchronize()
+  ok = (_np(b.status) == 0) & (_np(a.status) == 0)
+  sel = sample[ok[sample]]
+  return sys, q[sel], qd[sel], minv[sel], acts[warmup][sel], _np(b.q)[sel], _np(b.qd)[sel]
+
+
+def _legged_reset(sys, n, seed=1234):
+  rng = np.random.default_rng(seed)
+  q = (sys.init_q + rng.uniform(-0.1, 0.1, (n, sys.q_size()))).astype(np.float32)
+  qd = (0.1 * rng.normal(size=(n, sys.qd_size()))).astype(np.float32)
+  return q, qd
+
+
+def _humanoid_reset(sys, n, seed=700):
+  rng = np.random.default_rng(seed)
+  q = (sys.init_q + rng.uniform(-0.01, 0.01, (n, sys.q_size()))).astype(np.float32)
+  q[:, 3:7] /= np.linalg.norm(q[:, 3:7], axis=1, keepdims=True)
+  qd = (0.01 * rng.normal(size=(n, sys.qd_size()))).astype(np.float32)
+  return q, qd
+
+
+def _chain_reset(sys, n, seed=0):
+  rng = np.random.default_rng(seed)
+  q = rng.uniform(-np.pi / 4, np.pi / 4, (n, sys.q_size())).astype(np.float32)
+  qd = rng.normal(0, 0.1, (n, sys.qd_size())).astype(np.float32)
+  return q, qd
+
+
+def _uniform_act(sys, n, rng):
+  return rng.uniform(-1, 1, (n, sys.act_size()))
+
+
+def _humanoid_act(sys, n, rng):
+  return np.clip(rng.normal(0, 0.3, (n, sys.act_size())), -1, 1)
+
+
+def _zero_act(sys, n, rng):
+  return np.zeros((n, sys.act_size()))
+
+
+MODES = ['cholesky', 'newton_schulz']
+
+
+@pytest.mark.parametrize('mode', MODES)
+def test_quadruped_4096_benched_launch(mode):
+  P = _setup()
+  inv = P.CHOLESKY if mode == 'cholesky' else P.NEWTON_SCHULZ
+  n = 4096
+  sys, q, qd, minv, act, gq, gqd = _single_model(P, 'quadruped', n, 5, 10, inv, _uniform_act, _legged_reset,
+                                                 np.arange(n))
+  oracle_check(sys, q, qd, minv, act, 5, mode == 'cholesky', gq, gqd, f'quadruped 4096 {mode}', True)
+
+
+@pytest.mark.parametrize('mode', MODES)
+def test_chain3_128_benched_launch(mode):
+  P = _setup()
+  inv = P.CHOLESKY if mode == 'cholesky' else P.NEWTON_SCHULZ
+  n = 128
+  sys, q, qd, minv, act, gq, gqd = _single_model(P, 'chain3', n, 1, 10, inv, _zero_act, _chain_reset,
+                                                 np.arange(n))
+  oracle_check(sys, q, qd, minv, act, 1, mode == 'cholesky', gq, gqd, f'chain3 128 {mode}', True)
+
+
+@pytest.mark.parametrize('mode', MODES)
+def test_humanoid_like_16384_benched_launch(mode):
+  P = _setup()
+  inv = P.CHOLESKY if mode == 'cholesky' else P.NEWTON_SCHULZ
+  n = 16384
+  sys, q, qd, minv, act, gq, gqd = _single_model(P, 'humanoid_like', n, 5, 3, inv, _humanoid_act,
+                                                 _humanoid_reset, np.arange(0, n, 16))
+  oracle_check(sys, q, qd, minv, act, 5, mode == 'cholesky', gq, gqd, f'humanoid-like 16384 {mode}', False)
+
+
+@pytest.mark.parametrize('mode', MODES)
+def test_uneven_8192_benched_launch(mode):
+  """The uneven batch's persistent launch (default shapes) for one env step
+  after 8 warm-up env steps, every model against the oracle."""
+  P = _setup()
+  from brax_gb300 import workloads as W
+  from brax_gb300.batch import Batch
+  inv = P.CHOLESKY if mode == 'cholesky' else P.NEWTON_SCHULZ
+  mix = W.uneven_mix(8192, seed=0)
+  systems, n_env, n_frames = [m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix]
+  b = Batch(systems, n_env, n_frames, device=torch.device('cuda'))
+  rng = np.random.default_rng(900)
+  warmup = 8
+  qs, qds, acts = [], [], []
+  for s, n, _ in mix:
+    q, qd = W.reset(s, n, rng)
+    qs.append(q)
+    qds.append(qd)
+    acts.append(np.stack([W.actions(s, n, rng) for _ in range(warmup + 1)]).astype(np.float32))
+  table = b.concat_steps(acts, 'act')
+  s0 = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
+  s1, _ = b.rollout(s0, table[:warmup], inverse_mode=inv)
+  s2, _ = b.rollout(s1, table[warmup:warmup + 1], inverse_mode=inv)
+  torch.cuda.synchronize()
+  ins = [b.split(getattr(s1, f), f) for f in ('q', 'qd', 'mass_mx_inv', 'status')]
+  outs = [b.split(getattr(s2, f), f) for f in ('q', 'qd', 'status')]
+  for g, (s, n, nf) in enumerate(mix):
+    fam = W.family(s)
+    step = 1 if fam == 'chain' else 4
+    ok = (_np(ins[3][g]) == 0) & (_np(outs[2][g]) == 0)
+    sel = np.arange(0, n, step)
+    sel = sel[ok[sel]]
+    assert len(sel) >= 0.9 * len(np.arange(0, n, step)), (s.name, ok.mean())
+    nl = s.num_links()
+    well = fam == 'quadruped' or (fam == 'chain' and nl <= 12)
+    oracle_check(s, _np(ins[0][g])[sel], _np(ins[1][g])[sel], _np(ins[2][g])[sel], acts[g][warmup][sel], nf,
+                 mode == 'cholesky', _np(outs[0][g])[sel], _np(outs[1][g])[sel],
+                 f'uneven {s.name} x{len(sel)} {mode}', well)

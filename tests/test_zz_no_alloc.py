@@ -4,13 +4,14 @@ Some callers cannot allocate device memory (an XLA custom call without the
 scratch allocator, a plugin inside a framework that owns every allocation, a
 control loop that must stay out of the CUDA allocator).  For them the library
 keeps the gradient's checkpoint scratch in one fixed device array.  This test
-calls that entry point through the C ABI, twice in a row, and checks each
-result against braxg_rollout_vjp given a caller-allocated workspace, within
-the single-step gradient tolerance of tests/test_gpu_adjoint.py (2e-3
-relative); the two entry points run the same kernel, so the results agree far
-more closely.  It also checks that an oversized request is refused with a
-clear error.  This file is collected last on purpose, and passes on its own
-in a fresh process as well.
+calls that entry point through the C ABI, twice in a row, and checks that
+each result equals, bit for bit, braxg_rollout_vjp given a caller-allocated
+workspace: the two entry points run the same kernel, and the gradient does
+not depend on how many segments the workspace keeps resident (the fixed
+array holds more than the smallest workspace), so any difference would be a
+wrong scratch offset or stale scratch contents.  It also checks that an
+oversized request is refused with a clear error.  This file is collected
+last on purpose, and passes on its own in a fresh process as well.
 """
 
 import ctypes
@@ -30,12 +31,6 @@ def _setup():
   from brax_gb300 import _native as N
   from brax_gb300 import pipeline
   return N, pipeline
-
-
-def _rel(a, b):
-  a = a.reshape(a.shape[0], -1).astype(np.float64)
-  b = b.reshape(b.shape[0], -1).astype(np.float64)
-  return np.abs(a - b).max(-1) / np.maximum(np.abs(b).max(-1), 1e-6)
 
 
 def test_noalloc_rollout_vjp_matches_workspace_variant():
@@ -81,12 +76,10 @@ def test_noalloc_rollout_vjp_matches_workspace_variant():
             'braxg_rollout_vjp_noalloc')
     torch.cuda.synchronize()
     assert torch.equal(got[3], ref[3])
-    for g, r in zip(got[:3], ref[:3]):
-      g, r = g.cpu().numpy(), r.cpu().numpy()
-      if g.ndim == 3:
-        g, r = np.swapaxes(g, 0, 1), np.swapaxes(r, 0, 1)
-      assert np.isfinite(g).all()
-      assert _rel(g, r).max() <= 2e-3, (call, _rel(g, r).max())
+    for name, g, r in zip(('act_bar', 'q0_bar', 'qd0_bar'), got[:3], ref[:3]):
+      assert torch.isfinite(g).all(), (call, name)
+      # rtol = atol = 0: the same kernel on the same inputs
+      assert torch.equal(g, r), (call, name, (g - r).abs().max().item())
 
 
 def test_noalloc_rejects_oversized_request():
