@@ -24,7 +24,7 @@ FIELD_CLASS = {
     'x_rot': ('link', 4), 'xd_ang': ('link', 3), 'xd_vel': ('link', 3),
     'qf_smooth': ('qd', 1), 'qf_constraint': ('qd', 1), 'qdd': ('qd', 1),
     'root_com': ('link', 3), 'cinr_pos': ('link', 3), 'cinr_rot': ('link', 4),
-    'cinr_i': ('link', 9), 'cd': ('link', 6), 'cdof': ('qd', 6), 'cdofd': ('qd', 6),
+    'cinr_i': ('link', 9), 'cd_packed': ('link', 6), 'cdof_packed': ('qd', 6), 'cdofd_packed': ('qd', 6),
     'mass_mx': ('mass_mx', 1), 'con_jac': ('jac', 1), 'con_diag': ('row', 1),
     'con_aref': ('row', 1), 'status': ('env', 1),
 }
@@ -37,8 +37,8 @@ def _shape(m: P.Model, field: str):
       'q': (m.nq,), 'qd': (m.nv,), 'mass_mx_inv': (m.nv, m.nv), 'x_pos': (m.nl, 3),
       'x_rot': (m.nl, 4), 'xd_ang': (m.nl, 3), 'xd_vel': (m.nl, 3), 'qf_smooth': (m.nv,),
       'qf_constraint': (m.nv,), 'qdd': (m.nv,), 'root_com': (m.nl, 3), 'cinr_pos': (m.nl, 3),
-      'cinr_rot': (m.nl, 4), 'cinr_i': (m.nl, 3, 3), 'cd': (m.nl, 6), 'cdof': (m.nv, 6),
-      'cdofd': (m.nv, 6), 'mass_mx': (m.nv, m.nv), 'con_jac': (m.m, m.nv), 'con_diag': (m.m,),
+      'cinr_rot': (m.nl, 4), 'cinr_i': (m.nl, 3, 3), 'cd_packed': (m.nl, 6), 'cdof_packed': (m.nv, 6),
+      'cdofd_packed': (m.nv, 6), 'mass_mx': (m.nv, m.nv), 'con_jac': (m.m, m.nv), 'con_diag': (m.m,),
       'con_aref': (m.m,), 'status': (),
   }[field]
 

@@ -67,5 +67,43 @@ def build(verbose: bool = False, force: bool = False) -> str:
   return lib
 
 
+def xla_include_dir():
+  """jaxlib's FFI header directory ($BRAXG_XLA_INCLUDE, else
+  jax.ffi.include_dir()), or None where jax is not installed."""
+  d = os.environ.get('BRAXG_XLA_INCLUDE')
+  if d:
+    return d if os.path.exists(os.path.join(d, 'xla', 'ffi', 'api', 'ffi.h')) else None
+  try:
+    import jax  # noqa: F401
+    from jax import ffi
+    d = ffi.include_dir()
+  except Exception:  # jax absent or too old for jax.ffi
+    return None
+  return d if os.path.exists(os.path.join(d, 'xla', 'ffi', 'api', 'ffi.h')) else None
+
+
+XLA_LIB = os.path.join(OUT_DIR, 'libbraxg_xla.so')
+
+
+def build_xla(verbose: bool = False):
+  """Builds libbraxg_xla.so (the XLA FFI handlers of csrc/xla/braxg_xla.cc,
+  linked against libbraxg.so) when jaxlib's FFI headers are present; returns
+  its path, or None without them."""
+  inc = xla_include_dir()
+  if inc is None:
+    return None
+  lib = build(verbose)
+  src = os.path.join(CSRC, 'xla', 'braxg_xla.cc')
+  deps = [src, os.path.join(CSRC, 'xla', 'xla_core.h'), os.path.join(ROOT, 'include', 'braxg.h'), lib]
+  if _sources_newer(XLA_LIB, deps):
+    cmd = [_nvcc(), '-x', 'cu', *ARCH, '-O3', '-std=c++17', '-Xcompiler', '-fPIC', '-shared',
+           '-I', inc, '-I', os.path.join(ROOT, 'include'), '-I', os.path.join(CSRC, 'xla'), src,
+           '-o', XLA_LIB, '-L', OUT_DIR, '-lbraxg', '-Xlinker', '-rpath,$ORIGIN', '-lcudart']
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+      raise RuntimeError(f'nvcc failed: {" ".join(cmd)}\n{r.stdout}\n{r.stderr}')
+  return XLA_LIB
+
+
 if __name__ == '__main__':
   print(build(verbose='-v' in sys.argv, force='-f' in sys.argv))

@@ -222,6 +222,7 @@ int braxg_batch_init(const braxg_batch* b, void* stream, const float* q, const f
   s.qd_in = qd;
   s.out = *out;
   s.out.cache = nullptr;  // per-model arena sizes differ: batches keep no cache
+  s.out.contact_dist = s.out.contact_pos = s.out.contact_frame = nullptr;  // no per-slot offsets in batches
   return batch_launch(b, stream, s, opt);
 }
 
@@ -248,6 +249,7 @@ int braxg_batch_rollout(const braxg_batch* b, void* stream, int n_steps, const f
   s.act_step_stride = tot.act;
   s.out = *out;
   s.out.cache = nullptr;
+  s.out.contact_dist = s.out.contact_pos = s.out.contact_frame = nullptr;
   s.traj_q = traj_q;
   s.traj_qd = traj_qd;
   s.traj_q_stride = tot.q;

@@ -253,6 +253,20 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const EnvBase& B, 
     fin = tm.all(fin);
     if (tm.lane == 0) o.status[B.env + env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
   }
+  if ((o.contact_dist != nullptr || o.contact_pos != nullptr || o.contact_frame != nullptr) && md.ncon > 0) {
+    // contact.get(sys, state.x) of the output state (brax/contact.py:28-67),
+    // recomputed from x into scratch (free once the outputs above are read)
+    const int nc = md.ncon;
+    float* dist = w.at(L.scr);
+    float* cpos = dist + al4(nc);
+    float* frame = cpos + al4(3 * nc);
+    tm.sync();
+    stage_contacts<T>(md.w, w, dist, cpos, frame);
+    const long long e = B.env + env;
+    store_vec<T>(tm, o.contact_dist ? o.contact_dist + e * nc : nullptr, dist, nc);
+    store_vec<T>(tm, o.contact_pos ? o.contact_pos + e * nc * 3 : nullptr, cpos, 3 * nc);
+    store_vec<T>(tm, o.contact_frame ? o.contact_frame + e * nc * 9 : nullptr, frame, 9 * nc);
+  }
 }
 
 // The locomotion task after one env step (brax/envs/ant.py:233-279): every

@@ -19,7 +19,7 @@ import torch
 
 from brax_gb300 import _native as N
 from brax_gb300 import model_pack
-from brax_gb300.system import System
+from brax_gb300.system import Inertia, Motion, System, Transform
 
 NEWTON_SCHULZ = N.INV_NEWTON_SCHULZ
 CHOLESKY = N.INV_CHOLESKY
@@ -96,8 +96,47 @@ def model_for(sys, device=None) -> Model:
 
 
 @dataclasses.dataclass
+class Contact:
+  """brax.base.Contact (brax/base.py:359-368: mujoco.mjx's Contact plus
+  link_idx and elasticity) of every contact slot, with the batch axis:
+  dist [n, ncon], pos [n, ncon, 3], frame [n, ncon, 3, 3] from the kernel;
+  the per-slot constants of the model broadcast over envs."""
+  dist: torch.Tensor
+  pos: torch.Tensor
+  frame: torch.Tensor
+  includemargin: torch.Tensor
+  friction: torch.Tensor       # [n, ncon, 5]
+  solref: torch.Tensor         # [n, ncon, 2]
+  solreffriction: torch.Tensor  # [n, ncon, 2] (zero: MuJoCo's default)
+  solimp: torch.Tensor         # [n, ncon, 5]
+  dim: torch.Tensor            # [n, ncon] condim 3 (pyramid rows)
+  geom1: torch.Tensor
+  geom2: torch.Tensor
+  geom: torch.Tensor           # [n, ncon, 2]
+  link_idx: tuple              # ([n, ncon], [n, ncon]); -1 is the world
+  elasticity: torch.Tensor     # [n, ncon]
+
+
+# packed [ang(3), vel(3)] storage of the Motion fields; the C ABI names them
+# cd / cdof / cdofd
+_PACKED = {'cd': 'cd_packed', 'cdof': 'cdof_packed', 'cdofd': 'cdofd_packed'}
+
+
+def _motion(t: Optional[torch.Tensor]):
+  return None if t is None else Motion(ang=t[..., :3], vel=t[..., 3:])
+
+
+@dataclasses.dataclass
 class State:
-  """brax.generalized.base.State with a leading batch axis (torch tensors)."""
+  """brax.generalized.base.State with a leading batch axis (torch tensors).
+
+  The reference's nested pytree (brax/generalized/base.py:25-92 on
+  brax/base.py:396-412) is available as views of the flat device arrays:
+  ``x.pos`` / ``x.rot``, ``xd.ang`` / ``xd.vel``, ``cinr.transform.pos`` /
+  ``.rot``, ``cinr.i``, ``cinr.mass``, ``cd`` / ``cdof`` / ``cdofd`` ``.ang`` /
+  ``.vel`` (slices of the packed [..., 6] arrays, no copies), and ``contact``
+  after a ``debug=True`` call.  Fields that the call did not produce (the
+  position-level terms unless ``full=True``) are None."""
   q: torch.Tensor
   qd: torch.Tensor
   x_pos: torch.Tensor
@@ -113,14 +152,19 @@ class State:
   cinr_pos: Optional[torch.Tensor] = None
   cinr_rot: Optional[torch.Tensor] = None
   cinr_i: Optional[torch.Tensor] = None
-  cd: Optional[torch.Tensor] = None
-  cdof: Optional[torch.Tensor] = None
-  cdofd: Optional[torch.Tensor] = None
+  cinr_mass: Optional[torch.Tensor] = None  # [n, nl] the links' masses (constants of the System)
+  cd_packed: Optional[torch.Tensor] = None     # [n, nl, 6]
+  cdof_packed: Optional[torch.Tensor] = None   # [n, nv, 6]
+  cdofd_packed: Optional[torch.Tensor] = None  # [n, nv, 6]
   mass_mx: Optional[torch.Tensor] = None
   con_jac: Optional[torch.Tensor] = None
   con_diag: Optional[torch.Tensor] = None
   con_aref: Optional[torch.Tensor] = None
-  contact: None = None
+  contact: Optional[Contact] = None
+  # kernel outputs behind ``contact`` (debug=True)
+  contact_dist: Optional[torch.Tensor] = None
+  contact_pos: Optional[torch.Tensor] = None
+  contact_frame: Optional[torch.Tensor] = None
   # [n, Model.cache_words] position-level terms of this state, computed by
   # the call that made it; a step from this state reuses them for every env
   # whose q / qd / parameters are unchanged (bit for bit) instead of
@@ -129,6 +173,34 @@ class State:
 
   def replace(self, **kw) -> 'State':
     return dataclasses.replace(self, **kw)
+
+  # ---- the reference's nested views -------------------------------------
+  @property
+  def x(self) -> Optional[Transform]:
+    return None if self.x_pos is None else Transform(pos=self.x_pos, rot=self.x_rot)
+
+  @property
+  def xd(self) -> Optional[Motion]:
+    return None if self.xd_ang is None else Motion(ang=self.xd_ang, vel=self.xd_vel)
+
+  @property
+  def cinr(self) -> Optional[Inertia]:
+    if self.cinr_pos is None:
+      return None
+    return Inertia(transform=Transform(pos=self.cinr_pos, rot=self.cinr_rot), i=self.cinr_i,
+                   mass=self.cinr_mass)
+
+  @property
+  def cd(self) -> Optional[Motion]:
+    return _motion(self.cd_packed)
+
+  @property
+  def cdof(self) -> Optional[Motion]:
+    return _motion(self.cdof_packed)
+
+  @property
+  def cdofd(self) -> Optional[Motion]:
+    return _motion(self.cdofd_packed)
 
 
 def _alloc(m: Model, n: int, full: bool, dev, cache: bool = False) -> State:
@@ -139,11 +211,43 @@ def _alloc(m: Model, n: int, full: bool, dev, cache: bool = False) -> State:
             status=torch.empty(n, dtype=torch.int32, device=dev),
             cache=f(n, m.cache_words) if cache else None)
   if full:
+    mass = torch.as_tensor(m.sys.link.inertia.mass, dtype=torch.float32, device=dev)
     s = s.replace(root_com=f(n, m.nl, 3), cinr_pos=f(n, m.nl, 3), cinr_rot=f(n, m.nl, 4),
-                  cinr_i=f(n, m.nl, 3, 3), cd=f(n, m.nl, 6), cdof=f(n, m.nv, 6),
-                  cdofd=f(n, m.nv, 6), mass_mx=f(n, m.nv, m.nv), con_jac=f(n, m.m, m.nv),
+                  cinr_i=f(n, m.nl, 3, 3), cinr_mass=mass.reshape(1, m.nl).expand(n, m.nl),
+                  cd_packed=f(n, m.nl, 6), cdof_packed=f(n, m.nv, 6),
+                  cdofd_packed=f(n, m.nv, 6), mass_mx=f(n, m.nv, m.nv), con_jac=f(n, m.m, m.nv),
                   con_diag=f(n, m.m), con_aref=f(n, m.m))
   return s
+
+
+def _alloc_contacts(m: Model, s: State) -> State:
+  """Adds the debug contact outputs to a state about to be written."""
+  n, k = s.q.shape[0], m.ncon
+  f = lambda *sh: torch.empty(*sh, dtype=torch.float32, device=s.q.device)
+  return s.replace(contact_dist=f(n, k), contact_pos=f(n, k, 3), contact_frame=f(n, k, 3, 3))
+
+
+def _contact(m: Model, s: State) -> Optional[Contact]:
+  """brax.base.Contact of the kernel's contact outputs (None without contact
+  slots, as brax/contact.py:39-40)."""
+  k = m.ncon
+  if k == 0:
+    return None
+  n, dev = s.q.shape[0], s.q.device
+  c = m.sys.contacts
+
+  def const(a, dt=torch.float32):
+    t = torch.as_tensor(a, dtype=dt, device=dev)
+    return t.reshape(1, *t.shape).expand(n, *t.shape)
+
+  g1, g2 = const(c.geom1, torch.int32), const(c.geom2, torch.int32)
+  return Contact(
+      dist=s.contact_dist, pos=s.contact_pos, frame=s.contact_frame,
+      includemargin=const(torch.zeros(k)), friction=const(c.friction), solref=const(c.solref),
+      solreffriction=const(torch.zeros(k, 2)), solimp=const(c.solimp),
+      dim=const(torch.full((k,), 3), torch.int32), geom1=g1, geom2=g2, geom=torch.stack([g1, g2], -1),
+      link_idx=(const(c.link_a, torch.int32), const(c.link_b, torch.int32)),
+      elasticity=const(c.elasticity))
 
 
 def _ptr(t):
@@ -151,7 +255,7 @@ def _ptr(t):
 
 
 def _cstate(s: State) -> N.State:
-  return N.State(*[_ptr(getattr(s, f)) for f in N.STATE_FIELDS])
+  return N.State(*[_ptr(getattr(s, _PACKED.get(f, f))) for f in N.STATE_FIELDS])
 
 
 def _as_batch(x: torch.Tensor, width: int, name: str, dev) -> torch.Tensor:
@@ -230,15 +334,17 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
          full: bool = False, threads_per_env: int = 0, envs_per_cta: int = 0,
          randomization: Optional[dict] = None, cache: bool = True) -> State:
   """brax/generalized/pipeline.py:32-61 for a batch of envs.  ``cache``
-  gives the state (and the states stepped from it) a position-term cache."""
-  if debug:
-    raise NotImplementedError('debug contacts are not materialised')
+  gives the state (and the states stepped from it) a position-term cache;
+  ``debug`` adds ``state.contact`` (contact.get of the state, as the
+  reference's debug flag does)."""
   m = model_for(sys, q.device if isinstance(q, torch.Tensor) else None)
   q = _as_batch(q, m.nq, 'q', m.device)
   qd = _as_batch(qd, m.nv, 'qd', m.device)
   if q.shape[0] != qd.shape[0]:
     raise ValueError('q and qd batch sizes differ')
   out = _alloc(m, q.shape[0], full, m.device, cache)
+  if debug:
+    out = _alloc_contacts(m, out)
   cs = _cstate(out)
   dr, _keep = _randomization(m, q.shape[0], randomization)
   stream = torch.cuda.current_stream(m.device).cuda_stream
@@ -246,7 +352,7 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
                              qd.data_ptr(), ctypes.byref(cs),
                              ctypes.byref(_opts(NEWTON_SCHULZ, threads_per_env, envs_per_cta, dr=dr))),
           'braxg_init')
-  return out
+  return out.replace(contact=_contact(m, out)) if debug else out
 
 
 def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
@@ -255,9 +361,8 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
          profile: Optional[torch.Tensor] = None, relax_barriers: int = 0,
          randomization: Optional[dict] = None) -> State:
   """brax/generalized/pipeline.py:64-94; n_frames > 1 repeats it with the same
-  action (PipelineEnv.pipeline_step, brax/envs/base.py:128-137)."""
-  if debug:
-    raise NotImplementedError('debug contacts are not materialised')
+  action (PipelineEnv.pipeline_step, brax/envs/base.py:128-137).  ``debug``
+  adds ``state.contact`` of the output state."""
   m = model_for(sys, state.q.device)
   n = state.q.shape[0]
   act_p = None
@@ -268,6 +373,10 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
     act_p = act.data_ptr()
   if out is None:
     out = _alloc(m, n, full, m.device, state.cache is not None)
+  if debug and out.contact_dist is None:
+    out = _alloc_contacts(m, out)
+  elif not debug and (out.contact_dist is not None or out.contact is not None):
+    out = out.replace(contact=None, contact_dist=None, contact_pos=None, contact_frame=None)
   cin = _cstate(state)
   cout = _cstate(out)
   dr, _keep = _randomization(m, n, randomization)
@@ -277,7 +386,7 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
                              ctypes.byref(_opts(inverse_mode, threads_per_env, envs_per_cta,
                                                 profile, relax_barriers, dr))),
           'braxg_step')
-  return out
+  return out.replace(contact=_contact(m, out)) if debug else out
 
 
 def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = NEWTON_SCHULZ,

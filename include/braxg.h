@@ -99,6 +99,17 @@ typedef struct {
    * beyond the first 32 while it runs (so more envs fit per CTA).  The
    * braxg_batch_* calls neither read nor write it. */
   float* cache;
+  /* Optional contacts of the output state, contact.get(sys, state.x)
+   * (brax/contact.py:28-67), which the reference adds to the State when
+   * init / step run with debug=True (brax/generalized/pipeline.py:57-58,
+   * 91-92): one entry per contact slot (mjx's fixed ncon), dist < 0 meaning
+   * penetration, frame rows (normal, tangent1, tangent2) with the normal
+   * pointing from geom1 to geom2.  The per-slot constants (geoms, friction,
+   * solref, solimp, link_idx, elasticity) are the model's.  The braxg_batch_*
+   * calls do not write them. */
+  float* contact_dist;   /* [n, ncon] */
+  float* contact_pos;    /* [n, ncon, 3] */
+  float* contact_frame;  /* [n, ncon, 3, 3] */
 } braxg_state;
 
 /* Per-stage profile slots of braxg_options.stage_cycles (sums over envs of

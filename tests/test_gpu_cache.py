@@ -64,7 +64,7 @@ def test_full_outputs_from_cache():
   c2 = P.step(sys_, c, act, n_frames=2, inverse_mode=P.CHOLESKY, full=True)
   u2 = P.step(sys_, u, act, n_frames=2, inverse_mode=P.CHOLESKY, full=True)
   torch.cuda.synchronize()
-  _same(c2, u2, FIELDS + ('root_com', 'cinr_pos', 'cinr_i', 'cd', 'cdof', 'cdofd', 'mass_mx', 'con_jac',
+  _same(c2, u2, FIELDS + ('root_com', 'cinr_pos', 'cinr_i', 'cd_packed', 'cdof_packed', 'cdofd_packed', 'mass_mx', 'con_jac',
                           'con_diag', 'con_aref'))
 
 

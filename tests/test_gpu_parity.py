@@ -58,9 +58,9 @@ def test_init_full_state(name):
   pairs = [('x_pos', ref.x_pos), ('x_rot', ref.x_rot), ('xd_ang', ref.xd_ang),
            ('xd_vel', ref.xd_vel), ('root_com', ref.root_com), ('cinr_pos', ref.cinr_pos),
            ('cinr_rot', ref.cinr_rot), ('cinr_i', ref.cinr_i),
-           ('cd', np.concatenate([ref.cd_ang, ref.cd_vel], -1)),
-           ('cdof', np.concatenate([ref.cdof_ang, ref.cdof_vel], -1)),
-           ('cdofd', np.concatenate([ref.cdofd_ang, ref.cdofd_vel], -1)),
+           ('cd_packed', np.concatenate([ref.cd_ang, ref.cd_vel], -1)),
+           ('cdof_packed', np.concatenate([ref.cdof_ang, ref.cdof_vel], -1)),
+           ('cdofd_packed', np.concatenate([ref.cdofd_ang, ref.cdofd_vel], -1)),
            ('mass_mx', ref.mass_mx), ('con_jac', ref.con_jac), ('con_diag', ref.con_diag),
            ('con_aref', ref.con_aref)]
   for field, r in pairs:
@@ -224,3 +224,32 @@ def test_implicit_solve_path_lying_humanoid():
           f'fp32 oracle vs fp64 p99 {np.quantile(eo, 0.99):.2e}; rows > 32 in {(rows > 32).sum()} of {n}')
     assert np.quantile(e64, 0.99) <= max(1e-5, 3 * np.quantile(eo, 0.99)), field
     assert (e64 > max(1e-3, 3 * eo.max())).mean() <= 0.01, field
+
+
+@pytest.mark.parametrize('name', ['quadruped', 'humanoid_like'])
+def test_debug_contacts(name):
+  """init / step with debug=True return state.contact (brax/generalized/
+  pipeline.py:57-58, 91-92): dist, pos and frame of every contact slot against
+  the oracle's contact.get of the same output state (x from the kernel), and the
+  nested views read the same arrays."""
+  P = _pipeline()
+  from oracle.pipeline import Oracle
+  sys = load(name)
+  n = 128
+  o64 = Oracle(sys, np.float64)
+  s64, rng = _states(sys, o64, n, 8, seed=21)
+  st = P.init(sys, _t(s64.q), _t(s64.qd), debug=True)
+  out = P.step(sys, st, _t(actions(sys, n, rng)), debug=True, n_frames=2)
+  torch.cuda.synchronize()
+  for s in (st, out):
+    assert s.contact is not None and s.contact.dist.shape == (n, sys.contacts.n)
+    xp, xr = _np(s.x.pos).astype(np.float64), _np(s.x.rot).astype(np.float64)
+    d, p, f = Oracle(sys, np.float64).contacts(xp, xr)
+    scale = np.maximum(np.abs(p).max(), 1.0)
+    np.testing.assert_allclose(_np(s.contact.dist), d, atol=2e-6 * scale, rtol=0)
+    np.testing.assert_allclose(_np(s.contact.pos), p, atol=2e-6 * scale, rtol=0)
+    np.testing.assert_allclose(_np(s.contact.frame), f, atol=2e-6, rtol=0)
+    assert s.contact.dist is s.contact_dist
+  # a step without debug returns no contact
+  plain = P.step(sys, out, _t(actions(sys, n, rng)))
+  assert plain.contact is None
