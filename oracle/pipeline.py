@@ -216,12 +216,20 @@ class State:
 class Oracle:
   """Holds a System cast to ``dtype`` plus its static schedule."""
 
-  def __init__(self, sys: S.System, dtype=np.float64, exact_inverse: bool = False):
+  def __init__(self, sys: S.System, dtype=np.float64, exact_inverse: bool = False, perturb_seed=None):
     """exact_inverse=True replaces the Newton-Schulz update of mass_mx_inv by
     the exact SPD inverse (the kernel's Cholesky mode); the reference path is
-    exact_inverse=False."""
+    exact_inverse=False.
+
+    perturb_seed (for the parity tests' rounding envelope): when set, every
+    step moves the intermediates whose rounding depends on the summation
+    order (qf_smooth, mass_mx_inv, and the projected-gradient problem's A and
+    b; A symmetrically) by -1, 0 or +1 ulp at random, emulating an evaluation
+    of the same algorithm in another operation order.  Not part of the
+    reference's algorithm."""
     self.sys = sys
     self.exact_inverse = exact_inverse
+    self._rng = None if perturb_seed is None else np.random.default_rng(perturb_seed)
     self.dt_ = np.dtype(dtype)
     self.st = static(sys)
     f = lambda a: np.asarray(a, dtype=self.dt_)
@@ -246,6 +254,16 @@ class Oracle:
         a_bq=f(sys.actuator.bias_q), a_bqd=f(sys.actuator.bias_qd),
         viscosity=self.dt_.type(sys.viscosity), density=self.dt_.type(sys.density))
     self.matvecs = 0
+
+  def _nudge(self, x, symmetric=False):
+    """x moved by -1, 0 or +1 ulp per entry (identity unless perturbing)."""
+    if self._rng is None:
+      return x
+    d = self._rng.integers(-1, 2, x.shape)
+    if symmetric:  # the same move for (i, j) and (j, i)
+      d = np.tril(d) + np.swapaxes(np.tril(d, -1), -1, -2)
+    up, dn = np.nextafter(x, self.dt_.type(np.inf)), np.nextafter(x, self.dt_.type(-np.inf))
+    return np.where(d > 0, up, np.where(d < 0, dn, x)).astype(self.dt_)
 
   # -------------------------------------------------------------------------
   # kinematics.forward: brax/kinematics.py:31-108
@@ -453,8 +471,8 @@ class Oracle:
     a_inv = np.where(reset[:, None, None], alt, a_inv)
     r, err = r0, np.ones(a.shape[0], dt)
     for _ in range(num_iter):
-      nxt = a_inv @ (eye + r)
-      r_next = eye - a @ nxt
+      nxt = self._nudge(a_inv @ (eye + r))
+      r_next = self._nudge(eye - a @ nxt)
       err_next = safe_norm(r_next, 2)
       a_inv = np.where((err_next < err)[:, None, None], nxt, a_inv)
       r, err = r_next, err_next
@@ -475,7 +493,7 @@ class Oracle:
       minv = self.inv_approximate(mx, s.mass_mx_inv, num_iter)
     else:
       minv = self.spd_inverse(mx)
-    return s.replace(mass_mx=mx, mass_mx_inv=minv)
+    return s.replace(mass_mx=mx, mass_mx_inv=self._nudge(minv, symmetric=True))
 
   # -------------------------------------------------------------------------
   # contact.get (+ mujoco.mjx primitive collisions): brax/contact.py:28-67
@@ -729,6 +747,7 @@ class Oracle:
     a = jm @ np.swapaxes(s.con_jac, -1, -2)
     a = a + np.einsum('bi,ij->bij', s.con_diag, np.eye(a.shape[-1], dtype=dt))
     b = np.einsum('bij,bj->bi', jm, s.qf_smooth) - s.con_aref
+    a, b = self._nudge(a, symmetric=True), self._nudge(b)
     xs, cnt = self.pg_solve(a, b, sys.solver_iterations, sys.solver_maxls)
     return np.einsum('bij,bi->bj', s.con_jac, xs), cnt
 
@@ -831,7 +850,7 @@ class Oracle:
     return rotate(fa, xi_r), rotate(fv, xi_r), xi_p  # :80, Transform.do(Force) with pos 0
 
   def forward(self, s: State, tau):
-    return self.passive(s) - self.inverse(s) + tau
+    return self._nudge(self.passive(s) - self.inverse(s) + tau)
 
   # -------------------------------------------------------------------------
   # integrator.integrate: brax/generalized/integrator.py:26-84
