@@ -24,6 +24,8 @@ __host__ __device__ inline AdjLayout make_adj_layout(int nl, int nq, int nv, int
                                                      int pg_iters) {
   AdjLayout A;
   const int m = 4 * ncon + nlim;
+  // rows of the explicit solve's A cotangent; the row cotangents cover all m
+  // rows (the implicit solve's rows beyond kMaxExplicitRows too)
   const int na = m < kMaxExplicitRows ? m : kMaxExplicitRows;
   const int ldm = nv | 1, ldj = nv | 1, la = (na | 1);
   int o = 0;
@@ -47,13 +49,13 @@ __host__ __device__ inline AdjLayout make_adj_layout(int nl, int nq, int nv, int
   A.tb = take(nv);
   A.Minvb = take(nv * ldm);
   A.Mb = take(nv * ldm);
-  A.Jb = take(na * ldj);
-  A.diagb = take(na);
-  A.arefb = take(na);
-  A.bb = take(na);
-  A.xb = take(na);
+  A.Jb = take(m * ldj);
+  A.diagb = take(m);
+  A.arefb = take(m);
+  A.bb = take(m);
+  A.xb = take(m);
   A.Ab = take(na * la);
-  A.tape = take(kTapeHeadWords + pg_iters * kTapeIterWords);
+  A.tape = take(tape_words(m, pg_iters));
   A.xpb = take(3 * nl);
   A.xrb = take(4 * nl);
   A.cib = take(9 * nl);
@@ -71,6 +73,10 @@ __host__ __device__ inline AdjLayout make_adj_layout(int nl, int nq, int nv, int
   const int kA = (kMaxExplicitRows + 3) & ~3;
   const int lae = explicit_lda(na);
   t = t > na * lae + na * ldm + 4 * kA ? t : na * lae + na * ldm + 4 * kA;  // constraint: A, W, vectors
+  if (m > kMaxExplicitRows) {  // implicit solve: Ab J, Ab^T J, 4 row vectors, 6 dof vectors
+    const int ti = 2 * m * ldm + 4 * al4(m) + 6 * al4(nv);
+    t = t > ti ? t : ti;
+  }
   t += 16;
   A.tmp_words = al4(t);
   A.tmp = take(A.tmp_words);
@@ -174,6 +180,166 @@ __device__ __noinline__ void rev_qdd(const int* mw, Ws w, AWs a) {
 }
 
 // ---------------------------------------------------------------------------
+// constraint.force reverse on the implicit path (more than kMaxExplicitRows
+// active rows), where the forward applied A = J Minv J^T + diag without
+// forming it.  The unrolled iterations are reversed with the same implicit
+// matvecs; the cotangent of A, sum_k (r_k g_k^T + rb_k y_k^T), is never
+// formed: its products P = Ab J and Q = Ab^T J (nrow x nv) are accumulated
+// from J^T of the iteration vectors, and then
+//   Jb += (P + Q) Minv,   Minvb += J^T P,   diagb = diag(Ab),
+// the same contractions the explicit path takes through Ab.  b = J (Minv qfs)
+// - aref and qfc = J^T x* are reversed as there.
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ __noinline__ void rev_constraint_implicit(const int* mw, Ws w, AWs a, int iters, int nrow) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  const AdjLayout& A = *a.A;
+  const int nv = md.nv, ldj = L.ldj, ld = L.ldm, m = md.m;
+  const int kT = tape_stride(nrow);
+  const float* tape = a.at(A.tape);
+  const float* Minv = w.at(L.Minv);
+  const float* rdiag = w.at(L.rdiag);
+  const float* qfs = w.at(L.qfs);
+  const float* qfcb = a.at(A.qfcb);
+  float* Jb = a.at(A.Jb);
+  float* bb = a.at(A.bb);
+  float* xbar = a.at(A.xb);
+  float* diagb = a.at(A.diagb);
+  float* Pm = a.at(A.tmp);          // Ab J      [nrow, ld]
+  float* Qm = Pm + m * ld;          // Ab^T J    [nrow, ld]
+  float* ybar = Qm + m * ld;
+  float* vv = ybar + al4(m);
+  float* gb = vv + al4(m);
+  float* rb = gb + al4(m);
+  float* jg = rb + al4(m);          // J^T gb
+  float* jr = jg + al4(nv);         // J^T rb
+  float* jy = jr + al4(nv);         // J^T y
+  float* jry = jy + al4(nv);        // J^T ry
+  float* t2 = jry + al4(nv);        // Minv J^T v
+  // A v for the implicit A: out = J (Minv (J^T v)) + diag v, keeping J^T v in jtv
+  auto matvec = [&](const float* v, float* out, float* jtv) {
+    for (int d = tm.lane; d < nv; d += T) {
+      float s = 0.f;
+      for (int r = 0; r < nrow; ++r) s = fmaf(w.jrow(r)[d], v[r], s);
+      jtv[d] = s;
+    }
+    tm.sync();
+    for (int d = tm.lane; d < nv; d += T) {
+      float s = 0.f;
+      for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * ld + k], jtv[k], s);
+      t2[d] = s;
+    }
+    tm.sync();
+    for (int r = tm.lane; r < nrow; r += T) {
+      const float* jrow = w.jrow(r);
+      float s = 0.f;
+      for (int k = 0; k < nv; ++k) s = fmaf(jrow[k], t2[k], s);
+      out[r] = s + rdiag[r] * v[r];
+    }
+    tm.sync();
+  };
+  auto jt = [&](const float* v, float* out) {  // out = J^T v
+    for (int d = tm.lane; d < nv; d += T) {
+      float s = 0.f;
+      for (int r = 0; r < nrow; ++r) s = fmaf(w.jrow(r)[d], v[r], s);
+      out[d] = s;
+    }
+  };
+  // qfc = J^T x*: Jb = x* qfcb^T, xbar = J qfcb
+  const float* xs = tape + 4;
+  for (int e = tm.lane; e < nrow * nv; e += T) {
+    const int i = e / nv, d = e - i * nv;
+    Jb[i * ldj + d] = xs[i] * qfcb[d];
+    Pm[i * ld + d] = 0.f;
+    Qm[i * ld + d] = 0.f;
+  }
+  for (int i = tm.lane; i < nrow; i += T) {
+    const float* jrow = w.jrow(i);
+    float s = 0.f;
+    for (int d = 0; d < nv; ++d) s = fmaf(jrow[d], qfcb[d], s);
+    xbar[i] = s;
+    bb[i] = 0.f;
+    diagb[i] = 0.f;
+    ybar[i] = 0.f;
+  }
+  tm.sync();
+  for (int k = iters - 1; k >= 0; --k) {
+    const float* rec = tape + tape_head_words(nrow) + k * tape_iter_words(nrow);
+    const float step = rec[0], beta = rec[1];
+    const float* y = rec + 4;
+    const float* ry = rec + 4 + kT;
+    const float* zpos = rec + 4 + 2 * kT;
+    for (int i = tm.lane; i < nrow; i += T) {
+      const float nxb = xbar[i] + (1.f + beta) * ybar[i];
+      const float zb = nxb * zpos[i];
+      vv[i] = zb;
+      gb[i] = -step * zb;
+      xbar[i] = -beta * ybar[i];
+    }
+    tm.sync();
+    matvec(gb, rb, jg);  // rb = A gb (g = A^T r, r = A y + b), jg = J^T gb
+    jt(y, jy);
+    jt(ry, jry);
+    for (int i = tm.lane; i < nrow; i += T) {
+      bb[i] += rb[i];
+      diagb[i] += ry[i] * gb[i] + rb[i] * y[i];
+    }
+    tm.sync();
+    matvec(rb, ybar, jr);  // A rb, jr = J^T rb
+    for (int i = tm.lane; i < nrow; i += T) ybar[i] += vv[i];  // ybar = zb + A^T rb
+    // Ab += ry gb^T + rb y^T:  P += ry (J^T gb)^T + rb (J^T y)^T,  Q += gb (J^T ry)^T + y (J^T rb)^T
+    for (int e = tm.lane; e < nrow * nv; e += T) {
+      const int i = e / nv, d = e - i * nv;
+      Pm[i * ld + d] += ry[i] * jg[d] + rb[i] * jy[d];
+      Qm[i * ld + d] += gb[i] * jry[d] + y[i] * jr[d];
+    }
+    tm.sync();
+  }
+  // A = (J Minv) J^T + diag: Jb += (P + Q) Minv (Minv symmetric)
+  for (int e = tm.lane; e < nrow * nv; e += T) {
+    const int i = e / nv, d = e - i * nv;
+    float s = 0.f;
+    for (int k = 0; k < nv; ++k) s = fmaf(Pm[i * ld + k] + Qm[i * ld + k], Minv[k * ld + d], s);
+    Jb[i * ldj + d] += s;
+  }
+  // Minvb += J^T Ab J = J^T P
+  float* Minvb = a.at(A.Minvb);
+  for (int e = tm.lane; e < nv * nv; e += T) {
+    const int i2 = e / nv, j = e - i2 * nv;
+    float s = 0.f;
+    for (int r = 0; r < nrow; ++r) s = fmaf(w.jrow(r)[i2], Pm[r * ld + j], s);
+    Minvb[i2 * ld + j] += s;
+  }
+  tm.sync();
+  // b = J (Minv qfs) - aref
+  float* u = a.at(A.u);
+  float* tb = a.at(A.tb);
+  for (int d = tm.lane; d < nv; d += T) {
+    float s = 0.f, t = 0.f;
+    for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * ld + k], qfs[k], s);
+    for (int i = 0; i < nrow; ++i) t = fmaf(w.jrow(i)[d], bb[i], t);
+    u[d] = s;
+    tb[d] = t;
+  }
+  tm.sync();
+  float* arefb = a.at(A.arefb);
+  float* qfsb = a.at(A.qfsb);
+  for (int d = tm.lane; d < nv; d += T) {
+    for (int i = 0; i < nrow; ++i) Jb[i * ldj + d] += bb[i] * u[d];
+    float s = 0.f;
+    for (int k = 0; k < nv; ++k) {
+      Minvb[k * ld + d] += tb[k] * qfs[d];
+      s = fmaf(Minv[k * ld + d], tb[k], s);
+    }
+    qfsb[d] += s;
+  }
+  for (int i = tm.lane; i < nrow; i += T) arefb[i] = -bb[i];
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
 // constraint.force reverse: qfc = J^T x*, the unrolled projected gradient
 // (jaxopt ProximalGradient, constraint.py:229-238), A = (J Minv) J^T + diag,
 // b = (J Minv) qfs - aref.  Produces Jb, diagb, arefb for the active rows and
@@ -190,11 +356,16 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
   const float* tape = a.at(A.tape);
   const int iters = (int)tape[0];
   const int nrow = (int)tape[1];
-  if (iters < 0) return false;
+  if (iters < 0 || nrow > md.m) return false;
   if (nrow == 0) return true;
+  if (nrow > kMaxExplicitRows) {
+    rev_constraint_implicit<T>(mw, w, a, iters, nrow);
+    return true;
+  }
   const int lab = nrow | 1;  // Ab rows
   const int la = explicit_lda(nrow), n4 = al4(nrow) / 4;  // Am rows (16-byte matvecs, as the forward)
   constexpr int kA = (kMaxExplicitRows + 3) & ~3;
+  const int kT = tape_stride(nrow);  // the tape's row vectors
   const float* J = w.at(L.J);
   const float* Minv = w.at(L.Minv);
   const float* rdiag = w.at(L.rdiag);
@@ -282,11 +453,11 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
     return s0 + s1;
   };
   for (int k = iters - 1; k >= 0; --k) {
-    const float* rec = tape + kTapeHeadWords + k * kTapeIterWords;
+    const float* rec = tape + tape_head_words(nrow) + k * tape_iter_words(nrow);
     const float step = rec[0], beta = rec[1];
     const float* y = rec + 4;
-    const float* ry = rec + 4 + kA;
-    const float* zpos = rec + 4 + 2 * kA;
+    const float* ry = rec + 4 + kT;
+    const float* zpos = rec + 4 + 2 * kT;
     for (int i = tm.lane; i < nrow; i += T) {
       float nxb = xbar[i] + (1.f + beta) * ybar[i];
       float zb = nxb * zpos[i];
@@ -687,7 +858,6 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
   const int nrow = (int)tape[1];
   if (nrow <= 0) return;
   const int* rmap = reinterpret_cast<const int*>(w.at(L.rmap));
-  const float* J = w.at(L.J);
   const float* q = a.at(A.q0);
   const float* qd = a.at(A.qd0);
   const float* Jb = a.at(A.Jb);
@@ -779,7 +949,7 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
       float jr[4];
       for (int qq = 0; qq < 4; ++qq) {
         jr[qq] = Jb[(c0 + qq) * ldj + d] + velb[qq] * qd[d];
-        qdb[d] += velb[qq] * J[(c0 + qq) * ldj + d];
+        qdb[d] += velb[qq] * w.jrow(c0 + qq)[d];
       }
       if (!((mb >> d) & 1ull)) continue;
       f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);

@@ -20,7 +20,7 @@ extern "C" {
 
 // Words of one frame snapshot: the forward arena plus the projected-gradient tape.
 static int vjp_snap_words(const braxg_model* m) {
-  return m->L.total + braxg::al4(braxg::kTapeHeadWords + m->h[BXM_H_PG_ITERS] * braxg::kTapeIterWords);
+  return m->L.total + braxg::tape_words(m->dims.m, m->h[BXM_H_PG_ITERS]);
 }
 
 // Workspace of braxg_rollout_vjp: checkpoints [n_ckpt, n, nq + nv], then the

@@ -468,7 +468,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
           __syncthreads();
           pf.mark(BRAXG_PROF_SMOOTH);
           int mvs = 0;
-          if (active) mvs = stage_constraint<T>(smem, w);
+          if (active) mvs = stage_constraint<T>(smem, w, nullptr, exact_mode);
           if (!(a.relax & 1)) __syncthreads();  // launch-uniform condition
           pf.count(BRAXG_PROF_MATVECS, (unsigned long long)mvs);
           pf.mark(BRAXG_PROF_CONSTRAINT);

@@ -1297,9 +1297,11 @@ __device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
 // constraint.force: brax/generalized/constraint.py:194-240, with the
 // jaxopt.ProjectedGradient (FISTA + backtracking) iteration restated.
 // ---------------------------------------------------------------------------
+// out = A v (trans: A^T v) for A = J Minv J^T + diag, without forming A; A^T
+// differs from A where the carried Newton-Schulz Minv is not symmetric.
 template <int T>
 __device__ __noinline__ void matvec_A(const int* mw, Ws w, int nrow, const float* v, float* out, float* t1,
-                                      float* t2) {
+                                      float* t2, bool trans = false) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
@@ -1319,14 +1321,16 @@ __device__ __noinline__ void matvec_A(const int* mw, Ws w, int nrow, const float
     t1[d] = (s0 + s1) + (s2 + s3);
   }
   tm.sync();
-  for (int d = tm.lane; d < nv; d += T) {  // t2 = Minv t1
+  // t2 = Minv t1 (trans: Minv^T t1)
+  const int sr = trans ? 1 : ld, sc = trans ? ld : 1;
+  for (int d = tm.lane; d < nv; d += T) {
     float s0 = 0.f, s1 = 0.f;
     int k = 0;
     for (; k + 1 < nv; k += 2) {
-      s0 = fmaf(Minv[d * ld + k], t1[k], s0);
-      s1 = fmaf(Minv[d * ld + k + 1], t1[k + 1], s1);
+      s0 = fmaf(Minv[d * sr + k * sc], t1[k], s0);
+      s1 = fmaf(Minv[d * sr + (k + 1) * sc], t1[k + 1], s1);
     }
-    if (k < nv) s0 = fmaf(Minv[d * ld + k], t1[k], s0);
+    if (k < nv) s0 = fmaf(Minv[d * sr + k * sc], t1[k], s0);
     t2[d] = s0 + s1;
   }
   tm.sync();
@@ -1344,17 +1348,31 @@ __device__ __noinline__ void matvec_A(const int* mw, Ws w, int nrow, const float
   tm.sync();
 }
 
+// PG tape (reverse pass only) of a solve with `rows` active rows: [0]
+// iterations run, [1] rows, then x* (tape_stride(rows) words), then per
+// iteration 4 scalars (step, beta) and y, r(y), [z > 0], each
+// tape_stride(rows) words.  Both solve paths (explicit A up to
+// kMaxExplicitRows rows, implicit above) write the same tape; a model's tape
+// buffer holds tape_words(m, pg_iters) words, and a frame snapshot copies
+// only the tape_words(rows, iterations) its solve wrote.
+__host__ __device__ inline int tape_stride(int rows) { return al4(rows); }
+__host__ __device__ inline int tape_head_words(int rows) { return 4 + tape_stride(rows); }
+__host__ __device__ inline int tape_iter_words(int rows) { return 4 + 3 * tape_stride(rows); }
+__host__ __device__ inline int tape_words(int rows, int iters) {
+  return al4(tape_head_words(rows) + iters * tape_iter_words(rows));
+}
+
 // Projected gradient with A formed explicitly, in the reference's association:
 // W = J Minv, A = W J^T + diag(d), b = W qf_smooth - aref (constraint.py:208-210).
 // Used when nrow <= kMaxExplicitRows; each matvec is then one team pass.
-// PG tape (reverse pass only): [0] iterations run, then x* (al4(kMaxExplicitRows)
-// words), then per iteration 4 scalars (step, beta) and y, r(y), [z > 0],
-// each al4(kMaxExplicitRows) words.
-constexpr int kTapeIterWords = 4 + 3 * ((kMaxExplicitRows + 3) & ~3);
-constexpr int kTapeHeadWords = 4 + ((kMaxExplicitRows + 3) & ~3);
 
+// `sym`: Minv is symmetric bit for bit (the exact inverse), so A is built
+// from its lower triangle and A^T v is A v; otherwise (the carried
+// Newton-Schulz iterate, whose two triangles differ by rounding) every entry
+// of A is formed and the gradient A^T r of 0.5 |A x + b|^2 is a column matvec,
+// as the reference computes it.
 template <int T>
-__device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* tape) {
+__device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* tape, bool sym) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
@@ -1408,7 +1426,23 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     }
   }
   tm.sync();
-  {  // A = W J^T + diag: the lower triangle (row i, column c <= i), lanes over
+  if (!sym) {  // A = W J^T + diag, every entry (lanes over them)
+    for (int e = tm.lane; e < nrow * nrow; e += T) {
+      const int i = e / nrow, c = e - i * nrow;
+      float s0 = 0.f, s1 = 0.f;
+      int k = 0;
+      for (; k + 1 < nv; k += 2) {
+        s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+        s1 = fmaf(W[i * ld + k + 1], J[c * ldj + k + 1], s1);
+      }
+      if (k < nv) s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+      A[i * la + c] = (s0 + s1) + (i == c ? rdiag[i] : 0.f);
+    }
+    for (int e = tm.lane; e < nrow * (4 * n4 - nrow); e += T) {
+      const int r = e / (4 * n4 - nrow);
+      A[r * la + nrow + (e - r * (4 * n4 - nrow))] = 0.f;
+    }
+  } else {  // A = W J^T + diag: the lower triangle (row i, column c <= i), lanes over
      // its entries, mirrored into the upper one, so that A is symmetric bit
      // for bit (J Minv J^T is symmetric) and A^T v is A v
     int i = 0, c = tm.lane;
@@ -1475,12 +1509,32 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     }
     tm.sync();
   };
-  auto resid = [&](const float* v, float* out) { matvec(v, out, true); };   // A v + b
-  auto grad = [&](const float* v, float* out) { matvec(v, out, false); };  // A^T v = A v
+  // A^T v by columns (lanes over the output entries, consecutive columns)
+  auto matvec_t = [&](const float* v, float* out) {
+    for (int c = tm.lane; c < nrow; c += T) {
+      float s0 = 0.f, s1 = 0.f;
+      int i = 0;
+      for (; i + 1 < nrow; i += 2) {
+        s0 = fmaf(A[i * la + c], v[i], s0);
+        s1 = fmaf(A[(i + 1) * la + c], v[i + 1], s1);
+      }
+      if (i < nrow) s0 = fmaf(A[i * la + c], v[i], s0);
+      out[c] = s0 + s1;
+    }
+    tm.sync();
+  };
+  auto resid = [&](const float* v, float* out) { matvec(v, out, true); };  // A v + b
+  auto grad = [&](const float* v, float* out) {                           // A^T v
+    if (sym) {
+      matvec(v, out, false);
+    } else {
+      matvec_t(v, out);
+    }
+  };
   float t = 1.f, ss = 1.f, err = INFINITY;
   int matvecs = 0;
   int iters = 0;
-  constexpr int kA = (kMaxExplicitRows + 3) & ~3;
+  const int kA = tape_stride(nrow);
   // x = y = 0: residual b, gradient A b
   for (int i = tm.lane; i < nrow; i += T) {
     rx[i] = b[i];
@@ -1492,7 +1546,7 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   for (int i = tm.lane; i < nrow; i += T) gx[i] = gy[i];
   for (int it = 0; it < md.pg_iters; ++it) {
     if (it > 0 && !(err > md.pg_tol)) break;
-    float* rec = tape != nullptr ? tape + kTapeHeadWords + it * kTapeIterWords : nullptr;
+    float* rec = tape != nullptr ? tape + tape_head_words(nrow) + it * tape_iter_words(nrow) : nullptr;
     if (rec != nullptr)
       for (int i = tm.lane; i < nrow; i += T) {
         rec[4 + i] = y[i];
@@ -1580,8 +1634,10 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   return matvecs;
 }
 
+// `sym`: Minv is the exact (bitwise symmetric) inverse; false for the
+// carried Newton-Schulz iterate (see pg_explicit).
 template <int T>
-__device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = nullptr) {
+__device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape, bool sym) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
@@ -1597,9 +1653,9 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
     tm.sync();
     return 0;
   }
-  if (nrow <= kMaxExplicitRows) return pg_explicit<T>(md.w, w, nrow, tape);
-  if (tape != nullptr && tm.lane == 0) tape[0] = -1.f;  // too many rows for the taped path
+  if (nrow <= kMaxExplicitRows) return pg_explicit<T>(md.w, w, nrow, tape, sym);
   const int m = md.m;
+  const int kA = tape_stride(nrow);
   float* b = w.at(L.scr);
   float* x = b + al4(m);
   float* y = x + al4(m);
@@ -1631,18 +1687,24 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
   tm.sync();
   float t = 1.f, ss = 1.f, err = INFINITY;
   int matvecs = 0;
+  int iters = 0;
   for (int it = 0; it < md.pg_iters; ++it) {
     if (it > 0 && !(err > md.pg_tol)) break;
     // value and gradient at y
     matvec_A<T>(md.w, w, nrow, y, r, t1, t2);
     float fs = 0.f;
+    float* rec = tape != nullptr ? tape + tape_head_words(nrow) + it * tape_iter_words(nrow) : nullptr;
     for (int i = tm.lane; i < nrow; i += T) {
       r[i] = r[i] + b[i];
       fs += 0.5f * r[i] * r[i];
+      if (rec != nullptr) {
+        rec[4 + i] = y[i];
+        rec[4 + kA + i] = r[i];
+      }
     }
     float fy = tm.sum(fs);
     tm.sync();
-    matvec_A<T>(md.w, w, nrow, r, gy, t1, t2);
+    matvec_A<T>(md.w, w, nrow, r, gy, t1, t2, !sym);
     matvecs += 2;
     float cur = ss;
     for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
@@ -1675,6 +1737,14 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
     float nt = 0.5f * (1.f + sqrtf(1.f + 4.f * t * t));
     float beta = (t - 1.f) / nt;
     for (int i = tm.lane; i < nrow; i += T) ny[i] = nx[i] + beta * (nx[i] - x[i]);
+    if (rec != nullptr) {
+      for (int i = tm.lane; i < nrow; i += T) rec[4 + 2 * kA + i] = (y[i] + (-cur) * gy[i]) > 0.f ? 1.f : 0.f;
+      if (tm.lane == 0) {
+        rec[0] = cur;
+        rec[1] = beta;
+      }
+    }
+    iters = it + 1;
     tm.sync();
     // gradient at the new iterate and the stopping error
     if (!accepted) {  // an accepted trial already left A nx in r
@@ -1683,7 +1753,7 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
     }
     for (int i = tm.lane; i < nrow; i += T) r[i] = r[i] + b[i];
     tm.sync();
-    matvec_A<T>(md.w, w, nrow, r, gx, t1, t2);
+    matvec_A<T>(md.w, w, nrow, r, gx, t1, t2, !sym);
     matvecs += 1;
     float es = 0.f;
     for (int i = tm.lane; i < nrow; i += T) {
@@ -1702,6 +1772,13 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape = 
     float s = 0.f;
     for (int i = 0; i < nrow; ++i) s = fmaf(w.jrow(i)[d], x[i], s);
     qfc[d] = s;
+  }
+  if (tape != nullptr) {
+    for (int i = tm.lane; i < nrow; i += T) tape[4 + i] = x[i];
+    if (tm.lane == 0) {
+      tape[0] = (float)iters;
+      tape[1] = (float)nrow;
+    }
   }
   tm.sync();
   return matvecs;

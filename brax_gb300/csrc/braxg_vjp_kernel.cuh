@@ -14,7 +14,7 @@ template <int T, int NVB>
 __device__ __forceinline__ void fwd_frame(const int* mw, Ws w, bool active, bool has_act, float* tape, bool& ok) {
   if (active) stage_smooth<T>(mw, w, has_act);
   __syncthreads();
-  if (active) stage_constraint<T>(mw, w, tape);
+  if (active) stage_constraint<T>(mw, w, tape, true);  // gradients use the exact inverse
   __syncthreads();
   if (active) ok = stage_integrate<T>(mw, w) && ok;
   __syncthreads();
@@ -44,25 +44,33 @@ __device__ __forceinline__ void copy_vec(const Team<T>& tm, float* dst, const fl
 // A frame snapshot is the env's whole forward arena (every stage's values
 // after the frame's smooth, constraint and integrate stages) followed by the
 // projected-gradient tape; the reverse of that frame restores it instead of
-// recomputing the frame.  Both parts are whole float4s (al4 sizes, 16-byte
-// aligned arenas and slots).
+// recomputing the frame.  Of the tape only the words the frame's solve wrote
+// are copied (its header gives the iterations and rows), at most
+// `tape_cap` words.  All parts are whole float4s (al4 sizes, 16-byte aligned
+// arenas and slots).
+__device__ __forceinline__ int tape_used(const float* head, int tape_cap) {
+  const int iters = max((int)head[0], 0), rows = max((int)head[1], 0);
+  return min(tape_words(rows, iters), tape_cap);
+}
 template <int T>
 __device__ __forceinline__ void snap_save(const Team<T>& tm, float* slot, const float* arena, int arena_words,
-                                          const float* tape, int tape_words) {
+                                          const float* tape, int tape_cap) {
   float4* d = reinterpret_cast<float4*>(slot);
   const float4* x = reinterpret_cast<const float4*>(arena);
   const float4* t = reinterpret_cast<const float4*>(tape);
+  const int used = tape_used(tape, tape_cap);
   for (int i = tm.lane; i < arena_words / 4; i += T) d[i] = x[i];
-  for (int i = tm.lane; i < tape_words / 4; i += T) d[arena_words / 4 + i] = t[i];
+  for (int i = tm.lane; i < used / 4; i += T) d[arena_words / 4 + i] = t[i];
 }
 template <int T>
 __device__ __forceinline__ void snap_load(const Team<T>& tm, const float* slot, float* arena, int arena_words,
-                                          float* tape, int tape_words) {
+                                          float* tape, int tape_cap) {
   const float4* d = reinterpret_cast<const float4*>(slot);
   float4* x = reinterpret_cast<float4*>(arena);
   float4* t = reinterpret_cast<float4*>(tape);
+  const int used = tape_used(slot + arena_words, tape_cap);
   for (int i = tm.lane; i < arena_words / 4; i += T) x[i] = d[i];
-  for (int i = tm.lane; i < tape_words / 4; i += T) t[i] = d[arena_words / 4 + i];
+  for (int i = tm.lane; i < used / 4; i += T) t[i] = d[arena_words / 4 + i];
 }
 
 template <int T, int NVB>

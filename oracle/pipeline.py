@@ -216,20 +216,33 @@ class State:
 class Oracle:
   """Holds a System cast to ``dtype`` plus its static schedule."""
 
-  def __init__(self, sys: S.System, dtype=np.float64, exact_inverse: bool = False, perturb_seed=None):
+  # half-width, in ulps of the operands' magnitude, of the decision margin
+  # of the rounding envelope (about sqrt(n) for sums of tens of terms)
+  DECISION_ULPS = 8
+
+  def __init__(self, sys: S.System, dtype=np.float64, exact_inverse: bool = False, perturb_seed=None,
+               perturb_bias: int = 0):
     """exact_inverse=True replaces the Newton-Schulz update of mass_mx_inv by
     the exact SPD inverse (the kernel's Cholesky mode); the reference path is
     exact_inverse=False.
 
     perturb_seed (for the parity tests' rounding envelope): when set, every
     step moves the intermediates whose rounding depends on the summation
-    order (qf_smooth, mass_mx_inv, and the projected-gradient problem's A and
-    b; A symmetrically) by -1, 0 or +1 ulp at random, emulating an evaluation
-    of the same algorithm in another operation order.  Not part of the
-    reference's algorithm."""
+    order (qf_smooth, mass_mx_inv and the Newton-Schulz iterates, and the
+    projected-gradient problem's A and b; A symmetrically) by -1, 0 or +1 ulp
+    at random, and every discrete decision taken on two computed values (the
+    line search's sufficient-decrease test, the solver's stopping test, the
+    Newton-Schulz acceptance and reset tests) sees its two sides shifted by
+    up to DECISION_ULPS ulps of their magnitude: decisions whose sides agree
+    that closely may go either way in another operation order.
+    perturb_bias -1 / +1 shifts every such decision the same way (a draw
+    biased to one side), 0 draws each shift at random.  This emulates an
+    evaluation of the same algorithm in another operation order; it is not
+    part of the reference's algorithm."""
     self.sys = sys
     self.exact_inverse = exact_inverse
     self._rng = None if perturb_seed is None else np.random.default_rng(perturb_seed)
+    self._bias = perturb_bias
     self.dt_ = np.dtype(dtype)
     self.st = static(sys)
     f = lambda a: np.asarray(a, dtype=self.dt_)
@@ -254,6 +267,14 @@ class Oracle:
         a_bq=f(sys.actuator.bias_q), a_bqd=f(sys.actuator.bias_qd),
         viscosity=self.dt_.type(sys.viscosity), density=self.dt_.type(sys.density))
     self.matvecs = 0
+
+  def _margin(self, scale):
+    """Shift of a decision's comparison (zero unless perturbing): up to
+    DECISION_ULPS ulps of `scale` (the magnitude of the compared values)."""
+    if self._rng is None:
+      return np.zeros_like(scale)
+    u = self._rng.uniform(-1, 1, np.shape(scale)) if self._bias == 0 else float(self._bias)
+    return (u * self.DECISION_ULPS * np.finfo(self.dt_).eps * np.abs(scale)).astype(self.dt_)
 
   def _nudge(self, x, symmetric=False):
     """x moved by -1, 0 or +1 ulp per entry (identity unless perturbing)."""
@@ -465,7 +486,8 @@ class Oracle:
     n = a.shape[-1]
     eye = np.eye(n, dtype=dt)
     r0 = eye - a @ a_inv
-    reset = safe_norm(r0, 2) > 1
+    n0 = safe_norm(r0, 2)
+    reset = n0 > 1 + self._margin(np.maximum(n0, 1))
     tr = np.trace(a @ np.swapaxes(a, -1, -2), axis1=-2, axis2=-1)
     alt = 0.5 * np.swapaxes(a, -1, -2) / tr[:, None, None]
     a_inv = np.where(reset[:, None, None], alt, a_inv)
@@ -474,7 +496,8 @@ class Oracle:
       nxt = self._nudge(a_inv @ (eye + r))
       r_next = self._nudge(eye - a @ nxt)
       err_next = safe_norm(r_next, 2)
-      a_inv = np.where((err_next < err)[:, None, None], nxt, a_inv)
+      take = err_next < err + self._margin(np.maximum(err_next, err))
+      a_inv = np.where(take[:, None, None], nxt, a_inv)
       r, err = r_next, err_next
     return a_inv
 
@@ -706,7 +729,7 @@ class Oracle:
     one = dt.type(1.0)
     for it in range(maxiter):
       if it > 0:
-        active = active & (err > tol)
+        active = active & (err > tol + self._margin(np.maximum(err, tol)))
       if not active.any():
         break
       ry = resid(y, active)  # value_and_grad at y: one residual, one A^T r
@@ -718,7 +741,11 @@ class Oracle:
       ls_on = active.copy()
       for _ in range(maxls):
         dx = nx - y
-        cond = cur * (fun(nx, ls_on) - fy) > cur * np.sum(dx * gy, -1) + 0.5 * np.sum(dx * dx, -1)
+        fn = fun(nx, ls_on)
+        dv = np.sum(dx * gy, -1)
+        sq = np.sum(dx * dx, -1)
+        scale = np.abs(cur * fn) + np.abs(cur * fy) + cur * np.sum(np.abs(dx * gy), -1) + 0.5 * sq
+        cond = cur * (fn - fy) > cur * dv + 0.5 * sq + self._margin(scale)
         ls_on = ls_on & cond
         if not ls_on.any():
           break

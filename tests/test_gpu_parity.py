@@ -243,12 +243,19 @@ def test_debug_contacts(name):
   torch.cuda.synchronize()
   for s in (st, out):
     assert s.contact is not None and s.contact.dist.shape == (n, sys.contacts.n)
-    xp, xr = _np(s.x.pos).astype(np.float64), _np(s.x.rot).astype(np.float64)
-    d, p, f = Oracle(sys, np.float64).contacts(xp, xr)
+    xp, xr = _np(s.x.pos), _np(s.x.rot)
+    d, p, f = Oracle(sys, np.float64).contacts(xp.astype(np.float64), xr.astype(np.float64))
+    # the FP32 oracle's own error on the same x: the capsule-capsule normal
+    # (between the segments' closest points) is ill-conditioned in FP32 when
+    # those points are close
+    d32, p32, f32 = Oracle(sys, np.float32).contacts(xp, xr)
     scale = np.maximum(np.abs(p).max(), 1.0)
-    np.testing.assert_allclose(_np(s.contact.dist), d, atol=2e-6 * scale, rtol=0)
-    np.testing.assert_allclose(_np(s.contact.pos), p, atol=2e-6 * scale, rtol=0)
-    np.testing.assert_allclose(_np(s.contact.frame), f, atol=2e-6, rtol=0)
+    for got, ref, r32, floor in ((s.contact.dist, d, d32, 2e-6 * scale), (s.contact.pos, p, p32, 2e-6 * scale),
+                                 (s.contact.frame, f, f32, 2e-6)):
+      # per contact slot: max over its entries
+      err = np.abs(_np(got) - ref).reshape(n, sys.contacts.n, -1).max(-1)
+      bar = np.maximum(floor, 3 * np.abs(r32 - ref).reshape(n, sys.contacts.n, -1).max(-1))
+      assert (err <= bar).all(), (err.max(), np.unravel_index(np.argmax(err - bar), err.shape))
     assert s.contact.dist is s.contact_dist
   # a step without debug returns no contact
   plain = P.step(sys, out, _t(actions(sys, n, rng)))
