@@ -51,7 +51,7 @@ enum braxg_inverse_mode {
 enum braxg_env_flags {
   BRAXG_ENV_NONFINITE = 1,   /* q or qd not finite after the call */
   BRAXG_ENV_NOT_SPD = 2,     /* a Cholesky pivot was <= 0 */
-  BRAXG_ENV_NO_GRADIENT = 4, /* a step ran more than 32 active constraint rows: no gradient */
+  BRAXG_ENV_NO_GRADIENT = 4, /* a step's projected-gradient tape was missing or inconsistent: no gradient */
   BRAXG_ENV_SKIPPED = 8      /* not stepped: its batch work item did not fit the launch */
 };
 
@@ -269,8 +269,8 @@ int braxg_rollout_vjp_workspace_resident(const braxg_model* model, int n_env, in
  * qd0_bar [n, nv] and, optionally, the forward trajectory traj_q / traj_qd.
  * The mass-matrix inverse is exact (Cholesky); status bits as braxg_env_flags.
  * Supports hinge/slide/free joints, world-plane sphere and capsule contacts and
- * joint limits; envs whose steps exceed 32 active constraint rows get
- * BRAXG_ENV_NO_GRADIENT. */
+ * joint limits, with either constraint-solve path (A formed explicitly up to 32
+ * active rows, applied implicitly above). */
 int braxg_rollout_vjp(const braxg_model* model, void* stream, int n_env, int n_steps, int n_frames,
                       int ckpt_every, const float* act_seq, const float* q0, const float* qd0,
                       const float* q_bar, const float* qd_bar, float* act_bar, float* q0_bar,

@@ -148,3 +148,95 @@ def test_gradient_independent_of_resident_segments():
   for r in res[1:]:
     for a, b in zip(r[:4], res[0][:4]):
       torch.testing.assert_close(a, b, rtol=0, atol=0)
+
+
+def _lying_quadrupeds(sys_, n, seed):
+  """Quadrupeds pressed into the ground (torso 0.05-0.1 m high, legs as at
+  init): most envs have more than 32 active constraint rows, so every frame's
+  solve takes the implicit projected-gradient path."""
+  rng = np.random.default_rng(seed)
+  q = sys_.init_q[None] + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))
+  q[:, 2] = 0.05 + rng.uniform(0.0, 0.05, n)
+  qd = 0.1 * rng.normal(size=(n, sys_.qd_size()))
+  return q.astype(np.float32).astype(np.float64), qd.astype(np.float32).astype(np.float64), rng
+
+
+def test_single_step_vjp_implicit_solve():
+  """The reverse of a step whose constraint solve ran the implicit path (more
+  than 32 active rows, A applied as J (Minv (J^T x)) + diag x) against the
+  numpy reverse of the same step (oracle/adjoint.py), which differentiates the
+  dense A; no env may be flagged BRAXG_ENV_NO_GRADIENT."""
+  P = _P()
+  from oracle.adjoint import StepAdjoint
+  sys_ = load('quadruped')
+  n = 32
+  q, qd, rng = _lying_quadrupeds(sys_, n, 71)
+  full = P.init(sys_, _t(q), _t(qd), full=True)
+  torch.cuda.synchronize()
+  rows = (full.con_diag.cpu().numpy() != 0).sum(-1)
+  assert (rows > 32).mean() >= 0.5, rows
+  act = actions(sys_, n, rng).astype(np.float32).astype(np.float64)
+  qbo, qdbo = rng.normal(size=q.shape), rng.normal(size=qd.shape)
+  adj = StepAdjoint(sys_)
+  _, _, T = adj.forward(q, qd, act)
+  adj._xr = T['s'].x_rot
+  rq, rqd, ract = adj.vjp(T, qbo, qdbo)
+  act_bar, q0b, qd0b, status, _ = P.rollout_grad(
+      sys_, _t(q), _t(qd), _t(act[None]), _t(qbo[None]), _t(qdbo[None]), n_frames=1, ckpt_every=1)
+  torch.cuda.synchronize()
+  st = status.cpu().numpy()
+  assert (st == 0).all(), st
+  for nm, g, r in (('q', q0b, rq), ('qd', qd0b, rqd), ('act', act_bar[0], ract)):
+    e = _rel(g.cpu().numpy(), r)
+    big, small = e[rows > 32], e[rows <= 32]
+    print(f'lying quadruped (rows > 32 in {(rows > 32).sum()} of {n}) {nm}: implicit p50 {np.median(big):.2e} '
+          f'max {big.max():.2e}; explicit max {small.max() if small.size else 0:.2e}')
+    assert np.quantile(e, 0.95) <= 2e-3, (nm, np.sort(e)[-4:])
+
+
+def test_rollout_gradient_implicit_solve_finite_differences():
+  """Gradient of a 2-env-step x 2-frame rollout of the lying quadrupeds (every
+  solve on the implicit path) against FP64 central differences (eps 1e-5)."""
+  P = _P()
+  from oracle.pipeline import Oracle
+  sys_ = load('quadruped')
+  n, H, F = 8, 2, 2
+  q0, qd0, rng = _lying_quadrupeds(sys_, n, 72)
+  u = rng.uniform(-1, 1, (H, n, sys_.act_size()))
+  o = Oracle(sys_, np.float64, exact_inverse=True)
+
+  def loss(qd0_, u_):  # -mean_t torso x-velocity + 1e-3 sum |u|^2, per env
+    s = o.init(q0, qd0_)
+    tot = np.zeros(n)
+    for t in range(H):
+      s = o.env_step(s, u_[t], F)
+      tot += -s.qd[:, 0] / H
+    return tot + 1e-3 * np.sum(u_ ** 2, axis=(0, 2))
+
+  qd_bar = np.zeros((H, n, sys_.qd_size()))
+  qd_bar[:, :, 0] = -1.0 / H
+  act_bar, _, qd0b, status, _ = P.rollout_grad(
+      sys_, _t(q0), _t(qd0), _t(u), None, _t(qd_bar), n_frames=F, ckpt_every=1)
+  torch.cuda.synchronize()
+  assert (status.cpu().numpy() == 0).all()
+  g_u = act_bar.cpu().numpy() + 2e-3 * u
+  eps = 1e-5
+  fd_u = np.zeros_like(u)
+  for t in range(H):
+    for k in range(sys_.act_size()):
+      up, um = u.copy(), u.copy()
+      up[t, :, k] += eps
+      um[t, :, k] -= eps
+      fd_u[t, :, k] = (loss(qd0, up) - loss(qd0, um)) / (2 * eps)
+  fd_qd = np.zeros((n, sys_.qd_size()))
+  for k in range(sys_.qd_size()):
+    a, b = qd0.copy(), qd0.copy()
+    a[:, k] += eps
+    b[:, k] -= eps
+    fd_qd[:, k] = (loss(a, u) - loss(b, u)) / (2 * eps)
+  eu = _rel(np.swapaxes(g_u, 0, 1), np.swapaxes(fd_u, 0, 1))
+  eq = _rel(qd0b.cpu().numpy(), fd_qd)
+  print(f'lying quadruped rollout grad vs FP64 FD: act p50 {np.median(eu):.2e} max {eu.max():.2e}; '
+        f'qd0 p50 {np.median(eq):.2e} max {eq.max():.2e}')
+  assert np.median(eu) <= 1e-3 and (eu <= 1e-2).mean() >= 7 / 8
+  assert np.median(eq) <= 1e-3 and (eq <= 1e-2).mean() >= 7 / 8
