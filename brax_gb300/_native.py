@@ -17,7 +17,7 @@ STATE_FIELDS = (
     'q', 'qd', 'mass_mx_inv', 'x_pos', 'x_rot', 'xd_ang', 'xd_vel', 'qf_smooth',
     'qf_constraint', 'qdd', 'root_com', 'cinr_pos', 'cinr_rot', 'cinr_i', 'cd',
     'cdof', 'cdofd', 'mass_mx', 'con_jac', 'con_diag', 'con_aref', 'status', 'cache',
-    'contact_dist', 'contact_pos', 'contact_frame')
+    'contact_dist', 'contact_pos', 'contact_frame', 'solver_maxiter')
 
 EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims', 'braxg_model_cache_words', 'braxg_model_cache_span',
            'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_rollout_vjp_workspace',

@@ -253,6 +253,8 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const EnvBase& B, 
     fin = tm.all(fin);
     if (tm.lane == 0) o.status[B.env + env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
   }
+  if (o.solver_maxiter != nullptr && tm.lane == 0)
+    o.solver_maxiter[B.env + env] = reinterpret_cast<const int*>(w.at(L.misc))[12];
   if ((o.contact_dist != nullptr || o.contact_pos != nullptr || o.contact_frame != nullptr) && md.ncon > 0) {
     // contact.get(sys, state.x) of the output state (brax/contact.py:28-67),
     // recomputed from x into scratch (free once the outputs above are read)
@@ -437,7 +439,7 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   // the block): every arena access below is behind `active`
   if (active && tm.lane == 0) {
     int* mi = reinterpret_cast<int*>(w.at(L.misc));
-    mi[1] = mi[9] = mi[10] = 0;
+    mi[1] = mi[9] = mi[10] = mi[12] = mi[13] = 0;
   }
   tm.sync();
   pf.mark(BRAXG_PROF_IO);

@@ -109,7 +109,9 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.tau = take(nv);
   L.v1 = take(nv);
   L.v2 = take(nv);
-  L.misc = take(12);  // [0] active rows, [1] NS resets, [2..8] env-step task state, [9..10] PG cycles
+  // [0] active rows, [1] NS resets, [2..8] env-step task state, [9..10] PG
+  // cycles, [11] cache tag, [12] solves stopped at maxiter, [13] bounds flags
+  L.misc = take(16);
   L.xp = take(3 * nl);
   L.xr = take(4 * nl);
   L.xa = take(3 * nl);
@@ -1622,6 +1624,8 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     for (int i = 0; i < nrow; ++i) s = fmaf(J[i * ldj + d], x[i], s);
     qfc[d] = s;
   }
+  // the solve ran out of iterations with the error above tol
+  if (tm.lane == 0 && iters == md.pg_iters && err > md.pg_tol) reinterpret_cast<int*>(w.at(L.misc))[12] += 1;
   if (tape != nullptr) {
     for (int i = tm.lane; i < nrow; i += T) tape[4 + i] = x[i];
     if (tm.lane == 0) {
@@ -1773,6 +1777,7 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape, b
     for (int i = 0; i < nrow; ++i) s = fmaf(w.jrow(i)[d], x[i], s);
     qfc[d] = s;
   }
+  if (tm.lane == 0 && iters == md.pg_iters && err > md.pg_tol) reinterpret_cast<int*>(w.at(L.misc))[12] += 1;
   if (tape != nullptr) {
     for (int i = tm.lane; i < nrow; i += T) tape[4 + i] = x[i];
     if (tm.lane == 0) {

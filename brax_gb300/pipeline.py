@@ -165,6 +165,9 @@ class State:
   contact_dist: Optional[torch.Tensor] = None
   contact_pos: Optional[torch.Tensor] = None
   contact_frame: Optional[torch.Tensor] = None
+  # [n] int32: pipeline steps of the call whose projected-gradient solve
+  # stopped at solver_iterations with its error above tol (``solver_stats``)
+  solver_maxiter: Optional[torch.Tensor] = None
   # [n, Model.cache_words] position-level terms of this state, computed by
   # the call that made it; a step from this state reuses them for every env
   # whose q / qd / parameters are unchanged (bit for bit) instead of
@@ -359,10 +362,11 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
          full: bool = False, inverse_mode: int = NEWTON_SCHULZ, out: Optional[State] = None,
          threads_per_env: int = 0, envs_per_cta: int = 0,
          profile: Optional[torch.Tensor] = None, relax_barriers: int = 0,
-         randomization: Optional[dict] = None) -> State:
+         randomization: Optional[dict] = None, solver_stats: bool = False) -> State:
   """brax/generalized/pipeline.py:64-94; n_frames > 1 repeats it with the same
   action (PipelineEnv.pipeline_step, brax/envs/base.py:128-137).  ``debug``
-  adds ``state.contact`` of the output state."""
+  adds ``state.contact`` of the output state; ``solver_stats`` fills
+  ``state.solver_maxiter``."""
   m = model_for(sys, state.q.device)
   n = state.q.shape[0]
   act_p = None
@@ -373,6 +377,8 @@ def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
     act_p = act.data_ptr()
   if out is None:
     out = _alloc(m, n, full, m.device, state.cache is not None)
+  if solver_stats and out.solver_maxiter is None:
+    out = out.replace(solver_maxiter=torch.empty(n, dtype=torch.int32, device=m.device))
   if debug and out.contact_dist is None:
     out = _alloc_contacts(m, out)
   elif not debug and (out.contact_dist is not None or out.contact is not None):

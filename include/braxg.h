@@ -110,6 +110,11 @@ typedef struct {
   float* contact_dist;   /* [n, ncon] */
   float* contact_pos;    /* [n, ncon, 3] */
   float* contact_frame;  /* [n, ncon, 3, 3] */
+  /* Optional solver diagnostic, no counterpart in the reference (jaxopt
+   * returns no state there): per env, the number of the call's pipeline
+   * steps whose projected-gradient solve (brax/generalized/constraint.py:
+   * 229-238) stopped at solver_iterations with its error still above tol. */
+  int32_t* solver_maxiter;  /* [n] */
 } braxg_state;
 
 /* Per-stage profile slots of braxg_options.stage_cycles (sums over envs of

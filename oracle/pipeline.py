@@ -208,6 +208,8 @@ class State:
   # diagnostics of the last constraint solve
   contact_dist: Optional[np.ndarray] = None
   pg_matvecs: Optional[np.ndarray] = None
+  pg_maxiter: Optional[np.ndarray] = None  # the solve stopped at maxiter with err > tol
+  pg_err: Optional[np.ndarray] = None      # its final stopping error
 
   def replace(self, **kw):
     return dataclasses.replace(self, **kw)
@@ -762,6 +764,7 @@ class Oracle:
       t = np.where(active, nt, t)
       ss = np.where(active, nss, ss)
       err = np.where(active, e, err)
+    self.last_pg = {'maxiter': active & (err > tol) & (maxiter > 0) & (m > 0), 'err': err}
     return x, cnt
 
   def constraint_force(self, s: State):
@@ -769,6 +772,7 @@ class Oracle:
     sys = self.sys
     B, dt, nv = s.q.shape[0], self.dt_, self.st.nv
     if s.con_jac.shape[1] == 0:
+      self.last_pg = {'maxiter': np.zeros(B, bool), 'err': np.zeros(B, dt)}
       return np.zeros((B, nv), dt), np.zeros(B, np.int64)
     jm = s.con_jac @ s.mass_mx_inv
     a = jm @ np.swapaxes(s.con_jac, -1, -2)
@@ -941,7 +945,8 @@ class Oracle:
     tau = self.to_tau(act, s.q, s.qd)
     s = s.replace(qf_smooth=self.forward(s, tau))
     qfc, cnt = self.constraint_force(s)
-    s = s.replace(qf_constraint=qfc, pg_matvecs=cnt)
+    s = s.replace(qf_constraint=qfc, pg_matvecs=cnt, pg_maxiter=self.last_pg['maxiter'],
+                  pg_err=self.last_pg['err'])
     s = self.integrate(s)
     xp, xr, xa, xv = self.kinematics(s.q, s.qd)
     s = s.replace(x_pos=xp, x_rot=xr, xd_ang=xa, xd_vel=xv)

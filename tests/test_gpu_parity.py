@@ -260,3 +260,32 @@ def test_debug_contacts(name):
   # a step without debug returns no contact
   plain = P.step(sys, out, _t(actions(sys, n, rng)))
   assert plain.contact is None
+
+
+def test_solver_maxiter_diagnostic():
+  """state.solver_maxiter (solver_stats=True) counts the steps whose
+  projected-gradient solve stopped at solver_iterations with its error above
+  tol; one pipeline step of quadrupeds in contact against the FP32 oracle's
+  own stopping decision (the two may differ only where a line-search tie or
+  the stopping test itself went the other way)."""
+  P = _pipeline()
+  from oracle.pipeline import Oracle
+  sys = load('quadruped')
+  n = 512
+  o64 = Oracle(sys, np.float64, exact_inverse=True)
+  s64, rng = _states(sys, o64, n, 12, seed=41)
+  q, qd = s64.q.astype(np.float32), s64.qd.astype(np.float32)
+  act = actions(sys, n, rng).astype(np.float32)
+  o32 = Oracle(sys, np.float32, exact_inverse=True)
+  r32 = o32.step(o32.restore(q, qd, None), act)
+  st = P.init(sys, _t(q), _t(qd))
+  out = P.step(sys, st, _t(act), inverse_mode=P.CHOLESKY, solver_stats=True)
+  two = P.step(sys, st, _t(act), inverse_mode=P.CHOLESKY, solver_stats=True, n_frames=2)
+  torch.cuda.synchronize()
+  got = _np(out.solver_maxiter)
+  assert set(np.unique(got)) <= {0, 1}
+  assert set(np.unique(_np(two.solver_maxiter))) <= {0, 1, 2}
+  agree = (got == r32.pg_maxiter.astype(np.int32)).mean()
+  print(f'solver stopped at maxiter: GPU {got.mean():.3f}, FP32 oracle {r32.pg_maxiter.mean():.3f}, agree {agree:.4f}')
+  assert agree >= 0.98
+  assert got.sum() > 0
