@@ -11,7 +11,9 @@ import os
 import threading
 
 LIB_DIR = os.path.join(os.path.dirname(__file__), '_lib')
-LIB_PATH = os.path.join(LIB_DIR, 'libbraxg.so')
+# BRAXG_CHECK=1 selects the bounds-checked build (brax_gb300.build.build(check=True))
+CHECKED = os.environ.get('BRAXG_CHECK') == '1'
+LIB_PATH = os.path.join(LIB_DIR, 'check', 'libbraxg.so') if CHECKED else os.path.join(LIB_DIR, 'libbraxg.so')
 
 STATE_FIELDS = (
     'q', 'qd', 'mass_mx_inv', 'x_pos', 'x_rot', 'xd_ang', 'xd_vel', 'qf_smooth',
@@ -31,7 +33,7 @@ EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims', 'bra
 
 OK, ERR_INVALID, ERR_CUDA, ERR_UNSUPPORTED = 0, 1, 2, 3
 INV_NEWTON_SCHULZ, INV_CHOLESKY = 0, 1
-ENV_NONFINITE, ENV_NOT_SPD, ENV_NO_GRADIENT, ENV_SKIPPED = 1, 2, 4, 8
+ENV_NONFINITE, ENV_NOT_SPD, ENV_NO_GRADIENT, ENV_SKIPPED, ENV_BOUNDS = 1, 2, 4, 8, 16
 
 
 class State(ctypes.Structure):
@@ -107,7 +109,7 @@ def lib() -> ctypes.CDLL:
     if not os.path.exists(LIB_PATH):
       raise RuntimeError(
           f'braxg CUDA library not built ({LIB_PATH} missing); run '
-          '`python -c "import brax_gb300.build as b; b.build()"`')
+          f'`python -c "import brax_gb300.build as b; b.build(check={CHECKED})"`')
     l = ctypes.CDLL(LIB_PATH)
     vp, i32, P = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER
     l.braxg_model_create.argtypes = [vp, ctypes.c_size_t, i32, P(vp)]

@@ -10,7 +10,6 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(ROOT, 'brax_gb300', 'csrc')
 OUT_DIR = os.path.join(ROOT, 'brax_gb300', '_lib')
-BUILD_DIR = os.path.join(ROOT, 'brax_gb300', '_lib', 'obj')
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 # one translation unit per group of kernel instantiations so they compile in
 # parallel; braxg.cu holds the C ABI
@@ -36,20 +35,28 @@ def _sources_newer(target, deps):
   return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> str:
-  """Compiles (if stale) and returns the path of libbraxg.so."""
-  os.makedirs(BUILD_DIR, exist_ok=True)
+CHECK_DIR = os.path.join(OUT_DIR, 'check')
+
+
+def build(verbose: bool = False, force: bool = False, check: bool = False) -> str:
+  """Compiles (if stale) and returns the path of libbraxg.so.  check=True
+  builds the bounds-checked variant (-DBRAXG_CHECK) into _lib/check/ instead;
+  brax_gb300._native loads it when BRAXG_CHECK=1 is set."""
+  out_dir = CHECK_DIR if check else OUT_DIR
+  build_dir = os.path.join(out_dir, 'obj')
+  os.makedirs(build_dir, exist_ok=True)
   headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(('.cuh', '.h'))]
   headers.append(os.path.join(ROOT, 'include', 'braxg.h'))
   nvcc = _nvcc()
   jobs = []
   objs = []
+  extra = ['-DBRAXG_CHECK'] if check else []
   for u in UNITS:
     src = os.path.join(CSRC, u)
-    obj = os.path.join(BUILD_DIR, u.replace('.cu', '.o'))
+    obj = os.path.join(build_dir, u.replace('.cu', '.o'))
     objs.append(obj)
     if force or _sources_newer(obj, [src, *headers]):
-      jobs.append([nvcc, *_flags(['-Xptxas', '-v'] if verbose else []), '-c', src, '-o', obj])
+      jobs.append([nvcc, *_flags(extra + (['-Xptxas', '-v'] if verbose else [])), '-c', src, '-o', obj])
 
   def run(cmd):
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -61,7 +68,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     for log in ex.map(run, jobs):
       if verbose and log:
         print(log, file=sys.stderr)
-  lib = os.path.join(OUT_DIR, 'libbraxg.so')
+  lib = os.path.join(out_dir, 'libbraxg.so')
   if force or jobs or _sources_newer(lib, objs):
     run([nvcc, *ARCH, '-shared', '-o', lib, *objs, '-lcudart'])
   return lib
@@ -106,4 +113,4 @@ def build_xla(verbose: bool = False):
 
 
 if __name__ == '__main__':
-  print(build(verbose='-v' in sys.argv, force='-f' in sys.argv))
+  print(build(verbose='-v' in sys.argv, force='-f' in sys.argv, check='--check' in sys.argv))

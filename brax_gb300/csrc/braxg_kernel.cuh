@@ -121,6 +121,8 @@ __device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, 
   const Team<T> tm;
   const Model md(mw);
   const float* slot = a.cache_in + (B.env + env) * a.cache_stride;
+  // checked build: a misaligned slot is not used (and is flagged by the caller)
+  if (kChecked && ((reinterpret_cast<uintptr_t>(slot) | reinterpret_cast<uintptr_t>(w.b)) & 15u) != 0u) return false;
   // overflow rows: into the arena, or from the input's cache slot to the output's
   copy_position_terms<T>(tm, w.b, slot, *w.L, md.nv, md.m, w.b, w.L->ovf_g ? w.g : w.b, slot);
   tm.sync();
@@ -140,6 +142,7 @@ __device__ __noinline__ void store_cache(const StepArgs& a, const EnvBase& B, co
   if (tm.lane == 0) reinterpret_cast<int*>(w.at(w.L->misc))[11] = ok ? cache_tag<T>(w.L->ovf_g != 0, exact) : 0;
   tm.sync();
   float* slot = a.out.cache + (B.env + env) * a.cache_stride;
+  if (bx_misaligned<T>(w, slot, w.b)) return;
   // overflow rows: from the arena's scratch end, or already in this slot
   copy_position_terms<T>(tm, slot, w.b, *w.L, md.nv, md.m, w.b, slot, w.L->ovf_g ? slot : w.b);
 }
@@ -229,6 +232,7 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const EnvBase& B, 
     const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
     const int* rmap = reinterpret_cast<const int*>(w.at(L.rmap));
     int* inv = reinterpret_cast<int*>(w.at(L.scr));
+    if (bx_scratch<T>(w, scratch_outputs(L, m, md.ncon), w.at(L.scr) + m, nv)) return;
     for (int r = tm.lane; r < m; r += T) inv[r] = -1;
     tm.sync();
     for (int r = tm.lane; r < nrow; r += T) inv[rmap[r]] = r;
@@ -251,7 +255,10 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const EnvBase& B, 
     for (int i = tm.lane; i < nq; i += T) fin = fin && isfinite(w.at(L.q)[i]);
     for (int i = tm.lane; i < nv; i += T) fin = fin && isfinite(w.at(L.qd)[i]);
     fin = tm.all(fin);
-    if (tm.lane == 0) o.status[B.env + env] = (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD);
+    const bool bounds = w.failed();
+    if (tm.lane == 0)
+      o.status[B.env + env] =
+          (fin ? 0 : BRAXG_ENV_NONFINITE) | (ok ? 0 : BRAXG_ENV_NOT_SPD) | (bounds ? BRAXG_ENV_BOUNDS : 0);
   }
   if (o.solver_maxiter != nullptr && tm.lane == 0)
     o.solver_maxiter[B.env + env] = reinterpret_cast<const int*>(w.at(L.misc))[12];
@@ -263,6 +270,7 @@ __device__ __noinline__ void write_outputs(const StepArgs& a, const EnvBase& B, 
     float* cpos = dist + al4(nc);
     float* frame = cpos + al4(3 * nc);
     tm.sync();
+    if (bx_scratch<T>(w, scratch_outputs(L, md.m, nc), frame + 9 * nc, nv)) return;
     stage_contacts<T>(md.w, w, dist, cpos, frame);
     const long long e = B.env + env;
     store_vec<T>(tm, o.contact_dist ? o.contact_dist + e * nc : nullptr, dist, nc);
@@ -416,6 +424,8 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   w.b = arena + (size_t)team * w.L->total;
   if (sl->ovf_g) w.g = a.out.cache + (B.env + env) * a.cache_stride;
   const Layout& L = *w.L;
+  if (kChecked && active)
+    for (int i = tm.lane; i < kCanaryWords; i += T) reinterpret_cast<unsigned*>(w.b + L.canary)[i] = kCanary;
   const int nq = md.nq, nv = md.nv, nu = md.nu, ld = L.ldm;
   Prof pf(a.prof, active && tm.lane == 0);
 
@@ -440,6 +450,10 @@ __device__ __forceinline__ void run_team(const StepArgs& a, const EnvBase& B, co
   if (active && tm.lane == 0) {
     int* mi = reinterpret_cast<int*>(w.at(L.misc));
     mi[1] = mi[9] = mi[10] = mi[12] = mi[13] = 0;
+    if (kChecked && !a.init && a.cache_in != nullptr &&
+        ((reinterpret_cast<uintptr_t>(a.cache_in + (B.env + env) * a.cache_stride) | reinterpret_cast<uintptr_t>(w.b)) &
+         15u) != 0u)
+      mi[13] |= (int)kBoundsAlign;
   }
   tm.sync();
   pf.mark(BRAXG_PROF_IO);

@@ -2,6 +2,7 @@
 // per-env working state in shared memory, the packed model in shared memory
 // once per CTA.  Each stage cites the reference function it restates.
 #pragma once
+#include "braxg_check.h"
 #include "braxg_math.cuh"
 #include "model_layout.h"
 
@@ -55,6 +56,8 @@ struct Layout {
   int J, jcap, jovf, rdiag, raref, rmap;
   int prm;  // per-env parameters: friction [ncon], actuator gain, bias_q, bias_qd [nu each]
   int scr, scr_words, itmp;
+  int mrows;   // constraint rows of the model (4 ncon + nlim)
+  int canary;  // the checked build's canary words (kCanaryWords) follow the arena here
   int total;
   // 1: the Jacobian rows beyond jcap live outside the arena, at word jovf of
   // the env's slot of the output state's cache (global memory)
@@ -173,10 +176,63 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.scr = take(L.scr_words);
   if (!own_m) L.M = L.scr + m_off;
   L.itmp = L.scr + inv_off;
-  L.total = al4(o);
+  L.mrows = m;
+  L.canary = al4(o);
+  L.total = L.canary + kCanaryWords;
   L.ovf_g = ovf_global ? 1 : 0;
   L.jovf = ovf_global ? L.total : L.scr + L.scr_words - ovf;
   return L;
+}
+
+// The scratch words each stage lays its temporaries into ([start, end) arena
+// offsets, the carve-outs of the stage code below), and what it must leave
+// intact: the overflow Jacobian rows (live from the Jacobian stage through
+// the constraint solve and the outputs) and the mass matrix when it lives in
+// scratch (live from CRBA through the inverse, the Jacobian stage and the
+// outputs).  The layout sizes scratch for all of them; the checked build
+// verifies each against the layout and each stage's actual pointers against
+// its declaration.
+struct ScratchUse {
+  int start, end;
+  bool keep_ovf, keep_m;
+};
+__host__ __device__ inline ScratchUse scratch_fk(const Layout& L, int nl, int nv) {  // and transform_com
+  return {L.scr, L.scr + al4(14 * nl) + 4 * nv, false, false};
+}
+__host__ __device__ inline ScratchUse scratch_crba(const Layout& L, int nl, int nv) {
+  return {L.scr, L.scr + 13 * nl + 6 * nv, false, true};
+}
+__host__ __device__ inline ScratchUse scratch_inverse(const Layout& L, int nv, bool exact, bool rows4) {
+  const int words = exact ? nv * explicit_lda(nv) : (rows4 ? 3 * nv * ns_ldb(nv) : 2 * nv * L.ldm);
+  return {L.itmp, L.itmp + words, false, true};
+}
+__host__ __device__ inline ScratchUse scratch_jacobian(const Layout& L, int ncon) {
+  return {L.scr, L.scr + al4(ncon) + al4(3 * ncon) + al4(9 * ncon) + ncon, true, true};
+}
+__host__ __device__ inline ScratchUse scratch_smooth(const Layout& L, int nl, int nu, bool fluid) {
+  return {L.scr, L.scr + 12 * nl + al4(nu) + (fluid ? 9 * nl : 0), true, false};
+}
+__host__ __device__ inline ScratchUse scratch_pg_explicit(const Layout& L, int nrow) {
+  const int a = nrow * explicit_lda(nrow) + al4(nrow);
+  const int wv = nrow * L.ldm > 9 * al4(nrow) ? nrow * L.ldm : 9 * al4(nrow);
+  return {L.scr, L.scr + a + wv, false, false};
+}
+__host__ __device__ inline ScratchUse scratch_pg_implicit(const Layout& L, int m, int nv) {
+  return {L.scr, L.scr + 8 * al4(m) + 2 * al4(nv), true, false};
+}
+__host__ __device__ inline ScratchUse scratch_integrate(const Layout& L, int nv) {  // M + diag(damping) dt
+  return {L.scr, L.scr + nv * L.ldm, false, false};
+}
+__host__ __device__ inline ScratchUse scratch_outputs(const Layout& L, int m, int ncon) {
+  // the row map (before the outputs read the overflow rows), then the contacts
+  const int c = al4(ncon) + al4(3 * ncon) + 9 * ncon;
+  return {L.scr, L.scr + (m > c ? m : c), true, false};
+}
+// Whether a stage's declared use fits the layout (scratch_ok of braxg_check.h).
+__host__ __device__ inline bool scratch_use_ok(const Layout& L, const ScratchUse& u, int nv) {
+  const bool m_in = u.keep_m && L.M >= L.scr;
+  return scratch_ok(L.scr, L.scr_words, L.jovf, L.ovf_g == 0, u.keep_ovf, u.start, u.end, m_in ? L.M : 0,
+                    m_in ? L.M + nv * L.ldm : 0);
 }
 
 // Layout of a packed model descriptor (header words).
@@ -221,13 +277,62 @@ struct Ws {
   const Layout* L;
   float* g = nullptr;  // the env's slot of the output state's cache (overflow rows, L->ovf_g)
   __device__ __forceinline__ float* at(int off) const { return b + off; }
+  // checked build: record a failed check (misc[13]) / whether one failed
+  __device__ __forceinline__ void flag(unsigned bit) const {
+    if (kChecked) atomicOr(reinterpret_cast<unsigned*>(b + L->misc) + 13, bit);
+  }
+  __device__ __forceinline__ bool failed() const {
+    return kChecked && reinterpret_cast<const volatile unsigned*>(b + L->misc)[13] != 0u;
+  }
   // active constraint row r of the Jacobian (first jcap rows in their slot,
   // the rest at the end of scratch or in the env's cache slot)
   __device__ __forceinline__ float* jrow(int r) const {
+    if (kChecked && (r < 0 || r >= L->mrows)) {
+      flag(kBoundsRow);
+      return b + L->scr;
+    }
     if (r < L->jcap) return b + L->J + r * L->ldj;
     return (L->ovf_g ? g : b) + L->jovf + (r - L->jcap) * L->ldj;
   }
 };
+
+// Checked build: the entry test of every stage (the canary after the arena,
+// then any failed check of the env); true if the stage must return at once.
+template <int T>
+__device__ __forceinline__ bool bx_stop(Ws w) {
+  if (!kChecked) return false;
+  const Team<T> tm;
+  tm.sync();
+  const unsigned* c = reinterpret_cast<const unsigned*>(w.b + w.L->canary);
+  bool ok = true;
+  for (int i = tm.lane; i < kCanaryWords; i += T) ok = ok && c[i] == kCanary;
+  if (!tm.all(ok)) w.flag(kBoundsCanary);
+  tm.sync();
+  return w.failed();
+}
+
+// Checked build: a stage's declared scratch use against the layout, and the
+// end of its actual last region against the declaration; true (after
+// flagging) if either fails, and the stage must then return before writing.
+template <int T>
+__device__ __forceinline__ bool bx_scratch(Ws w, const ScratchUse& u, const float* actual_end, int nv) {
+  if (!kChecked) return false;
+  const bool bad = !scratch_use_ok(*w.L, u, nv) || actual_end > w.b + u.end;
+  if (bad) w.flag(kBoundsScratch);
+  Team<T>().sync();
+  return bad;
+}
+
+// Checked build: 16-byte alignment of float4 operands; true (after flagging)
+// if one is misaligned.
+template <int T>
+__device__ __forceinline__ bool bx_misaligned(Ws w, const void* p0, const void* p1 = nullptr) {
+  if (!kChecked) return false;
+  const bool bad = ((reinterpret_cast<uintptr_t>(p0) | reinterpret_cast<uintptr_t>(p1)) & 15u) != 0u;
+  if (bad) w.flag(kBoundsAlign);
+  Team<T>().sync();
+  return bad;
+}
 
 // ---------------------------------------------------------------------------
 // kinematics.forward: brax/kinematics.py:31-108
@@ -244,6 +349,7 @@ __device__ __noinline__ void stage_fk(const int* mw, Ws w) {
   float* ja_ = jr_ + 4 * md.nl;
   float* jv_ = ja_ + 3 * md.nl;
   float* jq_ = w.at(L.scr) + al4(14 * md.nl);  // [nv][4] joint rotation of each stacked dof
+  if (bx_stop<T>(w) || bx_scratch<T>(w, scratch_fk(L, md.nl, md.nv), jq_ + 4 * md.nv, md.nv)) return;
   const int* ltype = md.I(BXM_O_LINK_TYPE);
   const int* qadr = md.I(BXM_O_LINK_QADR);
   const int* dadr = md.I(BXM_O_LINK_DADR);
@@ -348,6 +454,7 @@ __device__ __noinline__ void stage_com(const int* mw, Ws w) {
   float* xir = xip + 3 * nl;
   float* jjp = xir + 4 * nl;
   float* jjr = jjp + 3 * nl;
+  if (bx_stop<T>(w) || bx_scratch<T>(w, scratch_fk(L, nl, md.nv), jjr + 4 * nl, md.nv)) return;
   const float* xp = w.at(L.xp);
   const float* xr = w.at(L.xr);
   const float* mass = md.F(BXM_O_LI_MASS);
@@ -520,6 +627,7 @@ __device__ __noinline__ void stage_crba(const int* mw, Ws w) {
   float* crbi = w.at(L.scr);
   float* crbp = crbi + 9 * nl;
   float* crbm = crbp + 3 * nl;
+  if (bx_stop<T>(w) || bx_scratch<T>(w, scratch_crba(L, nl, nv), crbm + nl + 6 * nv, nv)) return;
   const float* ci = w.at(L.ci);
   const float* cp = w.at(L.cp);
   const float* mass = md.F(BXM_O_LI_MASS);
@@ -788,7 +896,13 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   float* P = w.at(L.Minv);
   float* S1 = w.at(L.itmp);
   if (n == 0) return true;
-  if (exact) return spd_inverse_sweep<T>(tm, n, ld, M, S1, P);
+  if (bx_stop<T>(w)) return true;
+  if (exact) {
+    if (bx_scratch<T>(w, scratch_inverse(L, n, true, false), S1 + n * explicit_lda(n), n) ||
+        bx_misaligned<T>(w, S1))
+      return true;
+    return spd_inverse_sweep<T>(tm, n, ld, M, S1, P);
+  }
   if (num_iter <= 0) return true;
   // Up to 16 dofs the iterates and residuals live in rows of stride lb
   // (16-byte loads of every product's right-hand operand; columns n .. lb
@@ -800,6 +914,9 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
   float* cur = kRows4 ? S1 : P;
   float* nxt = kRows4 ? S1 + n * lb : S1 + n * ld;
   float* R = kRows4 ? S1 + 2 * n * lb : S1;
+  if (bx_scratch<T>(w, scratch_inverse(L, n, false, kRows4), kRows4 ? R + n * lb : nxt + n * ld, n) ||
+      bx_misaligned<T>(w, kRows4 ? S1 : nullptr))
+    return true;
   if (kRows4) {
     for (int e = tm.lane; e < 3 * n * lb; e += T) {
       const int i = e / lb, j = e - i * lb;  // rows of the three buffers in turn
@@ -1022,6 +1139,7 @@ __device__ __noinline__ void stage_jacobian(const int* mw, Ws w) {
   float* cpos = dist + al4(ncon);
   float* frame = cpos + al4(3 * ncon);
   int* rcon = reinterpret_cast<int*>(frame + al4(9 * ncon));
+  if (bx_stop<T>(w) || bx_scratch<T>(w, scratch_jacobian(L, ncon), frame + al4(9 * ncon) + ncon, nv)) return;
   int* rmap = reinterpret_cast<int*>(w.at(L.rmap));
   float* rdiag = w.at(L.rdiag);
   float* raref = w.at(L.raref);
@@ -1148,6 +1266,9 @@ __device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
   float* cdd = w.at(L.scr);
   float* cf = cdd + 6 * nl;
   float* force = cf + 6 * nl;
+  if (bx_stop<T>(w) ||
+      bx_scratch<T>(w, scratch_smooth(L, nl, md.nu, md.fluid), force + al4(md.nu) + (md.fluid ? 9 * nl : 0), nv))
+    return;
   const float* q = w.at(L.q);
   const float* qd = w.at(L.qd);
   const float* act = w.at(L.act);
@@ -1393,6 +1514,10 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   float* gx = rn + al4(nrow);
   float* gy = gx + al4(nrow);
   float* gn = gy + al4(nrow);
+  if (bx_scratch<T>(w, scratch_pg_explicit(L, nrow), (gn + al4(nrow) > W + nrow * ld) ? gn + al4(nrow) : W + nrow * ld,
+                    nv) ||
+      bx_misaligned<T>(w, A, A + la) || bx_misaligned<T>(w, b, x))
+    return 0;
   const float* J = w.at(L.J);
   const float* Minv = w.at(L.Minv);
   const float* rdiag = w.at(L.rdiag);
@@ -1648,6 +1773,11 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape, b
   const int nv = md.nv, ld = L.ldm;
   const int nrow = reinterpret_cast<const int*>(w.at(L.misc))[0];
   float* qfc = w.at(L.qfc);
+  if (bx_stop<T>(w)) return 0;
+  if (kChecked && (nrow < 0 || nrow > md.m)) {
+    w.flag(kBoundsRow);
+    return 0;
+  }
   if (nrow == 0) {
     for (int d = tm.lane; d < nv; d += T) qfc[d] = 0.f;
     if (tape != nullptr && tm.lane == 0) {
@@ -1670,6 +1800,7 @@ __device__ __noinline__ int stage_constraint(const int* mw, Ws w, float* tape, b
   float* ny = gx + al4(m);
   float* t1 = ny + al4(m);
   float* t2 = t1 + al4(nv);
+  if (bx_scratch<T>(w, scratch_pg_implicit(L, m, nv), t2 + al4(nv), nv)) return 0;
   const float* Minv = w.at(L.Minv);
   const float* raref = w.at(L.raref);
   const float* qfs = w.at(L.qfs);
@@ -1806,10 +1937,12 @@ __device__ __noinline__ bool stage_integrate(const int* mw, Ws w) {
   float* qd = w.at(L.qd);
   float* q = w.at(L.q);
   bool ok = true;
+  if (bx_stop<T>(w)) return true;
   for (int d = tm.lane; d < nv; d += T) v[d] = qfs[d] + qfc[d];
   tm.sync();
   if (md.ns_iters == 0) {  // (M + diag(damping) dt)^-1: integrator.py:58-62
     float* A = w.at(L.scr);
+    if (bx_scratch<T>(w, scratch_integrate(L, nv), A + nv * ld, nv)) return true;
     const float* M = w.at(L.M);
     const float* damp = md.F(BXM_O_D_DAMP);
     for (int idx = tm.lane; idx < nv * nv; idx += T) {

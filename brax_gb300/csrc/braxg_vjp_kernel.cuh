@@ -117,6 +117,16 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   const int tape_words = a.snap_words - L.total;
   // ---- forward with checkpoints ----
   if (active) {
+    if (tm.lane == 0) {  // the solve counter and the checked build's flags
+      reinterpret_cast<int*>(w.at(L.misc))[12] = 0;
+      reinterpret_cast<int*>(w.at(L.misc))[13] = 0;
+    }
+    tm.sync();
+    if (kChecked)
+      for (int i = tm.lane; i < kCanaryWords; i += T) reinterpret_cast<unsigned*>(w.b + L.canary)[i] = kCanary;
+    if (kChecked && ((reinterpret_cast<uintptr_t>(w.b) | reinterpret_cast<uintptr_t>(a.snap) |
+                      (uintptr_t)(a.snap_words * 4)) & 15u) != 0u)
+      w.flag(kBoundsAlign);
     copy_vec<T>(tm, w.at(L.q), a.q0 + env * nq, nq);
     copy_vec<T>(tm, w.at(L.qd), a.qd0 + env * nv, nv);
     load_params<T>(tm, braxg_randomization{}, md, w, env);  // the model's parameters
@@ -272,7 +282,8 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   if (a.q0_bar != nullptr) copy_vec<T>(tm, a.q0_bar + env * nq, qbo, nq);
   if (a.qd0_bar != nullptr) copy_vec<T>(tm, a.qd0_bar + env * nv, qdbo, nv);
   if (a.status != nullptr && tm.lane == 0)
-    a.status[env] = (ok ? 0 : BRAXG_ENV_NOT_SPD) | (taped ? 0 : BRAXG_ENV_NO_GRADIENT);
+    a.status[env] = (ok ? 0 : BRAXG_ENV_NOT_SPD) | (taped ? 0 : BRAXG_ENV_NO_GRADIENT) |
+                    (w.failed() ? BRAXG_ENV_BOUNDS : 0);
 }
 
 template <int T, int NVB>

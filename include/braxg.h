@@ -52,7 +52,8 @@ enum braxg_env_flags {
   BRAXG_ENV_NONFINITE = 1,   /* q or qd not finite after the call */
   BRAXG_ENV_NOT_SPD = 2,     /* a Cholesky pivot was <= 0 */
   BRAXG_ENV_NO_GRADIENT = 4, /* a step's projected-gradient tape was missing or inconsistent: no gradient */
-  BRAXG_ENV_SKIPPED = 8      /* not stepped: its batch work item did not fit the launch */
+  BRAXG_ENV_SKIPPED = 8,     /* not stepped: its batch work item did not fit the launch */
+  BRAXG_ENV_BOUNDS = 16      /* checked build only: an arena, row or alignment check failed */
 };
 
 typedef struct {
