@@ -230,11 +230,12 @@ class Oracle:
 
     perturb_seed (for the parity tests' rounding envelope): when set, every
     step moves the intermediates whose rounding depends on the summation
-    order (qf_smooth, mass_mx_inv and the Newton-Schulz iterates, and the
-    projected-gradient problem's A and b; A symmetrically) by -1, 0 or +1 ulp
-    at random, and every discrete decision taken on two computed values (the
-    line search's sufficient-decrease test, the solver's stopping test, the
-    Newton-Schulz acceptance and reset tests) sees its two sides shifted by
+    order (qf_smooth, the mass matrix, mass_mx_inv and the Newton-Schulz
+    iterates, and the projected-gradient problem's A and b; the symmetric ones
+    symmetrically) by -1, 0 or +1 ulp at random, and every discrete decision
+    taken on two computed values (the line search's sufficient-decrease test,
+    the solver's stopping test, the Newton-Schulz acceptance and reset tests,
+    the capsule-capsule closest-point choice) sees its two sides shifted by
     up to DECISION_ULPS ulps of their magnitude: decisions whose sides agree
     that closely may go either way in another operation order.
     perturb_bias -1 / +1 shifts every such decision the same way (a draw
@@ -511,7 +512,7 @@ class Oracle:
     return np.swapaxes(linv, -1, -2) @ linv
 
   def matrix_inv(self, s: State, num_iter: int) -> State:
-    mx = self.mass_matrix(s)
+    mx = self._nudge(self.mass_matrix(s), symmetric=True)
     if self.st.nv == 0:
       return s.replace(mass_mx=mx, mass_mx_inv=mx)
     if num_iter > 0 and not self.exact_inverse:
@@ -586,7 +587,7 @@ class Oracle:
       elif kind == S.CON_CAPSULE_CAPSULE:
         s1 = m1[..., :, 2] * size[g1, 1]
         s2 = m2[..., :, 2] * size[g2, 1]
-        a_, b_ = _closest_segment_to_segment_points(p1 - s1, p1 + s1, p2 - s2, p2 + s2)
+        a_, b_ = _closest_segment_to_segment_points(p1 - s1, p1 + s1, p2 - s2, p2 + s2, self._margin)
         d, ps, nrm = _sphere_sphere(a_, size[g1, 0], b_, size[g2, 0])
         dist[:, k], pos[:, k], frame[:, k] = d, ps, make_frame(nrm)
       else:
@@ -990,7 +991,7 @@ def _closest_segment_point_and_dist(a, b, pt):
   return p, dot(pt - p, pt - p)
 
 
-def _closest_segment_to_segment_points(a0, a1, b0, b1):
+def _closest_segment_to_segment_points(a0, a1, b0, b1, margin=None):
   dir_a, len_a = _norm_with_norm(a1 - a0)
   dir_b, len_b = _norm_with_norm(b1 - b0)
   half_a, half_b = len_a * 0.5, len_b * 0.5
@@ -1009,5 +1010,6 @@ def _closest_segment_to_segment_points(a0, a1, b0, b1):
   best_b = b_mid + dir_b * tb[..., None]
   new_a, d1 = _closest_segment_point_and_dist(a0, a1, best_b)
   new_b, d2 = _closest_segment_point_and_dist(b0, b1, best_a)
-  sel = (d1 < d2)[..., None]
+  # `margin` (the oracle's rounding envelope): the decision's two sides shifted
+  sel = (d1 < d2 + (0 if margin is None else margin(np.maximum(d1, d2))))[..., None]
   return np.where(sel, new_a, best_a), np.where(sel, best_b, new_b)

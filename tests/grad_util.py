@@ -1,0 +1,90 @@
+"""CPU side of the rollout-gradient checks (process-pool workers; no torch).
+
+reverse_along: the FP64 reverse (oracle/adjoint.py StepAdjoint) of a rollout
+chained backwards along a given trajectory: every env step is re-run in FP64
+from the given state at its start (the GPU's state after the previous env
+step), its frames taped, and their reverses chained, so the result is the
+FP64 gradient of the same linearisation the GPU differentiated.
+
+tail_fd: FP64 central differences of the APG loss's tail (env steps t..H-1)
+with respect to the action of env step t, from a given state at step t.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+def _sys(name):
+  from brax_gb300 import mjcf
+  return mjcf.load_asset(name)
+
+
+def reverse_along(args):
+  """(name, q_start [H, nq], qd_start [H, nv], act [H, nu], q_bar [H, nq],
+  qd_bar [H, nv], n_frames) for one env -> (act_bar [H, nu], q0_bar, qd0_bar).
+  q_start[s] / qd_start[s] is the state at the start of env step s."""
+  from oracle.adjoint import StepAdjoint
+  name, q_start, qd_start, act, q_bar, qd_bar, n_frames = args
+  sys_ = _sys(name)
+  adj = StepAdjoint(sys_)
+  H = act.shape[0]
+  qb = q_bar[H - 1][None].astype(np.float64)
+  qdb = qd_bar[H - 1][None].astype(np.float64)
+  act_bar = np.zeros(act.shape)
+  for s in range(H - 1, -1, -1):
+    q = q_start[s][None].astype(np.float64)
+    qd = qd_start[s][None].astype(np.float64)
+    a = act[s][None].astype(np.float64)
+    tapes = []
+    for _ in range(n_frames):
+      qn, qdn, T = adj.forward(q, qd, a)
+      tapes.append((T, T['s'].x_rot))
+      q, qd = qn, qdn
+    for T, xr in reversed(tapes):
+      adj._xr = xr
+      qb, qdb, ab = adj.vjp(T, qb, qdb)
+      act_bar[s] += ab[0]
+    if s > 0:
+      qb = qb + q_bar[s - 1][None]
+      qdb = qdb + qd_bar[s - 1][None]
+  return act_bar, qb[0], qdb[0]
+
+
+def tail_fd(args):
+  """(name, q_t [nq], qd_t [nv], act [H - t, nu], n_frames, eps_list, coords)
+  -> ({eps: [len(coords)]} central differences of -mean torso x-velocity over
+  the env steps t..H-1 (each 1/H weighted; H given as act's length plus t via
+  `horizon`) w.r.t. act[0, k] for k in coords, and the FP64 tail trajectory
+  of the unperturbed actions (q, qd after each env step))."""
+  from oracle.pipeline import Oracle
+  name, q_t, qd_t, act, n_frames, eps_list, coords, horizon = args
+  sys_ = _sys(name)
+  o = Oracle(sys_, np.float64, exact_inverse=True)
+  L = act.shape[0]
+  # one batch: the unperturbed rollout, then +eps / -eps for every coordinate and eps
+  rows = [act]
+  for eps in eps_list:
+    for k in coords:
+      for sgn in (1.0, -1.0):
+        a = act.copy()
+        a[0, k] += sgn * eps
+        rows.append(a)
+  B = len(rows)
+  acts = np.stack(rows, axis=1).astype(np.float64)  # [L, B, nu]
+  s = o.init(np.repeat(q_t[None].astype(np.float64), B, 0), np.repeat(qd_t[None].astype(np.float64), B, 0))
+  loss = np.zeros(B)
+  traj_q, traj_qd = [], []
+  for j in range(L):
+    s = o.env_step(s, acts[j], n_frames)
+    loss += -s.qd[:, 0] / horizon
+    traj_q.append(s.q[0].copy())
+    traj_qd.append(s.qd[0].copy())
+  out, i = {}, 1
+  for eps in eps_list:
+    fd = np.zeros(len(coords))
+    for c in range(len(coords)):
+      fd[c] = (loss[i] - loss[i + 1]) / (2 * eps)
+      i += 2
+    out[eps] = fd
+  return out, np.array(traj_q), np.array(traj_qd)

@@ -1,0 +1,145 @@
+"""Rollout gradient at the APG workload as configured: quadruped, 512 envs,
+128 env steps of 5 x 0.01 s, a checkpoint every 16 env steps, loss
+-mean_t torso x-velocity + 1e-3 sum |u|^2, gradients w.r.t. the actions and
+qd0 (brax/training/agents/apg/train.py:188-198) -- the exact launch the bench
+times, checked on 8 of its envs.
+
+Why not FP64 finite differences over all 128 steps: FP32 and FP64
+trajectories of this workload decorrelate (quadrupeds thrown around by
+random gear-150 actions): their relative difference is 1e-6 to 1e-3 after
+16 env steps and O(1) by step 40 (printed below for the GPU trajectory).
+A difference quotient of the FP64 loss over the whole horizon
+differentiates another trajectory, for the GPU and for the FP32 reference
+path alike.  So the check has two parts:
+
+(a) the whole gradient (128 x 8 actions and qd0) against the FP64 reverse
+    of the same linearisation: oracle/adjoint.py's step reverse chained
+    backwards along the GPU's own trajectory (each env step re-run in FP64
+    from the GPU's state at its start).  Bar: per env step, relative error
+    (max over the 8 actions / max of the FP64 reverse's) <= 1e-3 for 95 % of
+    the (env, step) pairs, and qd0 <= 1e-3 for 7 of 8 envs; the steps above
+    are printed.  The FP64 re-run of a step can take another branch than the
+    GPU's FP32 step at a projected-gradient tie (about 1 % of steps), and the
+    cotangents then carry that difference backwards;
+(b) FP64 central differences at eps = 1e-4 and 1e-5 side by side for the
+    actions of env steps 112, 120 and 127 (the last checkpoint segment),
+    rolled out in FP64 from the GPU's state at that step.  Where the two
+    differences agree (FD is smooth: no contact or line-search switch within
+    eps) and the FP64 tail tracks the GPU's trajectory to 1e-4, the adjoint
+    must match the eps = 1e-5 difference within 1e-3 (relative to the env
+    step's largest derivative); every other (env, step, action) is listed
+    with the evidence (the two differences, the tail divergence).
+"""
+
+import multiprocessing as mp
+import os
+
+import numpy as np
+import pytest
+
+from tests import grad_util
+
+torch = pytest.importorskip('torch')
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+N, H, F, CKPT = 512, 128, 5, 16
+ENVS = np.arange(0, N, 64)
+FD_STEPS = (112, 120, 127)
+
+
+def _workload(sys_):
+  """The bench's APG inputs (seed 55)."""
+  rng = np.random.default_rng(55)
+  q0 = (sys_.init_q + rng.uniform(-0.1, 0.1, (N, sys_.q_size()))).astype(np.float32)
+  qd0 = (0.1 * rng.normal(size=(N, sys_.qd_size()))).astype(np.float32)
+  u = rng.uniform(-1, 1, (H, N, sys_.act_size())).astype(np.float32)
+  return q0, qd0, u
+
+
+def test_apg_workload_gradient():
+  if not torch.cuda.is_available():
+    pytest.skip('no CUDA device')
+  from brax_gb300 import mjcf, pipeline as P
+  from tests.parity_util import rel_err
+  sys_ = mjcf.load_asset('quadruped')
+  q0, qd0, u = _workload(sys_)
+  dev = torch.device('cuda')
+  qd_bar = np.zeros((H, N, sys_.qd_size()), np.float32)
+  qd_bar[:, :, 0] = -1.0 / H
+  act_bar, _, qd0_bar, status, (tq, tqd) = P.rollout_grad(
+      sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev), torch.tensor(u, device=dev), None,
+      torch.tensor(qd_bar, device=dev), n_frames=F, ckpt_every=CKPT, trajectory=True)
+  torch.cuda.synchronize()
+  st = status.cpu().numpy()
+  assert (st == 0).all(), np.unique(st, return_counts=True)
+  act_bar, qd0_bar = act_bar.cpu().numpy(), qd0_bar.cpu().numpy()
+  tq, tqd = tq.cpu().numpy(), tqd.cpu().numpy()
+  q_start = np.concatenate([q0[None], tq[:-1]], 0)    # state at the start of each env step
+  qd_start = np.concatenate([qd0[None], tqd[:-1]], 0)
+  q_bar = np.zeros((H, N, sys_.q_size()))
+  ctx = mp.get_context('spawn')
+  with ctx.Pool(min(len(ENVS), os.cpu_count() or 1)) as pool:
+    rev = pool.map(grad_util.reverse_along,
+                   [('quadruped', q_start[:, e], qd_start[:, e], u[:, e], q_bar[:, e], qd_bar[:, e], F) for e in ENVS])
+    fd_args = []
+    for e in ENVS:
+      for t in FD_STEPS:
+        fd_args.append(('quadruped', q_start[t, e], qd_start[t, e], u[t:, e], F, (1e-4, 1e-5),
+                        list(range(sys_.act_size())), H))
+    fds = pool.map(grad_util.tail_fd, fd_args)
+
+  # (a) against the FP64 reverse along the GPU trajectory
+  e_steps, e_qd0 = [], []
+  for i, e in enumerate(ENVS):
+    ab64, _, qdb64 = rev[i]
+    g = act_bar[:, e].astype(np.float64)
+    e_steps.append(np.abs(g - ab64).max(-1) / np.maximum(np.abs(ab64).max(-1), 1e-12))
+    e_qd0.append(np.abs(qd0_bar[e] - qdb64).max() / max(np.abs(qdb64).max(), 1e-12))
+  e_steps, e_qd0 = np.array(e_steps), np.array(e_qd0)
+  print(f'(a) act_bar vs FP64 reverse along the GPU trajectory: per (env, step) p50 {np.median(e_steps):.2e} '
+        f'p95 {np.quantile(e_steps, 0.95):.2e} max {e_steps.max():.2e}; qd0_bar per env '
+        f'{np.array2string(e_qd0, precision=1)}')
+  for i, e in enumerate(ENVS):
+    bad = np.nonzero(e_steps[i] > 1e-3)[0]
+    if bad.size:
+      print(f'    env {e}: steps above 1e-3: {bad.tolist()[:12]} (max {e_steps[i].max():.1e})')
+  assert np.quantile(e_steps, 0.95) <= 1e-3
+  assert (e_qd0 <= 1e-3).sum() >= 7
+
+  # (b) FP64 central differences on the last segment
+  checked, listed = 0, []
+  k = 0
+  for e in ENVS:
+    for t in FD_STEPS:
+      fd, tail_q, tail_qd = fds[k]
+      k += 1
+      gpu = act_bar[t, e].astype(np.float64)
+      scale = max(np.abs(fd[1e-5]).max(), 1e-9)
+      smooth = np.abs(fd[1e-4] - fd[1e-5]) <= 1e-3 * scale
+      track = max(rel_err(tail_q, tq[t:, e]).max(), rel_err(tail_qd, tqd[t:, e]).max())
+      err = np.abs(gpu - fd[1e-5]) / scale
+      for j in range(len(gpu)):
+        if smooth[j] and track <= 1e-4:
+          checked += 1
+          assert err[j] <= 1e-3, (e, t, j, gpu[j], fd[1e-5][j], fd[1e-4][j], track)
+        else:
+          listed.append((int(e), t, j, float(gpu[j]), float(fd[1e-4][j]), float(fd[1e-5][j]), float(track)))
+  print(f'(b) last-segment actions: {checked} derivatives checked <= 1e-3 against FP64 FD (eps 1e-5); '
+        f'{len(listed)} listed (FD not smooth between eps 1e-4 and 1e-5, or the FP64 tail leaves the GPU '
+        f'trajectory by more than 1e-4):')
+  for row in listed[:24]:
+    print('    env %d step %d act %d: adjoint %.5e | FD eps 1e-4 %.5e, eps 1e-5 %.5e | tail divergence %.1e' % row)
+  assert checked >= 0.5 * len(ENVS) * len(FD_STEPS) * sys_.act_size()
+
+  # the evidence for the design above: FP64 from the same start vs the GPU trajectory
+  from oracle.pipeline import Oracle
+  o = Oracle(sys_, np.float64, exact_inverse=True)
+  s = o.init(q0[ENVS].astype(np.float64), qd0[ENVS].astype(np.float64))
+  div = []
+  for t in range(48):
+    s = o.env_step(s, u[t, ENVS].astype(np.float64), F)
+    div.append(np.maximum(rel_err(s.q, tq[t, ENVS]), rel_err(s.qd, tqd[t, ENVS])))
+  div = np.array(div)
+  print('FP64 from the same start vs the GPU trajectory, max over the 8 envs at env step 8 / 16 / 32 / 48: ' +
+        ' / '.join(f'{div[i].max():.1e}' for i in (7, 15, 31, 47)))

@@ -249,12 +249,19 @@ def test_debug_contacts(name):
     # (between the segments' closest points) is ill-conditioned in FP32 when
     # those points are close
     d32, p32, f32 = Oracle(sys, np.float32).contacts(xp, xr)
+    # the closest-point choice of two capsules is a decision on two nearly
+    # equal distances when they lie near parallel: both ways (biased draws)
+    alt = [Oracle(sys, np.float64, perturb_seed=7, perturb_bias=b).contacts(
+        xp.astype(np.float64), xr.astype(np.float64)) for b in (-1, 1)]
     scale = np.maximum(np.abs(p).max(), 1.0)
-    for got, ref, r32, floor in ((s.contact.dist, d, d32, 2e-6 * scale), (s.contact.pos, p, p32, 2e-6 * scale),
-                                 (s.contact.frame, f, f32, 2e-6)):
+    for i, (got, ref, r32, floor) in enumerate(((s.contact.dist, d, d32, 2e-6 * scale),
+                                                (s.contact.pos, p, p32, 2e-6 * scale),
+                                                (s.contact.frame, f, f32, 2e-6))):
       # per contact slot: max over its entries
-      err = np.abs(_np(got) - ref).reshape(n, sys.contacts.n, -1).max(-1)
-      bar = np.maximum(floor, 3 * np.abs(r32 - ref).reshape(n, sys.contacts.n, -1).max(-1))
+      per_slot = lambda x: np.abs(x).reshape(n, sys.contacts.n, -1).max(-1)
+      err = per_slot(_np(got) - ref)
+      env = np.maximum(per_slot(r32 - ref), np.maximum(per_slot(alt[0][i] - ref), per_slot(alt[1][i] - ref)))
+      bar = np.maximum(floor, 3 * env)
       assert (err <= bar).all(), (err.max(), np.unravel_index(np.argmax(err - bar), err.shape))
     assert s.contact.dist is s.contact_dist
   # a step without debug returns no contact
