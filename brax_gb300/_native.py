@@ -44,8 +44,12 @@ class Dims(ctypes.Structure):
   _fields_ = [(n, ctypes.c_int32) for n in ('nl', 'nq', 'nv', 'nu', 'ncon', 'nlim', 'm')]
 
 
+RANDOMIZATION_FIELDS = ('friction', 'act_gain', 'act_bias_q', 'act_bias_qd', 'link_mass', 'link_inertia',
+                        'dof_armature', 'dof_damping', 'dof_stiffness')
+
+
 class Randomization(ctypes.Structure):
-  _fields_ = [(n, ctypes.c_void_p) for n in ('friction', 'act_gain', 'act_bias_q', 'act_bias_qd')]
+  _fields_ = [(n, ctypes.c_void_p) for n in RANDOMIZATION_FIELDS]
 
 
 class Options(ctypes.Structure):

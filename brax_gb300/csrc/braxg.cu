@@ -58,7 +58,8 @@ struct Shape {
 };
 
 
-int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shape* s, bool ovf_global = false) {
+int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shape* s, bool ovf_global = false,
+                 bool dyn_dr = false) {
   int nv = m->dims.nv;
   s->NVB = nv <= 16 ? 16 : (nv <= 32 ? 32 : 64);
   // default lanes per env: 16 for small models (nv <= 8: two envs per warp),
@@ -68,7 +69,8 @@ int choose_shape(const braxg_model* m, const braxg_options* opt, int n_env, Shap
   if (T == 16 && s->NVB == 64) T = 32;
   s->T = T;
   int model_bytes = (braxg::al4(m->words) + braxg::kLayoutWords) * 4;
-  int env_bytes = (ovf_global ? m->Lg.total : m->L.total) * 4;
+  int env_bytes = (dyn_dr ? braxg::layout_of(m->h.data(), ovf_global ? 1 : 0, 1).total
+                           : (ovf_global ? m->Lg.total : m->L.total)) * 4;
   int max_epc = kMaxBlock / T;
   int fit = (kMaxSmem - model_bytes) / env_bytes;
   if (fit < 1)
@@ -105,7 +107,11 @@ int launch(const braxg_model* m, const braxg_options* opt, braxg::StepArgs& a, c
   // when it has them and that layout fits more envs per CTA
   a.ovf_global = (m->ovf_ok && a.out.cache != nullptr) ? 1 : 0;
   a.cache_stride = m->cache_words;
-  int rc = choose_shape(m, opt, a.n_env, &s, a.ovf_global != 0);
+  if (opt && opt->randomization) {
+    const braxg_randomization& r = *opt->randomization;
+    a.dyn_dr = (r.link_mass || r.link_inertia || r.dof_armature || r.dof_damping || r.dof_stiffness) ? 1 : 0;
+  }
+  int rc = choose_shape(m, opt, a.n_env, &s, a.ovf_global != 0, a.dyn_dr != 0);
   if (rc) return rc;
   if (a.n_env == 0) return BRAXG_OK;
   a.envs_per_cta = s.epc;
@@ -177,6 +183,10 @@ int braxg_model_create(const void* desc, size_t desc_bytes, int device, braxg_mo
     m->ovf_ok = fit_g > fit_s && m->Lg.total < m->L.total;
     const int ovf_words = (d.m - m->L.jcap) * m->L.ldj;
     m->cache_words = m->ovf_ok ? std::max(m->L.total, braxg::al4(m->Lg.total + ovf_words)) : m->L.total;
+    // calls with per-env dynamics parameters lay out a larger arena
+    const braxg::Layout Ld = braxg::layout_of(w, 0, 1), Lgd = braxg::layout_of(w, 1, 1);
+    m->cache_words = std::max(m->cache_words, Ld.total);
+    if (m->ovf_ok) m->cache_words = std::max(m->cache_words, braxg::al4(Lgd.total + ovf_words));
   }
   int cur = 0;
   cudaGetDevice(&cur);

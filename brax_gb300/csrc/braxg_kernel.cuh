@@ -38,6 +38,18 @@ __device__ __forceinline__ void load_params(const Team<T>& tm, const braxg_rando
     p[nc + nu + i] = dr.act_bias_q ? dr.act_bias_q[env * nu + i] : md.F(BXM_O_ACT_BQ)[i];
     p[nc + 2 * nu + i] = dr.act_bias_qd ? dr.act_bias_qd[env * nu + i] : md.F(BXM_O_ACT_BQD)[i];
   }
+  if (w.L->dprm >= 0) {  // dynamics parameters: link mass, inertia; dof armature, damping, stiffness
+    float* d = w.at(w.L->dprm);
+    const int nl = md.nl, nv = md.nv;
+    for (int i = tm.lane; i < nl; i += T) d[i] = dr.link_mass ? dr.link_mass[env * nl + i] : md.F(BXM_O_LI_MASS)[i];
+    for (int i = tm.lane; i < 9 * nl; i += T)
+      d[nl + i] = dr.link_inertia ? dr.link_inertia[env * 9 * nl + i] : md.F(BXM_O_LI_I)[i];
+    for (int i = tm.lane; i < nv; i += T) {
+      d[10 * nl + i] = dr.dof_armature ? dr.dof_armature[env * nv + i] : md.F(BXM_O_D_ARM)[i];
+      d[10 * nl + nv + i] = dr.dof_damping ? dr.dof_damping[env * nv + i] : md.F(BXM_O_D_DAMP)[i];
+      d[10 * nl + 2 * nv + i] = dr.dof_stiffness ? dr.dof_stiffness[env * nv + i] : md.F(BXM_O_D_STIFF)[i];
+    }
+  }
 }
 
 // Whether an env's arena, just restored from the input state's cache, holds
@@ -68,6 +80,20 @@ __device__ __forceinline__ bool cache_matches(const StepArgs& a, const EnvBase& 
     eq = eq && same(p[nc + i], dr.act_gain ? dr.act_gain[env * nu + i] : md.F(BXM_O_ACT_GAIN)[i]);
     eq = eq && same(p[nc + nu + i], dr.act_bias_q ? dr.act_bias_q[env * nu + i] : md.F(BXM_O_ACT_BQ)[i]);
     eq = eq && same(p[nc + 2 * nu + i], dr.act_bias_qd ? dr.act_bias_qd[env * nu + i] : md.F(BXM_O_ACT_BQD)[i]);
+  }
+  if (L.dprm >= 0) {
+    const float* d = w.at(L.dprm);
+    const int nl = md.nl;
+    for (int i = tm.lane; i < nl; i += T)
+      eq = eq && same(d[i], dr.link_mass ? dr.link_mass[env * nl + i] : md.F(BXM_O_LI_MASS)[i]);
+    for (int i = tm.lane; i < 9 * nl; i += T)
+      eq = eq && same(d[nl + i], dr.link_inertia ? dr.link_inertia[env * 9 * nl + i] : md.F(BXM_O_LI_I)[i]);
+    for (int i = tm.lane; i < nv; i += T) {
+      eq = eq && same(d[10 * nl + i], dr.dof_armature ? dr.dof_armature[env * nv + i] : md.F(BXM_O_D_ARM)[i]);
+      eq = eq && same(d[10 * nl + nv + i], dr.dof_damping ? dr.dof_damping[env * nv + i] : md.F(BXM_O_D_DAMP)[i]);
+      eq = eq && same(d[10 * nl + 2 * nv + i],
+                      dr.dof_stiffness ? dr.dof_stiffness[env * nv + i] : md.F(BXM_O_D_STIFF)[i]);
+    }
   }
   return tm.all(eq);
 }
@@ -103,13 +129,14 @@ __device__ __forceinline__ void copy_position_terms(const Team<T>& tm, float* ds
 }
 
 // Tag of a cached arena (misc[11]): the team width that computed it (lane
-// reductions make the terms depend on it bit for bit), where its overflow
-// Jacobian rows live (the arena layout), and whether its mass_mx_inv is the
-// exact inverse of its mass matrix.  An env whose launch flagged a
-// non-finite value stores tag 0, which no launch accepts.
+// reductions make the terms depend on it bit for bit), the arena layout
+// (where its overflow Jacobian rows live, whether it holds per-env dynamics
+// parameters), and whether its mass_mx_inv is the exact inverse of its mass
+// matrix.  An env whose launch flagged a non-finite value stores tag 0,
+// which no launch accepts.
 template <int T>
-__device__ __forceinline__ int cache_tag(bool ovf_g, bool exact_minv) {
-  return 4 * T + (ovf_g ? 2 : 0) + (exact_minv ? 1 : 0);
+__device__ __forceinline__ int cache_tag(const Layout& L, bool exact_minv) {
+  return (L.dprm >= 0 ? 256 : 0) + 4 * T + (L.ovf_g ? 2 : 0) + (exact_minv ? 1 : 0);
 }
 
 // Restores the env's arena from the input state's cache; true if it applies.
@@ -127,7 +154,7 @@ __device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, 
   copy_position_terms<T>(tm, w.b, slot, *w.L, md.nv, md.m, w.b, w.L->ovf_g ? w.g : w.b, slot);
   tm.sync();
   const int tag = reinterpret_cast<const int*>(w.at(w.L->misc))[11];
-  const int want = cache_tag<T>(w.L->ovf_g != 0, true);
+  const int want = cache_tag<T>(*w.L, true);
   const bool tag_ok = exact ? tag == want : (tag >> 1) == (want >> 1);
   return cache_matches<T>(a, B, mw, w, env, !exact) && tag_ok;
 }
@@ -139,7 +166,7 @@ __device__ __noinline__ void store_cache(const StepArgs& a, const EnvBase& B, co
   const Team<T> tm;
   const Model md(mw);
   tm.sync();
-  if (tm.lane == 0) reinterpret_cast<int*>(w.at(w.L->misc))[11] = ok ? cache_tag<T>(w.L->ovf_g != 0, exact) : 0;
+  if (tm.lane == 0) reinterpret_cast<int*>(w.at(w.L->misc))[11] = ok ? cache_tag<T>(*w.L, exact) : 0;
   tm.sync();
   float* slot = a.out.cache + (B.env + env) * a.cache_stride;
   if (bx_misaligned<T>(w, slot, w.b)) return;
@@ -527,7 +554,7 @@ __global__ void __launch_bounds__(512, 1) step_kernel(const StepArgs a) {
   Layout* shared_layout = reinterpret_cast<Layout*>(smem + al4(a.model_words));
   if (threadIdx.x == 0) {
     const int* w0 = a.model;
-    *shared_layout = layout_of(w0, a.ovf_global);
+    *shared_layout = layout_of(w0, a.ovf_global, a.dyn_dr);
   }
   __syncthreads();
   const int team = threadIdx.x / T;

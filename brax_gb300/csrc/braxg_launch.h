@@ -72,6 +72,7 @@ struct StepArgs {
   unsigned long long* prof;
   int relax;                 // braxg_options.relax_barriers
   braxg_randomization dr;    // per-env System parameters (NULL fields: the model's)
+  int dyn_dr;                // the arena holds per-env dynamics parameters (Layout::dprm)
   int has_task;              // fused env step (task, io) after every env step
   long long env_step_stride; // envs between env steps of io.reward / io.done
   braxg_task task;

@@ -55,6 +55,9 @@ struct Layout {
   int M, Minv;
   int J, jcap, jovf, rdiag, raref, rmap;
   int prm;  // per-env parameters: friction [ncon], actuator gain, bias_q, bias_qd [nu each]
+  // per-env dynamics parameters (randomised calls only; -1 otherwise): link
+  // mass [nl], link inertia [nl * 9], dof armature, damping, stiffness [nv each]
+  int dprm;
   int scr, scr_words, itmp;
   int mrows;   // constraint rows of the model (4 ncon + nlim)
   int canary;  // the checked build's canary words (kCanaryWords) follow the arena here
@@ -92,7 +95,7 @@ constexpr int kMaxExplicitRows = 32;
 // matrix lives in scratch too (from CRBA to the inverse, and to the outputs),
 // except for models whose integrator solves with M itself (ns_iters == 0).
 __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, int ncon, int nlim, int ns_iters,
-                                              int fluid = 0, int ovf_global = 0) {
+                                              int fluid = 0, int ovf_global = 0, int dyn_dr = 0) {
   Layout L;
   const int m = 4 * ncon + nlim;
   L.ldm = nv | 1;  // odd leading dimension: conflict-free strided lane access
@@ -134,6 +137,7 @@ __host__ __device__ inline Layout make_layout(int nl, int nq, int nv, int nu, in
   L.raref = take(m);
   L.rmap = take(m);
   L.prm = take(ncon + 3 * nu);
+  L.dprm = dyn_dr ? take(10 * nl + 3 * nv) : -1;
   // overflow Jacobian rows: at the scratch end, or outside the arena
   const int ovf = ovf_global ? 0 : (m - L.jcap) * L.ldj;
   const int nn = nv * L.ldm;
@@ -236,9 +240,9 @@ __host__ __device__ inline bool scratch_use_ok(const Layout& L, const ScratchUse
 }
 
 // Layout of a packed model descriptor (header words).
-__host__ __device__ inline Layout layout_of(const int* w, int ovf_global = 0) {
+__host__ __device__ inline Layout layout_of(const int* w, int ovf_global = 0, int dyn_dr = 0) {
   return make_layout(w[BXM_H_NL], w[BXM_H_NQ], w[BXM_H_NV], w[BXM_H_NU], w[BXM_H_NCON], w[BXM_H_NLIM],
-                     w[BXM_H_NS_ITERS], w[BXM_H_FLUID], ovf_global);
+                     w[BXM_H_NS_ITERS], w[BXM_H_FLUID], ovf_global, dyn_dr);
 }
 static_assert(sizeof(Layout) <= kLayoutWords * 4, "Layout must fit its shared slot");
 
@@ -269,6 +273,24 @@ struct Team {
     return (__ballot_sync(mask, p) & mask) >> base;
   }
 };
+
+// The dynamics parameters of an env: its own copy (randomised calls) or the
+// model's.
+__device__ __forceinline__ const float* link_mass(const Model& md, const Layout& L, const float* b) {
+  return L.dprm >= 0 ? b + L.dprm : md.F(BXM_O_LI_MASS);
+}
+__device__ __forceinline__ const float* link_inertia(const Model& md, const Layout& L, const float* b) {
+  return L.dprm >= 0 ? b + L.dprm + md.nl : md.F(BXM_O_LI_I);
+}
+__device__ __forceinline__ const float* dof_armature(const Model& md, const Layout& L, const float* b) {
+  return L.dprm >= 0 ? b + L.dprm + 10 * md.nl : md.F(BXM_O_D_ARM);
+}
+__device__ __forceinline__ const float* dof_damping(const Model& md, const Layout& L, const float* b) {
+  return L.dprm >= 0 ? b + L.dprm + 10 * md.nl + md.nv : md.F(BXM_O_D_DAMP);
+}
+__device__ __forceinline__ const float* dof_stiffness(const Model& md, const Layout& L, const float* b) {
+  return L.dprm >= 0 ? b + L.dprm + 10 * md.nl + 2 * md.nv : md.F(BXM_O_D_STIFF);
+}
 
 // Per-env workspace handle: the env's arena base and the (shared) layout.
 // Passed by value so out-of-line stages keep it in registers.
@@ -457,7 +479,7 @@ __device__ __noinline__ void stage_com(const int* mw, Ws w) {
   if (bx_stop<T>(w) || bx_scratch<T>(w, scratch_fk(L, nl, md.nv), jjr + 4 * nl, md.nv)) return;
   const float* xp = w.at(L.xp);
   const float* xr = w.at(L.xr);
-  const float* mass = md.F(BXM_O_LI_MASS);
+  const float* mass = link_mass(md, L, w.b);
   const int* parent = md.I(BXM_O_LINK_PARENT);
   const int* ltype = md.I(BXM_O_LINK_TYPE);
   for (int l = tm.lane; l < nl; l += T) {  // x_i = x.do(inertia.transform)  :37
@@ -498,7 +520,7 @@ __device__ __noinline__ void stage_com(const int* mw, Ws w) {
     f3 off = ld3(xip + 3 * l) - com;
     float R[9], RI[9];
     quat_to_3x3(ld4(xir + 4 * l), R);
-    const float* I = md.F(BXM_O_LI_I) + 9 * l;
+    const float* I = link_inertia(md, L, w.b) + 9 * l;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -630,7 +652,7 @@ __device__ __noinline__ void stage_crba(const int* mw, Ws w) {
   if (bx_stop<T>(w) || bx_scratch<T>(w, scratch_crba(L, nl, nv), crbm + nl + 6 * nv, nv)) return;
   const float* ci = w.at(L.ci);
   const float* cp = w.at(L.cp);
-  const float* mass = md.F(BXM_O_LI_MASS);
+  const float* mass = link_mass(md, L, w.b);
   const int* lstart = md.I(BXM_O_LEVEL_START);
   const int* llinks = md.I(BXM_O_LEVEL_LINKS);
   const int* cstart = md.I(BXM_O_CHILD_START);
@@ -657,7 +679,7 @@ __device__ __noinline__ void stage_crba(const int* mw, Ws w) {
   }
   const int* dlink = md.I(BXM_O_DOF_LINK);
   const float* cdof = w.at(L.cdof);
-  const float* arm = md.F(BXM_O_D_ARM);
+  const float* arm = dof_armature(md, L, w.b);
   float* M = w.at(L.M);
   float* F = crbm + nl;  // per dof: crb[link] * cdof (the row's force), after crb's words
   for (int r = tm.lane; r < nv; r += T) {
@@ -1315,7 +1337,7 @@ __device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
   const float* ci = w.at(L.ci);
   const float* cp = w.at(L.cp);
   const float* cd = w.at(L.cd);
-  const float* mass = md.F(BXM_O_LI_MASS);
+  const float* mass = link_mass(md, L, w.b);
   for (int l = tm.lane; l < nl; l += T) {
     f3 p = ld3(cp + 3 * l);
     f3 fa, fv, ga, gv, xa, xv;
@@ -1387,8 +1409,8 @@ __device__ __noinline__ void stage_smooth(const int* mw, Ws w, bool has_act) {
   // qf_smooth = passive - bias + tau: dynamics.py:182, 190-196, 232-234
   const int* dlink = md.I(BXM_O_DOF_LINK);
   const float* cdof = w.at(L.cdof);
-  const float* stiff = md.F(BXM_O_D_STIFF);
-  const float* damp = md.F(BXM_O_D_DAMP);
+  const float* stiff = dof_stiffness(md, L, w.b);
+  const float* damp = dof_damping(md, L, w.b);
   const int* qadr = md.I(BXM_O_LINK_QADR);
   float* qfs = w.at(L.qfs);
   for (int d = tm.lane; d < nv; d += T) {
@@ -1944,7 +1966,7 @@ __device__ __noinline__ bool stage_integrate(const int* mw, Ws w) {
     float* A = w.at(L.scr);
     if (bx_scratch<T>(w, scratch_integrate(L, nv), A + nv * ld, nv)) return true;
     const float* M = w.at(L.M);
-    const float* damp = md.F(BXM_O_D_DAMP);
+    const float* damp = dof_damping(md, L, w.b);
     for (int idx = tm.lane; idx < nv * nv; idx += T) {
       int i = idx / nv, j = idx - i * nv;
       A[i * ld + j] = M[i * ld + j] + (i == j ? damp[i] * h : 0.f);

@@ -273,13 +273,20 @@ def _as_batch(x: torch.Tensor, width: int, name: str, dev) -> torch.Tensor:
   return x.to(torch.float32).contiguous()
 
 
-_DR_FIELDS = ('friction', 'act_gain', 'act_bias_q', 'act_bias_qd')
+_DR_FIELDS = N.RANDOMIZATION_FIELDS
+
+
+def _dr_width(m: 'Model', k: str) -> int:
+  return {'friction': m.ncon, 'link_mass': m.nl, 'link_inertia': 9 * m.nl, 'dof_armature': m.nv,
+          'dof_damping': m.nv, 'dof_stiffness': m.nv}.get(k, m.nu)
 
 
 def _randomization(m: 'Model', n: int, randomization):
   """A C Randomization struct for a dict of per-env tensors (friction
-  [n, ncon], act_gain / act_bias_q / act_bias_qd [n, nu]), with the tensors it
-  points to (kept alive by the caller for the call)."""
+  [n, ncon]; act_gain / act_bias_q / act_bias_qd [n, nu]; link_mass [n, nl];
+  link_inertia [n, nl, 3, 3]; dof_armature / dof_damping / dof_stiffness
+  [n, nv]), with the tensors it points to (kept alive by the caller for the
+  call)."""
   if not randomization:
     return None, []
   keep = []
@@ -287,28 +294,42 @@ def _randomization(m: 'Model', n: int, randomization):
   for k, v in randomization.items():
     if k not in _DR_FIELDS:
       raise ValueError(f'unknown randomization field {k!r}; expected one of {_DR_FIELDS}')
-    width = m.ncon if k == 'friction' else m.nu
-    v = torch.as_tensor(v, dtype=torch.float32, device=m.device).reshape(n, width).contiguous()
+    v = torch.as_tensor(v, dtype=torch.float32, device=m.device).reshape(n, _dr_width(m, k)).contiguous()
     keep.append(v)
     ptrs[k] = v.data_ptr()
   return N.Randomization(*[ptrs.get(k) for k in _DR_FIELDS]), keep
 
 
 def randomize(sys, n: int, generator: Optional[torch.Generator] = None, friction_range=(0.6, 1.4),
-              gain_scale_range=(1.0, 1.0), device=None) -> dict:
+              gain_scale_range=(1.0, 1.0), mass_scale_range=(1.0, 1.0), damping_scale_range=(1.0, 1.0),
+              device=None) -> dict:
   """Per-env parameters in the manner of brax's domain randomisation
   examples: one sliding friction per env, uniform in friction_range, for
   every contact slot (every geom gets it, so every pair's mixed friction is
-  it), and the actuator gains scaled by a per-env factor."""
+  it); the actuator gains scaled by a per-env factor; the link masses and
+  inertias scaled together by a per-env factor (a uniformly denser body); the
+  dof damping scaled by a per-env factor."""
   m = model_for(sys, device)
-  f = torch.rand(n, 1, device=m.device, generator=generator)
-  f = friction_range[0] + (friction_range[1] - friction_range[0]) * f
+  dev = m.device
+
+  def scale(rng):
+    g = torch.rand(n, 1, device=dev, generator=generator)
+    return rng[0] + (rng[1] - rng[0]) * g
+
+  f = scale(friction_range)
   out = {'friction': f.expand(n, m.ncon).contiguous()}
   if m.nu and gain_scale_range != (1.0, 1.0):
-    g = torch.rand(n, 1, device=m.device, generator=generator)
-    g = gain_scale_range[0] + (gain_scale_range[1] - gain_scale_range[0]) * g
-    gain = torch.tensor(sys.actuator.gain, dtype=torch.float32, device=m.device)[None]
-    out['act_gain'] = (gain * g).contiguous()
+    gain = torch.tensor(sys.actuator.gain, dtype=torch.float32, device=dev)[None]
+    out['act_gain'] = (gain * scale(gain_scale_range)).contiguous()
+  if mass_scale_range != (1.0, 1.0):
+    s = scale(mass_scale_range)
+    mass = torch.tensor(sys.link.inertia.mass, dtype=torch.float32, device=dev)[None]
+    inertia = torch.tensor(sys.link.inertia.i, dtype=torch.float32, device=dev).reshape(1, -1)
+    out['link_mass'] = (mass * s).contiguous()
+    out['link_inertia'] = (inertia * s).reshape(n, m.nl, 3, 3).contiguous()
+  if damping_scale_range != (1.0, 1.0):
+    damp = torch.tensor(sys.dof.damping, dtype=torch.float32, device=dev)[None]
+    out['dof_damping'] = (damp * scale(damping_scale_range)).contiguous()
   return out
 
 

@@ -137,15 +137,24 @@ enum braxg_profile_slot {
 };
 
 /* Per-env System parameters (the fields brax's DomainRandomizationVmapWrapper,
- * brax/envs/wrappers/training.py:223-260, is used to randomise): each pointer
- * is [n, k] device memory overriding the model's value for every env, or
- * NULL to keep the model's.  Forward paths only (step, rollout, env
- * rollout); gradients use the model's values. */
+ * brax/envs/wrappers/training.py:223-260, vmaps over; System leaves of
+ * brax/base.py:415-540): each pointer is [n, k] device memory overriding the
+ * model's value for every env, or NULL to keep the model's.  Forward paths
+ * of single-model calls only (init, step, rollout, env rollout); gradients
+ * and batches use the model's values.  The dynamics fields (link masses and
+ * inertias, dof armature, damping and stiffness) take an extra per-env
+ * region of the kernel's shared-memory arena, only in calls that pass one of
+ * them.  Fluid forces keep the model's inertia-equivalent boxes. */
 typedef struct {
-  const float* friction;     /* [n, ncon] sliding friction of every contact slot */
-  const float* act_gain;     /* [n, nu] actuator gain */
-  const float* act_bias_q;   /* [n, nu] actuator bias on q */
-  const float* act_bias_qd;  /* [n, nu] actuator bias on qd */
+  const float* friction;       /* [n, ncon] sliding friction of every contact slot */
+  const float* act_gain;       /* [n, nu] actuator gain */
+  const float* act_bias_q;     /* [n, nu] actuator bias on q */
+  const float* act_bias_qd;    /* [n, nu] actuator bias on qd */
+  const float* link_mass;      /* [n, nl] link.inertia.mass */
+  const float* link_inertia;   /* [n, nl, 3, 3] link.inertia.i */
+  const float* dof_armature;   /* [n, nv] dof.armature */
+  const float* dof_damping;    /* [n, nv] dof.damping */
+  const float* dof_stiffness;  /* [n, nv] dof.stiffness */
 } braxg_randomization;
 
 typedef struct {

@@ -56,7 +56,12 @@ def test_model_values_change_nothing():
   dr = {'friction': np.tile(sys_.contacts.friction[:, 0], (n, 1)),
         'act_gain': np.tile(sys_.actuator.gain, (n, 1)),
         'act_bias_q': np.tile(sys_.actuator.bias_q, (n, 1)),
-        'act_bias_qd': np.tile(sys_.actuator.bias_qd, (n, 1))}
+        'act_bias_qd': np.tile(sys_.actuator.bias_qd, (n, 1)),
+        'link_mass': np.tile(sys_.link.inertia.mass, (n, 1)),
+        'link_inertia': np.tile(sys_.link.inertia.i[None], (n, 1, 1, 1)),
+        'dof_armature': np.tile(sys_.dof.armature, (n, 1)),
+        'dof_damping': np.tile(sys_.dof.damping, (n, 1)),
+        'dof_stiffness': np.tile(sys_.dof.stiffness, (n, 1))}
   a = P.step(sys_, s, act, n_frames=5, inverse_mode=P.CHOLESKY)
   b = P.step(sys_, s, act, n_frames=5, inverse_mode=P.CHOLESKY, randomization=dr)
   torch.cuda.synchronize()
@@ -65,7 +70,39 @@ def test_model_values_change_nothing():
   assert m.ncon == sys_.contacts.n
 
 
-@pytest.mark.parametrize('field', ['friction', 'act_gain'])
+def _with(sys_, field, v):
+  """A System copy carrying the value that group's envs get."""
+  if field == 'friction':
+    fr = sys_.contacts.friction.copy()
+    fr[:, 0] = v
+    return dataclasses.replace(sys_, contacts=dataclasses.replace(sys_.contacts, friction=fr))
+  if field == 'act_gain':
+    return dataclasses.replace(sys_, actuator=dataclasses.replace(sys_.actuator, gain=sys_.actuator.gain * v))
+  if field == 'link_mass':  # mass and inertia scaled together
+    ine = sys_.link.inertia
+    ine = dataclasses.replace(ine, mass=ine.mass * v, i=ine.i * v)
+    return dataclasses.replace(sys_, link=dataclasses.replace(sys_.link, inertia=ine))
+  if field == 'dof_damping':
+    return dataclasses.replace(sys_, dof=dataclasses.replace(sys_.dof, damping=sys_.dof.damping * v))
+  if field == 'dof_armature':
+    return dataclasses.replace(sys_, dof=dataclasses.replace(sys_.dof, armature=sys_.dof.armature + 0.05 * v))
+  raise ValueError(field)
+
+
+def _dr_values(sys_, field, groups, values):
+  if field == 'friction':
+    return {field: np.stack([np.full(sys_.contacts.n, values[g], np.float32) for g in groups])}
+  if field == 'act_gain':
+    return {field: np.stack([(sys_.actuator.gain * values[g]).astype(np.float32) for g in groups])}
+  if field == 'link_mass':
+    return {'link_mass': np.stack([(sys_.link.inertia.mass * values[g]).astype(np.float32) for g in groups]),
+            'link_inertia': np.stack([(sys_.link.inertia.i * values[g]).astype(np.float32) for g in groups])}
+  if field == 'dof_damping':
+    return {field: np.stack([(sys_.dof.damping * values[g]).astype(np.float32) for g in groups])}
+  return {field: np.stack([(sys_.dof.armature + 0.05 * values[g]).astype(np.float32) for g in groups])}
+
+
+@pytest.mark.parametrize('field', ['friction', 'act_gain', 'link_mass', 'dof_damping', 'dof_armature'])
 def test_per_env_values_match_oracle_with_those_values(field):
   P = _P()
   from oracle.pipeline import Oracle
@@ -73,24 +110,19 @@ def test_per_env_values_match_oracle_with_those_values(field):
   n = 48
   q, qd = _settled(sys_, n, 83)
   act = actions(sys_, n, np.random.default_rng(84)).astype(np.float32)
-  values = [0.5, 1.0, 1.6]  # per group of 16 envs: friction or a gain scale
+  values = [0.5, 1.0, 1.6]  # per group of 16 envs: friction, or a scale of the field
   groups = np.repeat(np.arange(3), n // 3)
-  if field == 'friction':
-    dr = np.stack([np.full(sys_.contacts.n, values[g], np.float32) for g in groups])
-  else:
-    dr = np.stack([(sys_.actuator.gain * values[g]).astype(np.float32) for g in groups])
-  s = P.init(sys_, _t(q), _t(qd), randomization={field: dr})
-  got = P.step(sys_, s, _t(act), n_frames=1, inverse_mode=P.CHOLESKY, randomization={field: dr})
+  dr = _dr_values(sys_, field, groups, values)
+  s = P.init(sys_, _t(q), _t(qd), randomization=dr)
+  got = P.step(sys_, s, _t(act), n_frames=1, inverse_mode=P.CHOLESKY, randomization=dr)
+  # the same step without the input state's position-term cache (recomputed
+  # with the randomised values) gives the same bits
+  nocache = P.step(sys_, s.replace(cache=None), _t(act), n_frames=1, inverse_mode=P.CHOLESKY, randomization=dr)
   torch.cuda.synchronize()
   assert (got.status.cpu().numpy() == 0).all()
+  torch.testing.assert_close(got.qd, nocache.qd, rtol=0, atol=0)
   for g, v in enumerate(values):
-    if field == 'friction':
-      fr = sys_.contacts.friction.copy()
-      fr[:, 0] = v
-      sys_g = dataclasses.replace(sys_, contacts=dataclasses.replace(sys_.contacts, friction=fr))
-    else:
-      sys_g = dataclasses.replace(sys_, actuator=dataclasses.replace(sys_.actuator,
-                                                                      gain=sys_.actuator.gain * v))
+    sys_g = _with(sys_, field, v)
     idx = groups == g
     o32 = Oracle(sys_g, np.float32, exact_inverse=True)
     o64 = Oracle(sys_g, np.float64, exact_inverse=True)
