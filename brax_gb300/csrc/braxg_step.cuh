@@ -1055,6 +1055,83 @@ __device__ __forceinline__ void closest_seg_seg(f3 a0, f3 a1, f3 b0, f3 b1, f3& 
   bb = bestb;
 }
 
+// mujoco.mjx plane-box (mujoco-mjx _src/collision_convex.py: the
+// plane-convex routine and its 4-point manifold): the box's 8 vertices (x
+// slowest, itertools.product order), in the box frame, against the plane of
+// normal n through p1; a vertex is a candidate when it lies below the plane
+// or within a 1 mm skin above it.  The manifold is a (the first candidate),
+// b (the candidate furthest from a), c (furthest from the line ab in the
+// plane), d (furthest from the edges bc or ac, bc's first); every argmax
+// keeps the first of equal values.  Slot `sub` takes the sub-th of (a, b, c,
+// d); a vertex already taken by an earlier slot gets dist 1 (inactive).
+__device__ __forceinline__ f3 box_vertex(int v, f3 h) {
+  return mk3((v & 4) ? h.x : -h.x, (v & 2) ? h.y : -h.y, (v & 1) ? h.z : -h.z);
+}
+__device__ __forceinline__ void plane_box(f3 p1, f3 n, f3 p2, const float* R2, f3 h, int sub, float& dist, f3& pos) {
+  const f3 dp = p1 - p2;  // box frame: R2^T (p1 - p2), R2^T n
+  const f3 rel = mk3(R2[0] * dp.x + R2[3] * dp.y + R2[6] * dp.z, R2[1] * dp.x + R2[4] * dp.y + R2[7] * dp.z,
+                     R2[2] * dp.x + R2[5] * dp.y + R2[8] * dp.z);
+  const f3 nl = mk3(R2[0] * n.x + R2[3] * n.y + R2[6] * n.z, R2[1] * n.x + R2[4] * n.y + R2[7] * n.z,
+                    R2[2] * n.x + R2[5] * n.y + R2[8] * n.z);
+  float support[8];
+  unsigned cand = 0u;
+#pragma unroll
+  for (int v = 0; v < 8; ++v) {
+    support[v] = dot3(rel - box_vertex(v, h), nl);
+    if (support[v] > -1e-3f) cand |= 1u << v;
+  }
+  auto dm = [&](int v) { return ((cand >> v) & 1u) ? 0.f : -1e6f; };
+  int ia = 0;  // first candidate (vertex 0 when there is none)
+  for (int v = 0; v < 8; ++v)
+    if ((cand >> v) & 1u) {
+      ia = v;
+      break;
+    }
+  const f3 a = box_vertex(ia, h);
+  int ib = 0;
+  float best = -INFINITY;
+  for (int v = 0; v < 8; ++v) {
+    const f3 e = a - box_vertex(v, h);
+    const float s = dot3(e, e) + dm(v);
+    if (s > best) {
+      best = s;
+      ib = v;
+    }
+  }
+  const f3 b = box_vertex(ib, h);
+  const f3 ab = cross3(nl, a - b);
+  int ic = 0;
+  best = -INFINITY;
+  for (int v = 0; v < 8; ++v) {
+    const float s = fabsf(dot3(a - box_vertex(v, h), ab)) + dm(v);
+    if (s > best) {
+      best = s;
+      ic = v;
+    }
+  }
+  const f3 c = box_vertex(ic, h);
+  const f3 ac = cross3(nl, a - c), bc = cross3(nl, b - c);
+  int id = 0;
+  best = -INFINITY;
+  for (int v = 0; v < 16; ++v) {  // [|(b - p).bc| over p, then |(a - p).ac| over p]
+    const f3 pv = box_vertex(v & 7, h);
+    const float s = (v < 8 ? fabsf(dot3(b - pv, bc)) : fabsf(dot3(a - pv, ac))) + dm(v & 7);
+    if (s > best) {
+      best = s;
+      id = v & 7;
+    }
+  }
+  const int idx[4] = {ia, ib, ic, id};
+  const int i = idx[sub];
+  bool unique = true;
+  for (int j = 0; j < sub; ++j) unique = unique && idx[j] != i;
+  dist = unique ? -support[i] : 1.f;
+  const f3 vl = box_vertex(i, h);
+  const f3 vw = mk3(R2[0] * vl.x + R2[1] * vl.y + R2[2] * vl.z, R2[3] * vl.x + R2[4] * vl.y + R2[5] * vl.z,
+                    R2[6] * vl.x + R2[7] * vl.y + R2[8] * vl.z);
+  pos = p2 + vw - n * (0.5f * dist);
+}
+
 // Writes dist[k], pos[k*3], frame[k*9] for every contact slot.
 template <int T>
 __device__ __noinline__ void stage_contacts(const int* mw, Ws w, float* dist, float* cpos, float* frame) {
@@ -1099,27 +1176,7 @@ __device__ __noinline__ void stage_contacts(const int* mw, Ws w, float* dist, fl
       st3(F + 6, cross3(n, b));
     } else if (kd == BXM_CON_PLANE_BOX) {
       f3 n = mk3(R1[2], R1[5], R1[8]);
-      // the sub-th deepest corner (ties broken by corner index)
-      float cd[8];
-      f3 cc[8];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        f3 loc = mk3((c & 4) ? g2s[3 * k] : -g2s[3 * k], (c & 2) ? g2s[3 * k + 1] : -g2s[3 * k + 1],
-                     (c & 1) ? g2s[3 * k + 2] : -g2s[3 * k + 2]);
-        cc[c] = p2 + mk3(R2[0] * loc.x + R2[1] * loc.y + R2[2] * loc.z, R2[3] * loc.x + R2[4] * loc.y + R2[5] * loc.z,
-                         R2[6] * loc.x + R2[7] * loc.y + R2[8] * loc.z);
-        cd[c] = dot3(cc[c] - p1, n);
-      }
-      int want = sub[k], pick = 0;
-#pragma unroll 1
-      for (int c = 0; c < 8; ++c) {
-        int rank = 0;
-#pragma unroll 1
-        for (int e = 0; e < 8; ++e) rank += (cd[e] < cd[c]) || (cd[e] == cd[c] && e < c);
-        if (rank == want) pick = c;
-      }
-      d = cd[pick];
-      pos = cc[pick] - n * (0.5f * d);
+      plane_box(p1, n, p2, R2, mk3(g2s[3 * k], g2s[3 * k + 1], g2s[3 * k + 2]), sub[k], d, pos);
       make_frame(n, F);
     } else if (kd == BXM_CON_SPHERE_SPHERE) {
       f3 n;

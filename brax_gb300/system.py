@@ -32,7 +32,7 @@ GEOM_ELLIPSOID, GEOM_CYLINDER, GEOM_BOX, GEOM_MESH = 4, 5, 6, 7
 # contact normal points from geom1 to geom2 (MuJoCo convention).
 CON_PLANE_SPHERE = 0    # 1 contact per pair
 CON_PLANE_CAPSULE = 1   # 2 contacts per pair (segment end +, end -)
-CON_PLANE_BOX = 2       # 4 contacts per pair (the 4 deepest corners)
+CON_PLANE_BOX = 2       # 4 contacts per pair (mjx's plane-convex manifold of the box's vertices)
 CON_SPHERE_SPHERE = 3   # 1 contact
 CON_SPHERE_CAPSULE = 4  # 1 contact
 CON_CAPSULE_CAPSULE = 5  # 1 contact

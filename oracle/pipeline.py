@@ -560,22 +560,8 @@ class Oracle:
         dist[:, k], pos[:, k] = d, ps
         frame[:, k] = np.stack([nrm, b, cross(nrm, b)], axis=-2)
       elif kind == S.CON_PLANE_BOX:
-        nrm = m1[..., :, 2]
-        corners = []
-        for sx in (-1, 1):
-          for sy in (-1, 1):
-            for sz in (-1, 1):
-              loc = np.array([sx, sy, sz], dt) * size[g2]
-              corners.append(p2 + np.einsum('bij,j->bi', m2, loc))
-        corners = np.stack(corners, axis=1)  # (B, 8, 3)
-        cd = np.sum((corners - p1[:, None]) * nrm[:, None], axis=-1)
-        order = np.argsort(cd, axis=1, kind='stable')
-        sel = order[:, sub]
-        cpt = corners[np.arange(B), sel]
-        d = cd[np.arange(B), sel]
-        dist[:, k] = d
-        pos[:, k] = cpt - nrm * (0.5 * d)[..., None]
-        frame[:, k] = make_frame(nrm)
+        d, ps, fr = _plane_box(p1, m1, p2, m2, size[g2], sub)
+        dist[:, k], pos[:, k], frame[:, k] = d, ps, fr
       elif kind == S.CON_SPHERE_SPHERE:
         d, ps, nrm = _sphere_sphere(p1, size[g1, 0], p2, size[g2, 0])
         dist[:, k], pos[:, k], frame[:, k] = d, ps, make_frame(nrm)
@@ -978,6 +964,57 @@ def _sphere_sphere(p1, r1, p2, r2):
   dist = d - (r1 + r2)
   pos = p1 + n * (r1 + 0.5 * dist)[..., None]
   return dist, pos, n
+
+
+# mujoco.mjx plane-box: the box as a convex polytope (its 8 vertices in
+# itertools.product((-1, 1), repeat=3) order, x slowest) against the plane
+# (mujoco-mjx _src/collision_convex.py: the plane-convex routine and its
+# 4-point manifold choice).  A vertex is a candidate when it lies below the
+# plane or within a 1 mm skin above it; of the candidates the manifold takes
+# a (the first), b (furthest from a), c (furthest from the line ab in the
+# plane) and d (furthest from the edges ac / bc); a point chosen twice keeps
+# only its first slot, the others get dist 1 (inactive).
+_BOX_VERTS = np.array([[sx, sy, sz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)], np.float64)
+
+
+def _box_manifold(vert, mask, n):
+  """Indices (B, 4) of the manifold points of `vert` (B, 8, 3) among the
+  candidates `mask` (B, 8), n (B, 3) the plane normal in the box frame."""
+  big = np.asarray(1e6, vert.dtype)
+  dm = np.where(mask, 0, -big).astype(vert.dtype)
+  ar = np.arange(vert.shape[0])
+  a_i = np.argmax(dm, axis=1)
+  a = vert[ar, a_i]
+  b_i = np.argmax(np.sum((a[:, None] - vert) ** 2, -1) + dm, axis=1)
+  b = vert[ar, b_i]
+  ab = cross(n, a - b)
+  ap = a[:, None] - vert
+  c_i = np.argmax(np.abs(np.sum(ap * ab[:, None], -1)) + dm, axis=1)
+  c = vert[ar, c_i]
+  ac, bc = cross(n, a - c), cross(n, b - c)
+  bp = b[:, None] - vert
+  d_bp = np.abs(np.sum(bp * bc[:, None], -1)) + dm
+  d_ap = np.abs(np.sum(ap * ac[:, None], -1)) + dm
+  d_i = np.argmax(np.concatenate([d_bp, d_ap], axis=1), axis=1) % vert.shape[1]
+  return np.stack([a_i, b_i, c_i, d_i], axis=1)
+
+
+def _plane_box(plane_pos, plane_mat, box_pos, box_mat, size, sub):
+  """Contact `sub` (0..3) of a plane and a box: dist, pos, frame."""
+  dt = box_pos.dtype
+  vert = (_BOX_VERTS.astype(dt) * size.astype(dt))[None]            # (1, 8, 3) box frame
+  rel = np.einsum('bji,bj->bi', box_mat, plane_pos - box_pos)       # box_mat^T (plane - box)
+  n_l = np.einsum('bji,bj->bi', box_mat, plane_mat[..., :, 2])
+  support = np.sum((rel[:, None] - vert) * n_l[:, None], -1)        # (B, 8): depth below the plane
+  B = box_pos.shape[0]
+  idx = _box_manifold(np.broadcast_to(vert, (B, 8, 3)), support > -1e-3, n_l)
+  i = idx[:, sub]
+  unique = np.all(idx[:, :sub] != i[:, None], axis=1) if sub > 0 else np.ones(B, bool)
+  ar = np.arange(B)
+  dist = np.where(unique, -support[ar, i], np.asarray(1, dt)).astype(dt)
+  n = plane_mat[..., :, 2]
+  pos = box_pos + np.einsum('bij,bj->bi', box_mat, vert[0][i]) - n * (0.5 * dist)[:, None]
+  return dist, pos, make_frame(n)
 
 
 def _closest_segment_point(a, b, pt):

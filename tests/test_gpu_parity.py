@@ -296,3 +296,53 @@ def test_solver_maxiter_diagnostic():
   print(f'solver stopped at maxiter: GPU {got.mean():.3f}, FP32 oracle {r32.pg_maxiter.mean():.3f}, agree {agree:.4f}')
   assert agree >= 0.98
   assert got.sum() > 0
+
+
+BOX_XML = """<mujoco model="box_drop">
+  <option timestep="0.005"/>
+  <worldbody>
+    <geom name="floor" type="plane" size="10 10 10"/>
+    <body name="box" pos="0 0 0.3">
+      <joint type="free"/>
+      <geom name="b" type="box" size="0.2 0.15 0.1" mass="1"/>
+    </body>
+  </worldbody>
+</mujoco>
+"""
+
+
+def test_box_plane_contacts_and_step():
+  """Box-plane contacts (mjx's plane-convex manifold) of randomly oriented
+  boxes near the plane, plus one box resting face-down (three distinct points,
+  the fourth slot inactive): every slot's dist / pos / frame against the FP64
+  oracle, and one pipeline step against the FP32 oracle."""
+  P = _pipeline()
+  from brax_gb300 import mjcf
+  from oracle.pipeline import Oracle
+  sys = mjcf.loads(BOX_XML)
+  assert sys.contacts.n == 4
+  n = 64
+  rng = np.random.default_rng(91)
+  qv = rng.normal(size=(n, 4))
+  qv /= np.linalg.norm(qv, axis=1, keepdims=True)
+  q = np.concatenate([rng.uniform(-1, 1, (n, 2)), rng.uniform(0.0, 0.25, (n, 1)), qv], axis=1)
+  q[0] = [0.0, 0.0, 0.09, 1.0, 0.0, 0.0, 0.0]  # face-down, 1 cm into the plane
+  qd = 0.1 * rng.normal(size=(n, 6))
+  q, qd = q.astype(np.float32), qd.astype(np.float32)
+  st = P.init(sys, _t(q), _t(qd), debug=True)
+  torch.cuda.synchronize()
+  d, p, f = Oracle(sys, np.float64).contacts(_np(st.x.pos).astype(np.float64), _np(st.x.rot).astype(np.float64))
+  np.testing.assert_allclose(_np(st.contact.dist), d, atol=2e-6, rtol=0)
+  np.testing.assert_allclose(_np(st.contact.pos), p, atol=2e-6, rtol=0)
+  np.testing.assert_allclose(_np(st.contact.frame), f, atol=2e-6, rtol=0)
+  np.testing.assert_allclose(_np(st.contact.dist)[0], [-0.01, -0.01, -0.01, 1.0], atol=1e-6)
+  assert ((_np(st.contact.dist) < 0).sum(1) > 0).mean() > 0.3  # many boxes touch the plane
+  got = P.step(sys, st, None, inverse_mode=P.CHOLESKY)
+  o32 = Oracle(sys, np.float32, exact_inverse=True)
+  r32 = o32.step(o32.init(q, qd), None)
+  torch.cuda.synchronize()
+  assert (_np(got.status) == 0).all()
+  for field in ('q', 'qd'):
+    e = rel_err(_np(getattr(got, field)), getattr(r32, field))
+    print(f'box on plane {field}: vs fp32 p50 {np.median(e):.2e} p99 {np.quantile(e, 0.99):.2e} max {e.max():.2e}')
+    assert np.quantile(e, 0.99) <= 1e-5, (field, np.sort(e)[-4:])

@@ -269,3 +269,25 @@ def test_humanoid_newton_schulz_loses_the_inverse():
     s = oq.step(s, actions(sys_q, 16, rng))
   resid = np.linalg.norm(np.eye(sys_q.qd_size()) - s.mass_mx @ s.mass_mx_inv, axis=(1, 2))
   assert resid.max() < 1e-6
+
+
+def test_plane_box_manifold():
+  """The restated mjx plane-box manifold: a box resting face-down on the plane
+  (every bottom vertex below it) gets three distinct contact points, the
+  corners a, b (diagonally opposite a) and c; the fourth choice ties with a
+  (equal distances of a and the last corner from the edge bc, first wins) and
+  its slot is inactive (dist 1).  A box well above the plane (beyond the 1 mm
+  skin) has no candidate vertex: the mask shifts every vertex alike, so the
+  slots take vertex 0 and the same geometric choices, all above the plane."""
+  from oracle.pipeline import _plane_box
+  eye = np.broadcast_to(np.eye(3), (1, 3, 3)).copy()
+  size = np.array([0.2, 0.15, 0.1])
+  zero = np.zeros((1, 3))
+  flat = [_plane_box(zero, eye, np.array([[0.0, 0.0, 0.09]]), eye, size, k) for k in range(4)]
+  d = np.array([f[0][0] for f in flat])
+  np.testing.assert_allclose(d, [-0.01, -0.01, -0.01, 1.0], atol=1e-12)
+  pts = np.array([f[1][0] for f in flat[:3]])
+  assert len({tuple(np.round(p, 9)) for p in pts}) == 3
+  np.testing.assert_allclose(pts[:, 2], -0.005, atol=1e-12)  # midway between the surfaces
+  high = [_plane_box(zero, eye, np.array([[0.0, 0.0, 0.5]]), eye, size, k)[0][0] for k in range(4)]
+  assert high[0] == pytest.approx(0.4) and min(high) > 0  # vertex 0 at its distance; nothing active
