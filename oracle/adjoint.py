@@ -281,9 +281,10 @@ class StepAdjoint:
       b = np.einsum('bij,bj->bi', jm, qfs) - aref
       xs, pg = self._pg_tape(a, b)
       qfc = np.einsum('bij,bi->bj', jac, xs)
-      T.update(a=a, b=b, xs=xs, pg=pg)
+      T.update(a=a, b=b, xs=xs, pg=pg, pg_gap=self.last_gap)
     else:
       qfc = np.zeros_like(qfs)
+      T.update(pg_gap=np.full(B, np.inf))
     s = s.replace(qf_constraint=qfc)
     s2 = o.integrate(s)
     T.update(qfs=qfs, qfc=qfc, s_int=s2)
@@ -330,6 +331,9 @@ class StepAdjoint:
     err = np.full(B, np.inf)
     active = np.ones(B, bool)
     tape = []
+    # the closest call of any decision of the solve, relative to the compared
+    # values' size: below ~1e-6 the same decision in FP32 is a tie
+    gap = np.full(B, np.inf)
     for it in range(sys.solver_iterations):
       if it > 0:
         active = active & (err > 1e-3)
@@ -344,7 +348,11 @@ class StepAdjoint:
       for _ in range(sys.solver_maxls):
         dx = nx - y
         r2 = mv(nx) + b
-        cond = cur * (np.sum(0.5 * r2 ** 2, -1) - fy) > cur * np.sum(dx * gy, -1) + 0.5 * np.sum(dx * dx, -1)
+        f2 = np.sum(0.5 * r2 ** 2, -1)
+        lhs, rhs = cur * (f2 - fy), cur * np.sum(dx * gy, -1) + 0.5 * np.sum(dx * dx, -1)
+        scale = np.abs(cur * f2) + np.abs(cur * fy) + cur * np.sum(np.abs(dx * gy), -1) + 0.5 * np.sum(dx * dx, -1)
+        gap = np.where(on, np.minimum(gap, np.abs(lhs - rhs) / np.maximum(scale, 1e-300)), gap)
+        cond = lhs > rhs
         on = on & cond
         if not on.any():
           break
@@ -359,12 +367,14 @@ class StepAdjoint:
       z = y - cur[:, None] * gy
       tape.append(dict(active=active.copy(), y=y.copy(), ry=ry, step=cur.copy(), beta=beta,
                        zpos=(z > 0)))
+      gap = np.where(active, np.minimum(gap, np.abs(e - 1e-3) / 1e-3), gap)
       on2 = active[:, None]
       x = np.where(on2, nx, x)
       y = np.where(on2, ny, y)
       t = np.where(active, nt, t)
       ss = np.where(active, nss, ss)
       err = np.where(active, e, err)
+    self.last_gap = gap
     return x, tape
 
   # -------------------------------------------------------------- reverse

@@ -22,8 +22,11 @@ def _sys(name):
 
 def reverse_along(args):
   """(name, q_start [H, nq], qd_start [H, nv], act [H, nu], q_bar [H, nq],
-  qd_bar [H, nv], n_frames) for one env -> (act_bar [H, nu], q0_bar, qd0_bar).
-  q_start[s] / qd_start[s] is the state at the start of env step s."""
+  qd_bar [H, nv], n_frames) for one env -> (act_bar [H, nu], q0_bar, qd0_bar,
+  gap [H]).  q_start[s] / qd_start[s] is the state at the start of env step
+  s; gap[s] is the closest call, relative to the compared values' size, of
+  any projected-gradient decision in the FP64 re-run of env step s (below
+  about 1e-6 the same decision is a tie in FP32)."""
   from oracle.adjoint import StepAdjoint
   name, q_start, qd_start, act, q_bar, qd_bar, n_frames = args
   sys_ = _sys(name)
@@ -32,6 +35,7 @@ def reverse_along(args):
   qb = q_bar[H - 1][None].astype(np.float64)
   qdb = qd_bar[H - 1][None].astype(np.float64)
   act_bar = np.zeros(act.shape)
+  gaps = np.full(H, np.inf)
   for s in range(H - 1, -1, -1):
     q = q_start[s][None].astype(np.float64)
     qd = qd_start[s][None].astype(np.float64)
@@ -40,6 +44,7 @@ def reverse_along(args):
     for _ in range(n_frames):
       qn, qdn, T = adj.forward(q, qd, a)
       tapes.append((T, T['s'].x_rot))
+      gaps[s] = min(gaps[s], float(T['pg_gap'][0]))
       q, qd = qn, qdn
     for T, xr in reversed(tapes):
       adj._xr = xr
@@ -48,7 +53,7 @@ def reverse_along(args):
     if s > 0:
       qb = qb + q_bar[s - 1][None]
       qdb = qdb + qd_bar[s - 1][None]
-  return act_bar, qb[0], qdb[0]
+  return act_bar, qb[0], qdb[0], gaps
 
 
 def tail_fd(args):

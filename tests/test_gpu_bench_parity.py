@@ -10,37 +10,40 @@ and, in Newton-Schulz mode, the carried mass_mx_inv):
 
 * quadruped: 4096 envs, 5 x 0.01 s, 10 warm-up env steps (the bench's);
 * chain3: 128 envs, 1 x 0.01 s, zero actions;
-* humanoid-like: 16384 envs, 5 x 0.003 s (oracle on every 16th env);
+* humanoid-like: 16384 envs, 5 x 0.003 s (oracle on every 32nd env);
 * the uneven batch: 8192 envs of 33 models in one persistent launch (oracle
   on every chain env, every 4th quadruped and every 4th humanoid-like env).
 
 rel_err per env = max |a - b| / max(max |b|, 1).  The bar:
 
-* single pipeline step (the same launch with n_frames = 1; quadruped and
-  humanoid-like): p99 of the error against the FP32 oracle <= 1e-5 over the
-  envs whose FP32 result is determined to 1e-5 (rounding envelope below,
-  <= 1e-5), the others held to their envelope;
-* whole env step: p99 of the error against the FP32 oracle and against the
-  FP64 oracle <= max(1e-5, 2 x p99 of the FP32 rounding envelope below, which
-  includes the FP32 oracle's own error against FP64).  A 5-frame env step of quadrupeds landing under random gear-150
-  actions, or of the humanoid-like model (cond(M) ~ 6.5e3), is itself
-  ill-conditioned in FP32: the FP32 reference path is off from FP64 by more
-  than 1e-5 there, and the kernel is held to the same accuracy;
-* every env: error against the FP32 oracle <= max(1e-5, 10 x a_env), where
-  a_env is the env's FP32 rounding envelope: the largest distance between the
-  FP32 oracle and (1) itself evaluated as in another operation order: every
-  order-dependent intermediate (smooth forces, the mass matrix, mass_mx_inv
-  and the Newton-Schulz iterates, the projected-gradient problem's A and b) moved by
-  one ulp, and every decision taken on two computed values (the line
-  search's sufficient-decrease test, the stopping test, the Newton-Schulz
-  acceptance and reset) free to go either way when its two sides agree to
-  within a few ulps (five draws: all such decisions one way, all the other
-  way, three at random) and (2) the FP64 oracle.  The line search is often
-  at such a tie: at step 1 its test reduces to |A g| <= |g|, and A =
-  J Minv J^T + diag has eigenvalues near 1 on these models, so the two sides
-  differ by 1e-8 of their size (below FP32 resolution) on about 1 % of envs
-  and the branch taken is set by rounding.  Every env above 1e-5 is printed
-  with its envelope.
+* every pipeline step of the launch (its state after frame f, from the
+  launch stopped there, against one oracle step from the state after frame
+  f - 1): p99 of the error against the FP32 oracle <= 1e-5 over the envs
+  whose FP32 result is determined to 1e-5 (rounding envelope below, <= 1e-5),
+  and every env within max(10 x its envelope, 3 x the model's p99 FP32
+  oracle error against FP64, 1e-5);
+* the whole env step (the launch's output against n_frames oracle steps
+  from its input): p99 of the error against the FP32 oracle and against the
+  FP64 oracle <= max(1e-5, 2 x p99 of the rounding envelope below, which
+  includes the FP32 oracle's own error against FP64).  A 5-frame env step of
+  quadrupeds landing under random gear-150 actions, or of the humanoid-like
+  model (cond(M) ~ 6.5e3), is itself ill-conditioned in FP32: the FP32
+  reference path is off from FP64 by more than 1e-5 there, and the kernel is
+  held to the same accuracy;
+* the rounding envelope a_env of an env: the largest distance between the
+  FP32 oracle and (1) itself evaluated as in another operation order (every
+  order-dependent intermediate -- smooth forces, the mass matrix,
+  mass_mx_inv and the Newton-Schulz iterates, the projected-gradient
+  problem's A and b -- moved by one ulp, and every decision taken on two
+  computed values -- the line search's sufficient-decrease test, the
+  stopping test, the Newton-Schulz acceptance and reset -- free to go either
+  way when its two sides agree to within a few ulps; five draws: all such
+  decisions one way, all the other way, three at random) and (2) the FP64
+  oracle.  The line search is often at such a tie: at step 1 its test
+  reduces to |A g| <= |g|, and A = J Minv J^T + diag has eigenvalues near 1
+  on these models, so the two sides differ by 1e-8 of their size (below FP32
+  resolution) on about 1 % of envs and the branch taken is set by rounding.
+  Every env above 1e-5 is printed with its envelope.
 """
 
 import numpy as np
@@ -70,8 +73,9 @@ def _np(x):
 
 def oracle_check(sys, q, qd, minv, act, n_frames, exact, got_q, got_qd, label, strict=False):
   """n_frames pipeline steps of the FP32 and FP64 oracles from the GPU's FP32
-  inputs; asserts the bar of this module on the GPU's q / qd (strict: the
-  single-step 1e-5 p99 bar) and returns the stats."""
+  inputs; asserts the bar of this module on the GPU's q / qd (strict: a
+  single pipeline step, the 1e-5 p99 bar and the per-env bound; else the
+  whole env step's p99 bars) and returns the stats."""
   from oracle.pipeline import Oracle
   mi = None if exact else minv
   act32 = act.astype(np.float32)
@@ -106,9 +110,10 @@ def oracle_check(sys, q, qd, minv, act, n_frames, exact, got_q, got_qd, label, s
     for i in out[np.argsort(-e32[out])][:12]:
       print(f'  env {i}: vs fp32 {e32[i]:.2e}, fp32 envelope {env[i]:.2e} (perturbed {spread[f][i]:.2e}, '
             f'fp32 oracle vs fp64 {eo[i]:.2e}), vs fp64 {e64[i]:.2e}')
-    bad = e32 > np.maximum(1e-5, 10 * env)
-    assert not bad.any(), (label, f, np.nonzero(bad)[0][:10], e32[bad][:10], env[bad][:10])
     if strict:
+      # per env: within its own envelope, or within the model's FP32 accuracy
+      bad = e32 > np.maximum(max(1e-5, 3 * st['fp32_oracle_vs_fp64_p99']), 10 * env)
+      assert not bad.any(), (label, f, np.nonzero(bad)[0][:10], e32[bad][:10], env[bad][:10])
       # envs whose FP32 result is determined to 1e-5 (envelope <= 1e-5)
       det = env <= 1e-5
       st['determined'] = float(det.mean())
@@ -143,13 +148,32 @@ def _single_model(P, name, n, n_frames, warmup, mode, act_fn, reset_fn, sample):
   # the benched launch: default shape, cache carried from the previous launch
   act = torch.tensor(acts[warmup], device=dev)
   P.step(sys, a, act, n_frames=n_frames, inverse_mode=mode, out=b)
-  # the same launch for one pipeline step
-  one = P.step(sys, a, act, n_frames=1, inverse_mode=mode)
+  # the same launch stopped after each frame: the kernel is deterministic, so
+  # these are the states between the benched launch's pipeline steps
+  frames = [P.step(sys, a, act, n_frames=f, inverse_mode=mode) for f in range(1, n_frames + 1)]
   torch.cuda.synchronize()
-  ok = (_np(b.status) == 0) & (_np(a.status) == 0) & (_np(one.status) == 0)
+  ok = (_np(b.status) == 0) & (_np(a.status) == 0)
+  for fs in frames:
+    ok &= _np(fs.status) == 0
+  assert torch.equal(frames[-1].q, b.q) and torch.equal(frames[-1].qd, b.qd)
   sel = sample[ok[sample]]
-  return (sys, q[sel], qd[sel], minv[sel], acts[warmup][sel], (_np(b.q)[sel], _np(b.qd)[sel]),
-          (_np(one.q)[sel], _np(one.qd)[sel]))
+  per_frame = [(q[sel], qd[sel], minv[sel])] + [(_np(fs.q)[sel], _np(fs.qd)[sel], _np(fs.mass_mx_inv)[sel])
+                                                for fs in frames]
+  return sys, acts[warmup][sel], per_frame
+
+
+def check_launch(sys, act, per_frame, exact, label):
+  """Every pipeline step of the launch from the GPU's previous frame (strict
+  bar), then the whole env step from the launch's input."""
+  n_frames = len(per_frame) - 1
+  for f in range(n_frames):
+    q, qd, minv = per_frame[f]
+    oracle_check(sys, q, qd, minv, act, 1, exact, per_frame[f + 1][0], per_frame[f + 1][1],
+                 f'{label} frame {f + 1}', strict=True)
+  if n_frames > 1:
+    q, qd, minv = per_frame[0]
+    oracle_check(sys, q, qd, minv, act, n_frames, exact, per_frame[-1][0], per_frame[-1][1],
+                 f'{label} env step')
 
 
 def _legged_reset(sys, n, seed=1234):
@@ -194,10 +218,8 @@ def test_quadruped_4096_benched_launch(mode):
   P = _setup()
   inv = P.CHOLESKY if mode == 'cholesky' else P.NEWTON_SCHULZ
   n = 4096
-  sys, q, qd, minv, act, g5, g1 = _single_model(P, 'quadruped', n, 5, 10, inv, _uniform_act, _legged_reset,
-                                                np.arange(n))
-  oracle_check(sys, q, qd, minv, act, 1, mode == 'cholesky', *g1, f'quadruped 4096 {mode} 1 frame', strict=True)
-  oracle_check(sys, q, qd, minv, act, 5, mode == 'cholesky', *g5, f'quadruped 4096 {mode} env step')
+  sys, act, per_frame = _single_model(P, 'quadruped', n, 5, 10, inv, _uniform_act, _legged_reset, np.arange(n))
+  check_launch(sys, act, per_frame, mode == 'cholesky', f'quadruped 4096 {mode}')
 
 
 @pytest.mark.parametrize('mode', MODES)
@@ -205,9 +227,8 @@ def test_chain3_128_benched_launch(mode):
   P = _setup()
   inv = P.CHOLESKY if mode == 'cholesky' else P.NEWTON_SCHULZ
   n = 128
-  sys, q, qd, minv, act, g1, _ = _single_model(P, 'chain3', n, 1, 10, inv, _zero_act, _chain_reset,
-                                               np.arange(n))
-  oracle_check(sys, q, qd, minv, act, 1, mode == 'cholesky', *g1, f'chain3 128 {mode}', strict=True)
+  sys, act, per_frame = _single_model(P, 'chain3', n, 1, 10, inv, _zero_act, _chain_reset, np.arange(n))
+  check_launch(sys, act, per_frame, mode == 'cholesky', f'chain3 128 {mode}')
 
 
 @pytest.mark.parametrize('mode', MODES)
@@ -215,11 +236,9 @@ def test_humanoid_like_16384_benched_launch(mode):
   P = _setup()
   inv = P.CHOLESKY if mode == 'cholesky' else P.NEWTON_SCHULZ
   n = 16384
-  sys, q, qd, minv, act, g5, g1 = _single_model(P, 'humanoid_like', n, 5, 3, inv, _humanoid_act,
-                                                _humanoid_reset, np.arange(0, n, 16))
-  oracle_check(sys, q, qd, minv, act, 1, mode == 'cholesky', *g1, f'humanoid-like 16384 {mode} 1 frame',
-               strict=True)
-  oracle_check(sys, q, qd, minv, act, 5, mode == 'cholesky', *g5, f'humanoid-like 16384 {mode} env step')
+  sys, act, per_frame = _single_model(P, 'humanoid_like', n, 5, 3, inv, _humanoid_act, _humanoid_reset,
+                                      np.arange(0, n, 32))
+  check_launch(sys, act, per_frame, mode == 'cholesky', f'humanoid-like 16384 {mode}')
 
 
 @pytest.mark.parametrize('mode', MODES)
@@ -244,17 +263,25 @@ def test_uneven_8192_benched_launch(mode):
   table = b.concat_steps(acts, 'act')
   s0 = b.init(b.concat(qs, 'q'), b.concat(qds, 'qd'))
   s1, _ = b.rollout(s0, table[:warmup], inverse_mode=inv)
-  s2, _ = b.rollout(s1, table[warmup:warmup + 1], inverse_mode=inv)
+  # the benched launch's env step, and the same launch stopped after each
+  # frame of the legged models (batches of the same models with fewer frames)
+  fmax = max(n_frames)
+  steps = []
+  for f in range(1, fmax + 1):
+    bf = b if f == fmax else Batch(systems, n_env, [min(nf, f) for nf in n_frames], device=torch.device('cuda'))
+    steps.append(bf.rollout(s1, table[warmup:warmup + 1], inverse_mode=inv)[0])
   torch.cuda.synchronize()
-  ins = [b.split(getattr(s1, f), f) for f in ('q', 'qd', 'mass_mx_inv', 'status')]
-  outs = [b.split(getattr(s2, f), f) for f in ('q', 'qd', 'status')]
+  split = lambda st, f: b.split(getattr(st, f), f)
+  ins = [split(s1, f) for f in ('q', 'qd', 'mass_mx_inv', 'status')]
   for g, (s, n, nf) in enumerate(mix):
     fam = W.family(s)
     step = 1 if fam == 'chain' else 4
-    ok = (_np(ins[3][g]) == 0) & (_np(outs[2][g]) == 0)
+    ok = _np(ins[3][g]) == 0
+    for st in steps[:nf]:
+      ok &= _np(split(st, 'status')[g]) == 0
     sel = np.arange(0, n, step)
     sel = sel[ok[sel]]
     assert len(sel) >= 0.9 * len(np.arange(0, n, step)), (s.name, ok.mean())
-    oracle_check(s, _np(ins[0][g])[sel], _np(ins[1][g])[sel], _np(ins[2][g])[sel], acts[g][warmup][sel], nf,
-                 mode == 'cholesky', _np(outs[0][g])[sel], _np(outs[1][g])[sel],
-                 f'uneven {s.name} x{len(sel)} {mode}')
+    per_frame = [tuple(_np(ins[k][g])[sel] for k in range(3))]
+    per_frame += [tuple(_np(split(st, fld)[g])[sel] for fld in ('q', 'qd', 'mass_mx_inv')) for st in steps[:nf]]
+    check_launch(s, acts[g][warmup][sel], per_frame, mode == 'cholesky', f'uneven {s.name} x{len(sel)} {mode}')

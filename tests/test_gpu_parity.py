@@ -250,9 +250,9 @@ def test_debug_contacts(name):
     # those points are close
     d32, p32, f32 = Oracle(sys, np.float32).contacts(xp, xr)
     # the closest-point choice of two capsules is a decision on two nearly
-    # equal distances when they lie near parallel: both ways (biased draws)
-    alt = [Oracle(sys, np.float64, perturb_seed=7, perturb_bias=b).contacts(
-        xp.astype(np.float64), xr.astype(np.float64)) for b in (-1, 1)]
+    # equal distances when they lie near parallel: both ways, at FP32
+    # resolution (the FP32 oracle's biased draws)
+    alt = [Oracle(sys, np.float32, perturb_seed=7, perturb_bias=b).contacts(xp, xr) for b in (-1, 1)]
     scale = np.maximum(np.abs(p).max(), 1.0)
     for i, (got, ref, r32, floor) in enumerate(((s.contact.dist, d, d32, 2e-6 * scale),
                                                 (s.contact.pos, p, p32, 2e-6 * scale),
