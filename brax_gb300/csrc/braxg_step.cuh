@@ -1778,7 +1778,10 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
       fn = tm.sum(fn);
       dv = tm.sum(dv);
       sq = tm.sum(sq);
-      if (!(cur * (fn - fy) > cur * dv + 0.5f * sq)) {
+      // sq == 0: the trial point is y itself, where the reference evaluates
+      // f twice identically and accepts; here fy comes from the momentum
+      // recurrence, so the test could see rounding instead of 0
+      if (!(cur * (fn - fy) > cur * dv + 0.5f * sq) || sq == 0.f) {
         accepted = true;
         break;
       }

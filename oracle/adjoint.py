@@ -318,8 +318,15 @@ class StepAdjoint:
     return out
 
   def _pg_tape(self, a, b):
-    """Oracle.pg_solve's iteration, recording what the reverse needs."""
+    """Oracle.pg_solve's iteration, recording what the reverse needs.
+
+    With self.force = (iterations, step sizes) set (one env), the solve takes
+    exactly those iterations and accepted step sizes instead of its own
+    stopping and line-search decisions: the branch another implementation
+    took (a GPU tape), so that its reverse can be compared on the same
+    branch."""
     sys = self.sys
+    force = getattr(self, 'force', None)
     B, m = b.shape
     relu = lambda v: np.maximum(v, 0)
     mv = lambda x: np.einsum('bij,bj->bi', a, x)
@@ -335,23 +342,29 @@ class StepAdjoint:
     # values' size: below ~1e-6 the same decision in FP32 is a tie
     gap = np.full(B, np.inf)
     for it in range(sys.solver_iterations):
-      if it > 0:
-        active = active & (err > 1e-3)
-      if not active.any():
-        break
+      if force is not None:
+        if it >= force[0]:
+          break
+      else:
+        if it > 0:
+          active = active & (err > 1e-3)
+        if not active.any():
+          break
       ry = mv(y) + b
       fy = np.sum(0.5 * ry ** 2, -1)
       gy = mvt(ry)
-      cur = ss.copy()
+      cur = ss.copy() if force is None else np.full(B, float(force[1][it]))
       nx = relu(y + (-cur)[:, None] * gy)
-      on = active.copy()
-      for _ in range(sys.solver_maxls):
+      on = active.copy() if force is None else np.zeros(B, bool)
+      for _ in range(sys.solver_maxls if force is None else 0):
         dx = nx - y
         r2 = mv(nx) + b
         f2 = np.sum(0.5 * r2 ** 2, -1)
         lhs, rhs = cur * (f2 - fy), cur * np.sum(dx * gy, -1) + 0.5 * np.sum(dx * dx, -1)
         scale = np.abs(cur * f2) + np.abs(cur * fy) + cur * np.sum(np.abs(dx * gy), -1) + 0.5 * np.sum(dx * dx, -1)
-        gap = np.where(on, np.minimum(gap, np.abs(lhs - rhs) / np.maximum(scale, 1e-300)), gap)
+        # a trial point equal to y (|dx| = 0) is accepted in any precision
+        sqd = np.sum(dx * dx, -1)
+        gap = np.where(on & (sqd > 0), np.minimum(gap, np.abs(lhs - rhs) / np.maximum(scale, 1e-300)), gap)
         cond = lhs > rhs
         on = on & cond
         if not on.any():

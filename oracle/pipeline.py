@@ -734,7 +734,8 @@ class Oracle:
         dv = np.sum(dx * gy, -1)
         sq = np.sum(dx * dx, -1)
         scale = np.abs(cur * fn) + np.abs(cur * fy) + cur * np.sum(np.abs(dx * gy), -1) + 0.5 * sq
-        cond = cur * (fn - fy) > cur * dv + 0.5 * sq + self._margin(scale)
+        # a trial point equal to y (sq = 0) is accepted in any precision
+        cond = (cur * (fn - fy) > cur * dv + 0.5 * sq + self._margin(scale)) & (sq > 0)
         ls_on = ls_on & cond
         if not ls_on.any():
           break

@@ -22,13 +22,18 @@ def _sys(name):
 
 def reverse_along(args):
   """(name, q_start [H, nq], qd_start [H, nv], act [H, nu], q_bar [H, nq],
-  qd_bar [H, nv], n_frames) for one env -> (act_bar [H, nu], q0_bar, qd0_bar,
-  gap [H]).  q_start[s] / qd_start[s] is the state at the start of env step
-  s; gap[s] is the closest call, relative to the compared values' size, of
-  any projected-gradient decision in the FP64 re-run of env step s (below
-  about 1e-6 the same decision is a tie in FP32)."""
+  qd_bar [H, nv], n_frames, forced) for one env -> (act_bar [H, nu], q0_bar,
+  qd0_bar, gap [H], mismatch [H]).  q_start[s] / qd_start[s] is the state at
+  the start of env step s.  forced[s][f] = (iterations, active rows, step
+  sizes) of another implementation's projected-gradient solve in frame f of
+  env step s (None: the FP64 solve's own decisions); the FP64 re-run then
+  takes that branch, and mismatch[s] records a frame whose FP64 active row
+  count differs from the given one (a contact within rounding of the
+  threshold).  gap[s] is the closest call, relative to the compared values'
+  size, of any projected-gradient decision the FP64 re-run of env step s took
+  itself (below about 1e-6 the same decision is a tie in FP32)."""
   from oracle.adjoint import StepAdjoint
-  name, q_start, qd_start, act, q_bar, qd_bar, n_frames = args
+  name, q_start, qd_start, act, q_bar, qd_bar, n_frames, forced = args
   sys_ = _sys(name)
   adj = StepAdjoint(sys_)
   H = act.shape[0]
@@ -36,13 +41,19 @@ def reverse_along(args):
   qdb = qd_bar[H - 1][None].astype(np.float64)
   act_bar = np.zeros(act.shape)
   gaps = np.full(H, np.inf)
+  mismatch = np.zeros(H, bool)
   for s in range(H - 1, -1, -1):
     q = q_start[s][None].astype(np.float64)
     qd = qd_start[s][None].astype(np.float64)
     a = act[s][None].astype(np.float64)
     tapes = []
-    for _ in range(n_frames):
+    for f in range(n_frames):
+      fr = None if forced is None else forced[s][f]
+      adj.force = None if fr is None else (fr[0], fr[2])
       qn, qdn, T = adj.forward(q, qd, a)
+      adj.force = None
+      if fr is not None and int(np.count_nonzero(T['s'].con_diag[0])) != fr[1]:
+        mismatch[s] = True
       tapes.append((T, T['s'].x_rot))
       gaps[s] = min(gaps[s], float(T['pg_gap'][0]))
       q, qd = qn, qdn
@@ -53,7 +64,7 @@ def reverse_along(args):
     if s > 0:
       qb = qb + q_bar[s - 1][None]
       qdb = qdb + qd_bar[s - 1][None]
-  return act_bar, qb[0], qdb[0], gaps
+  return act_bar, qb[0], qdb[0], gaps, mismatch
 
 
 def tail_fd(args):
