@@ -1,11 +1,13 @@
 """Launch-shape autotuner: lanes per env and envs per CTA for each nv bucket.
 
-For every nv bucket present in a batch (nv <= 8, 16, 32, 64) the tuner builds
-a batch of that bucket's models alone (with their env counts), times a short
-rollout of it for every candidate shape with CUDA events, and keeps the
-fastest.  Results are cached in a JSON file keyed by the GPU name, the bucket
-and the bucket's models and env counts, so a later process with the same batch
-reads them instead of timing again.  The cache lives next to the built library
+For the nv buckets present in a batch (nv <= 8, 16, 32, 64) the tuner runs a
+coordinate descent on the whole batch: each bucket's candidate shapes are
+timed (CUDA events, a short rollout of the whole batch, every model's work
+items interleaved in one launch as they run) with the other buckets at their
+current shapes, and a candidate is kept only if it beats the current shapes.
+Results are cached in a JSON file keyed by the GPU name and the batch's
+models, env counts and frames, so a later process with the same batch reads
+them instead of timing again.  The cache lives next to the built library
 (``brax_gb300/_lib/autotune.json``) unless ``BRAXG_TUNE_CACHE`` names another
 file.
 """
@@ -81,11 +83,6 @@ def _store(table: Dict):
   os.replace(tmp, path)
 
 
-def _time_shape(systems, n_env, n_frames, shape, device, n_steps: int, reps: int, smem: int) -> float:
-  return _time_batch(systems, n_env, n_frames, [(BUCKETS[-1], shape[0], shape[1])], device, n_steps, reps,
-                     smem)
-
-
 def _time_batch(systems, n_env, n_frames, shapes, device, n_steps: int, reps: int, smem: int = 0) -> float:
   """Median CUDA-event time (ms) of an n_steps rollout of the batch."""
   from brax_gb300.batch import Batch
@@ -114,70 +111,61 @@ def _time_batch(systems, n_env, n_frames, shapes, device, n_steps: int, reps: in
   return float(np.median(times))
 
 
+def default_shape(bucket: int) -> Tuple[int, int, int]:
+  """The shape a model of this bucket gets without tuning (braxg_batch_create:
+  16 lanes per env for nv <= 8, else 32; envs per CTA filling the CTA)."""
+  return (bucket, 16 if bucket <= 8 else 32, 0)
+
+
 def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Sequence[int]] = None,
-               device=None, n_steps: int = 8, reps: int = 5, use_cache: bool = True,
-               verbose: bool = False) -> List[Tuple[int, int, int]]:
-  """Shapes [(nv_max, threads_per_env, envs_per_cta)] for ``Batch(shapes=...)``,
-  one per nv bucket present, each the fastest candidate for that bucket's
-  models timed alone; the combination is then timed on the whole batch
-  against the default shape (32 lanes, envs per CTA filling the CTA) and the
-  faster of the two is returned (an empty list for the default)."""
+               device=None, n_steps: int = 16, reps: int = 5, use_cache: bool = True,
+               verbose: bool = False, min_gain: float = 0.01) -> List[Tuple[int, int, int]]:
+  """Shapes [(nv_max, threads_per_env, envs_per_cta)] for ``Batch(shapes=...)``
+  by coordinate descent on the whole batch: starting from the default shape
+  of every nv bucket present, each bucket in turn tries its candidates with
+  the other buckets at their current shapes, timing an n_steps rollout of the
+  whole batch (the models of all buckets interleaved in one launch, as they
+  run), and keeps a candidate only if it is at least ``min_gain`` faster than
+  the current shapes.  Returns [] when the default shapes are kept."""
   device = torch.device('cuda') if device is None else torch.device(device)
   if device.index is None:
     device = torch.device('cuda', torch.cuda.current_device())
   n_frames = [1] * len(systems) if n_frames is None else list(n_frames)
-  groups: Dict[int, List[int]] = {}
-  for g, s in enumerate(systems):
-    if n_env[g] > 0:
-      groups.setdefault(bucket_of(s.qd_size()), []).append(g)
+  live = [g for g in range(len(systems)) if n_env[g] > 0]
+  if not live:
+    return []
+  args = ([systems[g] for g in live], [n_env[g] for g in live], [n_frames[g] for g in live])
+  buckets = sorted({bucket_of(systems[g].qd_size()) for g in live})
+  key = _key(device, 0, *args) + '|descent'
   with _lock:
     table = _load() if use_cache else {}
-  shapes = []
-  dirty = False
-  for bucket in sorted(groups):
-    idx = groups[bucket]
-    sys_b = [systems[g] for g in idx]
-    ne_b = [n_env[g] for g in idx]
-    nf_b = [n_frames[g] for g in idx]
-    key = _key(device, bucket, sys_b, ne_b, nf_b)
-    hit = table.get(key)
-    if hit is None:
-      results = {}
-      for shape in candidates(bucket):
+  hit = table.get(key)
+  if hit is None:
+    cur = {b: default_shape(b) for b in buckets}
+    shape_list = lambda c: [c[b] for b in buckets]
+    best = default_ms = _time_batch(*args, shape_list(cur), device, n_steps, reps)
+    timed = {'default': default_ms}
+    for b in buckets:
+      for t, e in candidates(b):
+        trial = dict(cur)
+        trial[b] = (b, t, e)
+        if trial == cur:
+          continue
         try:
-          results[shape] = _time_shape(sys_b, ne_b, nf_b, shape, device, n_steps, reps, SMEM_PER_CTA)
+          ms = _time_batch(*args, shape_list(trial), device, n_steps, reps)
         except (ValueError, NotImplementedError):
-          continue  # shape does not fit this bucket's models
+          continue  # the shape does not fit this bucket's models
+        timed[f'nv<={b} {t}x{e}'] = ms
         if verbose:
-          print(f'nv<={bucket} threads {shape[0]} envs/cta {shape[1]}: {results[shape]:.3f} ms')
-      if not results:
-        raise NotImplementedError(f'no launch shape fits the nv<={bucket} models')
-      best = min(results, key=results.get)
-      hit = {'threads_per_env': best[0], 'envs_per_cta': best[1], 'ms': results[best],
-             'timed': {f'{t}x{e}': ms for (t, e), ms in results.items()}}
-      table[key] = hit
-      dirty = True
-    shapes.append((bucket, hit['threads_per_env'], hit['envs_per_cta']))
-  if len(groups) > 0:  # the combination against the default on the whole batch
-    all_idx = [g for idx in groups.values() for g in idx]
-    key = _key(device, 0, [systems[g] for g in all_idx], [n_env[g] for g in all_idx],
-               [n_frames[g] for g in all_idx]) + '|' + repr(shapes)
-    hit = table.get(key)
-    if hit is None:
-      live = [g for g in range(len(systems)) if n_env[g] > 0]
-      args = ([systems[g] for g in live], [n_env[g] for g in live], [n_frames[g] for g in live])
-      tuned = _time_batch(*args, shapes, device, 4 * n_steps, reps)
-      default = _time_batch(*args, [], device, 4 * n_steps, reps)
-      hit = {'use_tuned': tuned <= default, 'tuned_ms': tuned, 'default_ms': default}
-      table[key] = hit
-      dirty = True
-      if verbose:
-        print(f'whole batch: tuned {tuned:.3f} ms, default {default:.3f} ms')
-    if not hit['use_tuned']:
-      shapes = []
-  if dirty and use_cache:
-    with _lock:
-      merged = _load()
-      merged.update(table)
-      _store(merged)
-  return shapes
+          print(f'nv<={b} threads {t} envs/cta {e}: {ms:.3f} ms (current best {best:.3f})')
+        if ms < best * (1.0 - min_gain):
+          cur, best = trial, ms
+    shapes = [] if all(cur[b] == default_shape(b) for b in buckets) else shape_list(cur)
+    hit = {'shapes': shapes, 'ms': best, 'default_ms': default_ms, 'timed': timed}
+    table[key] = hit
+    if use_cache:
+      with _lock:
+        merged = _load()
+        merged[key] = hit
+        _store(merged)
+  return [tuple(s) for s in hit['shapes']]

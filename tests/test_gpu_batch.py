@@ -183,7 +183,8 @@ def test_autotuner_picks_one_shape_per_bucket(tmp_path, monkeypatch):
   mix = _mix(W)
   systems, n_env, n_frames = [m[0] for m in mix], [m[1] for m in mix], [m[2] for m in mix]
   shapes = autotune.tune_batch(systems, n_env, n_frames, n_steps=1, reps=1)
-  # one shape per bucket, or none when the default shape was faster on the whole batch
+  # one shape per bucket present, or none when the default shapes stayed fastest
+  # in the coordinate descent on the whole batch
   assert [s[0] for s in shapes] in ([8, 16, 32], [])
   for _, t, e in shapes:
     assert t in (16, 32) and 0 <= e <= 512 // t
