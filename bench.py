@@ -61,6 +61,8 @@ def parse(argv=None):
   p.add_argument('--no-adjoint', action='store_true')
   p.add_argument('--no-uneven', action='store_true')
   p.add_argument('--no-humanoid', action='store_true')
+  p.add_argument('--adjoint-horizon', type=int, default=128,
+                 help='env steps of the gradient workload (128 as configured; smaller for a profiler capture)')
   return p.parse_args(argv)
 
 
@@ -477,7 +479,8 @@ def run_braxg(args):
               'peak_source': hbm_src},
   }
   clocks = clk.summary()
-  adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank)
+  adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank,
+                                                        horizon=args.adjoint_horizon)
   uneven = None if args.no_uneven else bench_uneven(torch, dev, rank)
   env_step = bench_env(torch, dev, rank)
   humanoid = None if args.no_humanoid else bench_humanoid(torch, pipeline, dev, rank)
