@@ -481,6 +481,7 @@ def run_braxg(args):
   clocks = clk.summary()
   adjoint = None if args.no_adjoint else bench_adjoint(torch, pipeline, sys_, dev, rank,
                                                         horizon=args.adjoint_horizon)
+  apg_step = None if args.no_adjoint else bench_apg(torch, sys_, dev, rank)
   uneven = None if args.no_uneven else bench_uneven(torch, dev, rank)
   env_step = bench_env(torch, dev, rank)
   humanoid = None if args.no_humanoid else bench_humanoid(torch, pipeline, dev, rank)
@@ -498,7 +499,7 @@ def run_braxg(args):
                                                              args.envs_per_cta, n_env=n)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
       'other_inverse_mode': other_mode,
-      'adjoint': adjoint, 'uneven': uneven, 'env_step': env_step, 'humanoid': humanoid,
+      'adjoint': adjoint, 'apg_closed_loop': apg_step, 'uneven': uneven, 'env_step': env_step, 'humanoid': humanoid,
       'env_status_nonzero': int((status != 0).sum()),
   }
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -538,8 +539,8 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
     return statistics.median(best)
 
   def fwd():
-    s = pipeline.init(sys_, q0, qd0)
-    pipeline.rollout(sys_, s, u, n_frames=N_FRAMES, inverse_mode=pipeline.CHOLESKY, trajectory=True)
+    pipeline.rollout(sys_, pipeline.bare_state(q0, qd0), u, n_frames=N_FRAMES, inverse_mode=pipeline.CHOLESKY,
+                     trajectory=True)
 
   status = [None]
 
@@ -560,6 +561,55 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
           'fwd_adj_ms_smallest_workspace': round(1e3 * t_m, 3),
           'cost_ratio_smallest_workspace': round(t_m / t_f, 3),
           'envs_without_gradient': bad, 'gpu_launches_fwd_adj': 1}
+
+
+def bench_apg(torch, sys_, dev, rank, n=512, horizon=32, reps=3):
+  """The closed-loop APG training step (brax_gb300/apg.py after
+  brax/training/agents/apg/train.py:179-236): an MLP policy acts on each env
+  step's observation for `horizon` env steps (5 frames each), one physics
+  launch per env step forward and one adjoint launch per env step backward,
+  chained by torch.autograd through the policy.  Timed with CUDA events
+  around the host loop (the per-step launches and policy calls included):
+  the loss alone (no gradient) and the loss plus its backward."""
+  from brax_gb300 import apg
+  cfg = apg.Config(num_envs=n, horizon=horizon, n_frames=N_FRAMES)
+  torch.manual_seed(77 + rank)
+  policy = apg.make_policy(sys_.q_size() - 2 + sys_.qd_size(), sys_.act_size(), device=dev)
+  rng = np.random.default_rng(78 + rank)
+  q0 = torch.tensor((sys_.init_q + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))).astype(np.float32), device=dev)
+  qd0 = torch.tensor((0.1 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32), device=dev)
+  stream = torch.cuda.current_stream(dev)
+
+  def fwd():
+    with torch.no_grad():
+      apg.loss(sys_, policy, q0, qd0, cfg)
+
+  def fwd_bwd():
+    policy.zero_grad(set_to_none=True)
+    apg.loss(sys_, policy, q0, qd0, cfg).backward()
+
+  def timed(fn):
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+      e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+      e0.record(stream)
+      fn()
+      e1.record(stream)
+      torch.cuda.synchronize()
+      ts.append(e0.elapsed_time(e1) / 1e3)
+    return statistics.median(ts)
+
+  t_f = timed(fwd)
+  t_b = timed(fwd_bwd)
+  return {'workload': f'closed-loop APG step: quadruped, {n} envs, horizon {horizon} x {N_FRAMES} frames, '
+                      f'MLP policy (64, 64), one launch per env step each way',
+          'fwd_ms': round(1e3 * t_f, 3), 'fwd_bwd_ms': round(1e3 * t_b, 3),
+          'fwd_env_steps_per_s': round(n * horizon / t_f, 1),
+          'fwd_bwd_env_steps_per_s': round(n * horizon / t_b, 1),
+          'cost_ratio_fwd_bwd_over_fwd': round(t_b / t_f, 3),
+          'gpu_launches_fwd_bwd': 2 * horizon}
 
 
 def bench_env(torch, dev, rank, n=4096, steps=50, warmup=3):

@@ -32,11 +32,13 @@ class EnvStep(torch.autograd.Function):
 
   @staticmethod
   def forward(ctx, q, qd, act, sys, n_frames):
-    s = P.init(sys, q.detach(), qd.detach())
-    out, _ = P.rollout(sys, s, act.detach()[None], n_frames=n_frames, inverse_mode=P.CHOLESKY)
+    # one launch: an exact-inverse step reads only q and qd of its input
+    # state (the position terms are recomputed), so no init launch precedes it
+    out = P.step(sys, P.bare_state(q.detach(), qd.detach()), act.detach(), n_frames=n_frames,
+                 inverse_mode=P.CHOLESKY)
     ctx.save_for_backward(q, qd, act)
     ctx.sys, ctx.n_frames = sys, n_frames
-    return out.q.clone(), out.qd.clone()
+    return out.q, out.qd
 
   @staticmethod
   def backward(ctx, gq, gqd):

@@ -379,6 +379,17 @@ def init(sys, q, qd, unused_act=None, unused_ctrl=None, debug: bool = False,
   return out.replace(contact=_contact(m, out)) if debug else out
 
 
+def bare_state(q: torch.Tensor, qd: torch.Tensor) -> State:
+  """A State holding only q and qd: the input of an exact-inverse
+  (``CHOLESKY``) step or rollout, which reads nothing else of its input state
+  (a Newton-Schulz step also needs the carried ``mass_mx_inv``)."""
+  if q.dim() != 2 or qd.dim() != 2 or q.shape[0] != qd.shape[0]:
+    raise ValueError('q and qd must be [n, nq] and [n, nv]')
+  return State(q=q.to(torch.float32).contiguous(), qd=qd.to(torch.float32).contiguous(), x_pos=None,
+               x_rot=None, xd_ang=None, xd_vel=None, mass_mx_inv=None, qf_smooth=None, qf_constraint=None,
+               qdd=None, status=None)
+
+
 def step(sys, state: State, act, debug: bool = False, n_frames: int = 1,
          full: bool = False, inverse_mode: int = NEWTON_SCHULZ, out: Optional[State] = None,
          threads_per_env: int = 0, envs_per_cta: int = 0,
@@ -509,9 +520,8 @@ class Rollout(torch.autograd.Function):
 
   @staticmethod
   def forward(ctx, q0, qd0, act_seq, sys, n_frames, ckpt_every):
-    s = init(sys, q0, qd0)
-    _, (tq, tqd) = rollout(sys, s, act_seq, n_frames=n_frames, inverse_mode=CHOLESKY,
-                           trajectory=True)
+    _, (tq, tqd) = rollout(sys, bare_state(q0.detach(), qd0.detach()), act_seq.detach(), n_frames=n_frames,
+                           inverse_mode=CHOLESKY, trajectory=True)
     ctx.save_for_backward(q0, qd0, act_seq)
     ctx.sys, ctx.n_frames, ctx.ckpt_every = sys, n_frames, ckpt_every
     return tq, tqd

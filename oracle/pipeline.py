@@ -222,8 +222,11 @@ class Oracle:
   # of the rounding envelope (about sqrt(n) for sums of tens of terms)
   DECISION_ULPS = 8
 
+  # evaluation orders of the dense products (see __init__)
+  ORDERS = ('reference', 'right', 'rounded')
+
   def __init__(self, sys: S.System, dtype=np.float64, exact_inverse: bool = False, perturb_seed=None,
-               perturb_bias: int = 0):
+               perturb_bias: int = 0, order: str = 'reference'):
     """exact_inverse=True replaces the Newton-Schulz update of mass_mx_inv by
     the exact SPD inverse (the kernel's Cholesky mode); the reference path is
     exact_inverse=False.
@@ -241,7 +244,21 @@ class Oracle:
     perturb_bias -1 / +1 shifts every such decision the same way (a draw
     biased to one side), 0 draws each shift at random.  This emulates an
     evaluation of the same algorithm in another operation order; it is not
-    part of the reference's algorithm."""
+    part of the reference's algorithm.
+
+    order (also for the envelope; float32 only): how the dense products
+    whose terms cancel are evaluated -- J Minv J^T and J Minv qf_smooth of
+    the constraint problem, Minv (qf_smooth + qf_constraint) of the
+    integrator, the Newton-Schulz products and the exact inverse.
+    'reference' associates them as the reference's code does ((J Minv) J^T)
+    in numpy's summation order; 'right' associates them the other way
+    (J (Minv J^T)); 'rounded' evaluates each in float64 and rounds once (the
+    correctly rounded FP32 result).  Each is an exact evaluation of the same
+    formula; on ill-conditioned models (long hanging chains: mass matrices
+    of condition 1e4) they differ by far more than one ulp of the result."""
+    if order not in self.ORDERS:
+      raise ValueError(f'order must be one of {self.ORDERS}')
+    self.order = order if np.dtype(dtype) == np.float32 else 'reference'
     self.sys = sys
     self.exact_inverse = exact_inverse
     self._rng = None if perturb_seed is None else np.random.default_rng(perturb_seed)
@@ -288,6 +305,18 @@ class Oracle:
       d = np.tril(d) + np.swapaxes(np.tril(d, -1), -1, -2)
     up, dn = np.nextafter(x, self.dt_.type(np.inf)), np.nextafter(x, self.dt_.type(-np.inf))
     return np.where(d > 0, up, np.where(d < 0, dn, x)).astype(self.dt_)
+
+  def _mm(self, a, b):
+    """a @ b in this oracle's evaluation order ('rounded': float64, rounded once)."""
+    if self.order == 'rounded':
+      return (a.astype(np.float64) @ b.astype(np.float64)).astype(self.dt_)
+    return a @ b
+
+  def _mv(self, a, v):
+    """a [B, n, m] times v [B, m] in this oracle's evaluation order."""
+    if self.order == 'rounded':
+      return np.einsum('bij,bj->bi', a.astype(np.float64), v.astype(np.float64)).astype(self.dt_)
+    return np.einsum('bij,bj->bi', a, v)
 
   # -------------------------------------------------------------------------
   # kinematics.forward: brax/kinematics.py:31-108
@@ -488,7 +517,7 @@ class Oracle:
     dt = self.dt_
     n = a.shape[-1]
     eye = np.eye(n, dtype=dt)
-    r0 = eye - a @ a_inv
+    r0 = eye - self._mm(a, a_inv)
     n0 = safe_norm(r0, 2)
     reset = n0 > 1 + self._margin(np.maximum(n0, 1))
     tr = np.trace(a @ np.swapaxes(a, -1, -2), axis1=-2, axis2=-1)
@@ -496,8 +525,8 @@ class Oracle:
     a_inv = np.where(reset[:, None, None], alt, a_inv)
     r, err = r0, np.ones(a.shape[0], dt)
     for _ in range(num_iter):
-      nxt = self._nudge(a_inv @ (eye + r))
-      r_next = self._nudge(eye - a @ nxt)
+      nxt = self._nudge(self._mm(a_inv, eye + r))
+      r_next = self._nudge(eye - self._mm(a, nxt))
       err_next = safe_norm(r_next, 2)
       take = err_next < err + self._margin(np.maximum(err_next, err))
       a_inv = np.where(take[:, None, None], nxt, a_inv)
@@ -506,6 +535,11 @@ class Oracle:
 
   def spd_inverse(self, a):
     """jax.scipy.linalg.solve(a, I, assume_a='pos') (mass.py:104)."""
+    if self.order == 'rounded':
+      a64 = a.astype(np.float64)
+      l = np.linalg.cholesky(a64)
+      linv = np.linalg.solve(l, np.broadcast_to(np.eye(a.shape[-1]), a.shape))
+      return (np.swapaxes(linv, -1, -2) @ linv).astype(self.dt_)
     l = np.linalg.cholesky(a)
     n = a.shape[-1]
     linv = np.linalg.solve(l, np.broadcast_to(np.eye(n, dtype=a.dtype), a.shape))
@@ -560,7 +594,7 @@ class Oracle:
         dist[:, k], pos[:, k] = d, ps
         frame[:, k] = np.stack([nrm, b, cross(nrm, b)], axis=-2)
       elif kind == S.CON_PLANE_BOX:
-        d, ps, fr = _plane_box(p1, m1, p2, m2, size[g2], sub)
+        d, ps, fr = _plane_box(p1, m1, p2, m2, size[g2], sub, None if self._rng is None else self._margin)
         dist[:, k], pos[:, k], frame[:, k] = d, ps, fr
       elif kind == S.CON_SPHERE_SPHERE:
         d, ps, nrm = _sphere_sphere(p1, size[g1, 0], p2, size[g2, 0])
@@ -762,10 +796,15 @@ class Oracle:
     if s.con_jac.shape[1] == 0:
       self.last_pg = {'maxiter': np.zeros(B, bool), 'err': np.zeros(B, dt)}
       return np.zeros((B, nv), dt), np.zeros(B, np.int64)
-    jm = s.con_jac @ s.mass_mx_inv
-    a = jm @ np.swapaxes(s.con_jac, -1, -2)
+    jt = np.swapaxes(s.con_jac, -1, -2)
+    if self.order == 'right':  # J (Minv J^T), J (Minv qf_smooth)
+      a = s.con_jac @ (s.mass_mx_inv @ jt)
+      b = np.einsum('bij,bj->bi', s.con_jac, np.einsum('bij,bj->bi', s.mass_mx_inv, s.qf_smooth)) - s.con_aref
+    else:
+      jm = self._mm(s.con_jac, s.mass_mx_inv)
+      a = self._mm(jm, jt)
+      b = self._mv(jm, s.qf_smooth) - s.con_aref
     a = a + np.einsum('bi,ij->bij', s.con_diag, np.eye(a.shape[-1], dtype=dt))
-    b = np.einsum('bij,bj->bi', jm, s.qf_smooth) - s.con_aref
     a, b = self._nudge(a, symmetric=True), self._nudge(b)
     xs, cnt = self.pg_solve(a, b, sys.solver_iterations, sys.solver_maxls)
     return np.einsum('bij,bi->bj', s.con_jac, xs), cnt
@@ -882,7 +921,7 @@ class Oracle:
       minv = self.spd_inverse(mx)
     else:
       minv = s.mass_mx_inv
-    qdd = np.einsum('bij,bj->bi', minv, s.qf_smooth + s.qf_constraint)
+    qdd = self._mv(minv, s.qf_smooth + s.qf_constraint)
     qd = s.qd + qdd * h
     q = s.q.copy()
     for i, t in enumerate(st.types):
@@ -978,29 +1017,34 @@ def _sphere_sphere(p1, r1, p2, r2):
 _BOX_VERTS = np.array([[sx, sy, sz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)], np.float64)
 
 
-def _box_manifold(vert, mask, n):
+def _box_manifold(vert, mask, n, margin=None):
   """Indices (B, 4) of the manifold points of `vert` (B, 8, 3) among the
-  candidates `mask` (B, 8), n (B, 3) the plane normal in the box frame."""
+  candidates `mask` (B, 8), n (B, 3) the plane normal in the box frame.
+  `margin` (the oracle's rounding envelope) shifts every score of the b, c and
+  d choices by up to a few ulps: a box's symmetric vertices often score
+  exactly alike, and which of them another operation order ranks first is a
+  matter of rounding."""
   big = np.asarray(1e6, vert.dtype)
   dm = np.where(mask, 0, -big).astype(vert.dtype)
+  jit = (lambda x: x) if margin is None else (lambda x: x + margin(np.abs(x)))
   ar = np.arange(vert.shape[0])
   a_i = np.argmax(dm, axis=1)
   a = vert[ar, a_i]
-  b_i = np.argmax(np.sum((a[:, None] - vert) ** 2, -1) + dm, axis=1)
+  b_i = np.argmax(jit(np.sum((a[:, None] - vert) ** 2, -1)) + dm, axis=1)
   b = vert[ar, b_i]
   ab = cross(n, a - b)
   ap = a[:, None] - vert
-  c_i = np.argmax(np.abs(np.sum(ap * ab[:, None], -1)) + dm, axis=1)
+  c_i = np.argmax(jit(np.abs(np.sum(ap * ab[:, None], -1))) + dm, axis=1)
   c = vert[ar, c_i]
   ac, bc = cross(n, a - c), cross(n, b - c)
   bp = b[:, None] - vert
-  d_bp = np.abs(np.sum(bp * bc[:, None], -1)) + dm
-  d_ap = np.abs(np.sum(ap * ac[:, None], -1)) + dm
+  d_bp = jit(np.abs(np.sum(bp * bc[:, None], -1))) + dm
+  d_ap = jit(np.abs(np.sum(ap * ac[:, None], -1))) + dm
   d_i = np.argmax(np.concatenate([d_bp, d_ap], axis=1), axis=1) % vert.shape[1]
   return np.stack([a_i, b_i, c_i, d_i], axis=1)
 
 
-def _plane_box(plane_pos, plane_mat, box_pos, box_mat, size, sub):
+def _plane_box(plane_pos, plane_mat, box_pos, box_mat, size, sub, margin=None):
   """Contact `sub` (0..3) of a plane and a box: dist, pos, frame."""
   dt = box_pos.dtype
   vert = (_BOX_VERTS.astype(dt) * size.astype(dt))[None]            # (1, 8, 3) box frame
@@ -1008,7 +1052,7 @@ def _plane_box(plane_pos, plane_mat, box_pos, box_mat, size, sub):
   n_l = np.einsum('bji,bj->bi', box_mat, plane_mat[..., :, 2])
   support = np.sum((rel[:, None] - vert) * n_l[:, None], -1)        # (B, 8): depth below the plane
   B = box_pos.shape[0]
-  idx = _box_manifold(np.broadcast_to(vert, (B, 8, 3)), support > -1e-3, n_l)
+  idx = _box_manifold(np.broadcast_to(vert, (B, 8, 3)), support > -1e-3, n_l, margin)
   i = idx[:, sub]
   unique = np.all(idx[:, :sub] != i[:, None], axis=1) if sub > 0 else np.ones(B, bool)
   ar = np.arange(B)

@@ -68,13 +68,18 @@ def reverse_along(args):
 
 
 def tail_fd(args):
-  """(name, q_t [nq], qd_t [nv], act [H - t, nu], n_frames, eps_list, coords)
-  -> ({eps: [len(coords)]} central differences of -mean torso x-velocity over
-  the env steps t..H-1 (each 1/H weighted; H given as act's length plus t via
-  `horizon`) w.r.t. act[0, k] for k in coords, and the FP64 tail trajectory
-  of the unperturbed actions (q, qd after each env step))."""
+  """(name, q_t [nq], qd_t [nv], act [H - t, nu], n_frames, eps_list, coords,
+  horizon[, forced]) -> ({eps: [len(coords)]} central differences of -mean
+  torso x-velocity over the env steps t..H-1 (each 1/horizon weighted) w.r.t.
+  act[0, k] for k in coords, the FP64 tail trajectory of the unperturbed
+  actions (q, qd after each env step), and whether every frame's FP64 active
+  row count matched the forced tape's).  With `forced` ([H - t][n_frames]
+  (iterations, active rows, step sizes) of another implementation's
+  projected-gradient solves), every rollout of the difference takes those
+  solver decisions: the difference quotient of the same branch."""
   from oracle.pipeline import Oracle
-  name, q_t, qd_t, act, n_frames, eps_list, coords, horizon = args
+  name, q_t, qd_t, act, n_frames, eps_list, coords, horizon = args[:8]
+  forced = args[8] if len(args) > 8 else None
   sys_ = _sys(name)
   o = Oracle(sys_, np.float64, exact_inverse=True)
   L = act.shape[0]
@@ -88,14 +93,31 @@ def tail_fd(args):
         rows.append(a)
   B = len(rows)
   acts = np.stack(rows, axis=1).astype(np.float64)  # [L, B, nu]
-  s = o.init(np.repeat(q_t[None].astype(np.float64), B, 0), np.repeat(qd_t[None].astype(np.float64), B, 0))
+  q = np.repeat(q_t[None].astype(np.float64), B, 0)
+  qd = np.repeat(qd_t[None].astype(np.float64), B, 0)
   loss = np.zeros(B)
   traj_q, traj_qd = [], []
-  for j in range(L):
-    s = o.env_step(s, acts[j], n_frames)
-    loss += -s.qd[:, 0] / horizon
-    traj_q.append(s.q[0].copy())
-    traj_qd.append(s.qd[0].copy())
+  rows_ok = True
+  if forced is None:
+    s = o.init(q, qd)
+    for j in range(L):
+      s = o.env_step(s, acts[j], n_frames)
+      loss += -s.qd[:, 0] / horizon
+      traj_q.append(s.q[0].copy())
+      traj_qd.append(s.qd[0].copy())
+  else:
+    from oracle.adjoint import StepAdjoint
+    adj = StepAdjoint(sys_)
+    for j in range(L):
+      for f in range(n_frames):
+        iters, rows, steps = forced[j][f]
+        adj.force = (iters, steps)
+        q, qd, T = adj.forward(q, qd, acts[j])
+        adj.force = None
+        rows_ok = rows_ok and bool((np.count_nonzero(T['s'].con_diag, axis=1) == rows).all())
+      loss += -qd[:, 0] / horizon
+      traj_q.append(q[0].copy())
+      traj_qd.append(qd[0].copy())
   out, i = {}, 1
   for eps in eps_list:
     fd = np.zeros(len(coords))
@@ -103,4 +125,4 @@ def tail_fd(args):
       fd[c] = (loss[i] - loss[i + 1]) / (2 * eps)
       i += 2
     out[eps] = fd
-  return out, np.array(traj_q), np.array(traj_qd)
+  return out, np.array(traj_q), np.array(traj_qd), rows_ok

@@ -44,10 +44,14 @@ def load(name):
   return mjcf.load_asset(name)
 
 
-# draws of the FP32 rounding envelope: (seed, bias) of oracle.pipeline.Oracle's
-# perturbation; the two biased draws take every near-tie decision one way and
-# the other, the rest at random
-ENVELOPE_DRAWS = ((1000, -1), (1001, 1), (1002, 0), (1003, 0), (1004, 0))
+# draws of the FP32 rounding envelope: (seed, bias, order) of
+# oracle.pipeline.Oracle's perturbation; the two biased draws take every
+# near-tie decision one way and the other, three more at random, and two
+# evaluate the dense products whose terms cancel (J Minv J^T, J Minv
+# qf_smooth, Minv qf, the inverse) in another exact FP32 order without other
+# perturbation
+ENVELOPE_DRAWS = ((1000, -1, 'reference'), (1001, 1, 'reference'), (1002, 0, 'reference'),
+                  (1003, 0, 'reference'), (1004, 0, 'reference'), (None, 0, 'right'), (None, 0, 'rounded'))
 
 
 def oracle_check(sys, q, qd, minv, act, n_frames, exact, got_q, got_qd, label, strict=False):
@@ -65,8 +69,8 @@ def oracle_check(sys, q, qd, minv, act, n_frames, exact, got_q, got_qd, label, s
                                  None if exact else minv.astype(np.float64)),
                      act.astype(np.float64), n_frames)
   spread = {'q': np.zeros(q.shape[0]), 'qd': np.zeros(q.shape[0])}
-  for seed, bias in ENVELOPE_DRAWS:
-    op = Oracle(sys, np.float32, exact_inverse=exact, perturb_seed=seed, perturb_bias=bias)
+  for seed, bias, order in ENVELOPE_DRAWS:
+    op = Oracle(sys, np.float32, exact_inverse=exact, perturb_seed=seed, perturb_bias=bias, order=order)
     rp = op.env_step(op.restore(q, qd, mi), act32, n_frames)
     for f in spread:
       spread[f] = np.maximum(spread[f], rel_err(getattr(rp, f), getattr(r32, f)))

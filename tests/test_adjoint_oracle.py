@@ -49,3 +49,40 @@ def test_step_vjp_matches_finite_differences(name, steps):
   T = _fd_check(name, steps)
   if steps == 40:  # the landed quadruped exercises contact and limit rows
     assert (np.abs(T['s'].con_jac).max(-1) > 0).sum() > 0
+
+
+def test_tail_fd_forced_onto_its_own_branch():
+  """tests/grad_util.tail_fd with every projected-gradient solve forced onto
+  the decisions the FP64 rollout takes by itself reproduces the free tail and
+  its differences (the forcing the APG-workload check uses with the GPU's
+  decisions)."""
+  from oracle.adjoint import StepAdjoint
+  from oracle.pipeline import Oracle
+  from brax_gb300 import mjcf
+  from tests import grad_util
+  sys_ = mjcf.load_asset('quadruped')
+  rng = np.random.default_rng(5)
+  o = Oracle(sys_, np.float64, exact_inverse=True)
+  s = o.init((sys_.init_q + rng.uniform(-0.1, 0.1, sys_.q_size()))[None], np.zeros((1, sys_.qd_size())))
+  for _ in range(6):  # land
+    s = o.env_step(s, rng.uniform(-1, 1, (1, sys_.act_size())), 5)
+  L, F = 2, 2
+  act = rng.uniform(-1, 1, (L, sys_.act_size()))
+  adj = StepAdjoint(sys_)
+  q, qd, forced = s.q.copy(), s.qd.copy(), []
+  for j in range(L):
+    row = []
+    for _ in range(F):
+      q, qd, T = adj.forward(q, qd, act[j][None])
+      pg = T.get('pg', [])
+      row.append((len(pg), int(np.count_nonzero(T['s'].con_diag[0])), [float(r['step'][0]) for r in pg]))
+    forced.append(row)
+  assert sum(r[1] for rr in forced for r in rr) > 0  # in contact
+  args = ('quadruped', s.q[0], s.qd[0], act, F, (1e-4, 1e-5), [0, 3, 6], L)
+  free = grad_util.tail_fd(args)
+  pinned = grad_util.tail_fd(args + (forced,))
+  assert pinned[3]
+  np.testing.assert_allclose(pinned[1], free[1], rtol=0, atol=1e-10)
+  np.testing.assert_allclose(pinned[2], free[2], rtol=0, atol=1e-10)
+  for eps in (1e-4, 1e-5):
+    np.testing.assert_allclose(pinned[0][eps], free[0][eps], rtol=1e-4, atol=1e-8)

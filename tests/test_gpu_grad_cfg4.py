@@ -31,13 +31,18 @@ path alike.  So the check has two parts:
     checked, and qd0 within 1e-3 for envs without such a frame;
 (b) FP64 central differences at eps = 1e-4 and 1e-5 side by side for the
     actions of env steps 112, 120 and 127 (the last checkpoint segment),
-    rolled out in FP64 from the GPU's state at that step.  Where the two
-    differences agree (FD is smooth: no contact or line-search switch within
-    eps) and the FP64 tail tracks the GPU's trajectory to 1e-4, the adjoint
-    must match the eps = 1e-5 difference within max(1e-3, 2 x the FP32
-    adjoint's same-branch error at that env step from (a)), relative to the
-    env step's largest derivative; every other (env, step, action) is
-    listed with the evidence (the two differences, the tail divergence).
+    rolled out in FP64 from the GPU's state at that step with every frame's
+    projected-gradient solve forced onto the GPU's decisions (the same
+    branch, as in (a); a line-search tie in the 16-step tail otherwise puts
+    the FP64 rollouts on another branch than the one the GPU
+    differentiated).  Where the two differences agree (FD is smooth: no
+    contact or active-set switch within eps), every frame's FP64 active row
+    count equals the GPU's, and the FP64 tail tracks the GPU's trajectory to
+    1e-4, the adjoint must match the eps = 1e-5 difference within
+    max(1e-3, 2 x the FP32 adjoint's same-branch error at that env step from
+    (a)), relative to the env step's largest derivative; every other (env,
+    step, action) is listed with the evidence (the two differences, the
+    difference on the FP64 solves' own branches, the tail divergence).
 """
 
 import multiprocessing as mp
@@ -146,10 +151,10 @@ def test_apg_workload_gradient():
                    [('quadruped', q_start[:, e], qd_start[:, e], u[:, e], q_bar[:, e], qd_bar[:, e], F, forced[i])
                     for i, e in enumerate(ENVS)])
     fd_args = []
-    for e in ENVS:
+    for i, e in enumerate(ENVS):
       for t in FD_STEPS:
-        fd_args.append(('quadruped', q_start[t, e], qd_start[t, e], u[t:, e], F, (1e-4, 1e-5),
-                        list(range(sys_.act_size())), H))
+        a = ('quadruped', q_start[t, e], qd_start[t, e], u[t:, e], F, (1e-4, 1e-5), list(range(sys_.act_size())), H)
+        fd_args += [a + (forced[i][t:],), a]  # the GPU's branch; the FP64 solves' own branches
     fds = pool.map(grad_util.tail_fd, fd_args)
 
   # (a) against the FP64 reverse of the GPU's own branch, along the GPU
@@ -185,39 +190,48 @@ def test_apg_workload_gradient():
     if last_mis[i] < 0 and e_qd0[i] > 1e-3:
       fails.append(('(a) qd0_bar above 1e-3', int(ENVS[i]), float(e_qd0[i])))
 
-  # (b) FP64 central differences on the last segment
-  checked, listed, errs_b = 0, [], []
+  # (b) FP64 central differences on the last segment, every rollout of the
+  # difference on the GPU's branch (its projected-gradient decisions forced);
+  # the same differences on the FP64 solves' own branches are printed beside
+  checked, listed, errs_b, errs_free = 0, [], [], []
   k = 0
-  for e in ENVS:
+  for i, e in enumerate(ENVS):
     for t in FD_STEPS:
-      fd, tail_q, tail_qd = fds[k]
-      k += 1
+      (fd, tail_q, tail_qd, rows_ok), (fdu, _, _, _) = fds[k], fds[k + 1]
+      k += 2
       gpu = act_bar[t, e].astype(np.float64)
       scale = max(np.abs(fd[1e-5]).max(), 1e-9)
       smooth = np.abs(fd[1e-4] - fd[1e-5]) <= 1e-3 * scale
       track = max(rel_err(tail_q, tq[t:, e]).max(), rel_err(tail_qd, tqd[t:, e]).max())
       err = np.abs(gpu - fd[1e-5]) / scale
+      errs_free.append(float((np.abs(gpu - fdu[1e-5]) / max(np.abs(fdu[1e-5]).max(), 1e-9)).max()))
       # the FP32 adjoint's own rounding at this env step: its same-branch
       # difference from the FP64 reverse, part (a)
-      own = float(e_steps[list(ENVS).index(e), t])
+      own = float(e_steps[i, t])
       for j in range(len(gpu)):
-        if smooth[j] and track <= 1e-4:
+        if rows_ok and smooth[j] and track <= 1e-4:
           checked += 1
           errs_b.append(err[j])
           if err[j] > max(1e-3, 2 * own):
             fails.append(('(b) smooth, tracked derivative beyond max(1e-3, 2 x the FP32 error of its step)',
                           int(e), t, j, float(gpu[j]), float(fd[1e-5][j]), own))
         else:
-          listed.append((int(e), t, j, float(gpu[j]), float(fd[1e-4][j]), float(fd[1e-5][j]), float(track)))
+          listed.append((int(e), t, j, float(gpu[j]), float(fd[1e-4][j]), float(fd[1e-5][j]), float(fdu[1e-5][j]),
+                         float(track), 'rows' if not rows_ok else ''))
   eb = np.array(errs_b) if errs_b else np.zeros(1)
-  print(f'(b) last-segment actions: {checked} derivatives checked against FP64 FD (eps 1e-5): p50 '
+  print(f'(b) last-segment actions: {checked} derivatives checked against FP64 FD on the GPU branch (eps 1e-5): p50 '
         f'{np.median(eb):.1e} p95 {np.quantile(eb, 0.95):.1e} max {eb.max():.1e}, {(eb <= 1e-3).mean() * 100:.1f} % '
-        f'<= 1e-3; {len(listed)} listed (FD not smooth between eps 1e-4 and 1e-5, or the FP64 tail leaves the GPU '
-        f'trajectory by more than 1e-4):')
+        f'<= 1e-3; against FD on the FP64 solves\' own branches, per (env, step) max: p50 '
+        f'{np.median(errs_free):.1e} max {np.max(errs_free):.1e}; {len(listed)} listed (FD not smooth between eps '
+        f'1e-4 and 1e-5, the FP64 tail leaves the GPU trajectory by more than 1e-4, or an active-row count differs '
+        f'from the GPU tape):')
   for row in listed[:24]:
-    print('    env %d step %d act %d: adjoint %.5e | FD eps 1e-4 %.5e, eps 1e-5 %.5e | tail divergence %.1e' % row)
+    print('    env %d step %d act %d: adjoint %.5e | FD eps 1e-4 %.5e, eps 1e-5 %.5e (own branches %.5e) | '
+          'tail divergence %.1e %s' % row)
   if checked < 0.5 * len(ENVS) * len(FD_STEPS) * sys_.act_size():
     fails.append(('(b) fewer than half the derivatives checkable', checked))
+  for f_ in fails:
+    print('FAIL', f_)
 
   # the evidence for the design above: FP64 from the same start vs the GPU trajectory
   from oracle.pipeline import Oracle

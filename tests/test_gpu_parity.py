@@ -336,18 +336,30 @@ def test_box_plane_contacts_and_step():
   # adding -1e6, which in FP32 rounds their scores to multiples of 1/16, so
   # among those the choice is a tie that FP32 breaks by index and FP64 by the
   # scores' low digits
-  d, p, f = Oracle(sys, np.float32).contacts(_np(st.x.pos), _np(st.x.rot))
-  np.testing.assert_allclose(_np(st.contact.dist), d, atol=2e-6, rtol=0)
-  np.testing.assert_allclose(_np(st.contact.pos), p, atol=2e-6, rtol=0)
-  np.testing.assert_allclose(_np(st.contact.frame), f, atol=2e-6, rtol=0)
-  np.testing.assert_allclose(_np(st.contact.dist)[0], [-0.01, -0.01, -0.01, 1.0], atol=1e-6)
-  assert ((_np(st.contact.dist) < 0).sum(1) > 0).mean() > 0.3  # many boxes touch the plane
-  got = P.step(sys, st, None, inverse_mode=P.CHOLESKY)
+  xp, xr = _np(st.x.pos), _np(st.x.rot)
+  ref = Oracle(sys, np.float32).contacts(xp, xr)
+  # a box's symmetric vertices often score exactly alike in the manifold's
+  # choices, and which one an operation order ranks first is rounding: a slot
+  # that differs from the FP32 oracle must match one of the oracle's draws
+  # with those scores shifted by a few ulps at random
+  draws = [Oracle(sys, np.float32, perturb_seed=s, perturb_bias=0).contacts(xp, xr) for s in range(300, 332)]
+  got = [_np(st.contact.dist), _np(st.contact.pos), _np(st.contact.frame)]
+  close = lambda c: np.all([np.abs(g - r).reshape(n, 4, -1).max(-1) <= 2e-6 for g, r in zip(got, c)], axis=0)
+  same = close(ref)
+  tie = ~same & np.any([close(c) for c in draws], axis=0)
+  print(f'box manifold: {same.sum()} slots as the FP32 oracle, {tie.sum()} a tie taken the other way '
+        f'(envs {np.nonzero(tie.any(1))[0].tolist()})')
+  assert (same | tie).all(), np.argwhere(~(same | tie))[:8]
+  assert tie.mean() <= 0.25
+  np.testing.assert_allclose(got[0][0], [-0.01, -0.01, -0.01, 1.0], atol=1e-6)
+  assert ((got[0] < 0).sum(1) > 0).mean() > 0.3  # many boxes touch the plane
+  out = P.step(sys, st, None, inverse_mode=P.CHOLESKY)
   o32 = Oracle(sys, np.float32, exact_inverse=True)
   r32 = o32.step(o32.init(q, qd), None)
   torch.cuda.synchronize()
-  assert (_np(got.status) == 0).all()
+  assert (_np(out.status) == 0).all()
+  keep = ~tie.any(1)  # the step of an env whose contact point was a tie is the other branch's
   for field in ('q', 'qd'):
-    e = rel_err(_np(getattr(got, field)), getattr(r32, field))
+    e = rel_err(_np(getattr(out, field))[keep], getattr(r32, field)[keep])
     print(f'box on plane {field}: vs fp32 p50 {np.median(e):.2e} p99 {np.quantile(e, 0.99):.2e} max {e.max():.2e}')
     assert np.quantile(e, 0.99) <= 1e-5, (field, np.sort(e)[-4:])

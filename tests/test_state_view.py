@@ -82,3 +82,18 @@ def test_contact_pytree_constants():
   np.testing.assert_array_equal(c.geom[0, :, 0].numpy(), sys.contacts.geom1)
   assert (c.link_idx[0] == -1).all()  # every quadruped contact is against the world plane
   np.testing.assert_allclose(c.elasticity[0].numpy(), sys.contacts.elasticity)
+
+
+def test_bare_state_carries_only_q_and_qd():
+  q, qd = torch.randn(3, 7), torch.randn(3, 5, dtype=torch.float64)
+  s = P.bare_state(q, qd)
+  assert s.q.dtype == torch.float32 and s.qd.dtype == torch.float32
+  assert torch.equal(s.qd, qd.float())
+  # every other field the C ABI reads is a null pointer
+  cs = P._cstate(s)
+  for f in N.STATE_FIELDS:
+    if f not in ('q', 'qd'):
+      assert getattr(cs, f) is None, f
+  assert s.x is None and s.cache is None
+  with pytest.raises(ValueError):
+    P.bare_state(q, torch.randn(4, 5))
