@@ -485,6 +485,7 @@ def run_braxg(args):
   uneven = None if args.no_uneven else bench_uneven(torch, dev, rank)
   env_step = bench_env(torch, dev, rank)
   humanoid = None if args.no_humanoid else bench_humanoid(torch, pipeline, dev, rank)
+  chain3 = bench_chain3(torch, pipeline, dev, rank)
   out = {
       'metric': METRIC, 'value': round(value, 1), 'unit': 'env-steps/s', 'n_gpus': world,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': round(ms_per_step, 4),
@@ -499,7 +500,7 @@ def run_braxg(args):
                                                              args.envs_per_cta, n_env=n)))},
       'e2e': e2e, 'gpu_launches': launches, 'roofline': roofline, 'clocks': clocks,
       'other_inverse_mode': other_mode,
-      'adjoint': adjoint, 'apg_closed_loop': apg_step, 'uneven': uneven, 'env_step': env_step, 'humanoid': humanoid,
+      'adjoint': adjoint, 'apg_closed_loop': apg_step, 'uneven': uneven, 'env_step': env_step, 'humanoid': humanoid, 'chain3': chain3,
       'env_status_nonzero': int((status != 0).sum()),
   }
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -686,6 +687,38 @@ def bench_humanoid(torch, pipeline, dev, rank, n=16384, steps=20, warmup=3):
           'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
                                    model.launch_shape(pipeline.CHOLESKY, n_env=n))),
           'env_status_nonzero': int((last.status != 0).sum().item()), 'gpu_launches_per_step': 1}
+
+
+def bench_chain3(torch, pipeline, dev, rank, n=128, n_steps=1000):
+  """The plain 3-link chain workload (nq = nv = 3, no contacts): 128 envs,
+  q0 ~ U(-pi/4, pi/4), qd0 ~ N(0, 0.1), zero actions, 1000 pipeline steps of
+  0.01 s as one rollout launch (the reference's lax.scan of 1000 steps), in
+  both inverse modes.  Its inputs and outputs are a few KB: L2-resident."""
+  from brax_gb300 import mjcf
+  sys_ = mjcf.load_asset('chain3')
+  rng = np.random.default_rng(300 + rank)
+  q0 = torch.tensor(rng.uniform(-np.pi / 4, np.pi / 4, (n, 3)).astype(np.float32), device=dev)
+  qd0 = torch.tensor(rng.normal(0, 0.1, (n, 3)).astype(np.float32), device=dev)
+  acts = torch.zeros(n_steps, n, sys_.act_size(), device=dev)
+  stream = torch.cuda.current_stream(dev)
+  out = {'workload': f'chain3 (3 hinges, no contact), {n} envs, {n_steps} steps of {sys_.dt} s in one launch'}
+  for name, mode in (('exact', pipeline.CHOLESKY), ('newton_schulz', pipeline.NEWTON_SCHULZ)):
+    s = pipeline.init(sys_, q0, qd0)
+    pipeline.rollout(sys_, s, acts[:10], inverse_mode=mode)  # warm-up
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(3):
+      e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+      e0.record(stream)
+      last, _ = pipeline.rollout(sys_, s, acts, inverse_mode=mode)
+      e1.record(stream)
+      torch.cuda.synchronize()
+      ts.append(e0.elapsed_time(e1) / 1e3)
+    t = statistics.median(ts)
+    out[name] = {'env_steps_per_s': round(n * n_steps / t, 1), 'ms_per_rollout': round(1e3 * t, 3),
+                 'env_status_nonzero': int((last.status != 0).sum().item())}
+  out['gpu_launches_per_rollout'] = 1
+  return out
 
 
 def bench_uneven(torch, dev, rank, total=8192, n_steps=256):

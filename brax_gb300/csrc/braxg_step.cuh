@@ -1749,7 +1749,15 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
   tm.sync();
   grad(b, gy);
   matvecs += 1;
-  for (int i = tm.lane; i < nrow; i += T) gx[i] = gy[i];
+  float fy;  // f(y) = |A y + b|^2 / 2 of the current y
+  {
+    float fs = 0.f;
+    for (int i = tm.lane; i < nrow; i += T) {
+      gx[i] = gy[i];
+      fs += 0.5f * ry[i] * ry[i];
+    }
+    fy = tm.sum(fs);
+  }
   for (int it = 0; it < md.pg_iters; ++it) {
     if (it > 0 && !(err > md.pg_tol)) break;
     float* rec = tape != nullptr ? tape + tape_head_words(nrow) + it * tape_iter_words(nrow) : nullptr;
@@ -1758,9 +1766,6 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
         rec[4 + i] = y[i];
         rec[4 + kA + i] = ry[i];
       }
-    float fs = 0.f;
-    for (int i = tm.lane; i < nrow; i += T) fs += 0.5f * ry[i] * ry[i];
-    const float fy = tm.sum(fs);
     float cur = ss;
     for (int i = tm.lane; i < nrow; i += T) nx[i] = fmaxf(y[i] + (-cur) * gy[i], 0.f);
     tm.sync();
@@ -1809,19 +1814,24 @@ __device__ __noinline__ int pg_explicit(const int* mw, Ws w, int nrow, float* ta
     // stopping error at nx; then the momentum step, applied to the point, its
     // residual and its gradient alike (A is linear), so that y's residual and
     // gradient cost no matvec
-    float es = 0.f;
+    // (and f at the new y, reduced alongside: the same sum, in the same order,
+    // as over the stored residual)
+    float es = 0.f, fs = 0.f;
     for (int i = tm.lane; i < nrow; i += T) {
       const float xn = nx[i], r1 = rn[i], g1 = gn[i];
       const float e = fmaxf(xn + (-1.f) * g1, 0.f) - xn;
       es += e * e;
       y[i] = xn + beta * (xn - x[i]);
-      ry[i] = r1 + beta * (r1 - rx[i]);
+      const float r2 = r1 + beta * (r1 - rx[i]);
+      ry[i] = r2;
+      fs += 0.5f * r2 * r2;
       gy[i] = g1 + beta * (g1 - gx[i]);
       x[i] = xn;
       rx[i] = r1;
       gx[i] = g1;
     }
     err = sqrtf(tm.sum(es));
+    fy = tm.sum(fs);
     tm.sync();
     t = nt;
     ss = nss;

@@ -112,12 +112,25 @@ def tail_fd(args):
       for f in range(n_frames):
         iters, rows, steps = forced[j][f]
         adj.force = (iters, steps)
-        q, qd, T = adj.forward(q, qd, acts[j])
-        adj.force = None
-        rows_ok = rows_ok and bool((np.count_nonzero(T['s'].con_diag, axis=1) == rows).all())
+        try:
+          with np.errstate(all='ignore'):
+            q, qd, T = adj.forward(q, qd, acts[j])
+        except np.linalg.LinAlgError:  # a forced solve off its branch threw the state off
+          rows_ok = False
+          break
+        finally:
+          adj.force = None
+        if not (np.count_nonzero(T['s'].con_diag, axis=1) == rows).all():
+          rows_ok = False  # the tape belongs to another active set: forcing it means nothing
+          break
+      if not rows_ok:
+        break
       loss += -qd[:, 0] / horizon
       traj_q.append(q[0].copy())
       traj_qd.append(qd[0].copy())
+    if not rows_ok:
+      nan = {eps: np.full(len(coords), np.nan) for eps in eps_list}
+      return nan, np.full((L, q.shape[1]), np.nan), np.full((L, qd.shape[1]), np.nan), False
   out, i = {}, 1
   for eps in eps_list:
     fd = np.zeros(len(coords))
