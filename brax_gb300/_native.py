@@ -24,7 +24,7 @@ STATE_FIELDS = (
 EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims', 'braxg_model_cache_words', 'braxg_model_cache_span',
            'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_rollout_vjp_workspace',
            'braxg_rollout_vjp_workspace_resident',
-           'braxg_rollout_vjp', 'braxg_rollout_vjp_noalloc',
+           'braxg_rollout_vjp', 'braxg_rollout_vjp_fwd', 'braxg_rollout_vjp_bwd', 'braxg_rollout_vjp_noalloc',
            'braxg_rollout_vjp_noalloc_capacity', 'braxg_launch_shape',
            'braxg_batch_create', 'braxg_batch_destroy', 'braxg_batch_get_offsets',
            'braxg_batch_launch_info', 'braxg_batch_init', 'braxg_batch_rollout',
@@ -130,6 +130,10 @@ def lib() -> ctypes.CDLL:
                                                        P(ctypes.c_size_t)]
     l.braxg_rollout_vjp.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp,
                                     vp, vp, vp, ctypes.c_size_t, vp, P(Options)]
+    l.braxg_rollout_vjp_fwd.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp,
+                                        ctypes.c_size_t, vp, P(Options)]
+    l.braxg_rollout_vjp_bwd.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp,
+                                        vp, ctypes.c_size_t, vp, P(Options)]
     l.braxg_rollout_vjp_noalloc.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp,
                                             vp, vp, vp, vp, vp, P(Options)]
     l.braxg_rollout_vjp_noalloc_capacity.restype = ctypes.c_size_t

@@ -4,11 +4,12 @@ The training step of brax/training/agents/apg/train.py:179-236 in torch: a
 closed-loop policy acts on the observation for ``horizon`` env steps, the loss
 is the negative mean reward, and the gradient flows back through every env
 step to the policy parameters.  Each env step is ``EnvStep`` — a
-``torch.autograd.Function`` whose forward is one braxg_rollout env step
-(exact mass-matrix inverse) and whose backward is one braxg_rollout_vjp launch
-of that env step — so torch's autograd chains the physics adjoint with the
-policy network's backward, as ``jax.grad`` chains them through ``lax.scan`` in
-the reference.
+``torch.autograd.Function`` whose forward is the forward half of the
+gradient kernel for that env step (braxg_rollout_vjp_fwd: exact mass-matrix
+inverse, its frame snapshots kept) and whose backward is the reverse half
+(braxg_rollout_vjp_bwd) — so torch's autograd chains the physics adjoint with
+the policy network's backward, as ``jax.grad`` chains them through
+``lax.scan`` in the reference.
 
 The reward is the locomotion task's (brax/envs/ant.py:238-262): forward
 velocity of the torso (q[0] is its x position for a free-root model) over the
@@ -32,27 +33,28 @@ class EnvStep(torch.autograd.Function):
 
   @staticmethod
   def forward(ctx, q, qd, act, sys, n_frames):
-    # one launch: an exact-inverse step reads only q and qd of its input
-    # state (the position terms are recomputed), so no init launch precedes it
-    out = P.step(sys, P.bare_state(q.detach(), qd.detach()), act.detach(), n_frames=n_frames,
-                 inverse_mode=P.CHOLESKY)
-    ctx.save_for_backward(q, qd, act)
-    ctx.sys, ctx.n_frames = sys, n_frames
-    return out.q, out.qd
+    # one launch, the forward half of the gradient kernel: the env step's
+    # frame snapshots stay in a workspace for the backward, which then runs
+    # only the reverse (an exact-inverse step reads only q and qd of its
+    # input, so no init launch precedes it)
+    (tq, tqd), ctx.tape = P.rollout_vjp_fwd(sys, q.detach(), qd.detach(), act.detach()[None],
+                                            n_frames=n_frames, ckpt_every=1, resident_segments=1)
+    return tq[0], tqd[0]
 
   @staticmethod
   def backward(ctx, gq, gqd):
-    q, qd, act = ctx.saved_tensors
-    gq = torch.zeros_like(q) if gq is None else gq.contiguous()
-    gqd = torch.zeros_like(qd) if gqd is None else gqd.contiguous()
-    act_bar, q_bar, qd_bar, _, _ = P.rollout_grad(ctx.sys, q.detach(), qd.detach(), act.detach()[None],
-                                                  gq[None], gqd[None], n_frames=ctx.n_frames, ckpt_every=1,
-                                                  resident_segments=1)
+    act_bar, q_bar, qd_bar, _ = P.rollout_vjp_bwd(ctx.tape, None if gq is None else gq[None],
+                                                  None if gqd is None else gqd[None])
     return q_bar, qd_bar, act_bar[0], None, None
 
 
 def env_step(sys, q, qd, act, n_frames: int):
-  return EnvStep.apply(q, qd, act, sys, n_frames)
+  """One env step, differentiable when a gradient is being taken (else a
+  plain step launch)."""
+  if torch.is_grad_enabled() and any(t.requires_grad for t in (q, qd, act)):
+    return EnvStep.apply(q, qd, act, sys, n_frames)
+  out = P.step(sys, P.bare_state(q, qd), act, n_frames=n_frames, inverse_mode=P.CHOLESKY)
+  return out.q, out.qd
 
 
 @dataclasses.dataclass

@@ -64,11 +64,13 @@ int braxg_rollout_vjp_workspace(const braxg_model* m, int n_env, int n_steps, in
   return braxg_rollout_vjp_workspace_resident(m, n_env, n_steps, n_frames, ckpt_every, 1, bytes);
 }
 
-int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, int ckpt_every,
-                      const float* act_seq, const float* q0, const float* qd0, const float* q_bar,
-                      const float* qd_bar, float* act_bar, float* q0_bar, float* qd0_bar, float* traj_q,
-                      float* traj_qd, void* workspace, size_t workspace_bytes, int32_t* status,
-                      const braxg_options* opt) {
+// One launch of the gradient kernel: `phases` 3 (forward and reverse), 1 (the
+// forward: checkpoints, snapshots and trajectory into the workspace) or 2 (the
+// reverse, from a workspace a phase-1 launch with the same arguments filled).
+static int run_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, int ckpt_every,
+                   const float* act_seq, const float* q0, const float* qd0, const float* q_bar, const float* qd_bar,
+                   float* act_bar, float* q0_bar, float* qd0_bar, float* traj_q, float* traj_qd, void* workspace,
+                   size_t workspace_bytes, int32_t* status, const braxg_options* opt, int phases) {
   braxg::host::set_launches(0);
   size_t need = 0;
   int rc = braxg_rollout_vjp_workspace(m, n_env, n_steps, n_frames, ckpt_every, &need);
@@ -118,6 +120,7 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
   a.traj_qd = traj_qd;
   a.status = status;
   a.prof = opt ? opt->stage_cycles : nullptr;
+  a.phases = phases;
   braxg::AdjLayout A = braxg::make_adj_layout(m->dims.nl, m->dims.nq, m->dims.nv, m->dims.nu, m->dims.ncon,
                                               m->dims.nlim, m->h[BXM_H_PG_ITERS]);
   int head = (braxg::al4(m->words) + 2 * braxg::kLayoutWords) * 4;
@@ -140,6 +143,32 @@ int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps
   if (back != cudaSuccess) return cuda_fail(back, "restoring the current device");
   braxg::host::set_launches(1);
   return BRAXG_OK;
+}
+
+int braxg_rollout_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, int ckpt_every,
+                      const float* act_seq, const float* q0, const float* qd0, const float* q_bar,
+                      const float* qd_bar, float* act_bar, float* q0_bar, float* qd0_bar, float* traj_q,
+                      float* traj_qd, void* workspace, size_t workspace_bytes, int32_t* status,
+                      const braxg_options* opt) {
+  return run_vjp(m, stream, n_env, n_steps, n_frames, ckpt_every, act_seq, q0, qd0, q_bar, qd_bar, act_bar, q0_bar,
+                 qd0_bar, traj_q, traj_qd, workspace, workspace_bytes, status, opt, 3);
+}
+
+int braxg_rollout_vjp_fwd(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, int ckpt_every,
+                          const float* act_seq, const float* q0, const float* qd0, float* traj_q, float* traj_qd,
+                          void* workspace, size_t workspace_bytes, int32_t* status, const braxg_options* opt) {
+  if (n_env > 0 && (traj_q == nullptr || traj_qd == nullptr))
+    return fail(BRAXG_ERR_INVALID, "braxg_rollout_vjp_fwd: traj_q and traj_qd are required");
+  return run_vjp(m, stream, n_env, n_steps, n_frames, ckpt_every, act_seq, q0, qd0, nullptr, nullptr, nullptr,
+                 nullptr, nullptr, traj_q, traj_qd, workspace, workspace_bytes, status, opt, 1);
+}
+
+int braxg_rollout_vjp_bwd(const braxg_model* m, void* stream, int n_env, int n_steps, int n_frames, int ckpt_every,
+                          const float* act_seq, const float* q0, const float* qd0, const float* q_bar,
+                          const float* qd_bar, float* act_bar, float* q0_bar, float* qd0_bar, void* workspace,
+                          size_t workspace_bytes, int32_t* status, const braxg_options* opt) {
+  return run_vjp(m, stream, n_env, n_steps, n_frames, ckpt_every, act_seq, q0, qd0, q_bar, qd_bar, act_bar, q0_bar,
+                 qd0_bar, nullptr, nullptr, workspace, workspace_bytes, status, opt, 2);
 }
 
 // ---------------------------------------------------------------------------

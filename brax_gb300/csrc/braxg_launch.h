@@ -124,6 +124,8 @@ struct VjpArgs {
   float* traj_qd;       // [n_steps, n, nv]
   int* status;          // [n]
   unsigned long long* prof;  // optional per-phase cycle counters
+  int phases;           // 1: the forward (checkpoints, snapshots, trajectory) only; 2: the
+                        // reverse only, from a workspace a phase-1 launch filled; 3: both
 };
 
 // Launches vjp_kernel<T, NVB> (defined in braxg_vjp_kernel.cuh, instantiated

@@ -115,7 +115,8 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   const int res_s0 = first_res * a.ckpt_every;
   float* tape = aw.at(A.tape);
   const int tape_words = a.snap_words - L.total;
-  // ---- forward with checkpoints ----
+  // ---- set-up (every phase: a reverse-only launch recomputes segments from
+  // the checkpoints with the model's parameters) ----
   if (active) {
     if (tm.lane == 0) {  // the solve counter and the checked build's flags
       reinterpret_cast<int*>(w.at(L.misc))[12] = 0;
@@ -133,8 +134,9 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   }
   tm.sync();
   __syncthreads();
-  ok = pos_stage<T, NVB>(mw, w, active) && ok;
-  for (int s = 0; s < a.n_steps; ++s) {
+  // ---- forward with checkpoints ----
+  if (a.phases & 1) ok = pos_stage<T, NVB>(mw, w, active) && ok;
+  for (int s = 0; (a.phases & 1) && s < a.n_steps; ++s) {
     if (active && s % a.ckpt_every == 0) {
       float* c = a.ckpt + ((long long)(s / a.ckpt_every) * n + env) * S;
       copy_vec<T>(tm, c, w.at(L.q), nq);
@@ -159,6 +161,11 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
     if (active && a.traj_qd != nullptr) copy_vec<T>(tm, a.traj_qd + ((long long)s * n + env) * nv, w.at(L.qd), nv);
   }
   pf.mark(BRAXG_PROF_VJP_CHECKPOINT);
+  if (!(a.phases & 2)) {  // forward only: the reverse runs in a later launch on this workspace
+    if (active && a.status != nullptr && tm.lane == 0)
+      a.status[env] = (ok ? 0 : BRAXG_ENV_NOT_SPD) | (w.failed() ? BRAXG_ENV_BOUNDS : 0);
+    return;
+  }
   // ---- backward ----
   float* qbo = aw.at(A.qbo);
   float* qdbo = aw.at(A.qdbo);
@@ -281,9 +288,11 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   if (!active) return;
   if (a.q0_bar != nullptr) copy_vec<T>(tm, a.q0_bar + env * nq, qbo, nq);
   if (a.qd0_bar != nullptr) copy_vec<T>(tm, a.qd0_bar + env * nv, qdbo, nv);
-  if (a.status != nullptr && tm.lane == 0)
-    a.status[env] = (ok ? 0 : BRAXG_ENV_NOT_SPD) | (taped ? 0 : BRAXG_ENV_NO_GRADIENT) |
-                    (w.failed() ? BRAXG_ENV_BOUNDS : 0);
+  if (a.status != nullptr && tm.lane == 0) {
+    const int st = (ok ? 0 : BRAXG_ENV_NOT_SPD) | (taped ? 0 : BRAXG_ENV_NO_GRADIENT) |
+                   (w.failed() ? BRAXG_ENV_BOUNDS : 0);
+    a.status[env] = (a.phases & 1) ? st : (a.status[env] | st);  // reverse only: adds to the forward's
+  }
 }
 
 template <int T, int NVB>

@@ -106,6 +106,30 @@ ffi::Error RolloutVjpImpl(cudaStream_t stream, ffi::ScratchAllocator scratch, in
                                          qb.buf, qdb.buf, st.buf, ws, bytes));
 }
 
+using U8 = ffi::Buffer<ffi::U8>;
+using U8Out = ffi::Result<ffi::Buffer<ffi::U8>>;
+using S32 = ffi::Buffer<ffi::S32>;
+
+ffi::Error RolloutVjpFwdImpl(cudaStream_t stream, int64_t model, int32_t n_frames, int32_t ckpt_every, F32 q0,
+                             F32 qd0, F32 act_seq, F32Out traj_q, F32Out traj_qd, S32Out status, U8Out residual) {
+  View a = in(q0), b = in(qd0), c = in(act_seq);
+  View tq = out(traj_q), tqd = out(traj_qd), st = out(status), rs = out(residual);
+  return to_error(braxg_xla::rollout_vjp_fwd(model_of(model), stream, n_frames, ckpt_every, a.buf, b.buf, c.buf,
+                                             tq.buf, tqd.buf, st.buf, rs.buf));
+}
+
+// `status_in` is the forward's status; jax_ops aliases it with the `status`
+// result (input_output_aliases), so both name one buffer.
+ffi::Error RolloutVjpBwdImpl(cudaStream_t stream, int64_t model, int32_t n_frames, int32_t ckpt_every, F32 q0,
+                             F32 qd0, F32 act_seq, U8 residual, F32 q_bar, F32 qd_bar, S32 status_in,
+                             F32Out act_bar, F32Out q0_bar, F32Out qd0_bar, S32Out status) {
+  (void)status_in;
+  View a = in(q0), b = in(qd0), c = in(act_seq), r = in(residual), d = in(q_bar), e = in(qd_bar);
+  View ab = out(act_bar), qb = out(q0_bar), qdb = out(qd0_bar), st = out(status);
+  return to_error(braxg_xla::rollout_vjp_bwd(model_of(model), stream, n_frames, ckpt_every, a.buf, b.buf, c.buf,
+                                             r.buf, d.buf, e.buf, ab.buf, qb.buf, qdb.buf, st.buf));
+}
+
 }  // namespace
 
 XLA_FFI_DEFINE_HANDLER_SYMBOL(BraxgStepFfi, StepImpl,
@@ -156,6 +180,38 @@ XLA_FFI_DEFINE_HANDLER_SYMBOL(BraxgRolloutVjpFfi, RolloutVjpImpl,
                                   .Arg<F32>()   // act_seq
                                   .Arg<F32>()   // q_bar [T, .., nq]
                                   .Arg<F32>()   // qd_bar [T, .., nv]
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // act_bar [T, .., nu]
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // q0_bar
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // qd0_bar
+                                  .Ret<ffi::Buffer<ffi::S32>>());  // status
+
+XLA_FFI_DEFINE_HANDLER_SYMBOL(BraxgRolloutVjpFwdFfi, RolloutVjpFwdImpl,
+                              ffi::Ffi::Bind()
+                                  .Ctx<ffi::PlatformStream<cudaStream_t>>()
+                                  .Attr<int64_t>("model")
+                                  .Attr<int32_t>("n_frames")
+                                  .Attr<int32_t>("ckpt_every")
+                                  .Arg<F32>()   // q0
+                                  .Arg<F32>()   // qd0
+                                  .Arg<F32>()   // act_seq [T, .., nu]
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // traj_q [T, .., nq]
+                                  .Ret<ffi::Buffer<ffi::F32>>()   // traj_qd [T, .., nv]
+                                  .Ret<ffi::Buffer<ffi::S32>>()   // status
+                                  .Ret<ffi::Buffer<ffi::U8>>());  // residual [bytes]
+
+XLA_FFI_DEFINE_HANDLER_SYMBOL(BraxgRolloutVjpBwdFfi, RolloutVjpBwdImpl,
+                              ffi::Ffi::Bind()
+                                  .Ctx<ffi::PlatformStream<cudaStream_t>>()
+                                  .Attr<int64_t>("model")
+                                  .Attr<int32_t>("n_frames")
+                                  .Attr<int32_t>("ckpt_every")
+                                  .Arg<F32>()   // q0
+                                  .Arg<F32>()   // qd0
+                                  .Arg<F32>()   // act_seq
+                                  .Arg<U8>()    // residual
+                                  .Arg<F32>()   // q_bar [T, .., nq]
+                                  .Arg<F32>()   // qd_bar [T, .., nv]
+                                  .Arg<S32>()   // the forward's status (aliased with the status result)
                                   .Ret<ffi::Buffer<ffi::F32>>()   // act_bar [T, .., nu]
                                   .Ret<ffi::Buffer<ffi::F32>>()   // q0_bar
                                   .Ret<ffi::Buffer<ffi::F32>>()   // qd0_bar

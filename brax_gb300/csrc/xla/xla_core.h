@@ -231,6 +231,96 @@ inline std::string rollout_vjp(const braxg_model* m, void* stream, int n_frames,
   return rc ? last_error("braxg_rollout_vjp", rc) : "";
 }
 
+// Bytes of the residual rollout_vjp_fwd leaves for rollout_vjp_bwd: the
+// gradient workspace with every checkpoint segment resident, so that the
+// reverse only reads it (0 on a shape error).
+inline size_t rollout_vjp_residual_bytes(const braxg_model* m, int n_frames, int ckpt_every, const Buf& q0,
+                                         const Buf& act_seq) {
+  braxg_dims d;
+  if (braxg_model_dims(m, &d)) return 0;
+  const int64_t n = envs_of(q0, {d.nq});
+  if (n < 0 || act_seq.rank < 1) return 0;
+  size_t bytes = 0;
+  if (braxg_rollout_vjp_workspace_resident(m, static_cast<int>(n), static_cast<int>(act_seq.dims[0]), n_frames,
+                                           ckpt_every, 0, &bytes))
+    return 0;
+  return bytes;
+}
+
+// Checks the residual buffer (uint8 [bytes]) against what the sizes need.
+inline std::string expect_residual(const braxg_model* m, int n_frames, int ckpt_every, const Buf& q0,
+                                   const Buf& act_seq, const Buf& residual) {
+  const size_t need = rollout_vjp_residual_bytes(m, n_frames, ckpt_every, q0, act_seq);
+  if (need == 0) return "cannot size the gradient residual for q0 " + dims_str(q0);
+  if (residual.rank != 1 || static_cast<size_t>(residual.dims[0]) < need)
+    return "residual has shape " + dims_str(residual) + ", expected [" + std::to_string(need) + "]";
+  return "";
+}
+
+// jax.custom_vjp forward of the rollout: the trajectory traj_q [T, .., nq],
+// traj_qd [T, .., nv], status [..], and the residual (the forward's
+// checkpoints and frame snapshots) for rollout_vjp_bwd.
+inline std::string rollout_vjp_fwd(const braxg_model* m, void* stream, int n_frames, int ckpt_every, const Buf& q0,
+                                   const Buf& qd0, const Buf& act_seq, const Buf& traj_q, const Buf& traj_qd,
+                                   const Buf& status, const Buf& residual) {
+  braxg_dims d;
+  int rc = braxg_model_dims(m, &d);
+  if (rc) return last_error("braxg_model_dims", rc);
+  int64_t n = -1;
+  BRAXG_XLA_TRY(expect("q0", q0, {d.nq}, n));
+  BRAXG_XLA_TRY(expect("qd0", qd0, {d.nv}, n));
+  BRAXG_XLA_TRY(expect("act_seq", act_seq, {d.nu}, n, 1));
+  BRAXG_XLA_TRY(expect("traj_q", traj_q, {d.nq}, n, 1));
+  BRAXG_XLA_TRY(expect("traj_qd", traj_qd, {d.nv}, n, 1));
+  BRAXG_XLA_TRY(expect("status", status, {}, n));
+  const int64_t T = act_seq.dims[0];
+  if (traj_q.dims[0] != T || traj_qd.dims[0] != T)
+    return "act_seq, traj_q and traj_qd must share their leading (time) dimension";
+  if (n > INT32_MAX || T > INT32_MAX || T < 1) return "the rollout needs 1 .. 2^31-1 steps and envs";
+  BRAXG_XLA_TRY(expect_residual(m, n_frames, ckpt_every, q0, act_seq, residual));
+  braxg_options opt{};
+  opt.inverse_mode = BRAXG_INV_CHOLESKY;
+  rc = braxg_rollout_vjp_fwd(m, stream, static_cast<int>(n), static_cast<int>(T), n_frames, ckpt_every,
+                             d.nu ? act_seq.f() : nullptr, q0.f(), qd0.f(), traj_q.f(), traj_qd.f(), residual.data,
+                             static_cast<size_t>(residual.dims[0]), static_cast<int32_t*>(status.data), &opt);
+  return rc ? last_error("braxg_rollout_vjp_fwd", rc) : "";
+}
+
+// jax.custom_vjp backward from that residual (only read: every segment is
+// resident): cotangents q_bar [T, .., nq], qd_bar [T, .., nv] give act_bar
+// [T, .., nu], q0_bar, qd0_bar.  `status` holds the forward's status (the
+// handler aliases it) and gets the reverse's bits ORed in.
+inline std::string rollout_vjp_bwd(const braxg_model* m, void* stream, int n_frames, int ckpt_every, const Buf& q0,
+                                   const Buf& qd0, const Buf& act_seq, const Buf& residual, const Buf& q_bar,
+                                   const Buf& qd_bar, const Buf& act_bar, const Buf& q0_bar, const Buf& qd0_bar,
+                                   const Buf& status) {
+  braxg_dims d;
+  int rc = braxg_model_dims(m, &d);
+  if (rc) return last_error("braxg_model_dims", rc);
+  int64_t n = -1;
+  BRAXG_XLA_TRY(expect("q0", q0, {d.nq}, n));
+  BRAXG_XLA_TRY(expect("qd0", qd0, {d.nv}, n));
+  BRAXG_XLA_TRY(expect("act_seq", act_seq, {d.nu}, n, 1));
+  BRAXG_XLA_TRY(expect("q_bar", q_bar, {d.nq}, n, 1));
+  BRAXG_XLA_TRY(expect("qd_bar", qd_bar, {d.nv}, n, 1));
+  BRAXG_XLA_TRY(expect("act_bar", act_bar, {d.nu}, n, 1));
+  BRAXG_XLA_TRY(expect("q0_bar", q0_bar, {d.nq}, n));
+  BRAXG_XLA_TRY(expect("qd0_bar", qd0_bar, {d.nv}, n));
+  BRAXG_XLA_TRY(expect("status", status, {}, n));
+  const int64_t T = act_seq.dims[0];
+  if (q_bar.dims[0] != T || qd_bar.dims[0] != T || act_bar.dims[0] != T)
+    return "act_seq, q_bar, qd_bar and act_bar must share their leading (time) dimension";
+  if (n > INT32_MAX || T > INT32_MAX || T < 1) return "the rollout needs 1 .. 2^31-1 steps and envs";
+  BRAXG_XLA_TRY(expect_residual(m, n_frames, ckpt_every, q0, act_seq, residual));
+  braxg_options opt{};
+  opt.inverse_mode = BRAXG_INV_CHOLESKY;
+  rc = braxg_rollout_vjp_bwd(m, stream, static_cast<int>(n), static_cast<int>(T), n_frames, ckpt_every,
+                             d.nu ? act_seq.f() : nullptr, q0.f(), qd0.f(), q_bar.f(), qd_bar.f(),
+                             d.nu ? act_bar.f() : nullptr, q0_bar.f(), qd0_bar.f(), residual.data,
+                             static_cast<size_t>(residual.dims[0]), static_cast<int32_t*>(status.data), &opt);
+  return rc ? last_error("braxg_rollout_vjp_bwd", rc) : "";
+}
+
 #undef BRAXG_XLA_TRY
 
 }  // namespace braxg_xla

@@ -13,9 +13,12 @@ Here:
 * ``rollout(sys, q0, qd0, act_seq, n_frames, ckpt_every)`` returns the
   trajectory ``(traj_q [T, n, nq], traj_qd [T, n, nv])`` of ``act_seq
   [T, n, nu]`` from the state of ``pipeline.init(q0, qd0)`` and is a
-  ``jax.custom_vjp``: its backward is the hand-written checkpointed adjoint
-  (``braxg_rollout_vjp``), which the APG training step can call through
-  ``jax.grad`` unchanged.
+  ``jax.custom_vjp``: its forward under differentiation is the gradient
+  kernel's forward half (``braxg_rollout_vjp_fwd``), whose checkpoints and
+  frame snapshots are the residual, and its backward the reverse half
+  (``braxg_rollout_vjp_bwd``), which the APG training step can call through
+  ``jax.grad`` unchanged; ``rollout_grad`` is the fused launch
+  (``braxg_rollout_vjp``) for callers that hold the cotangents up front.
 
 The handlers live in ``libbraxg_xla.so`` (brax_gb300/csrc/xla/braxg_xla.cc),
 which ``brax_gb300.build.build_xla`` compiles only where jaxlib's FFI headers
@@ -45,7 +48,8 @@ from brax_gb300 import model_pack
 
 XLA_LIB = os.path.join(N.LIB_DIR, 'libbraxg_xla.so')
 TARGETS = {'braxg_step': 'BraxgStepFfi', 'braxg_rollout': 'BraxgRolloutFfi',
-           'braxg_rollout_vjp': 'BraxgRolloutVjpFfi'}
+           'braxg_rollout_vjp': 'BraxgRolloutVjpFfi', 'braxg_rollout_vjp_fwd': 'BraxgRolloutVjpFwdFfi',
+           'braxg_rollout_vjp_bwd': 'BraxgRolloutVjpBwdFfi'}
 
 AVAILABLE = jax is not None and os.path.exists(XLA_LIB)
 
@@ -83,7 +87,7 @@ def _require():
 
 
 def register():
-  """Registers the three custom-call targets for the CUDA platform (once)."""
+  """Registers the custom-call targets for the CUDA platform (once)."""
   global _registered
   _require()
   with _lock:
@@ -157,6 +161,41 @@ def _vjp_call(handle, nq, nv, nu, n_frames, ckpt_every, q0, qd0, act_seq, q_bar,
               ckpt_every=np.int32(ckpt_every))
 
 
+def _residual_bytes(handle, n_env, n_steps, n_frames, ckpt_every) -> int:
+  """Bytes of the gradient workspace with every segment resident (the
+  residual of the split forward)."""
+  nbytes = ctypes.c_size_t()
+  N.check(N.lib().braxg_rollout_vjp_workspace_resident(ctypes.c_void_p(handle), int(n_env), int(n_steps),
+                                                       int(n_frames), int(ckpt_every), 0, ctypes.byref(nbytes)),
+          'braxg_rollout_vjp_workspace_resident')
+  return int(nbytes.value)
+
+
+def _vjp_fwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq):
+  T, batch = act_seq.shape[0], q0.shape[:-1]
+  n = int(np.prod(batch)) if batch else 1
+  out_types = (jax.ShapeDtypeStruct((T,) + batch + (nq,), jnp.float32),
+               jax.ShapeDtypeStruct((T,) + batch + (nv,), jnp.float32),
+               jax.ShapeDtypeStruct(batch, jnp.int32),
+               jax.ShapeDtypeStruct((_residual_bytes(handle, n, T, n_frames, ckpt_every),), jnp.uint8))
+  call = jax.ffi.ffi_call('braxg_rollout_vjp_fwd', out_types, vmap_method='sequential')
+  return call(q0, qd0, act_seq, model=np.int64(handle), n_frames=np.int32(n_frames),
+              ckpt_every=np.int32(ckpt_every))
+
+
+def _vjp_bwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq, residual, status, q_bar, qd_bar):
+  batch = q0.shape[:-1]
+  out_types = (jax.ShapeDtypeStruct(act_seq.shape, jnp.float32),
+               jax.ShapeDtypeStruct(batch + (nq,), jnp.float32),
+               jax.ShapeDtypeStruct(batch + (nv,), jnp.float32),
+               jax.ShapeDtypeStruct(batch, jnp.int32))
+  # the forward's status (argument 6) is the status result: the reverse ORs its bits in
+  call = jax.ffi.ffi_call('braxg_rollout_vjp_bwd', out_types, vmap_method='sequential',
+                          input_output_aliases={6: 3})
+  return call(q0, qd0, act_seq, residual, q_bar, qd_bar, status, model=np.int64(handle),
+              n_frames=np.int32(n_frames), ckpt_every=np.int32(ckpt_every))
+
+
 @functools.lru_cache(maxsize=None)
 def _rollout_fn(handle: int, nq: int, nv: int, nu: int, n_frames: int, ckpt_every: int):
   """jax.custom_vjp rollout for one model and static configuration."""
@@ -167,17 +206,29 @@ def _rollout_fn(handle: int, nq: int, nv: int, nu: int, n_frames: int, ckpt_ever
     return tq, tqd
 
   def fwd(q0, qd0, act_seq):
-    return roll(q0, qd0, act_seq), (q0, qd0, act_seq)
+    tq, tqd, status, residual = _vjp_fwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq)
+    return (tq, tqd), (q0, qd0, act_seq, residual, status)
 
   def bwd(res, g):
-    q0, qd0, act_seq = res
+    q0, qd0, act_seq, residual, status = res
     gq, gqd = g
-    act_bar, q0_bar, qd0_bar, _ = _vjp_call(handle, nq, nv, nu, n_frames, ckpt_every, q0, qd0, act_seq,
-                                             jnp.asarray(gq, jnp.float32), jnp.asarray(gqd, jnp.float32))
+    act_bar, q0_bar, qd0_bar, _ = _vjp_bwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq, residual,
+                                                status, jnp.asarray(gq, jnp.float32), jnp.asarray(gqd, jnp.float32))
     return q0_bar, qd0_bar, act_bar
 
   roll.defvjp(fwd, bwd)
   return roll
+
+
+def rollout_grad(sys, q0, qd0, act_seq, q_bar, qd_bar, n_frames: int = 1, ckpt_every: int = 16,
+                 device_id: int = 0):
+  """(act_bar, q0_bar, qd0_bar, status) of the rollout for cotangents q_bar
+  [T, n, nq], qd_bar [T, n, nv] in one fused launch (braxg_rollout_vjp)."""
+  register()
+  nl, nq, nv, nu = _dims(sys)
+  return _vjp_call(model_handle(sys, device_id), nq, nv, nu, int(n_frames), int(ckpt_every),
+                   jnp.asarray(q0, jnp.float32), jnp.asarray(qd0, jnp.float32), jnp.asarray(act_seq, jnp.float32),
+                   jnp.asarray(q_bar, jnp.float32), jnp.asarray(qd_bar, jnp.float32))
 
 
 def rollout(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16, device_id: int = 0):

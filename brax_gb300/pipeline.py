@@ -484,12 +484,28 @@ def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int =
   if trajectory:
     tq, tqd = f(n_steps, n, m.nq), f(n_steps, n, m.nv)
   status = torch.zeros(n, dtype=torch.int32, device=dev)
-  nbytes = ctypes.c_size_t()
   lib = N.lib()
+  ws, nbytes = _vjp_workspace(m, n, n_steps, n_frames, ckpt_every, resident_segments)
+  stream = torch.cuda.current_stream(dev).cuda_stream
+  N.check(lib.braxg_rollout_vjp(
+      m.handle, ctypes.c_void_p(stream), n, n_steps, int(n_frames), int(ckpt_every),
+      act_seq.data_ptr() if m.nu else None, q0.data_ptr(), qd0.data_ptr(), _ptr(qb), _ptr(qdb),
+      act_bar.data_ptr() if m.nu else None, q0_bar.data_ptr(), qd0_bar.data_ptr(), _ptr(tq),
+      _ptr(tqd), ws.data_ptr(), nbytes, status.data_ptr(),
+      ctypes.byref(_opts(CHOLESKY, 0, 0, profile))), 'braxg_rollout_vjp')
+  return act_bar, q0_bar, qd0_bar, status, (tq, tqd)
+
+
+def _vjp_workspace(m: 'Model', n: int, n_steps: int, n_frames: int, ckpt_every: int,
+                   resident_segments: Optional[int]):
+  """(workspace tensor, bytes) of a gradient launch; resident_segments None
+  keeps as many checkpoint segments resident as fit a quarter of the free
+  device memory."""
+  lib = N.lib()
+  nbytes = ctypes.c_size_t()
   n_ckpt = (n_steps + int(ckpt_every) - 1) // int(ckpt_every)
   if resident_segments is None:
-    # as many segments resident as fit a quarter of the free device memory
-    free = torch.cuda.mem_get_info(dev)[0]
+    free = torch.cuda.mem_get_info(m.device)[0]
     resident_segments = 1
     for r in range(n_ckpt, 0, -1):
       N.check(lib.braxg_rollout_vjp_workspace_resident(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
@@ -500,40 +516,95 @@ def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int =
   N.check(lib.braxg_rollout_vjp_workspace_resident(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
                                                    int(resident_segments), ctypes.byref(nbytes)),
           'braxg_rollout_vjp_workspace_resident')
-  ws = torch.empty(max(nbytes.value, 4), dtype=torch.uint8, device=dev)
-  stream = torch.cuda.current_stream(dev).cuda_stream
-  N.check(lib.braxg_rollout_vjp(
+  return torch.empty(max(nbytes.value, 4), dtype=torch.uint8, device=m.device), nbytes.value
+
+
+@dataclasses.dataclass
+class VjpTape:
+  """What rollout_vjp_fwd leaves for rollout_vjp_bwd: the inputs, the sizes
+  and the workspace holding the forward's checkpoints and frame snapshots
+  (the residuals of a jax.custom_vjp forward)."""
+  model: 'Model'
+  q0: torch.Tensor
+  qd0: torch.Tensor
+  act_seq: torch.Tensor
+  n_frames: int
+  ckpt_every: int
+  workspace: torch.Tensor
+  nbytes: int
+  status: torch.Tensor
+
+
+def rollout_vjp_fwd(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16,
+                    resident_segments: Optional[int] = None):
+  """The forward half of rollout_grad (braxg_rollout_vjp_fwd): the rollout's
+  trajectory (traj_q [n_steps, n, nq], traj_qd [n_steps, n, nv]) and a
+  VjpTape for rollout_vjp_bwd.  The two halves give bitwise the result of
+  one rollout_grad call, and the reverse does not re-run the forward."""
+  m = model_for(sys, q0.device)
+  q0 = _as_batch(q0, m.nq, 'q0', m.device)
+  qd0 = _as_batch(qd0, m.nv, 'qd0', m.device)
+  n = q0.shape[0]
+  act_seq = act_seq.to(torch.float32).contiguous()
+  if act_seq.dim() != 3 or act_seq.shape[1] != n or act_seq.shape[2] != m.nu:
+    raise ValueError(f'act_seq must be (n_steps, {n}, {m.nu})')
+  n_steps = act_seq.shape[0]
+  ws, nbytes = _vjp_workspace(m, n, n_steps, n_frames, ckpt_every, resident_segments)
+  tq = torch.empty(n_steps, n, m.nq, dtype=torch.float32, device=m.device)
+  tqd = torch.empty(n_steps, n, m.nv, dtype=torch.float32, device=m.device)
+  status = torch.zeros(n, dtype=torch.int32, device=m.device)
+  stream = torch.cuda.current_stream(m.device).cuda_stream
+  N.check(N.lib().braxg_rollout_vjp_fwd(
       m.handle, ctypes.c_void_p(stream), n, n_steps, int(n_frames), int(ckpt_every),
-      act_seq.data_ptr() if m.nu else None, q0.data_ptr(), qd0.data_ptr(), _ptr(qb), _ptr(qdb),
-      act_bar.data_ptr() if m.nu else None, q0_bar.data_ptr(), qd0_bar.data_ptr(), _ptr(tq),
-      _ptr(tqd), ws.data_ptr(), nbytes.value, status.data_ptr(),
-      ctypes.byref(_opts(CHOLESKY, 0, 0, profile))), 'braxg_rollout_vjp')
-  return act_bar, q0_bar, qd0_bar, status, (tq, tqd)
+      act_seq.data_ptr() if m.nu else None, q0.data_ptr(), qd0.data_ptr(), tq.data_ptr(), tqd.data_ptr(),
+      ws.data_ptr(), nbytes, status.data_ptr(), ctypes.byref(_opts(CHOLESKY, 0, 0))), 'braxg_rollout_vjp_fwd')
+  return (tq, tqd), VjpTape(m, q0, qd0, act_seq, int(n_frames), int(ckpt_every), ws, nbytes, status)
+
+
+def rollout_vjp_bwd(tape: VjpTape, q_bar=None, qd_bar=None):
+  """The reverse half (braxg_rollout_vjp_bwd) on a VjpTape: q_bar / qd_bar
+  [n_steps, n, nq|nv] (None = zero) -> (act_bar, q0_bar, qd0_bar, status)."""
+  m, n, n_steps = tape.model, tape.q0.shape[0], tape.act_seq.shape[0]
+  f = lambda *sh: torch.zeros(*sh, dtype=torch.float32, device=m.device)
+  qb = None if q_bar is None else q_bar.to(torch.float32).contiguous()
+  qdb = None if qd_bar is None else qd_bar.to(torch.float32).contiguous()
+  act_bar, q0_bar, qd0_bar = f(n_steps, n, m.nu), f(n, m.nq), f(n, m.nv)
+  stream = torch.cuda.current_stream(m.device).cuda_stream
+  N.check(N.lib().braxg_rollout_vjp_bwd(
+      m.handle, ctypes.c_void_p(stream), n, n_steps, tape.n_frames, tape.ckpt_every,
+      tape.act_seq.data_ptr() if m.nu else None, tape.q0.data_ptr(), tape.qd0.data_ptr(), _ptr(qb), _ptr(qdb),
+      act_bar.data_ptr() if m.nu else None, q0_bar.data_ptr(), qd0_bar.data_ptr(), tape.workspace.data_ptr(),
+      tape.nbytes, tape.status.data_ptr(), ctypes.byref(_opts(CHOLESKY, 0, 0))), 'braxg_rollout_vjp_bwd')
+  return act_bar, q0_bar, qd0_bar, tape.status
 
 
 class Rollout(torch.autograd.Function):
   """Differentiable rollout for torch: (q0, qd0, act_seq) -> (traj_q, traj_qd).
 
-  The forward runs braxg_rollout (exact-inverse mode); the backward runs the
-  checkpointed hand-written adjoint (braxg_rollout_vjp).
+  The forward runs braxg_rollout_vjp_fwd (exact-inverse mode; the
+  checkpoints and frame snapshots stay in a workspace held by the graph); the
+  backward runs the hand-written reverse on it (braxg_rollout_vjp_bwd).
   """
 
   @staticmethod
   def forward(ctx, q0, qd0, act_seq, sys, n_frames, ckpt_every):
-    _, (tq, tqd) = rollout(sys, bare_state(q0.detach(), qd0.detach()), act_seq.detach(), n_frames=n_frames,
-                           inverse_mode=CHOLESKY, trajectory=True)
-    ctx.save_for_backward(q0, qd0, act_seq)
-    ctx.sys, ctx.n_frames, ctx.ckpt_every = sys, n_frames, ckpt_every
+    (tq, tqd), ctx.tape = rollout_vjp_fwd(sys, q0.detach(), qd0.detach(), act_seq.detach(), n_frames=n_frames,
+                                          ckpt_every=ckpt_every)
     return tq, tqd
 
   @staticmethod
   def backward(ctx, gq, gqd):
-    q0, qd0, act_seq = ctx.saved_tensors
-    act_bar, q0_bar, qd0_bar, _, _ = rollout_grad(
-        ctx.sys, q0, qd0, act_seq, gq, gqd, n_frames=ctx.n_frames, ckpt_every=ctx.ckpt_every)
+    act_bar, q0_bar, qd0_bar, _ = rollout_vjp_bwd(ctx.tape, gq, gqd)
     return q0_bar, qd0_bar, act_bar, None, None, None
 
 
 def differentiable_rollout(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16):
-  """torch.autograd-enabled rollout returning (traj_q, traj_qd)."""
-  return Rollout.apply(q0, qd0, act_seq, sys, n_frames, ckpt_every)
+  """torch.autograd-enabled rollout returning (traj_q, traj_qd).  With a
+  gradient to take, the forward is braxg_rollout_vjp_fwd (its checkpoints and
+  frame snapshots kept for the backward, which runs only the reverse);
+  without one, a plain braxg_rollout."""
+  if torch.is_grad_enabled() and any(t.requires_grad for t in (q0, qd0, act_seq)):
+    return Rollout.apply(q0, qd0, act_seq, sys, n_frames, ckpt_every)
+  _, (tq, tqd) = rollout(sys, bare_state(q0, qd0), act_seq, n_frames=n_frames, inverse_mode=CHOLESKY,
+                         trajectory=True)
+  return tq, tqd

@@ -292,6 +292,30 @@ int braxg_rollout_vjp(const braxg_model* model, void* stream, int n_env, int n_s
                       float* qd0_bar, float* traj_q, float* traj_qd, void* workspace,
                       size_t workspace_bytes, int32_t* status, const braxg_options* opt);
 
+/* braxg_rollout_vjp split in two launches, for a custom_vjp whose forward
+ * output is needed before the cotangents exist (jax.custom_vjp fwd / bwd of
+ * the scan, a torch.autograd.Function's forward / backward, the closed loop
+ * of brax/training/agents/apg/train.py:179-236 where each env step's
+ * cotangent comes back through the policy).  braxg_rollout_vjp_fwd runs the
+ * forward: traj_q / traj_qd [n_steps, n, nq|nv] (required) and the
+ * checkpoints and frame snapshots in the workspace (sized as for
+ * braxg_rollout_vjp; segments the workspace cannot keep resident are
+ * recomputed by the reverse); status gets the forward's bits.
+ * braxg_rollout_vjp_bwd then runs only the reverse and must get the same
+ * model, sizes, act_seq, q0, qd0 and the workspace (pointer and size) of the
+ * forward call, untouched since; it ORs its bits into status.  Together they
+ * give bitwise the gradient and trajectory of one braxg_rollout_vjp call, and
+ * the reverse does not recompute the resident segments' forward. */
+int braxg_rollout_vjp_fwd(const braxg_model* model, void* stream, int n_env, int n_steps, int n_frames,
+                          int ckpt_every, const float* act_seq, const float* q0, const float* qd0,
+                          float* traj_q, float* traj_qd, void* workspace, size_t workspace_bytes,
+                          int32_t* status, const braxg_options* opt);
+int braxg_rollout_vjp_bwd(const braxg_model* model, void* stream, int n_env, int n_steps, int n_frames,
+                          int ckpt_every, const float* act_seq, const float* q0, const float* qd0,
+                          const float* q_bar, const float* qd_bar, float* act_bar, float* q0_bar,
+                          float* qd0_bar, void* workspace, size_t workspace_bytes, int32_t* status,
+                          const braxg_options* opt);
+
 /* braxg_rollout_vjp without a workspace argument, for callers that cannot
  * allocate device memory: an XLA custom call registered without access to the
  * scratch allocator, a plugin whose host framework owns every device

@@ -150,6 +150,39 @@ def test_gradient_independent_of_resident_segments():
       torch.testing.assert_close(a, b, rtol=0, atol=0)
 
 
+@pytest.mark.parametrize('resident', [1, None])
+def test_split_forward_and_reverse_equal_the_fused_launch(resident):
+  """braxg_rollout_vjp_fwd then braxg_rollout_vjp_bwd on its workspace give
+  bitwise the trajectory and gradient of one braxg_rollout_vjp launch, with
+  every segment resident and with the smallest workspace (the reverse then
+  recomputes the non-resident segments from the forward's checkpoints)."""
+  P = _P()
+  sys_ = load('quadruped')
+  n, H, k = 24, 8, 2
+  q0, qd0 = seeded_inputs(sys_, n, 35)
+  rng = np.random.default_rng(36)
+  u = _t(rng.uniform(-1, 1, (H, n, sys_.act_size())))
+  qb = _t(rng.normal(size=(H, n, sys_.q_size())))
+  qdb = _t(rng.normal(size=(H, n, sys_.qd_size())))
+  fused = P.rollout_grad(sys_, _t(q0), _t(qd0), u, qb, qdb, n_frames=5, ckpt_every=k, trajectory=True,
+                         resident_segments=resident)
+  (tq, tqd), tape = P.rollout_vjp_fwd(sys_, _t(q0), _t(qd0), u, n_frames=5, ckpt_every=k,
+                                      resident_segments=resident)
+  act_bar, q0_bar, qd0_bar, status = P.rollout_vjp_bwd(tape, qb, qdb)
+  torch.cuda.synchronize()
+  assert (status == 0).all()
+  for a, b in ((act_bar, fused[0]), (q0_bar, fused[1]), (qd0_bar, fused[2]), (status, fused[3]),
+               (tq, fused[4][0]), (tqd, fused[4][1])):
+    torch.testing.assert_close(a, b, rtol=0, atol=0)
+  # the torch Function on the split halves: the same gradient as the fused launch
+  u2 = u.clone().requires_grad_(True)
+  qd2 = _t(qd0).requires_grad_(True)
+  tq2, tqd2 = P.differentiable_rollout(sys_, _t(q0), qd2, u2, n_frames=5, ckpt_every=k)
+  ((tq2 * qb).sum() + (tqd2 * qdb).sum()).backward()
+  torch.testing.assert_close(u2.grad, fused[0], rtol=0, atol=0)
+  torch.testing.assert_close(qd2.grad, fused[2], rtol=0, atol=0)
+
+
 def _lying_quadrupeds(sys_, n, seed):
   """Quadrupeds pressed into the ground (torso 0.05-0.1 m high, legs as at
   init): most envs have more than 32 active constraint rows, so every frame's

@@ -104,6 +104,52 @@ int braxg_rollout_vjp(const braxg_model*, void*, int n_env, int n_steps, int n_f
   g_calls.push_back(c);
   return 0;
 }
+int braxg_rollout_vjp_workspace_resident(const braxg_model*, int, int, int, int, int resident, size_t* bytes) {
+  *bytes = resident <= 0 ? 2 * g_ws_bytes : g_ws_bytes;  // every segment resident: the larger workspace
+  return 0;
+}
+int braxg_rollout_vjp_fwd(const braxg_model*, void*, int n_env, int n_steps, int n_frames, int ckpt_every,
+                          const float* act_seq, const float* q0, const float*, float* traj_q, float* traj_qd,
+                          void* workspace, size_t workspace_bytes, int32_t* status, const braxg_options* opt) {
+  Call c;
+  c.name = "vjp_fwd";
+  c.n_env = n_env;
+  c.n_steps = n_steps;
+  c.n_frames = n_frames;
+  c.ckpt = ckpt_every;
+  c.inverse_mode = opt->inverse_mode;
+  c.p[0] = act_seq;
+  c.p[1] = q0;
+  c.p[2] = traj_q;
+  c.p[3] = traj_qd;
+  c.p[4] = status;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  g_calls.push_back(c);
+  return 0;
+}
+int braxg_rollout_vjp_bwd(const braxg_model*, void*, int n_env, int n_steps, int n_frames, int ckpt_every,
+                          const float* act_seq, const float* q0, const float*, const float* q_bar, const float*,
+                          float* act_bar, float* q0_bar, float*, void* workspace, size_t workspace_bytes,
+                          int32_t* status, const braxg_options* opt) {
+  Call c;
+  c.name = "vjp_bwd";
+  c.n_env = n_env;
+  c.n_steps = n_steps;
+  c.n_frames = n_frames;
+  c.ckpt = ckpt_every;
+  c.inverse_mode = opt->inverse_mode;
+  c.p[0] = act_seq;
+  c.p[1] = q0;
+  c.p[2] = q_bar;
+  c.p[3] = act_bar;
+  c.p[4] = q0_bar;
+  c.p[5] = status;
+  c.ws = workspace;
+  c.ws_bytes = workspace_bytes;
+  g_calls.push_back(c);
+  return 0;
+}
 int braxg_rollout_vjp_noalloc(const braxg_model*, void*, int n_env, int n_steps, int, int, const float*,
                               const float*, const float*, const float*, const float*, float*, float*, float*, float*,
                               float*, int32_t*, const braxg_options*) {
@@ -248,6 +294,51 @@ int main() {
     e = braxg_xla::rollout_vjp(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), qb.buf(), qdb_bad.buf(), ab.buf(),
                                q0b.buf(), qd0b.buf(), st.buf(), ws.data(), bytes);
     CHECK(contains(e, "qd_bar has shape"));
+  }
+  // ---- rollout_vjp_fwd / rollout_vjp_bwd: the custom_vjp halves and their residual ----
+  {
+    const int n = 4, T = 6;
+    Arr q0({n, nq}), qd0({n, nv}), a({T, n, nu}), tq({T, n, nq}), tqd({T, n, nv}), st({n}), qb({T, n, nq}),
+        qdb({T, n, nv}), ab({T, n, nu}), q0b({n, nq}), qd0b({n, nv});
+    g_ws_bytes = 1000;
+    const size_t need = braxg_xla::rollout_vjp_residual_bytes(&m, 5, 2, q0.buf(), a.buf());
+    CHECK(need == 2000);  // the workspace with every segment resident
+    std::vector<int64_t> rdims = {static_cast<int64_t>(need)};
+    std::vector<unsigned char> res(need);
+    braxg_xla::Buf rbuf{res.data(), rdims.data(), 1};
+    g_calls.clear();
+    std::string e = braxg_xla::rollout_vjp_fwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), tq.buf(), tqd.buf(),
+                                               st.buf(), rbuf);
+    CHECK(e.empty() && g_calls.size() == 1 && g_calls[0].name == "vjp_fwd");
+    const Call& f = g_calls[0];
+    CHECK(f.n_env == n && f.n_steps == T && f.n_frames == 5 && f.ckpt == 2 && f.inverse_mode == BRAXG_INV_CHOLESKY);
+    CHECK(f.p[0] == a.data.data() && f.p[1] == q0.data.data() && f.p[2] == tq.data.data());
+    CHECK(f.p[3] == tqd.data.data() && f.p[4] == st.data.data());
+    CHECK(f.ws == res.data() && f.ws_bytes == need);
+    g_calls.clear();
+    e = braxg_xla::rollout_vjp_bwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), rbuf, qb.buf(), qdb.buf(),
+                                   ab.buf(), q0b.buf(), qd0b.buf(), st.buf());
+    CHECK(e.empty() && g_calls.size() == 1 && g_calls[0].name == "vjp_bwd");
+    const Call& b = g_calls[0];
+    CHECK(b.n_env == n && b.n_steps == T && b.ckpt == 2 && b.inverse_mode == BRAXG_INV_CHOLESKY);
+    CHECK(b.p[0] == a.data.data() && b.p[1] == q0.data.data() && b.p[2] == qb.data.data());
+    CHECK(b.p[3] == ab.data.data() && b.p[4] == q0b.data.data() && b.p[5] == st.data.data());
+    CHECK(b.ws == res.data() && b.ws_bytes == need);
+    // a residual smaller than the resident workspace is refused before any call
+    std::vector<int64_t> small = {static_cast<int64_t>(need - 1)};
+    braxg_xla::Buf rsmall{res.data(), small.data(), 1};
+    g_calls.clear();
+    e = braxg_xla::rollout_vjp_fwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), tq.buf(), tqd.buf(), st.buf(),
+                                   rsmall);
+    CHECK(contains(e, "residual has shape") && g_calls.empty());
+    e = braxg_xla::rollout_vjp_bwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), rsmall, qb.buf(), qdb.buf(),
+                                   ab.buf(), q0b.buf(), qd0b.buf(), st.buf());
+    CHECK(contains(e, "residual has shape") && g_calls.empty());
+    // the trajectory's time axis must match the actions'
+    Arr tq_bad({T - 1, n, nq});
+    e = braxg_xla::rollout_vjp_fwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), tq_bad.buf(), tqd.buf(),
+                                   st.buf(), rbuf);
+    CHECK(contains(e, "leading (time) dimension") && g_calls.empty());
   }
   std::printf("ok %d\n", g_checks);
   return 0;
