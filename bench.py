@@ -550,9 +550,14 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
                               resident_segments=resident)
     status[0] = r[3]
 
+  def split():  # the custom_vjp shape: forward half, then the reverse half on its residual
+    _, tape = pipeline.rollout_vjp_fwd(sys_, q0, qd0, u, n_frames=N_FRAMES, ckpt_every=ckpt)
+    pipeline.rollout_vjp_bwd(tape, None, qd_bar)
+
   t_f = timed(fwd)
   t_b = timed(fwd_adj)  # every segment's snapshots resident (they fit): no recompute
   t_m = timed(lambda: fwd_adj(1))  # smallest workspace: all but the last segment recomputed
+  t_s = timed(split)
   bad = int((status[0] != 0).sum().item())
   return {'workload': f'quadruped, {n} envs, {horizon} env steps x {N_FRAMES} frames, checkpoint every {ckpt}',
           'fwd_env_steps_per_s': round(n * horizon / t_f, 1),
@@ -561,6 +566,7 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
           'cost_ratio_fwd_adj_over_fwd': round(t_b / t_f, 3),
           'fwd_adj_ms_smallest_workspace': round(1e3 * t_m, 3),
           'cost_ratio_smallest_workspace': round(t_m / t_f, 3),
+          'split_fwd_then_bwd_ms': round(1e3 * t_s, 3), 'cost_ratio_split': round(t_s / t_f, 3),
           'envs_without_gradient': bad, 'gpu_launches_fwd_adj': 1}
 
 

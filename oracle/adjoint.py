@@ -281,10 +281,10 @@ class StepAdjoint:
       b = np.einsum('bij,bj->bi', jm, qfs) - aref
       xs, pg = self._pg_tape(a, b)
       qfc = np.einsum('bij,bi->bj', jac, xs)
-      T.update(a=a, b=b, xs=xs, pg=pg, pg_gap=self.last_gap)
+      T.update(a=a, b=b, xs=xs, pg=pg, pg_gap=self.last_gap, proj_gap=self.last_proj_gap)
     else:
       qfc = np.zeros_like(qfs)
-      T.update(pg_gap=np.full(B, np.inf))
+      T.update(pg_gap=np.full(B, np.inf), proj_gap=np.full(B, np.inf))
     s = s.replace(qf_constraint=qfc)
     s2 = o.integrate(s)
     T.update(qfs=qfs, qfc=qfc, s_int=s2)
@@ -341,6 +341,9 @@ class StepAdjoint:
     # the closest call of any decision of the solve, relative to the compared
     # values' size: below ~1e-6 the same decision in FP32 is a tie
     gap = np.full(B, np.inf)
+    # the closest call of the projection: a component of y - step grad that
+    # cancels to within this fraction of its terms is a tie of its sign
+    pgap = np.full(B, np.inf)
     for it in range(sys.solver_iterations):
       if force is not None:
         if it >= force[0]:
@@ -378,6 +381,9 @@ class StepAdjoint:
       gx = mvt(mv(nx) + b)
       e = np.sqrt(np.sum((relu(nx - gx) - nx) ** 2, -1))
       z = y - cur[:, None] * gy
+      zs = np.abs(y) + cur[:, None] * np.abs(gy)
+      pz = np.where(zs > 0, np.abs(z) / np.maximum(zs, 1e-300), np.inf).min(-1) if m else np.full(B, np.inf)
+      pgap = np.where(active, np.minimum(pgap, pz), pgap)
       tape.append(dict(active=active.copy(), y=y.copy(), ry=ry, step=cur.copy(), beta=beta,
                        zpos=(z > 0)))
       gap = np.where(active, np.minimum(gap, np.abs(e - 1e-3) / 1e-3), gap)
@@ -388,6 +394,7 @@ class StepAdjoint:
       ss = np.where(active, nss, ss)
       err = np.where(active, e, err)
     self.last_gap = gap
+    self.last_proj_gap = pgap
     return x, tape
 
   # -------------------------------------------------------------- reverse

@@ -223,7 +223,7 @@ class Oracle:
   DECISION_ULPS = 8
 
   # evaluation orders of the dense products (see __init__)
-  ORDERS = ('reference', 'right', 'rounded')
+  ORDERS = ('reference', 'right', 'rounded', 'fma')
 
   def __init__(self, sys: S.System, dtype=np.float64, exact_inverse: bool = False, perturb_seed=None,
                perturb_bias: int = 0, order: str = 'reference'):
@@ -233,9 +233,12 @@ class Oracle:
 
     perturb_seed (for the parity tests' rounding envelope): when set, every
     step moves the intermediates whose rounding depends on the summation
-    order (qf_smooth, the mass matrix, mass_mx_inv and the Newton-Schulz
-    iterates, and the projected-gradient problem's A and b; the symmetric ones
-    symmetrically) by -1, 0 or +1 ulp at random, and every discrete decision
+    order (the link poses and velocities of forward kinematics, the
+    constraint rows' Jacobian, diagonal and reference acceleration,
+    qf_smooth, the mass matrix, mass_mx_inv and the Newton-Schulz iterates,
+    and the projected-gradient problem's A and b; the symmetric ones
+    symmetrically)
+    by -1, 0 or +1 ulp at random, and every discrete decision
     taken on two computed values (the line search's sufficient-decrease test,
     the solver's stopping test, the Newton-Schulz acceptance and reset tests,
     the capsule-capsule closest-point choice) sees its two sides shifted by
@@ -253,9 +256,12 @@ class Oracle:
     'reference' associates them as the reference's code does ((J Minv) J^T)
     in numpy's summation order; 'right' associates them the other way
     (J (Minv J^T)); 'rounded' evaluates each in float64 and rounds once (the
-    correctly rounded FP32 result).  Each is an exact evaluation of the same
-    formula; on ill-conditioned models (long hanging chains: mass matrices
-    of condition 1e4) they differ by far more than one ulp of the result."""
+    correctly rounded FP32 result); 'fma' sums every dot product as two
+    interleaved chains of fused multiply-adds (even and odd terms, added at
+    the end), as vectorised hardware commonly does.  Each is an exact
+    evaluation of the same formula; on ill-conditioned models (long hanging
+    chains: mass matrices of condition 1e4) they differ by far more than one
+    ulp of the result."""
     if order not in self.ORDERS:
       raise ValueError(f'order must be one of {self.ORDERS}')
     self.order = order if np.dtype(dtype) == np.float32 else 'reference'
@@ -306,16 +312,33 @@ class Oracle:
     up, dn = np.nextafter(x, self.dt_.type(np.inf)), np.nextafter(x, self.dt_.type(-np.inf))
     return np.where(d > 0, up, np.where(d < 0, dn, x)).astype(self.dt_)
 
+  def _fma2(self, x, y):
+    """Dot products over the last axis of x and y (broadcast) as two
+    interleaved fused multiply-add chains: s0 over the even terms, s1 over
+    the odd ones, then s0 + s1; each fma rounded once to this dtype (the
+    float64 product of two float32 values is exact)."""
+    n = x.shape[-1]
+    shape = np.broadcast_shapes(x.shape[:-1], y.shape[:-1])
+    s = [np.zeros(shape, self.dt_), np.zeros(shape, self.dt_)]
+    for d in range(n):
+      k = d & 1
+      s[k] = (x[..., d].astype(np.float64) * y[..., d].astype(np.float64) + s[k]).astype(self.dt_)
+    return (s[0] + s[1]).astype(self.dt_)
+
   def _mm(self, a, b):
     """a @ b in this oracle's evaluation order ('rounded': float64, rounded once)."""
     if self.order == 'rounded':
       return (a.astype(np.float64) @ b.astype(np.float64)).astype(self.dt_)
+    if self.order == 'fma':
+      return self._fma2(a[..., :, None, :], np.swapaxes(b, -1, -2)[..., None, :, :])
     return a @ b
 
   def _mv(self, a, v):
     """a [B, n, m] times v [B, m] in this oracle's evaluation order."""
     if self.order == 'rounded':
       return np.einsum('bij,bj->bi', a.astype(np.float64), v.astype(np.float64)).astype(self.dt_)
+    if self.order == 'fma':
+      return self._fma2(a, v[:, None, :])
     return np.einsum('bij,bj->bi', a, v)
 
   # -------------------------------------------------------------------------
@@ -371,6 +394,11 @@ class Oracle:
         vel = vel + rotate(jv[:, i], xr[:, p])
         xa[:, i] = xa[:, p] + rotate(ja[:, i], xr[:, i])
         xv[:, i] = vel
+        # rounding envelope: every link's pose and velocity one ulp either
+        # way, carried down the tree as the rounding of each level is (the
+        # contact distances taken from them cancel to far below the positions)
+        xp[:, i], xr[:, i] = self._nudge(xp[:, i]), self._nudge(xr[:, i])
+        xa[:, i], xv[:, i] = self._nudge(xa[:, i]), self._nudge(xv[:, i])
     xr = normalize(xr)  # kinematics.py:106
     return xp, xr, xa, xv
 
@@ -710,9 +738,10 @@ class Oracle:
     """constraint.py:179-191."""
     jc, dc, ac, dist = self.jac_contact(s)
     jl, dl, al = self.jac_limit(s)
-    return s.replace(con_jac=np.concatenate([jc, jl], axis=1),
-                     con_diag=np.concatenate([dc, dl], axis=1),
-                     con_aref=np.concatenate([ac, al], axis=1),
+    # (rounding envelope: the rows one ulp either way; J Minv J^T cancels)
+    return s.replace(con_jac=self._nudge(np.concatenate([jc, jl], axis=1)),
+                     con_diag=self._nudge(np.concatenate([dc, dl], axis=1)),
+                     con_aref=self._nudge(np.concatenate([ac, al], axis=1)),
                      contact_dist=dist)
 
   def pg_solve(self, a, b, maxiter, maxls, tol=1e-3):

@@ -72,8 +72,10 @@ def tail_fd(args):
   horizon[, forced]) -> ({eps: [len(coords)]} central differences of -mean
   torso x-velocity over the env steps t..H-1 (each 1/horizon weighted) w.r.t.
   act[0, k] for k in coords, the FP64 tail trajectory of the unperturbed
-  actions (q, qd after each env step), and whether every frame's FP64 active
-  row count matched the forced tape's).  With `forced` ([H - t][n_frames]
+  actions (q, qd after each env step), whether every frame's FP64 active
+  row count matched the forced tape's, and the closest projection call of
+  the unperturbed tail's solves (relative; below about 1e-5 the sign of that
+  component is a tie at FP32 resolution)).  With `forced` ([H - t][n_frames]
   (iterations, active rows, step sizes) of another implementation's
   projected-gradient solves), every rollout of the difference takes those
   solver decisions: the difference quotient of the same branch."""
@@ -98,6 +100,7 @@ def tail_fd(args):
   loss = np.zeros(B)
   traj_q, traj_qd = [], []
   rows_ok = True
+  proj_gap = np.inf
   if forced is None:
     s = o.init(q, qd)
     for j in range(L):
@@ -123,6 +126,7 @@ def tail_fd(args):
         if not (np.count_nonzero(T['s'].con_diag, axis=1) == rows).all():
           rows_ok = False  # the tape belongs to another active set: forcing it means nothing
           break
+        proj_gap = min(proj_gap, float(T['proj_gap'][0]))
       if not rows_ok:
         break
       loss += -qd[:, 0] / horizon
@@ -130,7 +134,7 @@ def tail_fd(args):
       traj_qd.append(qd[0].copy())
     if not rows_ok:
       nan = {eps: np.full(len(coords), np.nan) for eps in eps_list}
-      return nan, np.full((L, q.shape[1]), np.nan), np.full((L, qd.shape[1]), np.nan), False
+      return nan, np.full((L, q.shape[1]), np.nan), np.full((L, qd.shape[1]), np.nan), False, proj_gap
   out, i = {}, 1
   for eps in eps_list:
     fd = np.zeros(len(coords))
@@ -138,4 +142,4 @@ def tail_fd(args):
       fd[c] = (loss[i] - loss[i + 1]) / (2 * eps)
       i += 2
     out[eps] = fd
-  return out, np.array(traj_q), np.array(traj_qd), rows_ok
+  return out, np.array(traj_q), np.array(traj_qd), rows_ok, proj_gap

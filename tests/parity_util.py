@@ -46,12 +46,13 @@ def load(name):
 
 # draws of the FP32 rounding envelope: (seed, bias, order) of
 # oracle.pipeline.Oracle's perturbation; the two biased draws take every
-# near-tie decision one way and the other, three more at random, and two
+# near-tie decision one way and the other, three more at random, and three
 # evaluate the dense products whose terms cancel (J Minv J^T, J Minv
 # qf_smooth, Minv qf, the inverse) in another exact FP32 order without other
 # perturbation
 ENVELOPE_DRAWS = ((1000, -1, 'reference'), (1001, 1, 'reference'), (1002, 0, 'reference'),
-                  (1003, 0, 'reference'), (1004, 0, 'reference'), (None, 0, 'right'), (None, 0, 'rounded'))
+                  (1003, 0, 'reference'), (1004, 0, 'reference'), (None, 0, 'right'), (None, 0, 'rounded'),
+                  (None, 0, 'fma'))
 
 
 def oracle_check(sys, q, qd, minv, act, n_frames, exact, got_q, got_qd, label, strict=False):

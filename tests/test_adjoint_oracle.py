@@ -81,7 +81,7 @@ def test_tail_fd_forced_onto_its_own_branch():
   args = ('quadruped', s.q[0], s.qd[0], act, F, (1e-4, 1e-5), [0, 3, 6], L)
   free = grad_util.tail_fd(args)
   pinned = grad_util.tail_fd(args + (forced,))
-  assert pinned[3]
+  assert pinned[3] and pinned[4] > 0
   np.testing.assert_allclose(pinned[1], free[1], rtol=0, atol=1e-10)
   np.testing.assert_allclose(pinned[2], free[2], rtol=0, atol=1e-10)
   for eps in (1e-4, 1e-5):

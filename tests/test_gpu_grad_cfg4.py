@@ -40,9 +40,13 @@ path alike.  So the check has two parts:
     count equals the GPU's, and the FP64 tail tracks the GPU's trajectory to
     1e-4, the adjoint must match the eps = 1e-5 difference within
     max(1e-3, 2 x the FP32 adjoint's same-branch error at that env step from
-    (a)), relative to the env step's largest derivative; every other (env,
-    step, action) is listed with the evidence (the two differences, the
-    difference on the FP64 solves' own branches, the tail divergence).
+    (a)), relative to the env step's largest derivative -- except where a
+    component of a tail projection (y - step grad, clamped at zero) cancels
+    to within 1e-5 of its terms, whose sign the forcing does not fix: those
+    are listed as projection ties, at most 5 % of the checked derivatives;
+    every other (env, step, action) is listed with the evidence (the two
+    differences, the difference on the FP64 solves' own branches, the tail
+    divergence).
 """
 
 import multiprocessing as mp
@@ -60,6 +64,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 N_ENV, H, F, CKPT = 512, 128, 5, 16
 ENVS = np.arange(0, N_ENV, 64)
 FD_STEPS = (112, 120, 127)
+PROJ_TIE = 1e-5  # a projection component cancelling to this fraction of its terms: a sign tie in FP32
 
 
 def _workload(sys_):
@@ -193,11 +198,11 @@ def test_apg_workload_gradient():
   # (b) FP64 central differences on the last segment, every rollout of the
   # difference on the GPU's branch (its projected-gradient decisions forced);
   # the same differences on the FP64 solves' own branches are printed beside
-  checked, listed, errs_b, errs_free = 0, [], [], []
+  checked, listed, errs_b, errs_free, ties = 0, [], [], [], []
   k = 0
   for i, e in enumerate(ENVS):
     for t in FD_STEPS:
-      (fd, tail_q, tail_qd, rows_ok), (fdu, _, _, _) = fds[k], fds[k + 1]
+      (fd, tail_q, tail_qd, rows_ok, proj_gap), fdu = fds[k], fds[k + 1][0]
       k += 2
       gpu = act_bar[t, e].astype(np.float64)
       scale = max(np.abs(fd[1e-5]).max(), 1e-9)
@@ -213,8 +218,14 @@ def test_apg_workload_gradient():
           checked += 1
           errs_b.append(err[j])
           if err[j] > max(1e-3, 2 * own):
-            fails.append(('(b) smooth, tracked derivative beyond max(1e-3, 2 x the FP32 error of its step)',
-                          int(e), t, j, float(gpu[j]), float(fd[1e-5][j]), own))
+            if proj_gap < PROJ_TIE:
+              # a component of the tail's projections is at zero to FP32
+              # resolution: the GPU's tape holds its sign, the FP64 rollout
+              # may hold the other (the forcing fixes steps, not signs)
+              ties.append((int(e), t, j, float(gpu[j]), float(fd[1e-5][j]), proj_gap))
+            else:
+              fails.append(('(b) smooth, tracked derivative beyond max(1e-3, 2 x the FP32 error of its step)',
+                            int(e), t, j, float(gpu[j]), float(fd[1e-5][j]), own, proj_gap))
         else:
           listed.append((int(e), t, j, float(gpu[j]), float(fd[1e-4][j]), float(fd[1e-5][j]), float(fdu[1e-5][j]),
                          float(track), 'rows' if not rows_ok else ''))
@@ -228,6 +239,11 @@ def test_apg_workload_gradient():
   for row in listed[:24]:
     print('    env %d step %d act %d: adjoint %.5e | FD eps 1e-4 %.5e, eps 1e-5 %.5e (own branches %.5e) | '
           'tail divergence %.1e %s' % row)
+  print(f'{len(ties)} checked derivatives beyond the bar at a projection tie (closest call below {PROJ_TIE:g}):')
+  for row in ties:
+    print('    env %d step %d act %d: adjoint %.5e | FD eps 1e-5 %.5e | closest projection call %.1e' % row)
+  if len(ties) > 0.05 * max(checked, 1):
+    fails.append(('(b) more than 5 % of the checked derivatives at projection ties', len(ties), checked))
   if checked < 0.5 * len(ENVS) * len(FD_STEPS) * sys_.act_size():
     fails.append(('(b) fewer than half the derivatives checkable', checked))
   for f_ in fails:
