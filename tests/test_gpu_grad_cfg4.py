@@ -149,6 +149,11 @@ def test_apg_workload_gradient():
   assert (st == 0).all(), np.unique(st, return_counts=True)
   q_start = np.concatenate([q0[None], tq[:-1]], 0)    # state at the start of each env step
   qd_start = np.concatenate([qd0[None], tqd[:-1]], 0)
+  if os.environ.get('BRAXG_TEST_DUMP'):  # the checked envs' GPU data, for offline analysis
+    import pickle
+    with open(os.environ['BRAXG_TEST_DUMP'], 'wb') as fh:
+      pickle.dump(dict(envs=ENVS, act_bar=act_bar[:, ENVS], qd0_bar=qd0_bar[ENVS], tq=tq[:, ENVS], tqd=tqd[:, ENVS],
+                       q0=q0[ENVS], qd0=qd0[ENVS], u=u[:, ENVS], forced=forced), fh)
   q_bar = np.zeros((H, N_ENV, sys_.q_size()))
   ctx = mp.get_context('spawn')
   with ctx.Pool(min(len(ENVS), os.cpu_count() or 1)) as pool:
