@@ -29,16 +29,20 @@ path alike.  So the check has two parts:
     <= 5e-3 -- the same-branch difference is the FP32 adjoint's own rounding
     over up to 640 reversed pipeline steps -- at least 75 % of the steps so
     checked, and qd0 within 1e-3 for envs without such a frame;
-(b) FP64 central differences at eps = 1e-4 and 1e-5 side by side for the
-    actions of env steps 112, 120 and 127 (the last checkpoint segment),
-    rolled out in FP64 from the GPU's state at that step with every frame's
-    projected-gradient solve forced onto the GPU's decisions (the same
-    branch, as in (a); a line-search tie in the 16-step tail otherwise puts
-    the FP64 rollouts on another branch than the one the GPU
-    differentiated).  Where the two differences agree (FD is smooth: no
-    contact or active-set switch within eps), every frame's FP64 active row
-    count equals the GPU's, and the FP64 tail tracks the GPU's trajectory to
-    1e-4, the adjoint must match the eps = 1e-5 difference within
+(b) FP64 central differences at eps = 1e-3, 1e-4 (the workload's own
+    step) and 1e-5 side by side for the actions of env steps 112, 116, 120,
+    124, 126 and 127 (the last checkpoint segment), rolled out in FP64 from
+    the GPU's state at that step with every frame's projected-gradient solve
+    forced onto the GPU's decisions (the same branch, as in (a); a
+    line-search tie in the 16-step tail otherwise puts the FP64 rollouts on
+    another branch than the one the GPU differentiated).  At eps 1e-5 and
+    below the FP64 difference is rounding-bound on these states: on a
+    one-step tail its error against the FP64 reverse grows as 1/eps (1.3e-5,
+    1.7e-4, 1.4e-3, 1.3e-2, 1.9e-1 at eps 1e-3 .. 1e-7), so the reference is
+    the difference at 1e-4.  Where it is corroborated by one neighbour a
+    decade away (within 1e-3: no switch within eps), every frame's FP64
+    active row count equals the GPU's, and the FP64 tail tracks the GPU's
+    trajectory to 1e-4, the adjoint must match it within
     max(1e-3, 2 x the FP32 adjoint's same-branch error at that env step from
     (a)), relative to the env step's largest derivative -- except where a
     component of a tail projection (y - step grad, clamped at zero) cancels
@@ -63,7 +67,8 @@ pytestmark = pytest.mark.gpu
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 N_ENV, H, F, CKPT = 512, 128, 5, 16
 ENVS = np.arange(0, N_ENV, 64)
-FD_STEPS = (112, 120, 127)
+FD_STEPS = (112, 116, 120, 124, 126, 127)
+FD_EPS = (1e-3, 1e-4, 1e-5)  # 1e-4 is the workload's own difference step
 PROJ_TIE = 1e-5  # a projection component cancelling to this fraction of its terms: a sign tie in FP32
 
 
@@ -163,8 +168,9 @@ def test_apg_workload_gradient():
     fd_args = []
     for i, e in enumerate(ENVS):
       for t in FD_STEPS:
-        a = ('quadruped', q_start[t, e], qd_start[t, e], u[t:, e], F, (1e-4, 1e-5), list(range(sys_.act_size())), H)
-        fd_args += [a + (forced[i][t:],), a]  # the GPU's branch; the FP64 solves' own branches
+        a = ('quadruped', q_start[t, e], qd_start[t, e], u[t:, e], F)
+        tail = (list(range(sys_.act_size())), H)
+        fd_args += [a + (FD_EPS,) + tail + (forced[i][t:],), a + ((1e-4,),) + tail]  # the GPU's branch; FP64's own
     fds = pool.map(grad_util.tail_fd, fd_args)
 
   # (a) against the FP64 reverse of the GPU's own branch, along the GPU
@@ -210,11 +216,14 @@ def test_apg_workload_gradient():
       (fd, tail_q, tail_qd, rows_ok, proj_gap), fdu = fds[k], fds[k + 1][0]
       k += 2
       gpu = act_bar[t, e].astype(np.float64)
-      scale = max(np.abs(fd[1e-5]).max(), 1e-9)
-      smooth = np.abs(fd[1e-4] - fd[1e-5]) <= 1e-3 * scale
+      scale = max(np.abs(fd[1e-4]).max(), 1e-9)
+      # smooth: the difference at eps 1e-4 is corroborated by one of its
+      # neighbours a decade away (no switch within eps, and neither the
+      # truncation nor the rounding of the difference above 1e-3)
+      smooth = ((np.abs(fd[1e-3] - fd[1e-4]) <= 1e-3 * scale) | (np.abs(fd[1e-4] - fd[1e-5]) <= 1e-3 * scale))
       track = max(rel_err(tail_q, tq[t:, e]).max(), rel_err(tail_qd, tqd[t:, e]).max())
-      err = np.abs(gpu - fd[1e-5]) / scale
-      errs_free.append(float((np.abs(gpu - fdu[1e-5]) / max(np.abs(fdu[1e-5]).max(), 1e-9)).max()))
+      err = np.abs(gpu - fd[1e-4]) / scale
+      errs_free.append(float((np.abs(gpu - fdu[1e-4]) / max(np.abs(fdu[1e-4]).max(), 1e-9)).max()))
       # the FP32 adjoint's own rounding at this env step: its same-branch
       # difference from the FP64 reverse, part (a)
       own = float(e_steps[i, t])
@@ -227,22 +236,22 @@ def test_apg_workload_gradient():
               # a component of the tail's projections is at zero to FP32
               # resolution: the GPU's tape holds its sign, the FP64 rollout
               # may hold the other (the forcing fixes steps, not signs)
-              ties.append((int(e), t, j, float(gpu[j]), float(fd[1e-5][j]), proj_gap))
+              ties.append((int(e), t, j, float(gpu[j]), float(fd[1e-4][j]), proj_gap))
             else:
               fails.append(('(b) smooth, tracked derivative beyond max(1e-3, 2 x the FP32 error of its step)',
-                            int(e), t, j, float(gpu[j]), float(fd[1e-5][j]), own, proj_gap))
+                            int(e), t, j, float(gpu[j]), float(fd[1e-4][j]), own, proj_gap))
         else:
-          listed.append((int(e), t, j, float(gpu[j]), float(fd[1e-4][j]), float(fd[1e-5][j]), float(fdu[1e-5][j]),
-                         float(track), 'rows' if not rows_ok else ''))
+          listed.append((int(e), t, j, float(gpu[j]), float(fd[1e-3][j]), float(fd[1e-4][j]), float(fd[1e-5][j]),
+                         float(fdu[1e-4][j]), float(track), 'rows' if not rows_ok else ''))
   eb = np.array(errs_b) if errs_b else np.zeros(1)
-  print(f'(b) last-segment actions: {checked} derivatives checked against FP64 FD on the GPU branch (eps 1e-5): p50 '
+  print(f'(b) last-segment actions: {checked} derivatives checked against FP64 FD on the GPU branch (eps 1e-4): p50 '
         f'{np.median(eb):.1e} p95 {np.quantile(eb, 0.95):.1e} max {eb.max():.1e}, {(eb <= 1e-3).mean() * 100:.1f} % '
         f'<= 1e-3; against FD on the FP64 solves\' own branches, per (env, step) max: p50 '
-        f'{np.median(errs_free):.1e} max {np.max(errs_free):.1e}; {len(listed)} listed (FD not smooth between eps '
-        f'1e-4 and 1e-5, the FP64 tail leaves the GPU trajectory by more than 1e-4, or an active-row count differs '
-        f'from the GPU tape):')
+        f'{np.median(errs_free):.1e} max {np.max(errs_free):.1e}; {len(listed)} listed (the difference at eps 1e-4 '
+        f'not corroborated at 1e-3 or 1e-5, the FP64 tail leaves the GPU trajectory by more than 1e-4, or an '
+        f'active-row count differs from the GPU tape):')
   for row in listed[:24]:
-    print('    env %d step %d act %d: adjoint %.5e | FD eps 1e-4 %.5e, eps 1e-5 %.5e (own branches %.5e) | '
+    print('    env %d step %d act %d: adjoint %.5e | FD eps 1e-3 %.5e, 1e-4 %.5e, 1e-5 %.5e (own branches %.5e) | '
           'tail divergence %.1e %s' % row)
   print(f'{len(ties)} checked derivatives beyond the bar at a projection tie (closest call below {PROJ_TIE:g}):')
   for row in ties:
