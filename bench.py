@@ -739,6 +739,7 @@ def bench_uneven(torch, dev, rank, total=8192, n_steps=256):
   t0 = time.perf_counter()
   shapes = autotune.tune_batch(systems, n_env, n_frames, device=dev)
   tune_s = time.perf_counter() - t0
+  tuned = autotune.report(systems, n_env, n_frames, device=dev) or {}
   b = Batch(systems, n_env, n_frames, shapes=shapes, device=dev)
   rng = np.random.default_rng(900 + rank)
   qs, qds, acts = [], [], []
@@ -790,7 +791,11 @@ def bench_uneven(torch, dev, rank, total=8192, n_steps=256):
           'env_steps_per_s_graph': round(total * n_steps / t_graph, 1),
           'ms_one_launch': round(1e3 * t_one, 3), 'ms_graph': round(1e3 * t_graph, 3),
           'graph_nodes_per_step': 3, 'shapes': shapes, 'launch': b.launch_info(),
-          'autotune_s': round(tune_s, 2), 'env_status_nonzero': bad,
+          'autotune_s': round(tune_s, 2),
+          'autotune': {'candidates_timed': len(tuned.get('timed', {})),
+                       'default_ms_16_steps': round(tuned.get('default_ms', float('nan')), 3),
+                       'kept_ms_16_steps': round(tuned.get('ms', float('nan')), 3)},
+          'env_status_nonzero': bad,
           'env_status_by_family': bad_by_family}
 
 

@@ -169,3 +169,18 @@ def tune_batch(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Seque
         merged[key] = hit
         _store(merged)
   return [tuple(s) for s in hit['shapes']]
+
+
+def report(systems: Sequence, n_env: Sequence[int], n_frames: Optional[Sequence[int]] = None,
+           device=None) -> Optional[Dict]:
+  """What tune_batch measured for this batch (from the cache): the default
+  shapes' time, the kept shapes' time and every candidate's, in ms of an
+  n_steps rollout of the whole batch; None if it was never tuned."""
+  device = torch.device('cuda') if device is None else torch.device(device)
+  if device.index is None:
+    device = torch.device('cuda', torch.cuda.current_device())
+  n_frames = [1] * len(systems) if n_frames is None else list(n_frames)
+  live = [g for g in range(len(systems)) if n_env[g] > 0]
+  args = ([systems[g] for g in live], [n_env[g] for g in live], [n_frames[g] for g in live])
+  with _lock:
+    return _load().get(_key(device, 0, *args) + '|descent')
