@@ -23,7 +23,78 @@ import numpy as np
 from brax_gb300 import system as S
 from oracle.pipeline import (Oracle, cross, dot, quat_mul, quat_rot_axis, quat_to_3x3, rotate,
                              normalize, tf_do_tf, inertia_mul, force_cross, motion_cross,
-                             _norm_with_norm, _plane_sphere)
+                             _norm_with_norm, _plane_sphere, safe_norm)
+
+
+# ---------------------------------------------------------------------------
+# Newton-Schulz inverse with its tape, and its reverse
+# ---------------------------------------------------------------------------
+
+
+def ns_forward(a, x0, num_iter):
+  """brax/math.py:278-305 on a batch (a, x0 [B, n, n]): the reset to
+  0.5 a^T / tr(a a^T) when |I - a x0| > 1, then num_iter updates
+  x <- x (I + r), r <- I - a x, each kept only if its residual norm is below
+  the previous one (r is carried either way).  Returns (x, tape)."""
+  B, n = a.shape[0], a.shape[-1]
+  eye = np.eye(n)
+  r0 = eye - a @ x0
+  reset = safe_norm(r0, 2) > 1
+  s = np.trace(a @ np.swapaxes(a, -1, -2), axis1=-2, axis2=-1)
+  alt = 0.5 * np.swapaxes(a, -1, -2) / s[:, None, None]
+  x = np.where(reset[:, None, None], alt, x0)
+  r, err = r0, np.ones(B)
+  xs, rs, cands, accs = [], [], [], []
+  for _ in range(num_iter):
+    xn = x @ (eye + r)
+    rn = eye - a @ xn
+    en = safe_norm(rn, 2)
+    acc = en < err
+    xs.append(x)
+    rs.append(r)
+    cands.append(xn)
+    accs.append(acc)
+    x = np.where(acc[:, None, None], xn, x)
+    r, err = rn, en
+  return x, dict(a=a, x0=x0, reset=reset, s=s, xs=xs, rs=rs, cands=cands, accs=accs)
+
+
+def ns_vjp(tape, xbar):
+  """Reverse of ns_forward: the cotangent of its result -> (a_bar, x0_bar).
+  The reset and acceptance decisions are piecewise constant (jnp.where in the
+  reference)."""
+  a = tape['a']
+  at = np.swapaxes(a, -1, -2)
+  n = a.shape[-1]
+  eye = np.eye(n)
+  abar = np.zeros_like(a)
+  rbar = np.zeros_like(a)
+  xbar = xbar.copy()
+  for k in range(len(tape['xs']) - 1, -1, -1):
+    acc = tape['accs'][k][:, None, None]
+    xnbar = np.where(acc, xbar, 0.0)
+    xkbar = np.where(acc, 0.0, xbar)
+    xn = tape['cands'][k]
+    # r_{k+1} = I - a xn_k
+    xnbar = xnbar - at @ rbar
+    abar -= rbar @ np.swapaxes(xn, -1, -2)
+    # xn_k = x_k (I + r_k)
+    xk, rk = tape['xs'][k], tape['rs'][k]
+    xkbar = xkbar + xnbar @ np.swapaxes(eye + rk, -1, -2)
+    rbar = np.swapaxes(xk, -1, -2) @ xnbar
+    xbar = xkbar
+  # r0 = I - a x0 (of the input, whether or not it was reset)
+  x0 = tape['x0']
+  x0bar = -at @ rbar
+  abar -= rbar @ np.swapaxes(x0, -1, -2)
+  # x after the reset: 0.5 a^T / s (s = tr(a a^T)) or x0
+  reset = tape['reset'][:, None, None]
+  s = tape['s'][:, None, None]
+  g = xbar
+  alt_bar = 0.5 * np.swapaxes(g, -1, -2) / s - (np.sum(at * g, axis=(-2, -1))[:, None, None] / s ** 2) * a
+  abar += np.where(reset, alt_bar, 0.0)
+  x0bar += np.where(reset, 0.0, g)
+  return abar, x0bar
 
 # ---------------------------------------------------------------------------
 # primitive reverses
@@ -154,10 +225,21 @@ def _ddiag_dimp(imp):
 
 
 class StepAdjoint:
-  """Forward with tape + reverse of brax/generalized/pipeline.py:64-94."""
+  """Forward with tape + reverse of brax/generalized/pipeline.py:64-94.
 
-  def __init__(self, sys: S.System):
+  With ``newton_schulz=True`` (and a model with matrix_inv_iterations > 0)
+  the step's mass_mx_inv is the reference's Newton-Schulz update of the
+  carried inverse (brax/generalized/mass.py:99-101): ``forward(q, qd, act,
+  minv_prev)`` takes the previous pipeline step's inverse (None: the exact
+  inverse, as pipeline.init computes it), ``T['s'].mass_mx_inv`` is the
+  inverse this step carries on, and ``vjp(T, qb, qdb, minvb_out)`` takes
+  that inverse's cotangent from the next step and leaves the cotangent of
+  ``minv_prev`` in ``self.minvb_prev``."""
+
+  def __init__(self, sys: S.System, newton_schulz: bool = False):
     self.sys = sys
+    self.ns_iters = sys.matrix_inv_iterations if newton_schulz else 0
+    self.minvb_prev = None
     self.o = Oracle(sys, np.float64, exact_inverse=True)
     self.st = self.o.st
     self.c = self.o.c
@@ -217,13 +299,17 @@ class StepAdjoint:
                 xr=normalize(xraw))
 
   # -------------------------------------------------------------- forward
-  def forward(self, q, qd, act):
-    """One pipeline step from (q, qd); returns (q', qd', tape)."""
+  def forward(self, q, qd, act, minv_prev=None):
+    """One pipeline step from (q, qd) (and, in Newton-Schulz mode, the
+    carried inverse); returns (q', qd', tape)."""
     o, st, c, sys = self.o, self.st, self.c, self.sys
     B = q.shape[0]
     T = dict(q=q, qd=qd, act=act)
     T['fk'] = fk = self._fk(q)
     s = o.init(q, qd)  # the position terms, exactly as the oracle computes them
+    if self.ns_iters > 0 and minv_prev is not None:
+      minv, T['ns'] = ns_forward(s.mass_mx, np.asarray(minv_prev, np.float64), self.ns_iters)
+      s = s.replace(mass_mx_inv=minv)
     assert np.allclose(s.x_pos, fk['xp']) and np.allclose(s.x_rot, fk['xr'])
     T['s'] = s
     # com-stage intermediates the reverse needs
@@ -398,8 +484,9 @@ class StepAdjoint:
     return x, tape
 
   # -------------------------------------------------------------- reverse
-  def vjp(self, T, qb_out, qdb_out):
-    """(q'_bar, qd'_bar) -> (q_bar, qd_bar, act_bar)."""
+  def vjp(self, T, qb_out, qdb_out, minvb_out=None):
+    """(q'_bar, qd'_bar) -> (q_bar, qd_bar, act_bar); minvb_out: the
+    cotangent of the inverse this step carries on (Newton-Schulz mode)."""
     st, c, sys = self.st, self.c, self.sys
     s = T['s']
     q, qd = T['q'], T['qd']
@@ -476,8 +563,14 @@ class StepAdjoint:
          ('cinr_i', 'cinr_pos', 'cd_ang', 'cd_vel', 'cdof_ang', 'cdof_vel', 'cdofd_ang',
           'cdofd_vel', 'root_com', 'x_pos', 'x_rot')}
     self._rne_vjp(s, -qfsb, P, qdb)
-    # ---- exact inverse, CRBA ----
-    mb = -np.swapaxes(minv, -1, -2) @ minvb @ np.swapaxes(minv, -1, -2)
+    # ---- the inverse (exact, or the Newton-Schulz update of the carried one), CRBA ----
+    if minvb_out is not None:
+      minvb = minvb + minvb_out
+    if 'ns' in T:
+      mb, self.minvb_prev = ns_vjp(T['ns'], minvb)
+    else:
+      mb = -np.swapaxes(minv, -1, -2) @ minvb @ np.swapaxes(minv, -1, -2)
+      self.minvb_prev = None
     self._crba_vjp(s, mb, P)
     # ---- constraint rows ----
     if m:

@@ -86,3 +86,67 @@ def test_tail_fd_forced_onto_its_own_branch():
   np.testing.assert_allclose(pinned[2], free[2], rtol=0, atol=1e-10)
   for eps in (1e-4, 1e-5):
     np.testing.assert_allclose(pinned[0][eps], free[0][eps], rtol=1e-4, atol=1e-8)
+
+
+@pytest.mark.parametrize('name,steps', [('chain3', 4), ('quadruped', 8), ('chain16', 3)])
+def test_newton_schulz_rollout_vjp_matches_finite_differences(name, steps):
+  """The reverse through the Newton-Schulz update of the carried inverse
+  (brax/math.py:278-305, reset and best-iterate acceptance piecewise
+  constant): three pipeline steps from an init state (exact inverse, as
+  pipeline.init), the later two carrying Newton-Schulz inverses, against FP64
+  central differences of the same Newton-Schulz rollout.  A hanging chain of
+  16 links (mass-matrix condition 2e5), whose inverse resets every step,
+  exercises the reset's derivative."""
+  if name.startswith('chain') and name != 'chain3':
+    from brax_gb300 import workloads
+    sys_ = workloads.chain(int(name[5:]))
+  else:
+    sys_ = load(name)
+  if sys_.matrix_inv_iterations == 0:
+    pytest.skip('model uses the exact inverse')
+  B, F = 4, 3
+  o = Oracle(sys_, np.float64, exact_inverse=False)
+  if name == 'chain16':
+    from brax_gb300 import workloads
+    q, qd = workloads.reset(sys_, B, np.random.default_rng(11))
+  else:
+    q, qd = seeded_inputs(sys_, B, 11)
+  s = o.init(q, qd)
+  rng = np.random.default_rng(12)
+  for _ in range(steps):
+    s = o.step(s, actions(sys_, B, rng))
+  q0, qd0 = s.q.copy(), s.qd.copy()
+  act = actions(sys_, B, rng)
+  adj = StepAdjoint(sys_, newton_schulz=True)
+  tapes, qq, qqd, minv = [], q0, qd0, None
+  for _ in range(F):
+    qn, qdn, T = adj.forward(qq, qqd, act, minv)
+    tapes.append((T, T['s'].x_rot))
+    qq, qqd, minv = qn, qdn, T['s'].mass_mx_inv
+  qbo, qdbo = rng.normal(size=qq.shape), rng.normal(size=qqd.shape)
+  qb, qdb, ab_tot, mb = qbo, qdbo, np.zeros_like(act), None
+  for T, xr in reversed(tapes):
+    adj._xr = xr
+    qb, qdb, ab = adj.vjp(T, qb, qdb, mb)
+    mb = adj.minvb_prev
+    ab_tot += ab
+  assert mb is None  # the first step's inverse is the exact one of pipeline.init
+  if name == 'chain16':
+    assert any(bool(T['ns']['reset'].any()) for T, _ in tapes[1:])
+
+  def f(q_, qd_, a_):
+    r = o.env_step(o.init(q_, qd_), a_, F)
+    return np.sum(qbo * r.q, -1) + np.sum(qdbo * r.qd, -1)
+
+  eps = 1e-6
+  for which, got in enumerate((qb, qdb, ab_tot)):
+    base = [q0, qd0, act]
+    fd = np.zeros_like(got)
+    for j in range(got.shape[1]):
+      a = [x.copy() for x in base]
+      a[which][:, j] += eps
+      fp = f(*a)
+      a[which][:, j] -= 2 * eps
+      fd[:, j] = (fp - f(*a)) / (2 * eps)
+    err = np.abs(got - fd).max(-1) / np.maximum(np.abs(fd).max(-1), 1e-9)
+    assert err.max() < 1e-5, (name, which, err)
