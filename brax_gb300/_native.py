@@ -23,7 +23,7 @@ STATE_FIELDS = (
 
 EXPORTS = ('braxg_model_create', 'braxg_model_destroy', 'braxg_model_dims', 'braxg_model_cache_words', 'braxg_model_cache_span',
            'braxg_init', 'braxg_step', 'braxg_rollout', 'braxg_rollout_vjp_workspace',
-           'braxg_rollout_vjp_workspace_resident',
+           'braxg_rollout_vjp_workspace_resident', 'braxg_rollout_vjp_workspace_mode',
            'braxg_rollout_vjp', 'braxg_rollout_vjp_fwd', 'braxg_rollout_vjp_bwd', 'braxg_rollout_vjp_noalloc',
            'braxg_rollout_vjp_noalloc_capacity', 'braxg_launch_shape',
            'braxg_batch_create', 'braxg_batch_destroy', 'braxg_batch_get_offsets',
@@ -128,6 +128,7 @@ def lib() -> ctypes.CDLL:
     l.braxg_rollout_vjp_workspace.argtypes = [vp, i32, i32, i32, i32, P(ctypes.c_size_t)]
     l.braxg_rollout_vjp_workspace_resident.argtypes = [vp, i32, i32, i32, i32, i32,
                                                        P(ctypes.c_size_t)]
+    l.braxg_rollout_vjp_workspace_mode.argtypes = [vp, i32, i32, i32, i32, i32, i32, P(ctypes.c_size_t)]
     l.braxg_rollout_vjp.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp,
                                     vp, vp, vp, ctypes.c_size_t, vp, P(Options)]
     l.braxg_rollout_vjp_fwd.argtypes = [vp, vp, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp,

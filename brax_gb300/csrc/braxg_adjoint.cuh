@@ -14,7 +14,7 @@ namespace braxg {
 
 struct AdjLayout {
   int q0, qd0, qb, qdb, qbo, qdbo, actb, qddb, qfsb, qfcb, vb, u, tb;
-  int Minvb, Mb, Jb, diagb, arefb, bb, xb, Ab, tape;
+  int Minvb, Mb, Minvbc, Jb, diagb, arefb, bb, xb, Ab, tape;
   int xpb, xrb, cib, cpb, cdb, rcb, cdofb, cdofdb;
   int tmp, tmp_words;
   int total;
@@ -49,6 +49,7 @@ __host__ __device__ inline AdjLayout make_adj_layout(int nl, int nq, int nv, int
   A.tb = take(nv);
   A.Minvb = take(nv * ldm);
   A.Mb = take(nv * ldm);
+  A.Minvbc = take(nv * ldm);  // Newton-Schulz mode: the carried inverse's cotangent, frame to frame
   A.Jb = take(m * ldj);
   A.diagb = take(m);
   A.arefb = take(m);
@@ -191,7 +192,7 @@ __device__ __noinline__ void rev_qdd(const int* mw, Ws w, AWs a) {
 // - aref and qfc = J^T x* are reversed as there.
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ __noinline__ void rev_constraint_implicit(const int* mw, Ws w, AWs a, int iters, int nrow) {
+__device__ __noinline__ void rev_constraint_implicit(const int* mw, Ws w, AWs a, int iters, int nrow, bool sym) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
@@ -218,17 +219,20 @@ __device__ __noinline__ void rev_constraint_implicit(const int* mw, Ws w, AWs a,
   float* jy = jr + al4(nv);         // J^T y
   float* jry = jy + al4(nv);        // J^T ry
   float* t2 = jry + al4(nv);        // Minv J^T v
-  // A v for the implicit A: out = J (Minv (J^T v)) + diag v, keeping J^T v in jtv
-  auto matvec = [&](const float* v, float* out, float* jtv) {
+  // A v for the implicit A: out = J (Minv (J^T v)) + diag v, keeping J^T v in
+  // jtv; `trans`: A^T v (Minv^T in the middle; the same unless the carried
+  // Newton-Schulz inverse is not symmetric)
+  auto matvec = [&](const float* v, float* out, float* jtv, bool trans = false) {
     for (int d = tm.lane; d < nv; d += T) {
       float s = 0.f;
       for (int r = 0; r < nrow; ++r) s = fmaf(w.jrow(r)[d], v[r], s);
       jtv[d] = s;
     }
     tm.sync();
+    const int si = trans ? 1 : ld, sk = trans ? ld : 1;
     for (int d = tm.lane; d < nv; d += T) {
       float s = 0.f;
-      for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * ld + k], jtv[k], s);
+      for (int k = 0; k < nv; ++k) s = fmaf(Minv[d * si + k * sk], jtv[k], s);
       t2[d] = s;
     }
     tm.sync();
@@ -287,7 +291,7 @@ __device__ __noinline__ void rev_constraint_implicit(const int* mw, Ws w, AWs a,
       diagb[i] += ry[i] * gb[i] + rb[i] * y[i];
     }
     tm.sync();
-    matvec(rb, ybar, jr);  // A rb, jr = J^T rb
+    matvec(rb, ybar, jr, !sym);  // A^T rb, jr = J^T rb
     for (int i = tm.lane; i < nrow; i += T) ybar[i] += vv[i];  // ybar = zb + A^T rb
     // Ab += ry gb^T + rb y^T:  P += ry (J^T gb)^T + rb (J^T y)^T,  Q += gb (J^T ry)^T + y (J^T rb)^T
     for (int e = tm.lane; e < nrow * nv; e += T) {
@@ -297,11 +301,15 @@ __device__ __noinline__ void rev_constraint_implicit(const int* mw, Ws w, AWs a,
     }
     tm.sync();
   }
-  // A = (J Minv) J^T + diag: Jb += (P + Q) Minv (Minv symmetric)
+  // A = (J Minv) J^T + diag: Jb += P Minv^T + Q Minv, (P + Q) Minv when Minv is symmetric
   for (int e = tm.lane; e < nrow * nv; e += T) {
     const int i = e / nv, d = e - i * nv;
     float s = 0.f;
-    for (int k = 0; k < nv; ++k) s = fmaf(Pm[i * ld + k] + Qm[i * ld + k], Minv[k * ld + d], s);
+    if (sym) {
+      for (int k = 0; k < nv; ++k) s = fmaf(Pm[i * ld + k] + Qm[i * ld + k], Minv[k * ld + d], s);
+    } else {
+      for (int k = 0; k < nv; ++k) s = fmaf(Pm[i * ld + k], Minv[d * ld + k], fmaf(Qm[i * ld + k], Minv[k * ld + d], s));
+    }
     Jb[i * ldj + d] += s;
   }
   // Minvb += J^T Ab J = J^T P
@@ -347,7 +355,7 @@ __device__ __noinline__ void rev_constraint_implicit(const int* mw, Ws w, AWs a,
 // path (more than kMaxExplicitRows active rows), which has no tape.
 // ---------------------------------------------------------------------------
 template <int T>
-__device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
+__device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a, bool sym = true) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
@@ -359,7 +367,7 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
   if (iters < 0 || nrow > md.m) return false;
   if (nrow == 0) return true;
   if (nrow > kMaxExplicitRows) {
-    rev_constraint_implicit<T>(mw, w, a, iters, nrow);
+    rev_constraint_implicit<T>(mw, w, a, iters, nrow, sym);
     return true;
   }
   const int lab = nrow | 1;  // Ab rows
@@ -397,7 +405,23 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
   for (int e = tm.lane; e < 4 * kA; e += T) ybar[e] = 0.f;  // ybar, vv, gb, rb with their padding
   for (int e = tm.lane; e < nrow * lab; e += T) Ab[e] = 0.f;
   tm.sync();
-  {
+  if (!sym) {  // every entry, as the forward formed A with a non-symmetric Newton-Schulz inverse
+    for (int e = tm.lane; e < nrow * nrow; e += T) {
+      const int i = e / nrow, c = e - i * nrow;
+      float s0 = 0.f, s1 = 0.f;
+      int k = 0;
+      for (; k + 1 < nv; k += 2) {
+        s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+        s1 = fmaf(W[i * ld + k + 1], J[c * ldj + k + 1], s1);
+      }
+      if (k < nv) s0 = fmaf(W[i * ld + k], J[c * ldj + k], s0);
+      Am[i * la + c] = (s0 + s1) + (i == c ? rdiag[i] : 0.f);
+    }
+    for (int e = tm.lane; e < nrow * (4 * n4 - nrow); e += T) {
+      const int r = e / (4 * n4 - nrow);
+      Am[r * la + nrow + (e - r * (4 * n4 - nrow))] = 0.f;
+    }
+  } else {
     int i = 0, c = tm.lane;
     while (c > i) {
       c -= i + 1;
@@ -474,19 +498,53 @@ __device__ __noinline__ bool rev_constraint(const int* mw, Ws w, AWs a) {
     tm.sync();
     for (int c = tm.lane; c < nrow; c += T)  // Ab += ry gb^T + rb y^T
       for (int i = 0; i < nrow; ++i) Ab[i * lab + c] += ry[i] * gb[c] + rb[i] * y[c];
-    for (int i = tm.lane; i < nrow; i += T) ybar[i] = vv[i] + matvec(rb, i);  // ybar = zb + A^T rb
+    if (sym) {
+      for (int i = tm.lane; i < nrow; i += T) ybar[i] = vv[i] + matvec(rb, i);  // ybar = zb + A^T rb
+    } else {
+      for (int i = tm.lane; i < nrow; i += T) {  // ybar = zb + A^T rb by columns
+        float s0 = 0.f, s1 = 0.f;
+        int r = 0;
+        for (; r + 1 < nrow; r += 2) {
+          s0 = fmaf(Am[r * la + i], rb[r], s0);
+          s1 = fmaf(Am[(r + 1) * la + i], rb[r + 1], s1);
+        }
+        if (r < nrow) s0 = fmaf(Am[r * la + i], rb[r], s0);
+        ybar[i] = vv[i] + (s0 + s1);
+      }
+    }
     tm.sync();
   }
-  // A = (J Minv) J^T + diag: Jb += (Ab + Ab^T) W (Minv symmetric), lanes over Jb's entries
+  // A = (J Minv) J^T + diag: Jb += Ab (J Minv^T) + Ab^T (J Minv), i.e.
+  // (Ab + Ab^T) W when Minv is symmetric; lanes over Jb's entries
   float* diagb = a.at(A.diagb);
   for (int e = tm.lane; e < nrow * nv; e += T) {
     const int i = e / nv, d = e - i * nv;
     float s = 0.f;
-    for (int c = 0; c < nrow; ++c) s = fmaf(Ab[i * lab + c] + Ab[c * lab + i], W[c * ld + d], s);
+    if (sym) {
+      for (int c = 0; c < nrow; ++c) s = fmaf(Ab[i * lab + c] + Ab[c * lab + i], W[c * ld + d], s);
+    } else {
+      for (int c = 0; c < nrow; ++c) s = fmaf(Ab[c * lab + i], W[c * ld + d], s);
+    }
     Jb[i * ldj + d] += s;
   }
   for (int i = tm.lane; i < nrow; i += T) diagb[i] = Ab[i * lab + i];
   tm.sync();
+  if (!sym) {  // W <- J Minv^T, then Jb += Ab W
+    for (int e = tm.lane; e < nrow * nv; e += T) {
+      const int i = e / nv, k = e - i * nv;
+      float s = 0.f;
+      for (int d = 0; d < nv; ++d) s = fmaf(J[i * ldj + d], Minv[k * ld + d], s);
+      W[i * ld + k] = s;
+    }
+    tm.sync();
+    for (int e = tm.lane; e < nrow * nv; e += T) {
+      const int i = e / nv, d = e - i * nv;
+      float s = 0.f;
+      for (int c = 0; c < nrow; ++c) s = fmaf(Ab[i * lab + c], W[c * ld + d], s);
+      Jb[i * ldj + d] += s;
+    }
+    tm.sync();
+  }
   // Minvb += J^T Ab J via Z = Ab J (reuses W's rows as Z)
   float* Z = W;
   for (int e = tm.lane; e < nrow * nv; e += T) {
@@ -724,6 +782,115 @@ __device__ __noinline__ void rev_inverse(const int* mw, Ws w, AWs a) {
   matmul<T, NVB>(tm, n, ld, w.at(L.Minv), T1, Mb, 0);
   for (int j = tm.lane; j < n; j += T)
     for (int i = 0; i < n; ++i) Mb[i * ld + j] = -Mb[i * ld + j];
+  tm.sync();
+}
+
+// n x n product by lanes over C's entries: C = alpha op(A) op(B + id I),
+// added to C when `acc`; op transposes when ta / tb.  Works on any memory.
+template <int T>
+__device__ void gemm_small(const Team<T>& tm, int n, const float* A, int lda, bool ta, const float* B, int ldb,
+                           bool tb, float id, float* C, int ldc, float alpha, bool acc) {
+  for (int e = tm.lane; e < n * n; e += T) {
+    const int i = e / n, j = e - i * n;
+    float s = 0.f;
+    for (int k = 0; k < n; ++k) {
+      const float av = ta ? A[k * lda + i] : A[i * lda + k];
+      const float bv = (tb ? B[j * ldb + k] : B[k * ldb + j]) + (k == j ? id : 0.f);
+      s = fmaf(av, bv, s);
+    }
+    C[i * ldc + j] = acc ? fmaf(alpha, s, C[i * ldc + j]) : alpha * s;
+  }
+  tm.sync();
+}
+
+// Words of rev_ns's per-env scratch (global memory).
+__host__ __device__ inline int ns_rev_scratch_words(int n, int nvb, int num_iter) {
+  const int ld = n | 1, lb = ns_tape_stride(n, nvb);
+  const int s1 = nvb <= 16 ? 3 * n * ns_ldb(n) : 2 * n * ld;
+  return al4(n * ld) + al4(s1) + al4(ns_tape_words(n, nvb, num_iter)) + 5 * al4(n * lb);
+}
+
+// mass.matrix_inv reverse in Newton-Schulz mode (brax/math.py:278-305, under
+// jax.grad): the frame's inverse is the update of the carried one against M.
+// From the frame's record (M, then the carried inverse before the update;
+// n x ld each) the update is recomputed with its tape (the same calls, so the
+// same decisions bit for bit), then reversed: Minvb (the result's cotangent)
+// -> Mb, and the carried inverse's cotangent into Minvbc.  The reset and the
+// acceptance decisions are piecewise constant.  `scr`: ns_rev_scratch_words
+// of global memory, 16-byte aligned.
+template <int T, int NVB>
+__device__ __noinline__ void rev_ns(const int* mw, Ws w, AWs a, const float* rec, float* scr, int num_iter) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  const AdjLayout& A = *a.A;
+  const int n = md.nv, ld = L.ldm, lb = ns_tape_stride(n, NVB);
+  const float* Mr = rec;
+  const float* X0 = rec + n * ld;
+  float* P = scr;
+  float* S1 = P + al4(n * ld);
+  float* tape = S1 + al4(NVB <= 16 ? 3 * n * ns_ldb(n) : 2 * n * ld);
+  float* xb = tape + al4(ns_tape_words(n, NVB, num_iter));
+  float* rbar = xb + al4(n * lb);
+  float* xnb = rbar + al4(n * lb);
+  float* cand = xnb + al4(n * lb);
+  float* x0b = cand + al4(n * lb);
+  const float* Minvb = a.at(A.Minvb);
+  float* Mb = a.at(A.Mb);
+  for (int e = tm.lane; e < n * ld; e += T) P[e] = X0[e];
+  tm.sync();
+  ns_update<T, NVB>(tm, n, Mr, ld, P, S1, num_iter, tape);
+  for (int e = tm.lane; e < n * n; e += T) {
+    const int i = e / n, j = e - i * n;
+    xb[i * lb + j] = Minvb[i * ld + j];
+    rbar[i * lb + j] = 0.f;
+    Mb[i * ld + j] = 0.f;
+  }
+  tm.sync();
+  for (int k = num_iter - 1; k >= 0; --k) {
+    const bool keep = tape[4 + k] != 0.f;
+    const float* Xk = tape + 4 + al4(num_iter) + 2 * k * n * lb;
+    const float* Rk = Xk + n * lb;
+    gemm_small<T>(tm, n, Xk, lb, false, Rk, lb, false, 1.f, cand, lb, 1.f, false);  // the candidate Xk (I + Rk)
+    for (int e = tm.lane; e < n * n; e += T) {  // kept: its cotangent is the result's; else the iterate's
+      const int i = e / n, j = e - i * n;
+      xnb[i * lb + j] = keep ? xb[i * lb + j] : 0.f;
+      if (keep) xb[i * lb + j] = 0.f;
+    }
+    tm.sync();
+    // r_{k+1} = I - M cand
+    gemm_small<T>(tm, n, Mr, ld, true, rbar, lb, false, 0.f, xnb, lb, -1.f, true);
+    gemm_small<T>(tm, n, rbar, lb, false, cand, lb, true, 0.f, Mb, ld, -1.f, true);
+    // cand = Xk (I + Rk)
+    gemm_small<T>(tm, n, xnb, lb, false, Rk, lb, true, 1.f, xb, lb, 1.f, true);
+    gemm_small<T>(tm, n, Xk, lb, true, xnb, lb, false, 0.f, rbar, lb, 1.f, false);
+  }
+  // r0 = I - M X0 (of the carried inverse, whether or not it was reset)
+  gemm_small<T>(tm, n, rbar, lb, false, X0, ld, true, 0.f, Mb, ld, -1.f, true);
+  gemm_small<T>(tm, n, Mr, ld, true, rbar, lb, false, 0.f, x0b, lb, -1.f, false);
+  float* Minvbc = a.at(A.Minvbc);
+  if (tape[0] != 0.f) {  // reset: x = 0.5 M^T / s, s = tr(M M^T)
+    float s = 0.f, t = 0.f;
+    for (int e = tm.lane; e < n * n; e += T) {
+      const int i = e / n, j = e - i * n;
+      const float v = Mr[i * ld + j];
+      s = fmaf(v, v, s);
+      t = fmaf(Mr[j * ld + i], xb[i * lb + j], t);
+    }
+    s = tm.sum(s);
+    t = tm.sum(t);
+    const float c = t / (s * s);
+    for (int e = tm.lane; e < n * n; e += T) {
+      const int i = e / n, j = e - i * n;
+      Mb[i * ld + j] += 0.5f * xb[j * lb + i] / s - c * Mr[i * ld + j];
+      Minvbc[i * ld + j] = x0b[i * lb + j];
+    }
+  } else {
+    for (int e = tm.lane; e < n * n; e += T) {
+      const int i = e / n, j = e - i * n;
+      Minvbc[i * ld + j] = x0b[i * lb + j] + xb[i * lb + j];
+    }
+  }
   tm.sync();
 }
 

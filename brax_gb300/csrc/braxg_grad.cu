@@ -30,22 +30,46 @@ static int vjp_snap_words(const braxg_model* m) {
 // recomputed segment; each part starts on a 256-byte boundary.
 static int vjp_n_ckpt(int n_steps, int ckpt_every) { return (n_steps + ckpt_every - 1) / ckpt_every; }
 
-static void vjp_sizes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, int resident,
-                      size_t* ckpt_floats, size_t* seg_floats, size_t* snap_floats) {
-  size_t S = (size_t)m->dims.nq + m->dims.nv;
+// In Newton-Schulz mode a checkpoint also holds the carried inverse
+// (nv x nv), and two parts follow the snapshots: per snapshotted frame its
+// record (M and the carried inverse its update started from, nv x ld each),
+// and per env the reverse's scratch (ns_rev_scratch_words).
+static int vjp_nvb(const braxg_model* m) { return m->dims.nv <= 16 ? 16 : 32; }
+static int vjp_ns_rec_words(const braxg_model* m) {
+  return braxg::al4(2 * m->dims.nv * (m->dims.nv | 1));
+}
+static int vjp_ns_scr_words(const braxg_model* m) {
+  return braxg::al4(braxg::ns_rev_scratch_words(m->dims.nv, vjp_nvb(m), m->ns_iters));
+}
+
+struct VjpSizes {
+  size_t ckpt, seg, snap, nsrec, nsscr;  // floats of each part (64-float multiples but the snapshots)
+  size_t total() const { return (ckpt + seg + snap + nsrec + nsscr) * sizeof(float); }
+};
+
+static VjpSizes vjp_sizes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, int resident,
+                          bool ns) {
+  const size_t S = (size_t)m->dims.nq + m->dims.nv;
+  const size_t SC = S + (ns ? (size_t)m->dims.nv * m->dims.nv : 0);
   const int n_ckpt = vjp_n_ckpt(n_steps, ckpt_every);
   const int first_res = n_ckpt - resident;
   const int steps = std::max(n_steps - first_res * ckpt_every, first_res > 0 ? ckpt_every : 0);
-  size_t frames = (size_t)steps * n_frames;
-  *ckpt_floats = ((size_t)n_ckpt * n_env * S + 63) / 64 * 64;
-  *seg_floats = (frames * n_env * S + 63) / 64 * 64;
-  *snap_floats = frames * n_env * (size_t)vjp_snap_words(m);
+  const size_t frames = (size_t)steps * n_frames;
+  VjpSizes z{};
+  z.ckpt = ((size_t)n_ckpt * n_env * SC + 63) / 64 * 64;
+  z.seg = (frames * n_env * S + 63) / 64 * 64;
+  z.snap = frames * n_env * (size_t)vjp_snap_words(m);
+  if (ns) {
+    z.snap = (z.snap + 63) / 64 * 64;
+    z.nsrec = (frames * n_env * (size_t)vjp_ns_rec_words(m) + 63) / 64 * 64;
+    z.nsscr = (size_t)n_env * vjp_ns_scr_words(m);
+  }
+  return z;
 }
 
-static size_t vjp_bytes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, int resident) {
-  size_t c, sg, sn;
-  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, resident, &c, &sg, &sn);
-  return (c + sg + sn) * sizeof(float);
+static size_t vjp_bytes(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every, int resident,
+                        bool ns = false) {
+  return vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, resident, ns).total();
 }
 
 int braxg_rollout_vjp_workspace_resident(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every,
@@ -64,6 +88,17 @@ int braxg_rollout_vjp_workspace(const braxg_model* m, int n_env, int n_steps, in
   return braxg_rollout_vjp_workspace_resident(m, n_env, n_steps, n_frames, ckpt_every, 1, bytes);
 }
 
+int braxg_rollout_vjp_workspace_mode(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every,
+                                     int resident, int inverse_mode, size_t* bytes) {
+  int rc = braxg_rollout_vjp_workspace_resident(m, n_env, n_steps, n_frames, ckpt_every, resident, bytes);
+  if (rc) return rc;
+  const int n_ckpt = vjp_n_ckpt(n_steps, ckpt_every);
+  if (resident <= 0 || resident > n_ckpt) resident = n_ckpt;
+  const bool ns = inverse_mode == BRAXG_INV_NEWTON_SCHULZ && m->ns_iters > 0;
+  *bytes = vjp_bytes(m, n_env, n_steps, n_frames, ckpt_every, resident, ns);
+  return BRAXG_OK;
+}
+
 // One launch of the gradient kernel: `phases` 3 (forward and reverse), 1 (the
 // forward: checkpoints, snapshots and trajectory into the workspace) or 2 (the
 // reverse, from a workspace a phase-1 launch with the same arguments filled).
@@ -75,6 +110,10 @@ static int run_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, i
   size_t need = 0;
   int rc = braxg_rollout_vjp_workspace(m, n_env, n_steps, n_frames, ckpt_every, &need);
   if (rc) return rc;
+  // the reference's inverse (Newton-Schulz, carried and updated every frame)
+  // when asked for and the model has iterations; else the exact inverse
+  const bool ns = opt != nullptr && opt->inverse_mode == BRAXG_INV_NEWTON_SCHULZ && m->ns_iters > 0;
+  if (ns) need = vjp_bytes(m, n_env, n_steps, n_frames, ckpt_every, 1, true);
   if (n_env == 0) return BRAXG_OK;
   if (q0 == nullptr || qd0 == nullptr) return fail(BRAXG_ERR_INVALID, "q0 and qd0 are required");
   if (workspace == nullptr || workspace_bytes < need)
@@ -90,10 +129,9 @@ static int run_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, i
   const int n_ckpt = vjp_n_ckpt(n_steps, ckpt_every);
   int resident = 1;
   while (resident < n_ckpt &&
-         vjp_bytes(m, n_env, n_steps, n_frames, ckpt_every, resident + 1) <= workspace_bytes)
+         vjp_bytes(m, n_env, n_steps, n_frames, ckpt_every, resident + 1, ns) <= workspace_bytes)
     ++resident;
-  size_t c, sg, sn;
-  vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, resident, &c, &sg, &sn);
+  const VjpSizes z = vjp_sizes(m, n_env, n_steps, n_frames, ckpt_every, resident, ns);
   if (reinterpret_cast<uintptr_t>(workspace) % 16 != 0)
     return fail(BRAXG_ERR_INVALID, "workspace must be 16-byte aligned");
   braxg::VjpArgs a{};
@@ -111,9 +149,18 @@ static int run_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, i
   a.act_bar = act_bar;
   a.q0_bar = q0_bar;
   a.qd0_bar = qd0_bar;
-  a.ckpt = static_cast<float*>(workspace);
-  a.seg = static_cast<float*>(workspace) + c;
-  a.snap = static_cast<float*>(workspace) + c + sg;
+  float* ws = static_cast<float*>(workspace);
+  a.ckpt = ws;
+  a.seg = ws + z.ckpt;
+  a.snap = ws + z.ckpt + z.seg;
+  a.ckpt_words = m->dims.nq + m->dims.nv + (ns ? m->dims.nv * m->dims.nv : 0);
+  a.ns_iters = ns ? m->ns_iters : 0;
+  if (ns) {
+    a.nsrec = a.snap + z.snap;
+    a.ns_rec_words = vjp_ns_rec_words(m);
+    a.nsscr = a.nsrec + z.nsrec;
+    a.ns_scr_words = vjp_ns_scr_words(m);
+  }
   a.snap_words = vjp_snap_words(m);
   a.resident = resident;
   a.traj_q = traj_q;

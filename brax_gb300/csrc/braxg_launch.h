@@ -126,6 +126,13 @@ struct VjpArgs {
   unsigned long long* prof;  // optional per-phase cycle counters
   int phases;           // 1: the forward (checkpoints, snapshots, trajectory) only; 2: the
                         // reverse only, from a workspace a phase-1 launch filled; 3: both
+  int ckpt_words;       // floats per env of a checkpoint: nq + nv (+ nv * nv in Newton-Schulz mode)
+  int ns_iters;         // > 0: Newton-Schulz mode (the carried inverse updated every frame after the first)
+  float* nsrec;         // [frames of the snapshot blocks, n, ns_rec_words]: per frame, M and the
+                        // carried inverse its update started from
+  int ns_rec_words;
+  float* nsscr;         // [n, ns_scr_words]: per env, the Newton-Schulz reverse's scratch
+  int ns_scr_words;
 };
 
 // Launches vjp_kernel<T, NVB> (defined in braxg_vjp_kernel.cuh, instantiated

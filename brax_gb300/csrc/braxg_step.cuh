@@ -903,6 +903,88 @@ __device__ bool spd_inverse_sweep(const Team<T>& tm, int n, int ld, const float*
   return ok;
 }
 
+// Words of ns_update's tape for n dofs and num_iter iterations, and the row
+// stride of its matrices (the stride the iteration itself uses).
+__host__ __device__ inline int ns_tape_stride(int n, int nvb) { return nvb <= 16 ? ns_ldb(n) : (n | 1); }
+__host__ __device__ inline int ns_tape_words(int n, int nvb, int num_iter) {
+  return 4 + al4(num_iter) + 2 * num_iter * n * ns_tape_stride(n, nvb);
+}
+
+// Newton-Schulz update of the carried inverse P (n x n, stride ld) against M
+// (brax/math.py:278-305): r0 = I - M P; when |r0| > 1, P restarts from
+// 0.5 M^T / tr(M M^T) (r0 is kept, as the reference does); then num_iter
+// updates x <- x (I + r), r <- I - M x, each kept only if its residual norm
+// is below the previous one.  S1: scratch of 3 n x ns_ldb(n) words up to 16
+// dofs (iterates and residuals in rows of that stride: 16-byte loads of every
+// product's right-hand operand, columns n .. stride zero), 2 n x ld above
+// (the iterate stays in P).  `tape` (optional; the gradient's recompute, in
+// global memory): word 0 the reset, words 4 .. 4 + num_iter whether each
+// iteration was kept, then per iteration its iterate and residual at the
+// iteration's start (n x ns_tape_stride each).  The same calls in the same
+// order with or without a tape, so a recompute from the same inputs takes the
+// same decisions bit for bit.  Returns whether it reset.
+template <int T, int NVB>
+__device__ bool ns_update(const Team<T>& tm, int n, const float* M, int ld, float* P, float* S1, int num_iter,
+                          float* tape) {
+  constexpr bool kRows4 = NVB <= 16;
+  const int lb = kRows4 ? ns_ldb(n) : ld;
+  float* cur = kRows4 ? S1 : P;
+  float* nxt = kRows4 ? S1 + n * lb : S1 + n * ld;
+  float* R = kRows4 ? S1 + 2 * n * lb : S1;
+  if (kRows4) {
+    for (int e = tm.lane; e < 3 * n * lb; e += T) {
+      const int i = e / lb, j = e - i * lb;  // rows of the three buffers in turn
+      S1[e] = (j < n && i < n) ? P[i * ld + j] : 0.f;
+    }
+    tm.sync();
+  }
+  matmul<T, NVB>(tm, n, M, ld, cur, lb, R, lb, 1, kRows4);  // r0 = I - A A_inv
+  float nr0 = safe_norm_mat<T>(tm, n, lb, R);
+  const bool reset = nr0 > 1.f;
+  if (reset) {  // reset to 0.5 A^T / tr(A A^T) (r0 is kept, as the reference does)
+    float s = 0.f;
+    for (int j = tm.lane; j < n; j += T)
+      for (int i = 0; i < n; ++i) {
+        float v = M[i * ld + j];
+        s += v * v;
+      }
+    s = tm.sum(s);
+    for (int j = tm.lane; j < n; j += T)
+      for (int i = 0; i < n; ++i) cur[i * lb + j] = 0.5f * M[j * ld + i] / s;
+    tm.sync();
+  }
+  if (tape != nullptr && tm.lane == 0) tape[0] = reset ? 1.f : 0.f;
+  float err = 1.f;
+  for (int it = 0; it < num_iter; ++it) {
+    if (tape != nullptr) {  // the iteration's iterate and residual at its start
+      float* xk = tape + 4 + al4(num_iter) + 2 * it * n * lb;
+      float* rk = xk + n * lb;
+      for (int e = tm.lane; e < n * lb; e += T) {
+        xk[e] = cur[e];
+        rk[e] = R[e];
+      }
+      tm.sync();
+    }
+    matmul<T, NVB>(tm, n, cur, lb, R, lb, nxt, lb, 2, kRows4);  // a_inv (I + r)
+    matmul<T, NVB>(tm, n, M, ld, nxt, lb, R, lb, 1, kRows4);    // I - a a_inv_next
+    float e = safe_norm_mat<T>(tm, n, lb, R);
+    const bool keep = e < err;
+    if (tape != nullptr && tm.lane == 0) tape[4 + it] = keep ? 1.f : 0.f;
+    if (keep) {
+      float* t = cur;
+      cur = nxt;
+      nxt = t;
+    }
+    err = e;
+  }
+  if (cur != P) {
+    for (int j = tm.lane; j < n; j += T)
+      for (int i = 0; i < n; ++i) P[i * ld + j] = cur[i * lb + j];
+    tm.sync();
+  }
+  return reset;
+}
+
 // ---------------------------------------------------------------------------
 // mass.matrix_inv: brax/generalized/mass.py:86-106 + brax/math.py:278-305
 // mode 0 keeps/updates Minv by Newton-Schulz (num_iter iterations; 0 keeps
@@ -926,58 +1008,13 @@ __device__ __noinline__ bool stage_inverse(const int* mw, Ws w, bool exact, int 
     return spd_inverse_sweep<T>(tm, n, ld, M, S1, P);
   }
   if (num_iter <= 0) return true;
-  // Up to 16 dofs the iterates and residuals live in rows of stride lb
-  // (16-byte loads of every product's right-hand operand; columns n .. lb
-  // zero; three such n x lb buffers are small there).  Larger models keep
-  // the iterate in place and use the arena's stride (two n x ld buffers).
-  // M stays in place as the left-hand operand.
   constexpr bool kRows4 = NVB <= 16;
   const int lb = kRows4 ? ns_ldb(n) : ld;
-  float* cur = kRows4 ? S1 : P;
-  float* nxt = kRows4 ? S1 + n * lb : S1 + n * ld;
-  float* R = kRows4 ? S1 + 2 * n * lb : S1;
-  if (bx_scratch<T>(w, scratch_inverse(L, n, false, kRows4), kRows4 ? R + n * lb : nxt + n * ld, n) ||
+  if (bx_scratch<T>(w, scratch_inverse(L, n, false, kRows4), S1 + (kRows4 ? 3 * n * lb : 2 * n * ld), n) ||
       bx_misaligned<T>(w, kRows4 ? S1 : nullptr))
     return true;
-  if (kRows4) {
-    for (int e = tm.lane; e < 3 * n * lb; e += T) {
-      const int i = e / lb, j = e - i * lb;  // rows of the three buffers in turn
-      S1[e] = (j < n && i < n) ? P[i * ld + j] : 0.f;
-    }
-    tm.sync();
-  }
-  matmul<T, NVB>(tm, n, M, ld, cur, lb, R, lb, 1, kRows4);  // r0 = I - A A_inv
-  float nr0 = safe_norm_mat<T>(tm, n, lb, R);
-  if (nr0 > 1.f) {  // reset to 0.5 A^T / tr(A A^T) (r0 is kept, as the reference does)
-    if (tm.lane == 0) reinterpret_cast<int*>(w.at(L.misc))[1] += 1;
-    float s = 0.f;
-    for (int j = tm.lane; j < n; j += T)
-      for (int i = 0; i < n; ++i) {
-        float v = M[i * ld + j];
-        s += v * v;
-      }
-    s = tm.sum(s);
-    for (int j = tm.lane; j < n; j += T)
-      for (int i = 0; i < n; ++i) cur[i * lb + j] = 0.5f * M[j * ld + i] / s;
-    tm.sync();
-  }
-  float err = 1.f;
-  for (int it = 0; it < num_iter; ++it) {
-    matmul<T, NVB>(tm, n, cur, lb, R, lb, nxt, lb, 2, kRows4);  // a_inv (I + r)
-    matmul<T, NVB>(tm, n, M, ld, nxt, lb, R, lb, 1, kRows4);    // I - a a_inv_next
-    float e = safe_norm_mat<T>(tm, n, lb, R);
-    if (e < err) {
-      float* t = cur;
-      cur = nxt;
-      nxt = t;
-    }
-    err = e;
-  }
-  if (cur != P) {
-    for (int j = tm.lane; j < n; j += T)
-      for (int i = 0; i < n; ++i) P[i * ld + j] = cur[i * lb + j];
-    tm.sync();
-  }
+  if (ns_update<T, NVB>(tm, n, M, ld, P, S1, num_iter, nullptr) && tm.lane == 0)
+    reinterpret_cast<int*>(w.at(L.misc))[1] += 1;
   return true;
 }
 

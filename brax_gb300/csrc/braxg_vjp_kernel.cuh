@@ -10,18 +10,26 @@ namespace braxg {
 
 
 
+// `sym`: the inverse is the exact (bitwise symmetric) one; false in
+// Newton-Schulz mode, where the solve forms every entry of A and takes A^T r.
 template <int T, int NVB>
-__device__ __forceinline__ void fwd_frame(const int* mw, Ws w, bool active, bool has_act, float* tape, bool& ok) {
+__device__ __forceinline__ void fwd_frame(const int* mw, Ws w, bool active, bool has_act, float* tape, bool& ok,
+                                          bool sym = true) {
   if (active) stage_smooth<T>(mw, w, has_act);
   __syncthreads();
-  if (active) stage_constraint<T>(mw, w, tape, true);  // gradients use the exact inverse
+  if (active) stage_constraint<T>(mw, w, tape, sym);
   __syncthreads();
   if (active) ok = stage_integrate<T>(mw, w) && ok;
   __syncthreads();
 }
 
+// Position terms of the arena's q.  ns_iters 0: the exact inverse of M;
+// else the Newton-Schulz update of the arena's (carried) inverse, after
+// copying M and that inverse to `rec` (the frame's record, for the reverse)
+// and the inverse to `minv_out` (a checkpoint's, n x n) when given.
 template <int T, int NVB>
-__device__ __forceinline__ bool pos_stage(const int* mw, Ws w, bool active) {
+__device__ __forceinline__ bool pos_stage(const int* mw, Ws w, bool active, int ns_iters = 0, float* rec = nullptr,
+                                          float* minv_out = nullptr) {
   bool ok = true;
   if (active) stage_fk<T>(mw, w);
   __syncthreads();
@@ -29,7 +37,30 @@ __device__ __forceinline__ bool pos_stage(const int* mw, Ws w, bool active) {
   __syncthreads();
   if (active) stage_crba<T>(mw, w);
   __syncthreads();
-  if (active) ok = stage_inverse<T, NVB>(mw, w, true, 0);
+  if (ns_iters > 0) {
+    if (active) {
+      const Model md(mw);
+      const Team<T> tm;
+      const Layout& L = *w.L;
+      const int n = md.nv, ld = L.ldm;
+      const float* M = w.at(L.M);
+      const float* P = w.at(L.Minv);
+      if (rec != nullptr)
+        for (int e = tm.lane; e < n * ld; e += T) {
+          rec[e] = M[e];
+          rec[n * ld + e] = P[e];
+        }
+      if (minv_out != nullptr)
+        for (int e = tm.lane; e < n * n; e += T) {
+          const int i = e / n, j = e - i * n;
+          minv_out[e] = P[i * ld + j];
+        }
+      tm.sync();
+      stage_inverse<T, NVB>(mw, w, false, ns_iters);
+    }
+  } else if (active) {
+    ok = stage_inverse<T, NVB>(mw, w, true, 0);
+  }
   __syncthreads();
   if (active) stage_jacobian<T>(mw, w);
   __syncthreads();
@@ -104,6 +135,8 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   const AdjLayout& A = *sal;
   const int nq = md.nq, nv = md.nv, nu = md.nu;
   const int S = nq + nv;
+  const int SC = a.ckpt_words;  // a checkpoint: q, qd (and the carried inverse in Newton-Schulz mode)
+  const bool ns = a.ns_iters > 0;
   const long long n = a.n_env;
   const bool has_act = a.act != nullptr && nu > 0;
   bool ok = true, taped = true;
@@ -138,7 +171,7 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   if (a.phases & 1) ok = pos_stage<T, NVB>(mw, w, active) && ok;
   for (int s = 0; (a.phases & 1) && s < a.n_steps; ++s) {
     if (active && s % a.ckpt_every == 0) {
-      float* c = a.ckpt + ((long long)(s / a.ckpt_every) * n + env) * S;
+      float* c = a.ckpt + ((long long)(s / a.ckpt_every) * n + env) * SC;
       copy_vec<T>(tm, c, w.at(L.q), nq);
       copy_vec<T>(tm, c + nq, w.at(L.qd), nv);
     }
@@ -153,9 +186,21 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
         copy_vec<T>(tm, a.seg + slot * S + nq, w.at(L.qd), nv);
       }
       tm.sync();
-      fwd_frame<T, NVB>(mw, w, active, has_act, snap ? tape : nullptr, ok);
+      fwd_frame<T, NVB>(mw, w, active, has_act, snap ? tape : nullptr, ok, !ns);
       if (active && snap) snap_save<T>(tm, a.snap + slot * a.snap_words, w.b, L.total, tape, tape_words);
-      ok = pos_stage<T, NVB>(mw, w, active) && ok;
+      // the next frame's position terms; in Newton-Schulz mode its record
+      // (when it is snapshotted) and, at a checkpoint's step, the carried
+      // inverse the checkpoint restarts from
+      float* rec = nullptr;
+      float* cmi = nullptr;
+      if (ns && active) {
+        const int sn = f + 1 < a.n_frames ? s : s + 1, fn = f + 1 < a.n_frames ? f + 1 : 0;
+        if (sn >= res_s0 && sn < a.n_steps)
+          rec = a.nsrec + ((long long)((sn - res_s0) * a.n_frames + fn) * n + env) * a.ns_rec_words;
+        if (fn == 0 && sn < a.n_steps && sn % a.ckpt_every == 0)
+          cmi = a.ckpt + ((long long)(sn / a.ckpt_every) * n + env) * SC + S;
+      }
+      ok = pos_stage<T, NVB>(mw, w, active, a.ns_iters, rec, cmi) && ok;
     }
     if (active && a.traj_q != nullptr) copy_vec<T>(tm, a.traj_q + ((long long)s * n + env) * nq, w.at(L.q), nq);
     if (active && a.traj_qd != nullptr) copy_vec<T>(tm, a.traj_qd + ((long long)s * n + env) * nv, w.at(L.qd), nv);
@@ -170,6 +215,7 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
   float* qbo = aw.at(A.qbo);
   float* qdbo = aw.at(A.qdbo);
   if (active) {
+    for (int i = tm.lane; i < md.nv * L.ldm; i += T) aw.at(A.Minvbc)[i] = 0.f;
     for (int i = tm.lane; i < nq; i += T)
       qbo[i] = a.q_bar ? a.q_bar[((long long)(a.n_steps - 1) * n + env) * nq + i] : 0.f;
     for (int i = tm.lane; i < nv; i += T)
@@ -184,13 +230,20 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
     const int base_s = sg >= first_res ? res_s0 : s0;
     if (sg < first_res) {  // recompute the segment, taping and snapshotting every frame
       if (active) {
-        const float* c = a.ckpt + ((long long)sg * n + env) * S;
+        const float* c = a.ckpt + ((long long)sg * n + env) * SC;
         copy_vec<T>(tm, w.at(L.q), c, nq);
         copy_vec<T>(tm, w.at(L.qd), c + nq, nv);
+        if (ns && s0 > 0)  // the carried inverse the segment's first update starts from
+          for (int e = tm.lane; e < md.nv * md.nv; e += T) {
+            const int i = e / md.nv, j = e - i * md.nv;
+            w.at(L.Minv)[i * L.ldm + j] = c[S + e];
+          }
       }
       tm.sync();
       __syncthreads();
-      pos_stage<T, NVB>(mw, w, active);
+      // the rollout's first frame takes the exact inverse (pipeline.init)
+      pos_stage<T, NVB>(mw, w, active, s0 > 0 ? a.ns_iters : 0,
+                        ns && s0 > 0 && active ? a.nsrec + ((long long)0 * n + env) * a.ns_rec_words : nullptr);
       for (int s = s0; s < s1; ++s) {
         if (active && has_act) copy_vec<T>(tm, w.at(L.act), a.act + ((long long)s * n + env) * nu, nu);
         for (int f = 0; f < a.n_frames; ++f) {
@@ -201,9 +254,14 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
           }
           tm.sync();
           bool dummy = true;
-          fwd_frame<T, NVB>(mw, w, active, has_act, tape, dummy);
+          fwd_frame<T, NVB>(mw, w, active, has_act, tape, dummy, !ns);
           if (active) snap_save<T>(tm, a.snap + slot * a.snap_words, w.b, L.total, tape, tape_words);
-          pos_stage<T, NVB>(mw, w, active);
+          float* rec = nullptr;
+          if (ns && active) {
+            const int sn = f + 1 < a.n_frames ? s : s + 1, fn = f + 1 < a.n_frames ? f + 1 : 0;
+            if (sn < s1) rec = a.nsrec + ((long long)((sn - base_s) * a.n_frames + fn) * n + env) * a.ns_rec_words;
+          }
+          pos_stage<T, NVB>(mw, w, active, a.ns_iters, rec);
         }
       }
     }
@@ -246,13 +304,26 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
         if (active) rev_qdd<T>(mw, w, aw);
         __syncthreads();
         pf.mark(BRAXG_PROF_REV_QDD);
-        if (active) taped = rev_constraint<T>(mw, w, aw) && taped;
+        if (active) taped = rev_constraint<T>(mw, w, aw, !ns) && taped;
         __syncthreads();
         pf.mark(BRAXG_PROF_REV_CONSTRAINT);
         if (active) rev_smooth<T>(mw, w, aw, has_act);
         __syncthreads();
         pf.mark(BRAXG_PROF_REV_SMOOTH);
-        if (active) rev_inverse<T, NVB>(mw, w, aw);
+        if (active) {
+          if (ns) {  // the cotangent the next frame's update carried back to this frame's inverse
+            float* mib = aw.at(A.Minvb);
+            const float* mic = aw.at(A.Minvbc);
+            for (int i = tm.lane; i < md.nv * L.ldm; i += T) mib[i] += mic[i];
+            tm.sync();
+          }
+          if (ns && (s > 0 || f > 0)) {
+            const long long slot = (long long)((s - base_s) * a.n_frames + f) * n + env;
+            rev_ns<T, NVB>(mw, w, aw, a.nsrec + slot * a.ns_rec_words, a.nsscr + env * a.ns_scr_words, a.ns_iters);
+          } else {
+            rev_inverse<T, NVB>(mw, w, aw);  // the exact inverse (the rollout's first frame: pipeline.init)
+          }
+        }
         __syncthreads();
         pf.mark(BRAXG_PROF_REV_INVERSE);
         if (active) rev_crba<T>(mw, w, aw);

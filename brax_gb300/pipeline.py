@@ -456,7 +456,8 @@ def rollout(sys, state: State, act_seq, n_frames: int = 1, inverse_mode: int = N
 
 def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int = 1,
                  ckpt_every: int = 16, trajectory: bool = False,
-                 profile: Optional[torch.Tensor] = None, resident_segments: Optional[int] = None):
+                 profile: Optional[torch.Tensor] = None, resident_segments: Optional[int] = None,
+                 inverse_mode: int = CHOLESKY):
   """Reverse-mode gradient of a rollout through the hand-written adjoint.
 
   Replaces ``jax.grad`` through ``lax.scan`` of ``pipeline_step``
@@ -464,7 +465,9 @@ def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int =
   [n_steps, n, nq|nv] are the loss cotangents of the state after every env step.
   ``resident_segments``: checkpoint segments whose frame snapshots stay
   resident from the checkpoint pass (the others are recomputed); None keeps
-  as many as fit a quarter of the free device memory.
+  as many as fit a quarter of the free device memory.  ``inverse_mode``
+  NEWTON_SCHULZ differentiates the reference's carried Newton-Schulz inverse
+  (exact at the first frame, as init computes it); CHOLESKY the exact one.
   Returns (act_bar, q0_bar, qd0_bar, status, (traj_q, traj_qd)).
   """
   m = model_for(sys, q0.device)
@@ -485,37 +488,36 @@ def rollout_grad(sys, q0, qd0, act_seq, q_bar=None, qd_bar=None, n_frames: int =
     tq, tqd = f(n_steps, n, m.nq), f(n_steps, n, m.nv)
   status = torch.zeros(n, dtype=torch.int32, device=dev)
   lib = N.lib()
-  ws, nbytes = _vjp_workspace(m, n, n_steps, n_frames, ckpt_every, resident_segments)
+  ws, nbytes = _vjp_workspace(m, n, n_steps, n_frames, ckpt_every, resident_segments, inverse_mode)
   stream = torch.cuda.current_stream(dev).cuda_stream
   N.check(lib.braxg_rollout_vjp(
       m.handle, ctypes.c_void_p(stream), n, n_steps, int(n_frames), int(ckpt_every),
       act_seq.data_ptr() if m.nu else None, q0.data_ptr(), qd0.data_ptr(), _ptr(qb), _ptr(qdb),
       act_bar.data_ptr() if m.nu else None, q0_bar.data_ptr(), qd0_bar.data_ptr(), _ptr(tq),
       _ptr(tqd), ws.data_ptr(), nbytes, status.data_ptr(),
-      ctypes.byref(_opts(CHOLESKY, 0, 0, profile))), 'braxg_rollout_vjp')
+      ctypes.byref(_opts(inverse_mode, 0, 0, profile))), 'braxg_rollout_vjp')
   return act_bar, q0_bar, qd0_bar, status, (tq, tqd)
 
 
 def _vjp_workspace(m: 'Model', n: int, n_steps: int, n_frames: int, ckpt_every: int,
-                   resident_segments: Optional[int]):
+                   resident_segments: Optional[int], inverse_mode: int = CHOLESKY):
   """(workspace tensor, bytes) of a gradient launch; resident_segments None
   keeps as many checkpoint segments resident as fit a quarter of the free
   device memory."""
   lib = N.lib()
   nbytes = ctypes.c_size_t()
   n_ckpt = (n_steps + int(ckpt_every) - 1) // int(ckpt_every)
+  size = lambda r: lib.braxg_rollout_vjp_workspace_mode(m.handle, n, n_steps, int(n_frames), int(ckpt_every), int(r),
+                                                        int(inverse_mode), ctypes.byref(nbytes))
   if resident_segments is None:
     free = torch.cuda.mem_get_info(m.device)[0]
     resident_segments = 1
     for r in range(n_ckpt, 0, -1):
-      N.check(lib.braxg_rollout_vjp_workspace_resident(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
-                                                       r, ctypes.byref(nbytes)), 'workspace')
+      N.check(size(r), 'workspace')
       if nbytes.value <= free // 4:
         resident_segments = r
         break
-  N.check(lib.braxg_rollout_vjp_workspace_resident(m.handle, n, n_steps, int(n_frames), int(ckpt_every),
-                                                   int(resident_segments), ctypes.byref(nbytes)),
-          'braxg_rollout_vjp_workspace_resident')
+  N.check(size(resident_segments), 'braxg_rollout_vjp_workspace_mode')
   return torch.empty(max(nbytes.value, 4), dtype=torch.uint8, device=m.device), nbytes.value
 
 
@@ -533,10 +535,11 @@ class VjpTape:
   workspace: torch.Tensor
   nbytes: int
   status: torch.Tensor
+  inverse_mode: int = CHOLESKY
 
 
 def rollout_vjp_fwd(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16,
-                    resident_segments: Optional[int] = None):
+                    resident_segments: Optional[int] = None, inverse_mode: int = CHOLESKY):
   """The forward half of rollout_grad (braxg_rollout_vjp_fwd): the rollout's
   trajectory (traj_q [n_steps, n, nq], traj_qd [n_steps, n, nv]) and a
   VjpTape for rollout_vjp_bwd.  The two halves give bitwise the result of
@@ -549,7 +552,7 @@ def rollout_vjp_fwd(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 
   if act_seq.dim() != 3 or act_seq.shape[1] != n or act_seq.shape[2] != m.nu:
     raise ValueError(f'act_seq must be (n_steps, {n}, {m.nu})')
   n_steps = act_seq.shape[0]
-  ws, nbytes = _vjp_workspace(m, n, n_steps, n_frames, ckpt_every, resident_segments)
+  ws, nbytes = _vjp_workspace(m, n, n_steps, n_frames, ckpt_every, resident_segments, inverse_mode)
   tq = torch.empty(n_steps, n, m.nq, dtype=torch.float32, device=m.device)
   tqd = torch.empty(n_steps, n, m.nv, dtype=torch.float32, device=m.device)
   status = torch.zeros(n, dtype=torch.int32, device=m.device)
@@ -557,8 +560,9 @@ def rollout_vjp_fwd(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 
   N.check(N.lib().braxg_rollout_vjp_fwd(
       m.handle, ctypes.c_void_p(stream), n, n_steps, int(n_frames), int(ckpt_every),
       act_seq.data_ptr() if m.nu else None, q0.data_ptr(), qd0.data_ptr(), tq.data_ptr(), tqd.data_ptr(),
-      ws.data_ptr(), nbytes, status.data_ptr(), ctypes.byref(_opts(CHOLESKY, 0, 0))), 'braxg_rollout_vjp_fwd')
-  return (tq, tqd), VjpTape(m, q0, qd0, act_seq, int(n_frames), int(ckpt_every), ws, nbytes, status)
+      ws.data_ptr(), nbytes, status.data_ptr(), ctypes.byref(_opts(inverse_mode, 0, 0))), 'braxg_rollout_vjp_fwd')
+  return (tq, tqd), VjpTape(m, q0, qd0, act_seq, int(n_frames), int(ckpt_every), ws, nbytes, status,
+                            int(inverse_mode))
 
 
 def rollout_vjp_bwd(tape: VjpTape, q_bar=None, qd_bar=None):
@@ -574,7 +578,7 @@ def rollout_vjp_bwd(tape: VjpTape, q_bar=None, qd_bar=None):
       m.handle, ctypes.c_void_p(stream), n, n_steps, tape.n_frames, tape.ckpt_every,
       tape.act_seq.data_ptr() if m.nu else None, tape.q0.data_ptr(), tape.qd0.data_ptr(), _ptr(qb), _ptr(qdb),
       act_bar.data_ptr() if m.nu else None, q0_bar.data_ptr(), qd0_bar.data_ptr(), tape.workspace.data_ptr(),
-      tape.nbytes, tape.status.data_ptr(), ctypes.byref(_opts(CHOLESKY, 0, 0))), 'braxg_rollout_vjp_bwd')
+      tape.nbytes, tape.status.data_ptr(), ctypes.byref(_opts(tape.inverse_mode, 0, 0))), 'braxg_rollout_vjp_bwd')
   return act_bar, q0_bar, qd0_bar, tape.status
 
 

@@ -273,6 +273,14 @@ int braxg_rollout_vjp_workspace_resident(const braxg_model* model, int n_env, in
                                          int n_frames, int ckpt_every, int resident,
                                          size_t* bytes);
 
+/* The same for an inverse mode: BRAXG_INV_NEWTON_SCHULZ (on a model with
+ * Newton-Schulz iterations) needs more (the carried inverse in every
+ * checkpoint, each snapshotted frame's update record, the reverse's scratch);
+ * the other sizes above are for the exact inverse. */
+int braxg_rollout_vjp_workspace_mode(const braxg_model* model, int n_env, int n_steps,
+                                     int n_frames, int ckpt_every, int resident, int inverse_mode,
+                                     size_t* bytes);
+
 /* Gradient of a rollout (the reverse of braxg_rollout), the replacement for
  * jax.grad through lax.scan of pipeline_step (brax/training/agents/apg/
  * train.py:188-198).  Runs the forward from (q0, qd0) with act_seq
@@ -282,7 +290,13 @@ int braxg_rollout_vjp_workspace_resident(const braxg_model* model, int n_env, in
  * [n_steps, n, nq|nv] are the loss cotangents of the state after each env step
  * (NULL = zero); outputs are act_bar [n_steps, n, nu], q0_bar [n, nq],
  * qd0_bar [n, nv] and, optionally, the forward trajectory traj_q / traj_qd.
- * The mass-matrix inverse is exact (Cholesky); status bits as braxg_env_flags.
+ * The mass-matrix inverse is exact (Cholesky) unless opt->inverse_mode is
+ * BRAXG_INV_NEWTON_SCHULZ on a model with Newton-Schulz iterations: then the
+ * rollout carries the reference's inverse (exact at the first frame, as
+ * pipeline.init computes it; updated by Newton-Schulz every frame after,
+ * brax/generalized/mass.py:99-101) and the reverse differentiates through
+ * those updates (brax/math.py:278-305, as jax.grad does; workspace from
+ * braxg_rollout_vjp_workspace_mode).  Status bits as braxg_env_flags.
  * Supports hinge/slide/free joints, world-plane sphere and capsule contacts and
  * joint limits, with either constraint-solve path (A formed explicitly up to 32
  * active rows, applied implicitly above). */

@@ -117,6 +117,80 @@ def test_rollout_gradient_matches_finite_differences():
   assert np.median(eq) <= 1e-3 and (eq <= 1e-2).mean() >= 7 / 8
 
 
+@pytest.mark.parametrize('name', ['chain3', 'quadruped'])
+def test_newton_schulz_gradient(name):
+  """Gradients in the reference's inverse mode (the carried Newton-Schulz
+  inverse, exact at the first frame as pipeline.init computes it): the
+  gradient kernel's forward is the Newton-Schulz rollout bit for bit, the
+  split halves and every residency give the fused launch's bits, and the
+  gradient matches FP64 central differences of the FP64 Newton-Schulz
+  rollout (brax/math.py:278-305 under jax.grad)."""
+  P = _P()
+  from oracle.pipeline import Oracle
+  sys_ = load(name)
+  n, H, F, k = 8, 4, (1 if name == 'chain3' else 5), 2
+  q0, qd0 = seeded_inputs(sys_, n, 23)
+  rng = np.random.default_rng(24)
+  u = actions(sys_, n * H, rng).reshape(H, n, -1) if sys_.act_size() else np.zeros((H, n, 0))
+  qd_bar = np.zeros((H, n, sys_.qd_size()))
+  qd_bar[:, :, 0] = -1.0 / H
+  q_bar = rng.normal(size=(H, n, sys_.q_size())) * 1e-2
+  NS = P.NEWTON_SCHULZ
+  fused = P.rollout_grad(sys_, _t(q0), _t(qd0), _t(u), _t(q_bar), _t(qd_bar), n_frames=F, ckpt_every=k,
+                         trajectory=True, inverse_mode=NS)
+  small = P.rollout_grad(sys_, _t(q0), _t(qd0), _t(u), _t(q_bar), _t(qd_bar), n_frames=F, ckpt_every=k,
+                         resident_segments=1, inverse_mode=NS)
+  (tq, tqd), tape = P.rollout_vjp_fwd(sys_, _t(q0), _t(qd0), _t(u), n_frames=F, ckpt_every=k, inverse_mode=NS)
+  split = P.rollout_vjp_bwd(tape, _t(q_bar), _t(qd_bar))
+  roll, (rq, rqd) = P.rollout(sys_, P.init(sys_, _t(q0), _t(qd0)), _t(u), n_frames=F, inverse_mode=NS,
+                              trajectory=True)
+  torch.cuda.synchronize()
+  assert (fused[3] == 0).all()
+  torch.testing.assert_close(fused[4][0], rq, rtol=0, atol=0)  # the Newton-Schulz rollout's trajectory
+  torch.testing.assert_close(fused[4][1], rqd, rtol=0, atol=0)
+  for other in (small, split):
+    for a_, b_ in zip(other[:3], fused[:3]):
+      torch.testing.assert_close(a_, b_, rtol=0, atol=0)
+  # against FP64 central differences of the Newton-Schulz rollout
+  o = Oracle(sys_, np.float64, exact_inverse=False)
+
+  def loss(q0_, qd0_, u_):
+    s = o.init(q0_, qd0_)
+    tot = np.zeros(n)
+    for t in range(H):
+      s = o.env_step(s, u_[t], F)
+      tot += np.sum(q_bar[t] * s.q, -1) + np.sum(qd_bar[t] * s.qd, -1)
+    return tot
+
+  eps = 1e-5
+  errs = []
+  for which, got in ((2, fused[2].cpu().numpy()), (0, fused[0].cpu().numpy())):
+    if which == 0 and sys_.act_size() == 0:
+      continue
+    base = [q0, qd0, u]
+    fd = np.zeros(got.shape)
+    if which == 2:
+      for j in range(sys_.qd_size()):
+        a_, b_ = qd0.copy(), qd0.copy()
+        a_[:, j] += eps
+        b_[:, j] -= eps
+        fd[:, j] = (loss(q0, a_, u) - loss(q0, b_, u)) / (2 * eps)
+      e = _rel(got, fd)
+    else:
+      for t in range(H):
+        for j in range(sys_.act_size()):
+          a_, b_ = u.copy(), u.copy()
+          a_[t, :, j] += eps
+          b_[t, :, j] -= eps
+          fd[t, :, j] = (loss(q0, qd0, a_) - loss(q0, qd0, b_)) / (2 * eps)
+      e = _rel(np.swapaxes(got, 0, 1), np.swapaxes(fd, 0, 1))
+    errs.append(e)
+    print(f'{name} Newton-Schulz gradient vs FP64 FD ({["act", "", "qd0"][which]}): p50 {np.median(e):.2e} '
+          f'max {e.max():.2e}')
+  for e in errs:
+    assert np.median(e) <= 1e-3 and (e <= 1e-2).mean() >= 7 / 8
+
+
 def test_torch_autograd_function():
   P = _P()
   sys_ = load('quadruped')
