@@ -554,10 +554,22 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
     _, tape = pipeline.rollout_vjp_fwd(sys_, q0, qd0, u, n_frames=N_FRAMES, ckpt_every=ckpt)
     pipeline.rollout_vjp_bwd(tape, None, qd_bar)
 
+  def fwd_ns():  # the reference's inverse: the Newton-Schulz rollout from init's exact inverse
+    pipeline.rollout(sys_, pipeline.init(sys_, q0, qd0), u, n_frames=N_FRAMES, inverse_mode=pipeline.NEWTON_SCHULZ,
+                     trajectory=True)
+
+  def fwd_adj_ns():
+    r = pipeline.rollout_grad(sys_, q0, qd0, u, None, qd_bar, n_frames=N_FRAMES, ckpt_every=ckpt,
+                              inverse_mode=pipeline.NEWTON_SCHULZ)
+    status_ns[0] = r[3]
+
+  status_ns = [None]
   t_f = timed(fwd)
   t_b = timed(fwd_adj)  # every segment's snapshots resident (they fit): no recompute
   t_m = timed(lambda: fwd_adj(1))  # smallest workspace: all but the last segment recomputed
   t_s = timed(split)
+  t_fn = timed(fwd_ns)
+  t_bn = timed(fwd_adj_ns)
   bad = int((status[0] != 0).sum().item())
   return {'workload': f'quadruped, {n} envs, {horizon} env steps x {N_FRAMES} frames, checkpoint every {ckpt}',
           'fwd_env_steps_per_s': round(n * horizon / t_f, 1),
@@ -567,6 +579,9 @@ def bench_adjoint(torch, pipeline, sys_, dev, rank, n=512, horizon=128, ckpt=16,
           'fwd_adj_ms_smallest_workspace': round(1e3 * t_m, 3),
           'cost_ratio_smallest_workspace': round(t_m / t_f, 3),
           'split_fwd_then_bwd_ms': round(1e3 * t_s, 3), 'cost_ratio_split': round(t_s / t_f, 3),
+          'newton_schulz': {'fwd_ms': round(1e3 * t_fn, 3), 'fwd_adj_ms': round(1e3 * t_bn, 3),
+                            'cost_ratio_fwd_adj_over_fwd': round(t_bn / t_fn, 3),
+                            'envs_without_gradient': int((status_ns[0] != 0).sum().item())},
           'envs_without_gradient': bad, 'gpu_launches_fwd_adj': 1}
 
 

@@ -91,43 +91,45 @@ ffi::Error RolloutImpl(cudaStream_t stream, ffi::ScratchAllocator scratch, int64
 }
 
 ffi::Error RolloutVjpImpl(cudaStream_t stream, ffi::ScratchAllocator scratch, int64_t model, int32_t n_frames,
-                          int32_t ckpt_every, F32 q0, F32 qd0, F32 act_seq, F32 q_bar, F32 qd_bar,
-                          F32Out act_bar, F32Out q0_bar, F32Out qd0_bar, S32Out status) {
+                          int32_t ckpt_every, int32_t inverse_mode, F32 q0, F32 qd0, F32 act_seq, F32 q_bar,
+                          F32 qd_bar, F32Out act_bar, F32Out q0_bar, F32Out qd0_bar, S32Out status) {
   View a = in(q0), b = in(qd0), c = in(act_seq), d = in(q_bar), e = in(qd_bar);
   View ab = out(act_bar), qb = out(q0_bar), qdb = out(qd0_bar), st = out(status);
   const braxg_model* m = model_of(model);
-  const size_t bytes = braxg_xla::rollout_vjp_workspace(m, n_frames, ckpt_every, a.buf, c.buf);
+  const size_t bytes = braxg_xla::rollout_vjp_workspace(m, n_frames, ckpt_every, a.buf, c.buf, inverse_mode);
   void* ws = nullptr;
   if (bytes > 0) {
     std::optional<void*> mem = scratch.Allocate(bytes, 256);
     if (mem.has_value()) ws = *mem;  // else: the library's fixed scratch (noalloc entry point)
   }
   return to_error(braxg_xla::rollout_vjp(m, stream, n_frames, ckpt_every, a.buf, b.buf, c.buf, d.buf, e.buf, ab.buf,
-                                         qb.buf, qdb.buf, st.buf, ws, bytes));
+                                         qb.buf, qdb.buf, st.buf, ws, bytes, inverse_mode));
 }
 
 using U8 = ffi::Buffer<ffi::U8>;
 using U8Out = ffi::Result<ffi::Buffer<ffi::U8>>;
 using S32 = ffi::Buffer<ffi::S32>;
 
-ffi::Error RolloutVjpFwdImpl(cudaStream_t stream, int64_t model, int32_t n_frames, int32_t ckpt_every, F32 q0,
-                             F32 qd0, F32 act_seq, F32Out traj_q, F32Out traj_qd, S32Out status, U8Out residual) {
+ffi::Error RolloutVjpFwdImpl(cudaStream_t stream, int64_t model, int32_t n_frames, int32_t ckpt_every,
+                             int32_t inverse_mode, F32 q0, F32 qd0, F32 act_seq, F32Out traj_q, F32Out traj_qd,
+                             S32Out status, U8Out residual) {
   View a = in(q0), b = in(qd0), c = in(act_seq);
   View tq = out(traj_q), tqd = out(traj_qd), st = out(status), rs = out(residual);
   return to_error(braxg_xla::rollout_vjp_fwd(model_of(model), stream, n_frames, ckpt_every, a.buf, b.buf, c.buf,
-                                             tq.buf, tqd.buf, st.buf, rs.buf));
+                                             tq.buf, tqd.buf, st.buf, rs.buf, inverse_mode));
 }
 
 // `status_in` is the forward's status; jax_ops aliases it with the `status`
 // result (input_output_aliases), so both name one buffer.
-ffi::Error RolloutVjpBwdImpl(cudaStream_t stream, int64_t model, int32_t n_frames, int32_t ckpt_every, F32 q0,
-                             F32 qd0, F32 act_seq, U8 residual, F32 q_bar, F32 qd_bar, S32 status_in,
-                             F32Out act_bar, F32Out q0_bar, F32Out qd0_bar, S32Out status) {
+ffi::Error RolloutVjpBwdImpl(cudaStream_t stream, int64_t model, int32_t n_frames, int32_t ckpt_every,
+                             int32_t inverse_mode, F32 q0, F32 qd0, F32 act_seq, U8 residual, F32 q_bar,
+                             F32 qd_bar, S32 status_in, F32Out act_bar, F32Out q0_bar, F32Out qd0_bar,
+                             S32Out status) {
   (void)status_in;
   View a = in(q0), b = in(qd0), c = in(act_seq), r = in(residual), d = in(q_bar), e = in(qd_bar);
   View ab = out(act_bar), qb = out(q0_bar), qdb = out(qd0_bar), st = out(status);
   return to_error(braxg_xla::rollout_vjp_bwd(model_of(model), stream, n_frames, ckpt_every, a.buf, b.buf, c.buf,
-                                             r.buf, d.buf, e.buf, ab.buf, qb.buf, qdb.buf, st.buf));
+                                             r.buf, d.buf, e.buf, ab.buf, qb.buf, qdb.buf, st.buf, inverse_mode));
 }
 
 }  // namespace
@@ -175,6 +177,7 @@ XLA_FFI_DEFINE_HANDLER_SYMBOL(BraxgRolloutVjpFfi, RolloutVjpImpl,
                                   .Attr<int64_t>("model")
                                   .Attr<int32_t>("n_frames")
                                   .Attr<int32_t>("ckpt_every")
+                                  .Attr<int32_t>("inverse_mode")
                                   .Arg<F32>()   // q0
                                   .Arg<F32>()   // qd0
                                   .Arg<F32>()   // act_seq
@@ -191,6 +194,7 @@ XLA_FFI_DEFINE_HANDLER_SYMBOL(BraxgRolloutVjpFwdFfi, RolloutVjpFwdImpl,
                                   .Attr<int64_t>("model")
                                   .Attr<int32_t>("n_frames")
                                   .Attr<int32_t>("ckpt_every")
+                                  .Attr<int32_t>("inverse_mode")
                                   .Arg<F32>()   // q0
                                   .Arg<F32>()   // qd0
                                   .Arg<F32>()   // act_seq [T, .., nu]
@@ -205,6 +209,7 @@ XLA_FFI_DEFINE_HANDLER_SYMBOL(BraxgRolloutVjpBwdFfi, RolloutVjpBwdImpl,
                                   .Attr<int64_t>("model")
                                   .Attr<int32_t>("n_frames")
                                   .Attr<int32_t>("ckpt_every")
+                                  .Attr<int32_t>("inverse_mode")
                                   .Arg<F32>()   // q0
                                   .Arg<F32>()   // qd0
                                   .Arg<F32>()   // act_seq

@@ -175,16 +175,17 @@ inline size_t rollout_scratch_floats(const braxg_model* m, int64_t n) {
   return 2 * static_cast<size_t>(n) * d.nv * d.nv;
 }
 
-// Workspace bytes of rollout_vjp for these buffers (0 on a shape error).
+// Workspace bytes of rollout_vjp for these buffers (0 on a shape error);
+// inverse_mode as braxg_options.inverse_mode.
 inline size_t rollout_vjp_workspace(const braxg_model* m, int n_frames, int ckpt_every, const Buf& q0,
-                                    const Buf& act_seq) {
+                                    const Buf& act_seq, int inverse_mode = BRAXG_INV_CHOLESKY) {
   braxg_dims d;
   if (braxg_model_dims(m, &d)) return 0;
   const int64_t n = envs_of(q0, {d.nq});
   if (n < 0 || act_seq.rank < 1) return 0;
   size_t bytes = 0;
-  if (braxg_rollout_vjp_workspace(m, static_cast<int>(n), static_cast<int>(act_seq.dims[0]), n_frames, ckpt_every,
-                                  &bytes))
+  if (braxg_rollout_vjp_workspace_mode(m, static_cast<int>(n), static_cast<int>(act_seq.dims[0]), n_frames,
+                                       ckpt_every, 1, inverse_mode, &bytes))
     return 0;
   return bytes;
 }
@@ -197,7 +198,7 @@ inline size_t rollout_vjp_workspace(const braxg_model* m, int n_frames, int ckpt
 inline std::string rollout_vjp(const braxg_model* m, void* stream, int n_frames, int ckpt_every, const Buf& q0,
                                const Buf& qd0, const Buf& act_seq, const Buf& q_bar, const Buf& qd_bar,
                                const Buf& act_bar, const Buf& q0_bar, const Buf& qd0_bar, const Buf& status,
-                               void* workspace, size_t workspace_bytes) {
+                               void* workspace, size_t workspace_bytes, int inverse_mode = BRAXG_INV_CHOLESKY) {
   braxg_dims d;
   int rc = braxg_model_dims(m, &d);
   if (rc) return last_error("braxg_model_dims", rc);
@@ -216,7 +217,7 @@ inline std::string rollout_vjp(const braxg_model* m, void* stream, int n_frames,
     return "act_seq, q_bar, qd_bar and act_bar must share their leading (time) dimension";
   if (n > INT32_MAX || T > INT32_MAX || T < 1) return "the rollout needs 1 .. 2^31-1 steps and envs";
   braxg_options opt{};
-  opt.inverse_mode = BRAXG_INV_CHOLESKY;
+  opt.inverse_mode = inverse_mode;
   float* ab = d.nu ? act_bar.f() : nullptr;
   const float* as = d.nu ? act_seq.f() : nullptr;
   if (workspace == nullptr) {
@@ -235,22 +236,22 @@ inline std::string rollout_vjp(const braxg_model* m, void* stream, int n_frames,
 // gradient workspace with every checkpoint segment resident, so that the
 // reverse only reads it (0 on a shape error).
 inline size_t rollout_vjp_residual_bytes(const braxg_model* m, int n_frames, int ckpt_every, const Buf& q0,
-                                         const Buf& act_seq) {
+                                         const Buf& act_seq, int inverse_mode = BRAXG_INV_CHOLESKY) {
   braxg_dims d;
   if (braxg_model_dims(m, &d)) return 0;
   const int64_t n = envs_of(q0, {d.nq});
   if (n < 0 || act_seq.rank < 1) return 0;
   size_t bytes = 0;
-  if (braxg_rollout_vjp_workspace_resident(m, static_cast<int>(n), static_cast<int>(act_seq.dims[0]), n_frames,
-                                           ckpt_every, 0, &bytes))
+  if (braxg_rollout_vjp_workspace_mode(m, static_cast<int>(n), static_cast<int>(act_seq.dims[0]), n_frames,
+                                       ckpt_every, 0, inverse_mode, &bytes))
     return 0;
   return bytes;
 }
 
 // Checks the residual buffer (uint8 [bytes]) against what the sizes need.
 inline std::string expect_residual(const braxg_model* m, int n_frames, int ckpt_every, const Buf& q0,
-                                   const Buf& act_seq, const Buf& residual) {
-  const size_t need = rollout_vjp_residual_bytes(m, n_frames, ckpt_every, q0, act_seq);
+                                   const Buf& act_seq, const Buf& residual, int inverse_mode) {
+  const size_t need = rollout_vjp_residual_bytes(m, n_frames, ckpt_every, q0, act_seq, inverse_mode);
   if (need == 0) return "cannot size the gradient residual for q0 " + dims_str(q0);
   if (residual.rank != 1 || static_cast<size_t>(residual.dims[0]) < need)
     return "residual has shape " + dims_str(residual) + ", expected [" + std::to_string(need) + "]";
@@ -259,10 +260,11 @@ inline std::string expect_residual(const braxg_model* m, int n_frames, int ckpt_
 
 // jax.custom_vjp forward of the rollout: the trajectory traj_q [T, .., nq],
 // traj_qd [T, .., nv], status [..], and the residual (the forward's
-// checkpoints and frame snapshots) for rollout_vjp_bwd.
+// checkpoints and frame snapshots) for rollout_vjp_bwd; inverse_mode as
+// braxg_options.inverse_mode (the same for both halves).
 inline std::string rollout_vjp_fwd(const braxg_model* m, void* stream, int n_frames, int ckpt_every, const Buf& q0,
                                    const Buf& qd0, const Buf& act_seq, const Buf& traj_q, const Buf& traj_qd,
-                                   const Buf& status, const Buf& residual) {
+                                   const Buf& status, const Buf& residual, int inverse_mode = BRAXG_INV_CHOLESKY) {
   braxg_dims d;
   int rc = braxg_model_dims(m, &d);
   if (rc) return last_error("braxg_model_dims", rc);
@@ -277,9 +279,9 @@ inline std::string rollout_vjp_fwd(const braxg_model* m, void* stream, int n_fra
   if (traj_q.dims[0] != T || traj_qd.dims[0] != T)
     return "act_seq, traj_q and traj_qd must share their leading (time) dimension";
   if (n > INT32_MAX || T > INT32_MAX || T < 1) return "the rollout needs 1 .. 2^31-1 steps and envs";
-  BRAXG_XLA_TRY(expect_residual(m, n_frames, ckpt_every, q0, act_seq, residual));
+  BRAXG_XLA_TRY(expect_residual(m, n_frames, ckpt_every, q0, act_seq, residual, inverse_mode));
   braxg_options opt{};
-  opt.inverse_mode = BRAXG_INV_CHOLESKY;
+  opt.inverse_mode = inverse_mode;
   rc = braxg_rollout_vjp_fwd(m, stream, static_cast<int>(n), static_cast<int>(T), n_frames, ckpt_every,
                              d.nu ? act_seq.f() : nullptr, q0.f(), qd0.f(), traj_q.f(), traj_qd.f(), residual.data,
                              static_cast<size_t>(residual.dims[0]), static_cast<int32_t*>(status.data), &opt);
@@ -293,7 +295,7 @@ inline std::string rollout_vjp_fwd(const braxg_model* m, void* stream, int n_fra
 inline std::string rollout_vjp_bwd(const braxg_model* m, void* stream, int n_frames, int ckpt_every, const Buf& q0,
                                    const Buf& qd0, const Buf& act_seq, const Buf& residual, const Buf& q_bar,
                                    const Buf& qd_bar, const Buf& act_bar, const Buf& q0_bar, const Buf& qd0_bar,
-                                   const Buf& status) {
+                                   const Buf& status, int inverse_mode = BRAXG_INV_CHOLESKY) {
   braxg_dims d;
   int rc = braxg_model_dims(m, &d);
   if (rc) return last_error("braxg_model_dims", rc);
@@ -311,9 +313,9 @@ inline std::string rollout_vjp_bwd(const braxg_model* m, void* stream, int n_fra
   if (q_bar.dims[0] != T || qd_bar.dims[0] != T || act_bar.dims[0] != T)
     return "act_seq, q_bar, qd_bar and act_bar must share their leading (time) dimension";
   if (n > INT32_MAX || T > INT32_MAX || T < 1) return "the rollout needs 1 .. 2^31-1 steps and envs";
-  BRAXG_XLA_TRY(expect_residual(m, n_frames, ckpt_every, q0, act_seq, residual));
+  BRAXG_XLA_TRY(expect_residual(m, n_frames, ckpt_every, q0, act_seq, residual, inverse_mode));
   braxg_options opt{};
-  opt.inverse_mode = BRAXG_INV_CHOLESKY;
+  opt.inverse_mode = inverse_mode;
   rc = braxg_rollout_vjp_bwd(m, stream, static_cast<int>(n), static_cast<int>(T), n_frames, ckpt_every,
                              d.nu ? act_seq.f() : nullptr, q0.f(), qd0.f(), q_bar.f(), qd_bar.f(),
                              d.nu ? act_bar.f() : nullptr, q0_bar.f(), qd0_bar.f(), residual.data,

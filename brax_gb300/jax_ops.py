@@ -140,17 +140,17 @@ def step(sys, state: JaxState, act, n_frames: int = 1, inverse_mode: int = NEWTO
   return JaxState(*outs)
 
 
-def _rollout_call(handle, nq, nv, n_frames, q0, qd0, act_seq):
+def _rollout_call(handle, nq, nv, n_frames, q0, qd0, act_seq, inverse_mode=CHOLESKY):
   T, batch = act_seq.shape[0], q0.shape[:-1]
   out_types = (jax.ShapeDtypeStruct((T,) + batch + (nq,), jnp.float32),
                jax.ShapeDtypeStruct((T,) + batch + (nv,), jnp.float32),
                jax.ShapeDtypeStruct(batch, jnp.int32))
   call = jax.ffi.ffi_call('braxg_rollout', out_types, vmap_method='sequential')
   return call(q0, qd0, act_seq, model=np.int64(handle), n_frames=np.int32(n_frames),
-              inverse_mode=np.int32(CHOLESKY))
+              inverse_mode=np.int32(inverse_mode))
 
 
-def _vjp_call(handle, nq, nv, nu, n_frames, ckpt_every, q0, qd0, act_seq, q_bar, qd_bar):
+def _vjp_call(handle, nq, nv, nu, n_frames, ckpt_every, q0, qd0, act_seq, q_bar, qd_bar, inverse_mode=CHOLESKY):
   batch = q0.shape[:-1]
   out_types = (jax.ShapeDtypeStruct(act_seq.shape, jnp.float32),
                jax.ShapeDtypeStruct(batch + (nq,), jnp.float32),
@@ -158,32 +158,35 @@ def _vjp_call(handle, nq, nv, nu, n_frames, ckpt_every, q0, qd0, act_seq, q_bar,
                jax.ShapeDtypeStruct(batch, jnp.int32))
   call = jax.ffi.ffi_call('braxg_rollout_vjp', out_types, vmap_method='sequential')
   return call(q0, qd0, act_seq, q_bar, qd_bar, model=np.int64(handle), n_frames=np.int32(n_frames),
-              ckpt_every=np.int32(ckpt_every))
+              ckpt_every=np.int32(ckpt_every), inverse_mode=np.int32(inverse_mode))
 
 
-def _residual_bytes(handle, n_env, n_steps, n_frames, ckpt_every) -> int:
+def _residual_bytes(handle, n_env, n_steps, n_frames, ckpt_every, inverse_mode=CHOLESKY) -> int:
   """Bytes of the gradient workspace with every segment resident (the
-  residual of the split forward)."""
+  residual of the split forward), for the inverse mode's records."""
   nbytes = ctypes.c_size_t()
-  N.check(N.lib().braxg_rollout_vjp_workspace_resident(ctypes.c_void_p(handle), int(n_env), int(n_steps),
-                                                       int(n_frames), int(ckpt_every), 0, ctypes.byref(nbytes)),
-          'braxg_rollout_vjp_workspace_resident')
+  N.check(N.lib().braxg_rollout_vjp_workspace_mode(ctypes.c_void_p(handle), int(n_env), int(n_steps),
+                                                   int(n_frames), int(ckpt_every), 0, int(inverse_mode),
+                                                   ctypes.byref(nbytes)),
+          'braxg_rollout_vjp_workspace_mode')
   return int(nbytes.value)
 
 
-def _vjp_fwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq):
+def _vjp_fwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq, inverse_mode=CHOLESKY):
   T, batch = act_seq.shape[0], q0.shape[:-1]
   n = int(np.prod(batch)) if batch else 1
   out_types = (jax.ShapeDtypeStruct((T,) + batch + (nq,), jnp.float32),
                jax.ShapeDtypeStruct((T,) + batch + (nv,), jnp.float32),
                jax.ShapeDtypeStruct(batch, jnp.int32),
-               jax.ShapeDtypeStruct((_residual_bytes(handle, n, T, n_frames, ckpt_every),), jnp.uint8))
+               jax.ShapeDtypeStruct((_residual_bytes(handle, n, T, n_frames, ckpt_every, inverse_mode),),
+                                    jnp.uint8))
   call = jax.ffi.ffi_call('braxg_rollout_vjp_fwd', out_types, vmap_method='sequential')
   return call(q0, qd0, act_seq, model=np.int64(handle), n_frames=np.int32(n_frames),
-              ckpt_every=np.int32(ckpt_every))
+              ckpt_every=np.int32(ckpt_every), inverse_mode=np.int32(inverse_mode))
 
 
-def _vjp_bwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq, residual, status, q_bar, qd_bar):
+def _vjp_bwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq, residual, status, q_bar, qd_bar,
+                  inverse_mode=CHOLESKY):
   batch = q0.shape[:-1]
   out_types = (jax.ShapeDtypeStruct(act_seq.shape, jnp.float32),
                jax.ShapeDtypeStruct(batch + (nq,), jnp.float32),
@@ -193,27 +196,29 @@ def _vjp_bwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq, residu
   call = jax.ffi.ffi_call('braxg_rollout_vjp_bwd', out_types, vmap_method='sequential',
                           input_output_aliases={6: 3})
   return call(q0, qd0, act_seq, residual, q_bar, qd_bar, status, model=np.int64(handle),
-              n_frames=np.int32(n_frames), ckpt_every=np.int32(ckpt_every))
+              n_frames=np.int32(n_frames), ckpt_every=np.int32(ckpt_every), inverse_mode=np.int32(inverse_mode))
 
 
 @functools.lru_cache(maxsize=None)
-def _rollout_fn(handle: int, nq: int, nv: int, nu: int, n_frames: int, ckpt_every: int):
+def _rollout_fn(handle: int, nq: int, nv: int, nu: int, n_frames: int, ckpt_every: int, inverse_mode: int):
   """jax.custom_vjp rollout for one model and static configuration."""
 
   @jax.custom_vjp
   def roll(q0, qd0, act_seq):
-    tq, tqd, _ = _rollout_call(handle, nq, nv, n_frames, q0, qd0, act_seq)
+    tq, tqd, _ = _rollout_call(handle, nq, nv, n_frames, q0, qd0, act_seq, inverse_mode)
     return tq, tqd
 
   def fwd(q0, qd0, act_seq):
-    tq, tqd, status, residual = _vjp_fwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq)
+    tq, tqd, status, residual = _vjp_fwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq,
+                                              inverse_mode)
     return (tq, tqd), (q0, qd0, act_seq, residual, status)
 
   def bwd(res, g):
     q0, qd0, act_seq, residual, status = res
     gq, gqd = g
     act_bar, q0_bar, qd0_bar, _ = _vjp_bwd_call(handle, nq, nv, n_frames, ckpt_every, q0, qd0, act_seq, residual,
-                                                status, jnp.asarray(gq, jnp.float32), jnp.asarray(gqd, jnp.float32))
+                                                status, jnp.asarray(gq, jnp.float32), jnp.asarray(gqd, jnp.float32),
+                                                inverse_mode)
     return q0_bar, qd0_bar, act_bar
 
   roll.defvjp(fwd, bwd)
@@ -221,21 +226,24 @@ def _rollout_fn(handle: int, nq: int, nv: int, nu: int, n_frames: int, ckpt_ever
 
 
 def rollout_grad(sys, q0, qd0, act_seq, q_bar, qd_bar, n_frames: int = 1, ckpt_every: int = 16,
-                 device_id: int = 0):
+                 device_id: int = 0, inverse_mode: int = CHOLESKY):
   """(act_bar, q0_bar, qd0_bar, status) of the rollout for cotangents q_bar
   [T, n, nq], qd_bar [T, n, nv] in one fused launch (braxg_rollout_vjp)."""
   register()
   nl, nq, nv, nu = _dims(sys)
   return _vjp_call(model_handle(sys, device_id), nq, nv, nu, int(n_frames), int(ckpt_every),
                    jnp.asarray(q0, jnp.float32), jnp.asarray(qd0, jnp.float32), jnp.asarray(act_seq, jnp.float32),
-                   jnp.asarray(q_bar, jnp.float32), jnp.asarray(qd_bar, jnp.float32))
+                   jnp.asarray(q_bar, jnp.float32), jnp.asarray(qd_bar, jnp.float32), int(inverse_mode))
 
 
-def rollout(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16, device_id: int = 0):
-  """Differentiable rollout (exact-inverse mode): ``(traj_q, traj_qd)`` of
-  act_seq [T, n, nu] from q0 [n, nq], qd0 [n, nv]; gradients through the
-  hand-written adjoint."""
+def rollout(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16, device_id: int = 0,
+            inverse_mode: int = CHOLESKY):
+  """Differentiable rollout: ``(traj_q, traj_qd)`` of act_seq [T, n, nu]
+  from q0 [n, nq], qd0 [n, nv]; gradients through the hand-written adjoint.
+  inverse_mode CHOLESKY (default) computes the exact inverse every frame;
+  NEWTON_SCHULZ carries init's exact inverse through the reference's
+  Newton-Schulz update, and the gradient differentiates that update."""
   register()
   nl, nq, nv, nu = _dims(sys)
-  fn = _rollout_fn(model_handle(sys, device_id), nq, nv, nu, int(n_frames), int(ckpt_every))
+  fn = _rollout_fn(model_handle(sys, device_id), nq, nv, nu, int(n_frames), int(ckpt_every), int(inverse_mode))
   return fn(jnp.asarray(q0, jnp.float32), jnp.asarray(qd0, jnp.float32), jnp.asarray(act_seq, jnp.float32))

@@ -108,6 +108,13 @@ int braxg_rollout_vjp_workspace_resident(const braxg_model*, int, int, int, int,
   *bytes = resident <= 0 ? 2 * g_ws_bytes : g_ws_bytes;  // every segment resident: the larger workspace
   return 0;
 }
+// Newton-Schulz mode adds the per-frame records: 500 bytes more in the stub
+int braxg_rollout_vjp_workspace_mode(const braxg_model* m, int n_env, int n_steps, int n_frames, int ckpt_every,
+                                     int resident, int inverse_mode, size_t* bytes) {
+  braxg_rollout_vjp_workspace_resident(m, n_env, n_steps, n_frames, ckpt_every, resident, bytes);
+  if (inverse_mode == BRAXG_INV_NEWTON_SCHULZ) *bytes += 500;
+  return 0;
+}
 int braxg_rollout_vjp_fwd(const braxg_model*, void*, int n_env, int n_steps, int n_frames, int ckpt_every,
                           const float* act_seq, const float* q0, const float*, float* traj_q, float* traj_qd,
                           void* workspace, size_t workspace_bytes, int32_t* status, const braxg_options* opt) {
@@ -294,6 +301,15 @@ int main() {
     e = braxg_xla::rollout_vjp(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), qb.buf(), qdb_bad.buf(), ab.buf(),
                                q0b.buf(), qd0b.buf(), st.buf(), ws.data(), bytes);
     CHECK(contains(e, "qd_bar has shape"));
+    // the reference's inverse mode: its workspace and the option reach the call
+    const size_t ns_bytes = braxg_xla::rollout_vjp_workspace(&m, 5, 2, q0.buf(), a.buf(), BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(ns_bytes == 12345 + 500);
+    std::vector<char> ws_ns(ns_bytes);
+    g_calls.clear();
+    e = braxg_xla::rollout_vjp(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), qb.buf(), qdb.buf(), ab.buf(),
+                               q0b.buf(), qd0b.buf(), st.buf(), ws_ns.data(), ns_bytes, BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(e.empty() && g_calls.size() == 1 && g_calls[0].inverse_mode == BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(g_calls[0].ws_bytes == ns_bytes);
   }
   // ---- rollout_vjp_fwd / rollout_vjp_bwd: the custom_vjp halves and their residual ----
   {
@@ -339,6 +355,25 @@ int main() {
     e = braxg_xla::rollout_vjp_fwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), tq_bad.buf(), tqd.buf(),
                                    st.buf(), rbuf);
     CHECK(contains(e, "leading (time) dimension") && g_calls.empty());
+    // Newton-Schulz mode: its residual holds the per-frame records too, and
+    // the Cholesky-sized residual is refused for it
+    const size_t need_ns =
+        braxg_xla::rollout_vjp_residual_bytes(&m, 5, 2, q0.buf(), a.buf(), BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(need_ns == 2500);
+    g_calls.clear();
+    e = braxg_xla::rollout_vjp_fwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), tq.buf(), tqd.buf(), st.buf(),
+                                   rbuf, BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(contains(e, "residual has shape") && g_calls.empty());
+    std::vector<int64_t> nsdims = {static_cast<int64_t>(need_ns)};
+    std::vector<unsigned char> res_ns(need_ns);
+    braxg_xla::Buf rns{res_ns.data(), nsdims.data(), 1};
+    e = braxg_xla::rollout_vjp_fwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), tq.buf(), tqd.buf(), st.buf(),
+                                   rns, BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(e.empty() && g_calls.size() == 1 && g_calls[0].inverse_mode == BRAXG_INV_NEWTON_SCHULZ);
+    e = braxg_xla::rollout_vjp_bwd(&m, nullptr, 5, 2, q0.buf(), qd0.buf(), a.buf(), rns, qb.buf(), qdb.buf(),
+                                   ab.buf(), q0b.buf(), qd0b.buf(), st.buf(), BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(e.empty() && g_calls.size() == 2 && g_calls[1].inverse_mode == BRAXG_INV_NEWTON_SCHULZ);
+    CHECK(g_calls[1].ws_bytes == need_ns);
   }
   std::printf("ok %d\n", g_checks);
   return 0;
