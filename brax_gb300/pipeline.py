@@ -585,30 +585,34 @@ def rollout_vjp_bwd(tape: VjpTape, q_bar=None, qd_bar=None):
 class Rollout(torch.autograd.Function):
   """Differentiable rollout for torch: (q0, qd0, act_seq) -> (traj_q, traj_qd).
 
-  The forward runs braxg_rollout_vjp_fwd (exact-inverse mode; the
-  checkpoints and frame snapshots stay in a workspace held by the graph); the
-  backward runs the hand-written reverse on it (braxg_rollout_vjp_bwd).
+  The forward runs braxg_rollout_vjp_fwd (the checkpoints and frame
+  snapshots stay in a workspace held by the graph); the backward runs the
+  hand-written reverse on it (braxg_rollout_vjp_bwd).
   """
 
   @staticmethod
-  def forward(ctx, q0, qd0, act_seq, sys, n_frames, ckpt_every):
+  def forward(ctx, q0, qd0, act_seq, sys, n_frames, ckpt_every, inverse_mode=CHOLESKY):
     (tq, tqd), ctx.tape = rollout_vjp_fwd(sys, q0.detach(), qd0.detach(), act_seq.detach(), n_frames=n_frames,
-                                          ckpt_every=ckpt_every)
+                                          ckpt_every=ckpt_every, inverse_mode=inverse_mode)
     return tq, tqd
 
   @staticmethod
   def backward(ctx, gq, gqd):
     act_bar, q0_bar, qd0_bar, _ = rollout_vjp_bwd(ctx.tape, gq, gqd)
-    return q0_bar, qd0_bar, act_bar, None, None, None
+    return q0_bar, qd0_bar, act_bar, None, None, None, None
 
 
-def differentiable_rollout(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16):
+def differentiable_rollout(sys, q0, qd0, act_seq, n_frames: int = 1, ckpt_every: int = 16,
+                           inverse_mode: int = CHOLESKY):
   """torch.autograd-enabled rollout returning (traj_q, traj_qd).  With a
   gradient to take, the forward is braxg_rollout_vjp_fwd (its checkpoints and
   frame snapshots kept for the backward, which runs only the reverse);
-  without one, a plain braxg_rollout."""
+  without one, a plain braxg_rollout.  inverse_mode CHOLESKY computes the
+  exact inverse every frame; NEWTON_SCHULZ carries pipeline.init's exact
+  inverse through the reference's Newton-Schulz update (and differentiates
+  it)."""
   if torch.is_grad_enabled() and any(t.requires_grad for t in (q0, qd0, act_seq)):
-    return Rollout.apply(q0, qd0, act_seq, sys, n_frames, ckpt_every)
-  _, (tq, tqd) = rollout(sys, bare_state(q0, qd0), act_seq, n_frames=n_frames, inverse_mode=CHOLESKY,
-                         trajectory=True)
+    return Rollout.apply(q0, qd0, act_seq, sys, n_frames, ckpt_every, int(inverse_mode))
+  s0 = bare_state(q0, qd0) if inverse_mode == CHOLESKY else init(sys, q0, qd0)
+  _, (tq, tqd) = rollout(sys, s0, act_seq, n_frames=n_frames, inverse_mode=inverse_mode, trajectory=True)
   return tq, tqd

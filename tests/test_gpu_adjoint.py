@@ -151,6 +151,17 @@ def test_newton_schulz_gradient(name):
   for other in (small, split):
     for a_, b_ in zip(other[:3], fused[:3]):
       torch.testing.assert_close(a_, b_, rtol=0, atol=0)
+  # torch.autograd through differentiable_rollout: the same bits, and without
+  # a gradient to take the plain Newton-Schulz rollout
+  ut = _t(u).requires_grad_(True)
+  dq, dqd = P.differentiable_rollout(sys_, _t(q0), _t(qd0), ut, n_frames=F, ckpt_every=k, inverse_mode=NS)
+  ((dq * _t(q_bar)).sum() + (dqd * _t(qd_bar)).sum()).backward()
+  with torch.no_grad():
+    pq, pqd = P.differentiable_rollout(sys_, _t(q0), _t(qd0), _t(u), n_frames=F, inverse_mode=NS)
+  torch.cuda.synchronize()
+  for a_, b_ in ((dq, rq), (dqd, rqd), (pq, rq), (pqd, rqd)):
+    torch.testing.assert_close(a_.detach(), b_, rtol=0, atol=0)
+  torch.testing.assert_close(ut.grad, fused[0], rtol=0, atol=0)
   # against FP64 central differences of the Newton-Schulz rollout
   o = Oracle(sys_, np.float64, exact_inverse=False)
 
@@ -189,6 +200,63 @@ def test_newton_schulz_gradient(name):
           f'max {e.max():.2e}')
   for e in errs:
     assert np.median(e) <= 1e-3 and (e <= 1e-2).mean() >= 7 / 8
+
+
+def test_newton_schulz_gradient_reset():
+  """The reset branch of the Newton-Schulz update on the GPU: a hanging chain
+  of 16 links (mass-matrix condition 2e5) whose carried inverse resets to
+  0.5 M^T / tr(M M^T) (brax/math.py:292-295) on the frames after the first;
+  one env step of 3 frames, gradient against FP64 central differences of the
+  FP64 Newton-Schulz rollout.  The oracle's tape of the same step shows the
+  resets."""
+  P = _P()
+  from brax_gb300 import workloads
+  from oracle.adjoint import StepAdjoint
+  from oracle.pipeline import Oracle
+  sys_ = workloads.chain(16)
+  n, F = 4, 3
+  o = Oracle(sys_, np.float64, exact_inverse=False)
+  q, qd = workloads.reset(sys_, n, np.random.default_rng(11))
+  s = o.init(q, qd)
+  rng = np.random.default_rng(12)
+  for _ in range(3):
+    s = o.step(s, actions(sys_, n, rng))
+  q0, qd0 = s.q.astype(np.float32).astype(np.float64), s.qd.astype(np.float32).astype(np.float64)
+  act = actions(sys_, n, rng).astype(np.float32).astype(np.float64)
+  # the resets happen on this step (FP64 tape of the same frames)
+  adj = StepAdjoint(sys_, newton_schulz=True)
+  qq, qqd, minv, resets = q0, qd0, None, 0
+  for f in range(F):
+    qq, qqd, T = adj.forward(qq, qqd, act, minv)
+    minv = T['s'].mass_mx_inv
+    if f > 0:
+      resets += int(T['ns']['reset'].sum())
+  assert resets > 0
+  qbo, qdbo = rng.normal(size=(n, sys_.q_size())), rng.normal(size=(n, sys_.qd_size()))
+  act_bar, q0_bar, qd0_bar, status, _ = P.rollout_grad(
+      sys_, _t(q0), _t(qd0), _t(act[None]), _t(qbo[None]), _t(qdbo[None]), n_frames=F, ckpt_every=1,
+      inverse_mode=P.NEWTON_SCHULZ)
+  torch.cuda.synchronize()
+  assert (status.cpu().numpy() == 0).all()
+
+  def f(q_, qd_, a_):
+    r = o.env_step(o.init(q_, qd_), a_, F)
+    return np.sum(qbo * r.q, -1) + np.sum(qdbo * r.qd, -1)
+
+  eps = 1e-6
+  for which, got in enumerate((q0_bar.cpu().numpy(), qd0_bar.cpu().numpy(), act_bar[0].cpu().numpy())):
+    base = [q0, qd0, act]
+    fd = np.zeros_like(got, dtype=np.float64)
+    for j in range(got.shape[1]):
+      a_ = [x.copy() for x in base]
+      a_[which][:, j] += eps
+      fp = f(*a_)
+      a_[which][:, j] -= 2 * eps
+      fd[:, j] = (fp - f(*a_)) / (2 * eps)
+    e = _rel(got, fd)
+    print(f'chain16 Newton-Schulz (resets {resets}) gradient vs FP64 FD ({["q0", "qd0", "act"][which]}): '
+          f'per env {np.array2string(e, precision=2)}')
+    assert np.median(e) <= 1e-2
 
 
 def test_torch_autograd_function():
