@@ -17,11 +17,14 @@ struct AdjLayout {
   int Minvb, Mb, Minvbc, Jb, diagb, arefb, bb, xb, Ab, tape;
   int xpb, xrb, cib, cpb, cdb, rcb, cdofb, cdofdb;
   int tmp, tmp_words;
+  int ns;  // Newton-Schulz mode: the inverse reverse's working set (ns_rev_smem_words), else -1
   int total;
 };
 
+// `ns_words`: words of the Newton-Schulz reverse's shared working set (0
+// in exact-inverse mode).
 __host__ __device__ inline AdjLayout make_adj_layout(int nl, int nq, int nv, int nu, int ncon, int nlim,
-                                                     int pg_iters) {
+                                                     int pg_iters, int ns_words = 0) {
   AdjLayout A;
   const int m = 4 * ncon + nlim;
   // rows of the explicit solve's A cotangent; the row cotangents cover all m
@@ -81,6 +84,7 @@ __host__ __device__ inline AdjLayout make_adj_layout(int nl, int nq, int nv, int
   t += 16;
   A.tmp_words = al4(t);
   A.tmp = take(A.tmp_words);
+  A.ns = ns_words > 0 ? take(ns_words) : -1;
   A.total = al4(o);
   return A;
 }
@@ -787,37 +791,69 @@ __device__ __noinline__ void rev_inverse(const int* mw, Ws w, AWs a) {
 
 // n x n product by lanes over C's entries: C = alpha op(A) op(B + id I),
 // added to C when `acc`; op transposes when ta / tb.  Works on any memory.
+// Each lane runs four of its entries' dot products side by side (four
+// independent chains, their loads in flight together); every entry is still
+// one chain over k in ascending order.
 template <int T>
 __device__ void gemm_small(const Team<T>& tm, int n, const float* A, int lda, bool ta, const float* B, int ldb,
                            bool tb, float id, float* C, int ldc, float alpha, bool acc) {
-  for (int e = tm.lane; e < n * n; e += T) {
-    const int i = e / n, j = e - i * n;
-    float s = 0.f;
-    for (int k = 0; k < n; ++k) {
-      const float av = ta ? A[k * lda + i] : A[i * lda + k];
-      const float bv = (tb ? B[j * ldb + k] : B[k * ldb + j]) + (k == j ? id : 0.f);
-      s = fmaf(av, bv, s);
+  constexpr int G = 4;
+  const int nn = n * n;
+  const int sa = ta ? lda : 1, sb = tb ? 1 : ldb;
+  for (int e0 = tm.lane; e0 < nn; e0 += G * T) {
+    const float* pa[G];
+    const float* pb[G];
+    int jj[G];
+    float s[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int e = e0 + g * T < nn ? e0 + g * T : e0;  // past the end: a copy of the first entry, not stored
+      const int i = e / n, j = e - i * n;
+      pa[g] = ta ? A + i : A + i * lda;
+      pb[g] = tb ? B + j * ldb : B + j;
+      jj[g] = j;
+      s[g] = 0.f;
     }
-    C[i * ldc + j] = acc ? fmaf(alpha, s, C[i * ldc + j]) : alpha * s;
+    for (int k = 0; k < n; ++k) {
+#pragma unroll
+      for (int g = 0; g < G; ++g) s[g] = fmaf(pa[g][k * sa], pb[g][k * sb] + (k == jj[g] ? id : 0.f), s[g]);
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      const int e = e0 + g * T;
+      if (e < nn) {
+        const int i = e / n, j = e - i * n;
+        C[i * ldc + j] = acc ? fmaf(alpha, s[g], C[i * ldc + j]) : alpha * s[g];
+      }
+    }
   }
   tm.sync();
 }
 
-// Words of rev_ns's per-env scratch (global memory).
+// Words of rev_ns's per-env scratch in global memory: the recompute's tape.
 __host__ __device__ inline int ns_rev_scratch_words(int n, int nvb, int num_iter) {
+  return al4(ns_tape_words(n, nvb, num_iter));
+}
+// Words of rev_ns's shared working set (the AdjLayout's `ns` region): M and
+// the iterate (n x ld each), the update's scratch, the staged iterate and
+// residual of one iteration, and five cotangents (n x tape stride each).
+__host__ __device__ inline int ns_rev_smem_words(int n, int nvb) {
   const int ld = n | 1, lb = ns_tape_stride(n, nvb);
   const int s1 = nvb <= 16 ? 3 * n * ns_ldb(n) : 2 * n * ld;
-  return al4(n * ld) + al4(s1) + al4(ns_tape_words(n, nvb, num_iter)) + 5 * al4(n * lb);
+  return 2 * al4(n * ld) + al4(s1) + 7 * al4(n * lb);
 }
 
 // mass.matrix_inv reverse in Newton-Schulz mode (brax/math.py:278-305, under
 // jax.grad): the frame's inverse is the update of the carried one against M.
 // From the frame's record (M, then the carried inverse before the update;
-// n x ld each) the update is recomputed with its tape (the same calls, so the
-// same decisions bit for bit), then reversed: Minvb (the result's cotangent)
-// -> Mb, and the carried inverse's cotangent into Minvbc.  The reset and the
-// acceptance decisions are piecewise constant.  `scr`: ns_rev_scratch_words
-// of global memory, 16-byte aligned.
+// n x ld each, global memory) the update is recomputed with its tape (the
+// same calls, so the same decisions bit for bit), then reversed: Minvb (the
+// result's cotangent) -> Mb, and the carried inverse's cotangent into
+// Minvbc.  The reset and the acceptance decisions are piecewise constant.
+// The recompute and the products run in the env's shared `ns` region
+// (ns_rev_smem_words); only the tape goes to `scr` (ns_rev_scratch_words of
+// global memory), and each iteration's iterate and residual are staged back
+// into shared memory before its reverse.
 template <int T, int NVB>
 __device__ __noinline__ void rev_ns(const int* mw, Ws w, AWs a, const float* rec, float* scr, int num_iter) {
   const Model md(mw);
@@ -825,19 +861,30 @@ __device__ __noinline__ void rev_ns(const int* mw, Ws w, AWs a, const float* rec
   const Layout& L = *w.L;
   const AdjLayout& A = *a.A;
   const int n = md.nv, ld = L.ldm, lb = ns_tape_stride(n, NVB);
-  const float* Mr = rec;
-  const float* X0 = rec + n * ld;
-  float* P = scr;
+  float* Mr = a.at(A.ns);
+  float* P = Mr + al4(n * ld);
   float* S1 = P + al4(n * ld);
-  float* tape = S1 + al4(NVB <= 16 ? 3 * n * ns_ldb(n) : 2 * n * ld);
-  float* xb = tape + al4(ns_tape_words(n, NVB, num_iter));
+  float* Xk = S1 + al4(NVB <= 16 ? 3 * n * ns_ldb(n) : 2 * n * ld);
+  float* Rk = Xk + al4(n * lb);
+  float* xb = Rk + al4(n * lb);
   float* rbar = xb + al4(n * lb);
   float* xnb = rbar + al4(n * lb);
   float* cand = xnb + al4(n * lb);
   float* x0b = cand + al4(n * lb);
+  float* tape = scr;
   const float* Minvb = a.at(A.Minvb);
   float* Mb = a.at(A.Mb);
-  for (int e = tm.lane; e < n * ld; e += T) P[e] = X0[e];
+  for (int e = tm.lane; e < n * ld; e += T) {
+    Mr[e] = rec[e];
+    P[e] = rec[n * ld + e];
+  }
+  tm.sync();
+  // the carried inverse X0 (P before the update overwrites it) waits in
+  // x0b's words for the reverse of r0 = I - M X0, which x0b's own product follows
+  for (int e = tm.lane; e < n * n; e += T) {
+    const int i = e / n, j = e - i * n;
+    x0b[i * lb + j] = P[i * ld + j];
+  }
   tm.sync();
   ns_update<T, NVB>(tm, n, Mr, ld, P, S1, num_iter, tape);
   for (int e = tm.lane; e < n * n; e += T) {
@@ -849,8 +896,14 @@ __device__ __noinline__ void rev_ns(const int* mw, Ws w, AWs a, const float* rec
   tm.sync();
   for (int k = num_iter - 1; k >= 0; --k) {
     const bool keep = tape[4 + k] != 0.f;
-    const float* Xk = tape + 4 + al4(num_iter) + 2 * k * n * lb;
-    const float* Rk = Xk + n * lb;
+    {  // stage the iteration's iterate and residual (n x lb each, consecutive in the tape)
+      const float* src = tape + 4 + al4(num_iter) + 2 * k * n * lb;
+      for (int e = tm.lane; e < n * lb; e += T) {
+        Xk[e] = src[e];
+        Rk[e] = src[n * lb + e];
+      }
+      tm.sync();
+    }
     gemm_small<T>(tm, n, Xk, lb, false, Rk, lb, false, 1.f, cand, lb, 1.f, false);  // the candidate Xk (I + Rk)
     for (int e = tm.lane; e < n * n; e += T) {  // kept: its cotangent is the result's; else the iterate's
       const int i = e / n, j = e - i * n;
@@ -866,7 +919,7 @@ __device__ __noinline__ void rev_ns(const int* mw, Ws w, AWs a, const float* rec
     gemm_small<T>(tm, n, Xk, lb, true, xnb, lb, false, 0.f, rbar, lb, 1.f, false);
   }
   // r0 = I - M X0 (of the carried inverse, whether or not it was reset)
-  gemm_small<T>(tm, n, rbar, lb, false, X0, ld, true, 0.f, Mb, ld, -1.f, true);
+  gemm_small<T>(tm, n, rbar, lb, false, x0b, lb, true, 0.f, Mb, ld, -1.f, true);
   gemm_small<T>(tm, n, Mr, ld, true, rbar, lb, false, 0.f, x0b, lb, -1.f, false);
   float* Minvbc = a.at(A.Minvbc);
   if (tape[0] != 0.f) {  // reset: x = 0.5 M^T / s, s = tr(M M^T)

@@ -33,7 +33,8 @@ static int vjp_n_ckpt(int n_steps, int ckpt_every) { return (n_steps + ckpt_ever
 // In Newton-Schulz mode a checkpoint also holds the carried inverse
 // (nv x nv), and two parts follow the snapshots: per snapshotted frame its
 // record (M and the carried inverse its update started from, nv x ld each),
-// and per env the reverse's scratch (ns_rev_scratch_words).
+// and per env the reverse's scratch (ns_rev_scratch_words: the recompute's
+// tape; the reverse's other matrices live in shared memory).
 static int vjp_nvb(const braxg_model* m) { return m->dims.nv <= 16 ? 16 : 32; }
 static int vjp_ns_rec_words(const braxg_model* m) {
   return braxg::al4(2 * m->dims.nv * (m->dims.nv | 1));
@@ -169,7 +170,8 @@ static int run_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, i
   a.prof = opt ? opt->stage_cycles : nullptr;
   a.phases = phases;
   braxg::AdjLayout A = braxg::make_adj_layout(m->dims.nl, m->dims.nq, m->dims.nv, m->dims.nu, m->dims.ncon,
-                                              m->dims.nlim, m->h[BXM_H_PG_ITERS]);
+                                              m->dims.nlim, m->h[BXM_H_PG_ITERS],
+                                              ns ? braxg::ns_rev_smem_words(m->dims.nv, vjp_nvb(m)) : 0);
   int head = (braxg::al4(m->words) + 2 * braxg::kLayoutWords) * 4;
   int env_bytes = (m->L.total + A.total) * 4;
   int epc = (kMaxSmem - head) / env_bytes;

@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256, 1) vjp_kernel(const VjpArgs a) {
     const int* w0 = a.model;
     *sl = layout_of(w0);
     *sal = make_adj_layout(w0[BXM_H_NL], w0[BXM_H_NQ], w0[BXM_H_NV], w0[BXM_H_NU], w0[BXM_H_NCON], w0[BXM_H_NLIM],
-                           w0[BXM_H_PG_ITERS]);
+                           w0[BXM_H_PG_ITERS], a.ns_iters > 0 ? ns_rev_smem_words(w0[BXM_H_NV], NVB) : 0);
   }
   __syncthreads();
   const int* mw = smem;

@@ -208,7 +208,9 @@ def test_newton_schulz_gradient_reset():
   0.5 M^T / tr(M M^T) (brax/math.py:292-295) on the frames after the first;
   one env step of 3 frames, gradient against FP64 central differences of the
   FP64 Newton-Schulz rollout.  The oracle's tape of the same step shows the
-  resets."""
+  resets.  Bar: every env within 5e-3; FP32 rounding in this model's
+  inverse is of order cond(M) x 6e-8 ~ 1e-2 relative in the worst
+  direction (measured: 5e-5 .. 2.4e-3)."""
   P = _P()
   from brax_gb300 import workloads
   from oracle.adjoint import StepAdjoint
@@ -255,8 +257,8 @@ def test_newton_schulz_gradient_reset():
       fd[:, j] = (fp - f(*a_)) / (2 * eps)
     e = _rel(got, fd)
     print(f'chain16 Newton-Schulz (resets {resets}) gradient vs FP64 FD ({["q0", "qd0", "act"][which]}): '
-          f'per env {np.array2string(e, precision=2)}')
-    assert np.median(e) <= 1e-2
+          f'per env {" ".join(f"{v:.2e}" for v in e)}')
+    assert e.max() <= 5e-3
 
 
 def test_torch_autograd_function():
