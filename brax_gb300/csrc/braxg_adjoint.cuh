@@ -789,43 +789,60 @@ __device__ __noinline__ void rev_inverse(const int* mw, Ws w, AWs a) {
   tm.sync();
 }
 
-// n x n product by lanes over C's entries: C = alpha op(A) op(B + id I),
-// added to C when `acc`; op transposes when ta / tb.  Works on any memory.
-// Each lane runs four of its entries' dot products side by side (four
-// independent chains, their loads in flight together); every entry is still
-// one chain over k in ascending order.
-template <int T>
-__device__ void gemm_small(const Team<T>& tm, int n, const float* A, int lda, bool ta, const float* B, int ldb,
-                           bool tb, float id, float* C, int ldc, float alpha, bool acc) {
-  constexpr int G = 4;
-  const int nn = n * n;
-  const int sa = ta ? lda : 1, sb = tb ? 1 : ldb;
-  for (int e0 = tm.lane; e0 < nn; e0 += G * T) {
-    const float* pa[G];
-    const float* pb[G];
-    int jj[G];
-    float s[G];
+// n x n product C = alpha A B of row-major NVB x NVB blocks (rows and
+// columns from n up to NVB zero), added to C when `acc`; C's entry (i, j)
+// goes to C[i * cr + j * cc] (cc = NVB, cr = 1 writes the transpose).
+// Register-tiled like matmul: the lanes form an RB x CB grid, each lane owns
+// a TR x TC block of C, and A's rows and B's rows are read with 16-byte loads;
+// every entry is one chain over k in ascending order (the zero padding adds
+// exact zeros past n).
+template <int T, int NVB>
+__device__ void gemm_rr(const Team<T>& tm, int n, const float* A, const float* B, float* C, int cr, int cc,
+                        float alpha, bool acc) {
+  using G = MMTile<T, NVB>;
+  static_assert(G::tiled && G::TC % 4 == 0, "gemm_rr needs a register tile of 16-byte rows");
+  constexpr int lr = NVB;
+  const int rb = tm.lane / G::CB, cb = tm.lane - rb * G::CB;
+  const int i0 = rb * G::TR, j0 = cb * G::TC;
+  if (i0 < n && j0 < n) {
+    float s[G::TR][G::TC];
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int e = e0 + g * T < nn ? e0 + g * T : e0;  // past the end: a copy of the first entry, not stored
-      const int i = e / n, j = e - i * n;
-      pa[g] = ta ? A + i : A + i * lda;
-      pb[g] = tb ? B + j * ldb : B + j;
-      jj[g] = j;
-      s[g] = 0.f;
-    }
-    for (int k = 0; k < n; ++k) {
+    for (int r = 0; r < G::TR; ++r)
 #pragma unroll
-      for (int g = 0; g < G; ++g) s[g] = fmaf(pa[g][k * sa], pb[g][k * sb] + (k == jj[g] ? id : 0.f), s[g]);
-    }
+      for (int c = 0; c < G::TC; ++c) s[r][c] = 0.f;
+    for (int k4 = 0; k4 < n; k4 += 4) {
+      float4 a4[G::TR];
 #pragma unroll
-    for (int g = 0; g < G; ++g) {
-      const int e = e0 + g * T;
-      if (e < nn) {
-        const int i = e / n, j = e - i * n;
-        C[i * ldc + j] = acc ? fmaf(alpha, s[g], C[i * ldc + j]) : alpha * s[g];
+      for (int r = 0; r < G::TR; ++r) a4[r] = *reinterpret_cast<const float4*>(A + (i0 + r) * lr + k4);
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {
+        float bv[G::TC];
+#pragma unroll
+        for (int c4 = 0; c4 < G::TC / 4; ++c4) {
+          const float4 v = *reinterpret_cast<const float4*>(B + (k4 + kk) * lr + j0 + 4 * c4);
+          bv[4 * c4] = v.x;
+          bv[4 * c4 + 1] = v.y;
+          bv[4 * c4 + 2] = v.z;
+          bv[4 * c4 + 3] = v.w;
+        }
+#pragma unroll
+        for (int r = 0; r < G::TR; ++r) {
+          const float av = kk == 0 ? a4[r].x : kk == 1 ? a4[r].y : kk == 2 ? a4[r].z : a4[r].w;
+#pragma unroll
+          for (int c = 0; c < G::TC; ++c) s[r][c] = fmaf(av, bv[c], s[r][c]);
+        }
       }
     }
+#pragma unroll
+    for (int r = 0; r < G::TR; ++r)
+#pragma unroll
+      for (int c = 0; c < G::TC; ++c) {
+        const int i = i0 + r, j = j0 + c;
+        if (i < n && j < n) {
+          float* o = C + i * cr + j * cc;
+          *o = acc ? fmaf(alpha, s[r][c], *o) : alpha * s[r][c];
+        }
+      }
   }
   tm.sync();
 }
@@ -834,13 +851,15 @@ __device__ void gemm_small(const Team<T>& tm, int n, const float* A, int lda, bo
 __host__ __device__ inline int ns_rev_scratch_words(int n, int nvb, int num_iter) {
   return al4(ns_tape_words(n, nvb, num_iter));
 }
-// Words of rev_ns's shared working set (the AdjLayout's `ns` region): M and
-// the iterate (n x ld each), the update's scratch, the staged iterate and
-// residual of one iteration, and five cotangents (n x tape stride each).
+// Words of rev_ns's shared working set (the AdjLayout's `ns` region): M
+// (n x ld), the carried inverse's transpose (an nvb x nvb block), then the
+// recompute's iterate and scratch, whose words the reverse's ten nvb x nvb
+// blocks take over once the recompute is done.
 __host__ __device__ inline int ns_rev_smem_words(int n, int nvb) {
-  const int ld = n | 1, lb = ns_tape_stride(n, nvb);
+  const int ld = n | 1;
   const int s1 = nvb <= 16 ? 3 * n * ns_ldb(n) : 2 * n * ld;
-  return 2 * al4(n * ld) + al4(s1) + 7 * al4(n * lb);
+  const int upd = al4(n * ld) + al4(s1), rev = 10 * nvb * nvb;
+  return al4(n * ld) + nvb * nvb + (upd > rev ? upd : rev);
 }
 
 // mass.matrix_inv reverse in Newton-Schulz mode (brax/math.py:278-305, under
@@ -852,75 +871,91 @@ __host__ __device__ inline int ns_rev_smem_words(int n, int nvb) {
 // Minvbc.  The reset and the acceptance decisions are piecewise constant.
 // The recompute and the products run in the env's shared `ns` region
 // (ns_rev_smem_words); only the tape goes to `scr` (ns_rev_scratch_words of
-// global memory), and each iteration's iterate and residual are staged back
-// into shared memory before its reverse.
+// global memory).  The reverse keeps every matrix as a zero-padded NVB x NVB
+// row-major block, transposes included (M^T, X0^T, and per iteration the
+// staged X_k, X_k^T, I + R_k and its transpose), so that each product is a
+// gemm_rr of 16-byte rows.
 template <int T, int NVB>
 __device__ __noinline__ void rev_ns(const int* mw, Ws w, AWs a, const float* rec, float* scr, int num_iter) {
   const Model md(mw);
   const Team<T> tm;
   const Layout& L = *w.L;
   const AdjLayout& A = *a.A;
+  constexpr int lr = NVB, bb = NVB * NVB;
   const int n = md.nv, ld = L.ldm, lb = ns_tape_stride(n, NVB);
   float* Mr = a.at(A.ns);
-  float* P = Mr + al4(n * ld);
+  float* X0T = Mr + al4(n * ld);
+  float* P = X0T + bb;  // the recompute: the iterate, then the update's scratch
   float* S1 = P + al4(n * ld);
-  float* Xk = S1 + al4(NVB <= 16 ? 3 * n * ns_ldb(n) : 2 * n * ld);
-  float* Rk = Xk + al4(n * lb);
-  float* xb = Rk + al4(n * lb);
-  float* rbar = xb + al4(n * lb);
-  float* xnb = rbar + al4(n * lb);
-  float* cand = xnb + al4(n * lb);
-  float* x0b = cand + al4(n * lb);
+  float* MrT = P;  // the reverse, once the recompute is done
+  float* Xk = MrT + bb;
+  float* XkT = Xk + bb;
+  float* RkI = XkT + bb;
+  float* RkIT = RkI + bb;
+  float* candT = RkIT + bb;
+  float* xb = candT + bb;
+  float* rbar = xb + bb;
+  float* xnb = rbar + bb;
+  float* x0b = xnb + bb;
   float* tape = scr;
   const float* Minvb = a.at(A.Minvb);
   float* Mb = a.at(A.Mb);
+  for (int e = tm.lane; e < bb; e += T) X0T[e] = 0.f;
   for (int e = tm.lane; e < n * ld; e += T) {
     Mr[e] = rec[e];
     P[e] = rec[n * ld + e];
   }
   tm.sync();
-  // the carried inverse X0 (P before the update overwrites it) waits in
-  // x0b's words for the reverse of r0 = I - M X0, which x0b's own product follows
-  for (int e = tm.lane; e < n * n; e += T) {
+  for (int e = tm.lane; e < n * n; e += T) {  // X0^T, before the update overwrites P
     const int i = e / n, j = e - i * n;
-    x0b[i * lb + j] = P[i * ld + j];
+    X0T[j * lr + i] = P[i * ld + j];
   }
   tm.sync();
   ns_update<T, NVB>(tm, n, Mr, ld, P, S1, num_iter, tape);
+  {
+    float4* z = reinterpret_cast<float4*>(MrT);
+    for (int e = tm.lane; e < 10 * bb / 4; e += T) z[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    tm.sync();
+  }
   for (int e = tm.lane; e < n * n; e += T) {
     const int i = e / n, j = e - i * n;
-    xb[i * lb + j] = Minvb[i * ld + j];
-    rbar[i * lb + j] = 0.f;
+    MrT[j * lr + i] = Mr[i * ld + j];
+    xb[i * lr + j] = Minvb[i * ld + j];
     Mb[i * ld + j] = 0.f;
   }
   tm.sync();
   for (int k = num_iter - 1; k >= 0; --k) {
     const bool keep = tape[4 + k] != 0.f;
-    {  // stage the iteration's iterate and residual (n x lb each, consecutive in the tape)
+    {  // stage the iteration's iterate X_k and I + R_k (the factor both products use), and their transposes
       const float* src = tape + 4 + al4(num_iter) + 2 * k * n * lb;
-      for (int e = tm.lane; e < n * lb; e += T) {
-        Xk[e] = src[e];
-        Rk[e] = src[n * lb + e];
+      for (int e = tm.lane; e < n * n; e += T) {
+        const int i = e / n, j = e - i * n;
+        const float x = src[i * lb + j];
+        const float r = src[n * lb + i * lb + j] + (i == j ? 1.f : 0.f);
+        Xk[i * lr + j] = x;
+        XkT[j * lr + i] = x;
+        RkI[i * lr + j] = r;
+        RkIT[j * lr + i] = r;
       }
       tm.sync();
     }
-    gemm_small<T>(tm, n, Xk, lb, false, Rk, lb, false, 1.f, cand, lb, 1.f, false);  // the candidate Xk (I + Rk)
+    gemm_rr<T, NVB>(tm, n, Xk, RkI, candT, 1, lr, 1.f, false);  // the candidate Xk (I + Rk), transposed
     for (int e = tm.lane; e < n * n; e += T) {  // kept: its cotangent is the result's; else the iterate's
       const int i = e / n, j = e - i * n;
-      xnb[i * lb + j] = keep ? xb[i * lb + j] : 0.f;
-      if (keep) xb[i * lb + j] = 0.f;
+      xnb[i * lr + j] = keep ? xb[i * lr + j] : 0.f;
+      if (keep) xb[i * lr + j] = 0.f;
     }
     tm.sync();
     // r_{k+1} = I - M cand
-    gemm_small<T>(tm, n, Mr, ld, true, rbar, lb, false, 0.f, xnb, lb, -1.f, true);
-    gemm_small<T>(tm, n, rbar, lb, false, cand, lb, true, 0.f, Mb, ld, -1.f, true);
+    gemm_rr<T, NVB>(tm, n, MrT, rbar, xnb, lr, 1, -1.f, true);
+    gemm_rr<T, NVB>(tm, n, rbar, candT, Mb, ld, 1, -1.f, true);
     // cand = Xk (I + Rk)
-    gemm_small<T>(tm, n, xnb, lb, false, Rk, lb, true, 1.f, xb, lb, 1.f, true);
-    gemm_small<T>(tm, n, Xk, lb, true, xnb, lb, false, 0.f, rbar, lb, 1.f, false);
+    gemm_rr<T, NVB>(tm, n, xnb, RkIT, xb, lr, 1, 1.f, true);
+    gemm_rr<T, NVB>(tm, n, XkT, xnb, rbar, lr, 1, 1.f, false);
   }
   // r0 = I - M X0 (of the carried inverse, whether or not it was reset)
-  gemm_small<T>(tm, n, rbar, lb, false, x0b, lb, true, 0.f, Mb, ld, -1.f, true);
-  gemm_small<T>(tm, n, Mr, ld, true, rbar, lb, false, 0.f, x0b, lb, -1.f, false);
+  gemm_rr<T, NVB>(tm, n, rbar, X0T, Mb, ld, 1, -1.f, true);
+  gemm_rr<T, NVB>(tm, n, MrT, rbar, x0b, lr, 1, -1.f, false);
   float* Minvbc = a.at(A.Minvbc);
   if (tape[0] != 0.f) {  // reset: x = 0.5 M^T / s, s = tr(M M^T)
     float s = 0.f, t = 0.f;
@@ -928,20 +963,20 @@ __device__ __noinline__ void rev_ns(const int* mw, Ws w, AWs a, const float* rec
       const int i = e / n, j = e - i * n;
       const float v = Mr[i * ld + j];
       s = fmaf(v, v, s);
-      t = fmaf(Mr[j * ld + i], xb[i * lb + j], t);
+      t = fmaf(Mr[j * ld + i], xb[i * lr + j], t);
     }
     s = tm.sum(s);
     t = tm.sum(t);
     const float c = t / (s * s);
     for (int e = tm.lane; e < n * n; e += T) {
       const int i = e / n, j = e - i * n;
-      Mb[i * ld + j] += 0.5f * xb[j * lb + i] / s - c * Mr[i * ld + j];
-      Minvbc[i * ld + j] = x0b[i * lb + j];
+      Mb[i * ld + j] += 0.5f * xb[j * lr + i] / s - c * Mr[i * ld + j];
+      Minvbc[i * ld + j] = x0b[i * lr + j];
     }
   } else {
     for (int e = tm.lane; e < n * n; e += T) {
       const int i = e / n, j = e - i * n;
-      Minvbc[i * ld + j] = x0b[i * lb + j] + xb[i * lb + j];
+      Minvbc[i * ld + j] = x0b[i * lr + j] + xb[i * lr + j];
     }
   }
   tm.sync();
