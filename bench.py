@@ -103,6 +103,16 @@ def profiled_traffic(kernel: str):
   return None
 
 
+STATUS_BITS = {1: 'nonfinite', 2: 'not_spd', 4: 'no_gradient', 8: 'skipped', 16: 'bounds'}
+
+
+def status_bits(status):
+  """Envs per braxg_env_flags bit of a status array (bits that no env set are left out)."""
+  import numpy as np
+  st = np.asarray(status)
+  return {name: int(((st & bit) != 0).sum()) for bit, name in STATUS_BITS.items() if ((st & bit) != 0).any()}
+
+
 def max_over_ranks(seconds: float, device) -> float:
   """The slowest rank's time (one all-reduce MAX); the value itself on one rank."""
   import torch
@@ -502,6 +512,7 @@ def run_braxg(args):
       'other_inverse_mode': other_mode,
       'adjoint': adjoint, 'apg_closed_loop': apg_step, 'uneven': uneven, 'env_step': env_step, 'humanoid': humanoid, 'chain3': chain3,
       'env_status_nonzero': int((status != 0).sum()),
+      'env_status_bits': status_bits(status),
   }
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
     out['cpu_baseline'] = cpu_baseline(args.cpu_sample_envs)
