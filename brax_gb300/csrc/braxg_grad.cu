@@ -242,7 +242,8 @@ int braxg_rollout_vjp_noalloc(const braxg_model* m, void* stream, int n_env, int
                               float* qd0_bar, float* traj_q, float* traj_qd, int32_t* status,
                               const braxg_options* opt) {
   size_t need = 0;
-  int rc = braxg_rollout_vjp_workspace(m, n_env, n_steps, n_frames, ckpt_every, &need);
+  int rc = braxg_rollout_vjp_workspace_mode(m, n_env, n_steps, n_frames, ckpt_every, 1,
+                                            opt ? opt->inverse_mode : BRAXG_INV_CHOLESKY, &need);
   if (rc) return rc;
   if (need > kNoAllocScratchBytes)
     return fail(BRAXG_ERR_INVALID,

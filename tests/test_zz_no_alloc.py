@@ -33,7 +33,8 @@ def _setup():
   return N, pipeline
 
 
-def test_noalloc_rollout_vjp_matches_workspace_variant():
+@pytest.mark.parametrize('mode', ['exact', 'newton_schulz'])
+def test_noalloc_rollout_vjp_matches_workspace_variant(mode):
   N, P = _setup()
   lib = N.lib()
   sys_ = load('quadruped')
@@ -47,10 +48,11 @@ def test_noalloc_rollout_vjp_matches_workspace_variant():
   u = torch.tensor(rng.uniform(-1, 1, (steps, n, m.nu)).astype(np.float32), device=dev)
   qd_bar = torch.tensor(rng.normal(size=(steps, n, m.nv)).astype(np.float32), device=dev)
   stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
-  opt = N.Options(N.INV_CHOLESKY, 0, 0, 0, None)
+  inv = N.INV_CHOLESKY if mode == 'exact' else N.INV_NEWTON_SCHULZ
+  opt = N.Options(inv, 0, 0, 0, None)
 
-  need = ctypes.c_size_t()
-  N.check(lib.braxg_rollout_vjp_workspace(m.handle, n, steps, frames, ckpt, ctypes.byref(need)),
+  need = ctypes.c_size_t()  # one resident segment, as the noalloc entry point sizes its request
+  N.check(lib.braxg_rollout_vjp_workspace_mode(m.handle, n, steps, frames, ckpt, 1, inv, ctypes.byref(need)),
           'workspace')
   assert need.value <= lib.braxg_rollout_vjp_noalloc_capacity()
 
