@@ -296,7 +296,10 @@ int braxg_rollout_vjp_workspace_mode(const braxg_model* model, int n_env, int n_
  * pipeline.init computes it; updated by Newton-Schulz every frame after,
  * brax/generalized/mass.py:99-101) and the reverse differentiates through
  * those updates (brax/math.py:278-305, as jax.grad does; workspace from
- * braxg_rollout_vjp_workspace_mode).  Status bits as braxg_env_flags.
+ * braxg_rollout_vjp_workspace_mode; the reverse of each update also takes
+ * shared memory per env: 12 KB up to 16 dofs, 48 KB up to 32, so a model
+ * that no longer fits the launch gets BRAXG_ERR_UNSUPPORTED in that mode
+ * only).  Status bits as braxg_env_flags.
  * Supports hinge/slide/free joints, world-plane sphere and capsule contacts and
  * joint limits, with either constraint-solve path (A formed explicitly up to 32
  * active rows, applied implicitly above). */
