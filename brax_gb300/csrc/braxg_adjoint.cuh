@@ -9,6 +9,7 @@
 #pragma once
 #include "braxg_adjoint_math.cuh"
 #include "braxg_step.cuh"
+#include "braxg_adjoint_contact.cuh"
 
 namespace braxg {
 
@@ -637,11 +638,9 @@ __device__ __noinline__ void rev_smooth(const int* mw, Ws w, AWs a, bool has_act
       float gear = md.F(BXM_O_ACT_GEAR)[k], gain = md.F(BXM_O_ACT_GAIN)[k];
       float bq = md.F(BXM_O_ACT_BQ)[k], bqd = md.F(BXM_O_ACT_BQD)[k];
       float u = fminf(fmaxf(act[k], cr[0]), cr[1]);
-      bool inu = act[k] >= cr[0] && act[k] <= cr[1];
       float f0 = gain * u + gear * (q[aqid[k]] * bq + qd[aqdid[k]] * bqd);
-      bool inf = f0 >= fr[0] && f0 <= fr[1];
-      float fb = inf ? qfsb[aqdid[k]] * gear : 0.f;
-      actb[k] += inu ? fb * gain : 0.f;
+      float fb = qfsb[aqdid[k]] * gear * clip_grad(f0, fr[0], fr[1]);
+      actb[k] += fb * gain * clip_grad(act[k], cr[0], cr[1]);
       qb[aqid[k]] += fb * gear * bq;
       qdb[aqdid[k]] += fb * gear * bqd;
     }
@@ -1152,37 +1151,52 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
     if (orig >= 4 * ncon) break;  // contact rows come first
     int kc = orig >> 2;
     int kind = md.I(BXM_O_CON_KIND)[kc], sub = md.I(BXM_O_CON_SUB)[kc];
-    int lb = md.I(BXM_O_CON_LB)[kc];
-    // recompute the contact (world plane as geom1)
-    f3 p1 = ld3(md.F(BXM_O_CON_G1POS) + 3 * kc);
+    int la = md.I(BXM_O_CON_LA)[kc], lb = md.I(BXM_O_CON_LB)[kc];
+    // two moving geoms (sphere / capsule pairs) or a geom against the world plane
+    const bool two = kind == BXM_CON_SPHERE_SPHERE || kind == BXM_CON_SPHERE_CAPSULE || kind == BXM_CON_CAPSULE_CAPSULE;
+    // recompute the contact
+    f3 p1, p2;
     float R1[9], R2[9];
-    quat_to_3x3(ld4(md.F(BXM_O_CON_G1QUAT) + 4 * kc), R1);
-    f3 n = mk3(R1[2], R1[5], R1[8]);
-    q4 xrl = ld4(xr + 4 * lb);
-    f3 gpos = ld3(md.F(BXM_O_CON_G2POS) + 3 * kc);
-    q4 gquat = ld4(md.F(BXM_O_CON_G2QUAT) + 4 * kc);
-    f3 p2 = ld3(xp + 3 * lb) + rotate(gpos, xrl);
-    q4 gq = qmul(xrl, gquat);
-    quat_to_3x3(gq, R2);
+    geom_pose(xp, xr, la, md.F(BXM_O_CON_G1POS) + 3 * kc, md.F(BXM_O_CON_G1QUAT) + 4 * kc, p1, R1);
+    geom_pose(xp, xr, lb, md.F(BXM_O_CON_G2POS) + 3 * kc, md.F(BXM_O_CON_G2QUAT) + 4 * kc, p2, R2);
+    const float r1 = md.F(BXM_O_CON_G1SIZE)[3 * kc], h1 = md.F(BXM_O_CON_G1SIZE)[3 * kc + 1];
     float rad = md.F(BXM_O_CON_G2SIZE)[3 * kc], hl = md.F(BXM_O_CON_G2SIZE)[3 * kc + 1];
-    f3 axis = mk3(R2[2], R2[5], R2[8]);
-    f3 center = p2, wv = mk3(0.f, 0.f, 0.f), t1, t2;
-    float bn = 1.f;
-    if (kind == BXM_CON_PLANE_CAPSULE) {
-      center = sub == 0 ? p2 + axis * hl : p2 - axis * hl;
-      wv = axis - n * dot3(n, axis);
-      f3 bvec = normalize_with_norm(wv, bn);
-      if (bn < 0.5f) bvec = (-0.5f < n.y && n.y < 0.5f) ? mk3(0.f, 1.f, 0.f) : mk3(0.f, 0.f, 1.f);
-      t1 = bvec;
-      t2 = cross3(n, bvec);
-    } else {
+    f3 n, axis = mk3(R2[2], R2[5], R2[8]);
+    f3 wv = mk3(0.f, 0.f, 0.f), t1, t2, pos;
+    float dist, bn = 1.f;
+    if (two) {
+      f3 ca = p1, cb = p2;
+      if (kind == BXM_CON_SPHERE_CAPSULE) {
+        cb = closest_segment_point(p2 - axis * hl, p2 + axis * hl, p1);
+      } else if (kind == BXM_CON_CAPSULE_CAPSULE) {
+        const f3 s1 = mk3(R1[2], R1[5], R1[8]) * h1;
+        closest_seg_seg(p1 - s1, p1 + s1, p2 - axis * hl, p2 + axis * hl, ca, cb);
+      }
+      sphere_sphere(ca, r1, cb, rad, dist, pos, n);
       float F[9];
       make_frame(n, F);
+      n = ld3(F);
       t1 = ld3(F + 3);
       t2 = ld3(F + 6);
+    } else {  // the world plane as geom1
+      n = mk3(R1[2], R1[5], R1[8]);
+      f3 center = p2;
+      if (kind == BXM_CON_PLANE_CAPSULE) {
+        center = sub == 0 ? p2 + axis * hl : p2 - axis * hl;
+        wv = axis - n * dot3(n, axis);
+        f3 bvec = normalize_with_norm(wv, bn);
+        if (bn < 0.5f) bvec = (-0.5f < n.y && n.y < 0.5f) ? mk3(0.f, 1.f, 0.f) : mk3(0.f, 0.f, 1.f);
+        t1 = bvec;
+        t2 = cross3(n, bvec);
+      } else {
+        float F[9];
+        make_frame(n, F);
+        t1 = ld3(F + 3);
+        t2 = ld3(F + 6);
+      }
+      dist = dot3(center - p1, n) - rad;
+      pos = center - n * (rad + 0.5f * dist);
     }
-    float dist = dot3(center - p1, n) - rad;
-    f3 pos = center - n * (rad + 0.5f * dist);
     float mu = md.F(BXM_O_CON_FRIC)[kc], tw = md.F(BXM_O_CON_INVW)[kc];
     const float* params = md.F(BXM_O_CON_SOLP) + 7 * kc;
     float imp, dimp, bco, kco;
@@ -1196,29 +1210,43 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
       float impb = -kco * dist * ab + db * (tw + mu * mu * tw) * 2.f * mu * mu * ddiag_dimp(imp);
       distb += -kco * imp * ab + impb * dimp;
     }
-    f3 offb_part = mk3(0.f, 0.f, 0.f);
+    // the rows are (J_b(pos) - J_a(pos)) . v_q with J_l(pos) = cdof_v - (pos - root_com_l) x cdof_a
+    // over the dofs of l's ancestors (link a: none for the world plane)
+    f3 offb_part = mk3(0.f, 0.f, 0.f), offa_part = offb_part;
     f3 v0b = mk3(0.f, 0.f, 0.f), v1b = v0b, v2b = v0b, v3b = v0b;
-    uint64_t mb = md.anc(lb);
+    uint64_t mb = md.anc(lb), ma = la >= 0 ? md.anc(la) : 0ull;
     f3 off = pos - ld3(rc + 3 * lb);
+    f3 offa = la >= 0 ? pos - ld3(rc + 3 * la) : mk3(0.f, 0.f, 0.f);
     for (int d = tm.lane; d < nv; d += T) {
       float jr[4];
       for (int qq = 0; qq < 4; ++qq) {
         jr[qq] = Jb[(c0 + qq) * ldj + d] + velb[qq] * qd[d];
         qdb[d] += velb[qq] * w.jrow(c0 + qq)[d];
       }
-      if (!((mb >> d) & 1ull)) continue;
+      const bool inb = (mb >> d) & 1ull, ina = (ma >> d) & 1ull;
+      if (!inb && !ina) continue;
       f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
-      f3 diff = cv - cross3(off, ca);
+      f3 diff = mk3(0.f, 0.f, 0.f);
+      if (inb) diff = cv - cross3(off, ca);
+      if (ina) diff = diff - (cv - cross3(offa, ca));
       v0b = v0b + diff * jr[0];
       v1b = v1b + diff * jr[1];
       v2b = v2b + diff * jr[2];
       v3b = v3b + diff * jr[3];
       f3 diffb = vq[0] * jr[0] + vq[1] * jr[1] + vq[2] * jr[2] + vq[3] * jr[3];
-      add3(cdofb + 6 * d + 3, diffb);
-      add3(cdofb + 6 * d, -cross3(diffb, off));
-      offb_part = offb_part - cross3(ca, diffb);
+      if (inb) {
+        add3(cdofb + 6 * d + 3, diffb);
+        add3(cdofb + 6 * d, -cross3(diffb, off));
+        offb_part = offb_part - cross3(ca, diffb);
+      }
+      if (ina) {
+        add3(cdofb + 6 * d + 3, -diffb);
+        add3(cdofb + 6 * d, cross3(diffb, offa));
+        offa_part = offa_part + cross3(ca, diffb);
+      }
     }
     f3 offb = mk3(tm.sum(offb_part.x), tm.sum(offb_part.y), tm.sum(offb_part.z));
+    f3 offab = mk3(tm.sum(offa_part.x), tm.sum(offa_part.y), tm.sum(offa_part.z));
     v0b = mk3(tm.sum(v0b.x), tm.sum(v0b.y), tm.sum(v0b.z));
     v1b = mk3(tm.sum(v1b.x), tm.sum(v1b.y), tm.sum(v1b.z));
     v2b = mk3(tm.sum(v2b.x), tm.sum(v2b.y), tm.sum(v2b.z));
@@ -1226,31 +1254,66 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
     if (tm.lane == 0) {
       add3(rcb + 3 * lb, -offb);
       f3 t1b = mu * (v0b - v1b), t2b = mu * (v2b - v3b);
-      // pos = center - n (r + 0.5 dist); dist = (center - p1) . n - r
-      f3 centerb = offb;
-      float db2 = distb - 0.5f * dot3(offb, n);
-      centerb = centerb + n * db2;
-      f3 p2b = centerb;
-      float R2b[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-      if (kind == BXM_CON_PLANE_CAPSULE) {
-        f3 axisb = centerb * (sub == 0 ? hl : -hl);
-        if (bn >= 0.5f) {
-          f3 bb = t1b + cross3(t2b, n);
-          f3 wb = normalize3_vjp(wv, bb);
-          axisb = axisb + wb - n * dot3(n, wb);
+      if (two) {
+        if (la >= 0) add3(rcb + 3 * la, -offab);
+        const f3 posb = offb + offab, nb = v0b + v1b + v2b + v3b;
+        const float cot[13] = {distb, posb.x, posb.y, posb.z, nb.x, nb.y, nb.z,
+                               t1b.x, t1b.y, t1b.z, t2b.x, t2b.y, t2b.z};
+        float inb[kContactIn];
+        two_geom_contact_vjp(kind, p1, mk3(R1[2], R1[5], R1[8]), r1, h1, p2, axis, rad, hl, cot, inb);
+        // each geom: p = x_pos + rotate(geom_pos, x_rot), u = third column of
+        // quat_to_3x3(x_rot * geom_quat)
+        for (int g = 0; g < 2; ++g) {
+          const int l = g == 0 ? la : lb;
+          if (l < 0) continue;  // a world geom does not move
+          const f3 gp = ld3(md.F(g == 0 ? BXM_O_CON_G1POS : BXM_O_CON_G2POS) + 3 * kc);
+          const q4 gqr = ld4(md.F(g == 0 ? BXM_O_CON_G1QUAT : BXM_O_CON_G2QUAT) + 4 * kc);
+          const q4 xl = ld4(xr + 4 * l);
+          const f3 pb = mk3(inb[6 * g], inb[6 * g + 1], inb[6 * g + 2]);
+          float Rb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+          Rb[2] = inb[6 * g + 3];
+          Rb[5] = inb[6 * g + 4];
+          Rb[8] = inb[6 * g + 5];
+          const q4 gq = qmul(xl, gqr);
+          const q4 gqb = quat_to_3x3_vjp(gq, Rb);
+          q4 xrb1, gqt, xrb2;
+          f3 gpb;
+          qmul_vjp(xl, gqr, gqb, xrb1, gqt);
+          rotate_vjp(gp, xl, pb, gpb, xrb2);
+          add3(xpb + 3 * l, pb);
+          add4(xrb + 4 * l, qadd(xrb1, xrb2));
         }
-        R2b[2] = axisb.x;
-        R2b[5] = axisb.y;
-        R2b[8] = axisb.z;
+      } else {
+        // pos = center - n (r + 0.5 dist); dist = (center - p1) . n - r
+        f3 centerb = offb;
+        float db2 = distb - 0.5f * dot3(offb, n);
+        centerb = centerb + n * db2;
+        f3 p2b = centerb;
+        float R2b[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (kind == BXM_CON_PLANE_CAPSULE) {
+          f3 axisb = centerb * (sub == 0 ? hl : -hl);
+          if (bn >= 0.5f) {
+            f3 bb = t1b + cross3(t2b, n);
+            f3 wb = normalize3_vjp(wv, bb);
+            axisb = axisb + wb - n * dot3(n, wb);
+          }
+          R2b[2] = axisb.x;
+          R2b[5] = axisb.y;
+          R2b[8] = axisb.z;
+        }
+        const q4 xrl = ld4(xr + 4 * lb);
+        const f3 gpos = ld3(md.F(BXM_O_CON_G2POS) + 3 * kc);
+        const q4 gquat = ld4(md.F(BXM_O_CON_G2QUAT) + 4 * kc);
+        const q4 gq = qmul(xrl, gquat);
+        q4 gqb = quat_to_3x3_vjp(gq, R2b);
+        q4 xrb1, gqt;
+        qmul_vjp(xrl, gquat, gqb, xrb1, gqt);
+        f3 gpb;
+        q4 xrb2;
+        rotate_vjp(gpos, xrl, p2b, gpb, xrb2);
+        add3(xpb + 3 * lb, p2b);
+        add4(xrb + 4 * lb, qadd(xrb1, xrb2));
       }
-      q4 gqb = quat_to_3x3_vjp(gq, R2b);
-      q4 xrb1, gqt;
-      qmul_vjp(xrl, gquat, gqb, xrb1, gqt);
-      f3 gpb;
-      q4 xrb2;
-      rotate_vjp(gpos, xrl, p2b, gpb, xrb2);
-      add3(xpb + 3 * lb, p2b);
-      add4(xrb + 4 * lb, qadd(xrb1, xrb2));
     }
     tm.sync();
   }

@@ -161,6 +161,16 @@ __device__ __forceinline__ void imp_parts(const float* p, float pos, float& imp,
   k = timeconst <= 0.f ? -timeconst / (dmax * dmax) : k;
 }
 
+// d jnp.clip(x, lo, hi) / dx: jnp.clip is maximum(lo, x) then minimum(hi, .),
+// and jax differentiates maximum / minimum with ties split evenly (1 inside,
+// 1/2 on a bound, 0 beyond; brax/actuator.py:44,52 clip the controls and forces)
+__device__ __forceinline__ float clip_grad(float x, float lo, float hi) {
+  const float m = fmaxf(lo, x);
+  const float dm = x > lo ? 1.f : (x == lo ? 0.5f : 0.f);
+  const float dh = m < hi ? 1.f : (m == hi ? 0.5f : 0.f);
+  return dm * dh;
+}
+
 __device__ __forceinline__ float ddiag_dimp(float imp) {
   return -1.f / (imp + 1e-8f) - (1.f - imp) / ((imp + 1e-8f) * (imp + 1e-8f));
 }

@@ -192,6 +192,16 @@ def quat_rot_axis_vjp_angle(axis, angle, qb):
   return qb[..., 0] * (-0.5 * s) + dot(qb[..., 1:], axis) * (0.5 * c)
 
 
+def clip_grad(x, lo, hi):
+  """d jnp.clip(x, lo, hi) / dx (brax/actuator.py:44,52): jnp.clip is
+  maximum(lo, x) then minimum(hi, .), and jax differentiates maximum /
+  minimum with ties split evenly: 1 inside, 1/2 on a bound, 0 beyond."""
+  m = np.maximum(lo, x)
+  dm = np.where(x > lo, 1.0, np.where(x == lo, 0.5, 0.0))
+  dh = np.where(m < hi, 1.0, np.where(m == hi, 0.5, 0.0))
+  return dm * dh
+
+
 def imp_parts(params, pos, vel):
   """_imp_aref (constraint.py:29-65) plus d imp / d pos, b and k."""
   timeconst, dampratio, dmin, dmax, width, mid, power = [params[..., k] for k in range(7)]
@@ -612,10 +622,10 @@ class StepAdjoint:
     actb = np.zeros((q.shape[0], nu))
     if nu and act is not None:
       qid, qdid = sys.actuator.q_id, sys.actuator.qd_id
-      inu = (act >= c['a_cr'][:, 0]) & (act <= c['a_cr'][:, 1])
+      inu = clip_grad(act, c['a_cr'][:, 0], c['a_cr'][:, 1])
       u = np.clip(act, c['a_cr'][:, 0], c['a_cr'][:, 1])
       f0 = c['a_gain'] * u + c['a_gear'] * (q[:, qid] * c['a_bq'] + qd[:, qdid] * c['a_bqd'])
-      inf = (f0 >= c['a_fr'][:, 0]) & (f0 <= c['a_fr'][:, 1])
+      inf = clip_grad(f0, c['a_fr'][:, 0], c['a_fr'][:, 1])
       fb = taub[:, qdid] * c['a_gear'] * inf
       actb = fb * c['a_gain'] * inu
       for k in range(nu):

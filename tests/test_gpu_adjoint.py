@@ -39,6 +39,20 @@ def _rel(a, b):
   return np.abs(a - b).max(-1) / np.maximum(np.abs(b).max(-1), 1e-6)
 
 
+def _fd_median(loss, x, index, eps_list=(1e-5, 1e-6, 1e-7)):
+  """Central differences of loss (per env) in x[index], at three step sizes,
+  the median of the three per env: a perturbation that moves a discrete
+  decision of the solve (a line-search test, an iteration count) spoils one
+  of the three, not the median."""
+  out = []
+  for eps in eps_list:
+    a_, b_ = x.copy(), x.copy()
+    a_[index] += eps
+    b_[index] -= eps
+    out.append((loss(a_) - loss(b_)) / (2 * eps))
+  return np.median(np.stack(out), 0)
+
+
 @pytest.mark.parametrize('name,steps', [('chain3', 3), ('quadruped', 3), ('quadruped', 40)])
 def test_single_step_vjp_matches_numpy_reverse(name, steps):
   P = _P()
@@ -417,3 +431,168 @@ def test_rollout_gradient_implicit_solve_finite_differences():
         f'qd0 p50 {np.median(eq):.2e} max {eq.max():.2e}')
   assert np.median(eu) <= 1e-3 and (eu <= 1e-2).mean() >= 7 / 8
   assert np.median(eq) <= 1e-3 and (eq <= 1e-2).mean() >= 7 / 8
+
+
+def _humanoid_inputs(sys_, n, pose, seed):
+  """Humanoid-like envs standing (the reset of the workload) or lying on the
+  ground (torso turned 90 degrees about x, 0.05-0.2 m high: most envs above
+  32 active rows, the implicit solve path)."""
+  from brax_gb300 import workloads
+  rng = np.random.default_rng(seed)
+  if pose == 'standing':
+    q, qd = workloads.reset(sys_, n, rng)
+    q, qd = np.asarray(q, np.float64), np.asarray(qd, np.float64)
+  else:
+    q = sys_.init_q[None] + rng.uniform(-0.1, 0.1, (n, sys_.q_size()))
+    qd = 0.1 * rng.normal(size=(n, sys_.qd_size()))
+    q[:, 3:7] = [np.cos(np.pi / 4), np.sin(np.pi / 4), 0.0, 0.0]
+    q[:, 2] = rng.uniform(0.05, 0.2, n)
+  return q.astype(np.float32).astype(np.float64), qd.astype(np.float32).astype(np.float64), rng
+
+
+@pytest.mark.parametrize('mode', ['exact', 'newton_schulz'])
+@pytest.mark.parametrize('pose', ['standing', 'lying'])
+def test_humanoid_gradient(mode, pose):
+  """The gradient kernel on 27 dofs (vjp_kernel<32, 32>): 4 humanoid-like
+  envs, 2 env steps of 2 frames (dt 0.003), in both inverse modes (the
+  reference's K = 20 Newton-Schulz inverse resets every step on this model),
+  standing and lying (the implicit solve path); the model's contacts include
+  the feet's capsule-capsule pair.  The gradient kernel's
+  forward is the plain rollout bit for bit, the split halves give the fused
+  launch's bits, and the gradient matches FP64 central differences of the
+  FP64 rollout in the same mode."""
+  P = _P()
+  from oracle.pipeline import Oracle
+  sys_ = load('humanoid_like')
+  n, H, F = 4, 2, 2
+  q0, qd0, rng = _humanoid_inputs(sys_, n, pose, 81)
+  u = np.clip(rng.normal(0.0, 0.3, (H, n, sys_.act_size())), -1, 1).astype(np.float32).astype(np.float64)
+  q_bar = rng.normal(size=(H, n, sys_.q_size())) * 1e-2
+  qd_bar = rng.normal(size=(H, n, sys_.qd_size())) * 1e-2
+  inv = P.CHOLESKY if mode == 'exact' else P.NEWTON_SCHULZ
+  fused = P.rollout_grad(sys_, _t(q0), _t(qd0), _t(u), _t(q_bar), _t(qd_bar), n_frames=F, ckpt_every=1,
+                         trajectory=True, inverse_mode=inv)
+  (tq, tqd), tape = P.rollout_vjp_fwd(sys_, _t(q0), _t(qd0), _t(u), n_frames=F, ckpt_every=1, inverse_mode=inv)
+  split = P.rollout_vjp_bwd(tape, _t(q_bar), _t(qd_bar))
+  s0 = P.bare_state(_t(q0), _t(qd0)) if mode == 'exact' else P.init(sys_, _t(q0), _t(qd0))
+  _, (rq, rqd) = P.rollout(sys_, s0, _t(u), n_frames=F, inverse_mode=inv, trajectory=True)
+  full = P.init(sys_, _t(q0), _t(qd0), full=True)
+  torch.cuda.synchronize()
+  rows = (full.con_diag.cpu().numpy() != 0).sum(-1)
+  assert (fused[3] == 0).all(), fused[3]
+  if pose == 'lying':
+    assert (rows > 32).any(), rows
+  torch.testing.assert_close(fused[4][0], rq, rtol=0, atol=0)
+  torch.testing.assert_close(fused[4][1], rqd, rtol=0, atol=0)
+  for a_, b_ in zip(split[:3], fused[:3]):
+    torch.testing.assert_close(a_, b_, rtol=0, atol=0)
+  o = Oracle(sys_, np.float64, exact_inverse=mode == 'exact')
+
+  def loss(q0_, qd0_, u_):
+    s = o.init(q0_, qd0_)
+    tot = np.zeros(n)
+    for t in range(H):
+      s = o.env_step(s, u_[t], F)
+      tot += np.sum(q_bar[t] * s.q, -1) + np.sum(qd_bar[t] * s.qd, -1)
+    return tot
+
+  errs = {}
+  fd = np.zeros((n, sys_.qd_size()))
+  for j in range(sys_.qd_size()):
+    fd[:, j] = _fd_median(lambda x: loss(q0, x, u), qd0, (slice(None), j))
+  errs['qd0'] = _rel(fused[2].cpu().numpy(), fd)
+  fdu = np.zeros(u.shape)
+  for t in range(H):
+    for j in range(sys_.act_size()):
+      fdu[t, :, j] = _fd_median(lambda x: loss(q0, qd0, x), u, (t, slice(None), j))
+  errs['act'] = _rel(np.swapaxes(fused[0].cpu().numpy(), 0, 1), np.swapaxes(fdu, 0, 1))
+  for k, e in errs.items():
+    print(f'humanoid-like {pose} {mode} gradient vs FP64 FD ({k}; rows {rows.tolist()}): '
+          f'per env {" ".join(f"{v:.2e}" for v in e)}')
+  for e in errs.values():
+    assert np.median(e) <= 1e-4 and e.max() <= 1e-3
+
+
+# Two free bodies whose geoms overlap by about 1 cm at the start: the contact
+# between two moving geoms (mujoco.mjx's sphere / capsule pairs), without a
+# plane.
+_PAIR_XML = {
+    'capsule_capsule': '''<mujoco model="pair_cc"><option timestep="0.005"/><worldbody>
+      <body name="a" pos="0 0 1"><freejoint/><geom type="capsule" fromto="-0.2 0 0 0.2 0 0" size="0.05"/></body>
+      <body name="b" pos="0 0 1.09"><freejoint/><geom type="capsule" fromto="0 -0.2 0 0 0.2 0" size="0.05"/></body>
+      </worldbody></mujoco>''',
+    'sphere_sphere': '''<mujoco model="pair_ss"><option timestep="0.005"/><worldbody>
+      <body name="a" pos="0 0 1"><freejoint/><geom type="sphere" size="0.06"/></body>
+      <body name="b" pos="0.02 0 1.11"><freejoint/><geom type="sphere" size="0.06"/></body>
+      </worldbody></mujoco>''',
+    'sphere_capsule': '''<mujoco model="pair_sc"><option timestep="0.005"/><worldbody>
+      <body name="a" pos="0.05 0 1.1"><freejoint/><geom type="sphere" size="0.06"/></body>
+      <body name="b" pos="0 0 1"><freejoint/><geom type="capsule" fromto="-0.2 0 0 0.2 0 0" size="0.05"/></body>
+      </worldbody></mujoco>''',
+}
+
+
+@pytest.mark.parametrize('mode', ['exact', 'newton_schulz'])
+@pytest.mark.parametrize('pair', sorted(_PAIR_XML))
+def test_two_geom_contact_gradient(pair, mode):
+  """The reverse of a contact between two moving geoms (brax/contact.py:28-67
+  with mujoco.mjx's sphere-sphere, sphere-capsule and capsule-capsule
+  primitives; both links' point Jacobians in the rows, constraint.py:135-176):
+  8 envs of two overlapping free bodies, positions and orientations jittered,
+  2 env steps of 2 frames, against FP64 central differences of the FP64
+  rollout (the median of three step sizes); the gradient kernel's forward is
+  the plain rollout bit for bit.  Bar: median env within 1e-3, every env
+  within 1e-2: where the first frame's projected-gradient solve stops at a
+  different iteration in FP32 than in FP64 (sphere-capsule env 4: 124
+  against 53 matvecs, the stopping test near the tolerance) the two
+  gradients are of different branches (measured 4e-3 there, <= 6e-4
+  elsewhere)."""
+  P = _P()
+  from brax_gb300 import mjcf
+  from oracle.pipeline import Oracle
+  sys_ = mjcf.loads(_PAIR_XML[pair])
+  n, H, F = 8, 2, 2
+  rng = np.random.default_rng(91)
+  q0 = np.tile(sys_.init_q, (n, 1)).astype(np.float64)
+  for b in range(2):  # free joint b: position q[7b:7b+3], quaternion q[7b+3:7b+7]
+    q0[:, 7 * b:7 * b + 3] += rng.uniform(-0.01, 0.01, (n, 3))
+    quat = q0[:, 7 * b + 3:7 * b + 7] + rng.uniform(-0.05, 0.05, (n, 4))
+    q0[:, 7 * b + 3:7 * b + 7] = quat / np.linalg.norm(quat, axis=1, keepdims=True)
+  qd0 = 0.1 * rng.normal(size=(n, sys_.qd_size()))
+  q0, qd0 = q0.astype(np.float32).astype(np.float64), qd0.astype(np.float32).astype(np.float64)
+  u = np.zeros((H, n, 0))
+  q_bar = rng.normal(size=(H, n, sys_.q_size()))
+  qd_bar = rng.normal(size=(H, n, sys_.qd_size()))
+  inv = P.CHOLESKY if mode == 'exact' else P.NEWTON_SCHULZ
+  fused = P.rollout_grad(sys_, _t(q0), _t(qd0), _t(u), _t(q_bar), _t(qd_bar), n_frames=F, ckpt_every=1,
+                         trajectory=True, inverse_mode=inv)
+  s0 = P.bare_state(_t(q0), _t(qd0)) if mode == 'exact' else P.init(sys_, _t(q0), _t(qd0))
+  _, (rq, rqd) = P.rollout(sys_, s0, _t(u), n_frames=F, inverse_mode=inv, trajectory=True)
+  full = P.init(sys_, _t(q0), _t(qd0), full=True)
+  torch.cuda.synchronize()
+  rows = (full.con_diag.cpu().numpy() != 0).sum(-1)
+  assert (rows > 0).sum() >= n // 2, rows  # the pair touches in most envs
+  assert (fused[3] == 0).all(), fused[3]
+  torch.testing.assert_close(fused[4][0], rq, rtol=0, atol=0)
+  torch.testing.assert_close(fused[4][1], rqd, rtol=0, atol=0)
+  o = Oracle(sys_, np.float64, exact_inverse=mode == 'exact')
+
+  def loss(q0_, qd0_):
+    s = o.init(q0_, qd0_)
+    tot = np.zeros(n)
+    for t in range(H):
+      s = o.env_step(s, u[t], F)
+      tot += np.sum(q_bar[t] * s.q, -1) + np.sum(qd_bar[t] * s.qd, -1)
+    return tot
+
+  errs = {}
+  for which, (x0, got) in enumerate(((q0, fused[1]), (qd0, fused[2]))):
+    fd = np.zeros(x0.shape)
+    f = (lambda x: loss(x, qd0)) if which == 0 else (lambda x: loss(q0, x))
+    for j in range(x0.shape[1]):
+      fd[:, j] = _fd_median(f, x0, (slice(None), j))
+    errs[['q0', 'qd0'][which]] = _rel(got.cpu().numpy(), fd)
+  for k, e in errs.items():
+    print(f'{pair} {mode} gradient vs FP64 FD ({k}; rows {rows.tolist()}): per env {" ".join(f"{v:.2e}" for v in e)}')
+  for e in errs.values():
+    assert np.median(e) <= 1e-3 and e.max() <= 1e-2
