@@ -626,6 +626,122 @@ __device__ __noinline__ void rev_smooth(const int* mw, Ws w, AWs a, bool has_act
     qdb[d] += -md.F(BXM_O_D_DAMP)[d] * qfsb[d];
   }
   tm.sync();
+  // fluid forces (dynamics.py:198-211, fluid.py:53-82): each link's drag
+  // recomputed as the forward forms it (the inertia-box drag of its com
+  // point's velocity in the inertia frame, rotated back to world), then
+  // qf_smooth += sum_k J_k(x_i.pos) . f_k reversed into cdof, the drag's
+  // inputs (cd, the com offset from the tree's com), and x
+  if (md.fluid) {
+    const float* xp = w.at(L.xp);
+    const float* xr = w.at(L.xr);
+    const float* rc = w.at(L.rc);
+    const float* cd = w.at(L.cd);
+    const float* cdof = w.at(L.cdof);
+    const float* lip = md.F(BXM_O_LI_POS);
+    const float* lir = md.F(BXM_O_LI_ROT);
+    const float* box = md.F(BXM_O_LI_BOX);
+    float* cdofb = a.at(A.cdofb);
+    float* cdb = a.at(A.cdb);
+    float* rcb = a.at(A.rcb);
+    float* xpb = a.at(A.xpb);
+    float* xrb = a.at(A.xrb);
+    float* fw = a.at(A.tmp);  // per link: world force ang, vel, then the com offset
+    // the drag of link l from its com velocity in the inertia frame (wa, wv),
+    // and d f / d w per component (the drag is componentwise)
+    auto drag = [&](int l, f3 wa, f3 wv, f3& fa, f3& fv, f3& dfa, f3& dfv) {
+      const f3 b = ld3(box + 3 * l);
+      const float diam = (b.x + b.y + b.z) / 3.f;
+      const float ang_scale = -kPi * (diam * diam * diam) * md.visc;
+      const float vel_scale = -3.f * kPi * diam * md.visc;
+      const float dv = -0.5f * md.dens, da = -1.f * md.dens;
+      const f3 ev = mk3(b.y * b.z, b.x * b.z, b.x * b.y);
+      const float b4x = (b.x * b.x) * (b.x * b.x), b4y = (b.y * b.y) * (b.y * b.y), b4z = (b.z * b.z) * (b.z * b.z);
+      const f3 ea = mk3(b.x * (b4y + b4z), b.y * (b4x + b4z), b.z * (b4x + b4y));
+      fa = ang_scale * wa + mk3(da * ea.x * fabsf(wa.x) * wa.x / 64.f, da * ea.y * fabsf(wa.y) * wa.y / 64.f,
+                                da * ea.z * fabsf(wa.z) * wa.z / 64.f);
+      fv = vel_scale * wv + mk3(dv * ev.x * fabsf(wv.x) * wv.x, dv * ev.y * fabsf(wv.y) * wv.y,
+                                dv * ev.z * fabsf(wv.z) * wv.z);
+      dfa = mk3(ang_scale + da * ea.x * 2.f * fabsf(wa.x) / 64.f, ang_scale + da * ea.y * 2.f * fabsf(wa.y) / 64.f,
+                ang_scale + da * ea.z * 2.f * fabsf(wa.z) / 64.f);
+      dfv = mk3(vel_scale + dv * ev.x * 2.f * fabsf(wv.x), vel_scale + dv * ev.y * 2.f * fabsf(wv.y),
+                vel_scale + dv * ev.z * 2.f * fabsf(wv.z));
+    };
+    for (int l = tm.lane; l < nl; l += T) {
+      f3 ip;
+      q4 ir;
+      tf_do(ld3(xp + 3 * l), ld4(xr + 4 * l), ld3(lip + 3 * l), ld4(lir + 4 * l), ip, ir);
+      const f3 off = ip - ld3(rc + 3 * l);
+      const q4 rt = q4{ir.w, -ir.x, -ir.y, -ir.z};
+      const f3 ca = ld3(cd + 6 * l), cv = ld3(cd + 6 * l + 3);
+      f3 fa, fv, dfa, dfv;
+      drag(l, rotate(ca, rt), rotate(cv - cross3(off, ca), rt), fa, fv, dfa, dfv);
+      st3(fw + 9 * l, rotate(fa, ir));
+      st3(fw + 9 * l + 3, rotate(fv, ir));
+      st3(fw + 9 * l + 6, off);
+    }
+    tm.sync();
+    // term (cv_d - off_k x ca_d) . Fv_k + ca_d . Fa_k for every link k that dof d moves
+    for (int d = tm.lane; d < nv; d += T) {
+      f3 sv = mk3(0.f, 0.f, 0.f), sa = sv;
+      for (int k = 0; k < nl; ++k) {
+        if (!((md.anc(k) >> d) & 1ull)) continue;
+        const f3 Fa = ld3(fw + 9 * k), Fv = ld3(fw + 9 * k + 3), off = ld3(fw + 9 * k + 6);
+        sv = sv + Fv;
+        sa = sa + Fa + cross3(off, Fv);
+      }
+      add3(cdofb + 6 * d + 3, sv * qfsb[d]);
+      add3(cdofb + 6 * d, sa * qfsb[d]);
+    }
+    for (int l = tm.lane; l < nl; l += T) {
+      const f3 Fv = ld3(fw + 9 * l + 3), off = ld3(fw + 9 * l + 6);
+      f3 Fvb = mk3(0.f, 0.f, 0.f), Fab = Fvb, offb = Fvb;
+      for (int d = 0; d < nv; ++d) {
+        if (!((md.anc(l) >> d) & 1ull)) continue;
+        const float g = qfsb[d];
+        const f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
+        Fvb = Fvb + (cv - cross3(off, ca)) * g;
+        Fab = Fab + ca * g;
+        offb = offb + cross3(Fv, ca) * g;
+      }
+      f3 ip;
+      q4 ir;
+      const f3 xpl = ld3(xp + 3 * l);
+      const q4 xrl = ld4(xr + 4 * l);
+      tf_do(xpl, xrl, ld3(lip + 3 * l), ld4(lir + 4 * l), ip, ir);
+      const q4 rt = q4{ir.w, -ir.x, -ir.y, -ir.z};
+      const f3 ca = ld3(cd + 6 * l), cv = ld3(cd + 6 * l + 3);
+      const f3 u = cv - cross3(off, ca);
+      const f3 wa = rotate(ca, rt), wv = rotate(u, rt);
+      f3 fa, fv, dfa, dfv;
+      drag(l, wa, wv, fa, fv, dfa, dfv);
+      // F = rotate(f, ir)
+      f3 fab, fvb;
+      q4 irb1, irb2;
+      rotate_vjp(fa, ir, Fab, fab, irb1);
+      rotate_vjp(fv, ir, Fvb, fvb, irb2);
+      const f3 wab = mk3(fab.x * dfa.x, fab.y * dfa.y, fab.z * dfa.z);
+      const f3 wvb = mk3(fvb.x * dfv.x, fvb.y * dfv.y, fvb.z * dfv.z);
+      // wa = rotate(ca, rt), wv = rotate(cv - off x ca, rt)
+      f3 cab, ub;
+      q4 rtb1, rtb2;
+      rotate_vjp(ca, rt, wab, cab, rtb1);
+      rotate_vjp(u, rt, wvb, ub, rtb2);
+      add3(cdb + 6 * l, cab + cross3(off, ub));
+      add3(cdb + 6 * l + 3, ub);
+      offb = offb + cross3(ub, ca);
+      // rt = quat_inv(ir); off = ip - root_com
+      const q4 rtb = qadd(rtb1, rtb2);
+      const q4 irb = qadd(qadd(irb1, irb2), q4{rtb.w, -rtb.x, -rtb.y, -rtb.z});
+      add3(rcb + 3 * l, -offb);
+      // (ip, ir) = x_l . inertia transform
+      f3 apb, bpb;
+      q4 arb, brb;
+      tf_do_vjp(xpl, xrl, ld3(lip + 3 * l), ld4(lir + 4 * l), offb, irb, apb, arb, bpb, brb);
+      add3(xpb + 3 * l, apb);
+      add4(xrb + 4 * l, arb);
+    }
+    tm.sync();
+  }
   // actuators (lane 0 scatters: several actuators may share a dof)
   if (has_act && tm.lane == 0) {
     const float* act = w.at(L.act);

@@ -120,7 +120,6 @@ static int run_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, i
   if (workspace == nullptr || workspace_bytes < need)
     return fail(BRAXG_ERR_INVALID, "workspace of %zu bytes required (got %zu)", need, workspace_bytes);
   if (m->dims.nv > 32) return fail(BRAXG_ERR_UNSUPPORTED, "gradients support nv <= 32");
-  if (m->h[BXM_H_FLUID]) return fail(BRAXG_ERR_UNSUPPORTED, "gradients do not cover fluid forces");
   for (int k = 0; k < m->dims.ncon; ++k) {
     const int kind = m->h[m->h[BXM_O_CON_KIND] + k], la = m->h[m->h[BXM_O_CON_LA] + k];
     const bool plane = (kind == BXM_CON_PLANE_SPHERE || kind == BXM_CON_PLANE_CAPSULE) && la < 0;

@@ -301,9 +301,9 @@ int braxg_rollout_vjp_workspace_mode(const braxg_model* model, int n_env, int n_
  * that no longer fits the launch gets BRAXG_ERR_UNSUPPORTED in that mode
  * only).  Status bits as braxg_env_flags.
  * Supports hinge/slide/free joints, world-plane sphere and capsule contacts,
- * sphere / capsule pairs between two moving geoms, and joint limits, with
- * either constraint-solve path (A formed explicitly up to 32 active rows,
- * applied implicitly above); other contact kinds (box-plane) return
+ * sphere / capsule pairs between two moving geoms, joint limits and fluid
+ * drag, with either constraint-solve path (A formed explicitly up to 32
+ * active rows, applied implicitly above); box-plane contacts return
  * BRAXG_ERR_UNSUPPORTED. */
 int braxg_rollout_vjp(const braxg_model* model, void* stream, int n_env, int n_steps, int n_frames,
                       int ckpt_every, const float* act_seq, const float* q0, const float* qd0,

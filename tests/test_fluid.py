@@ -160,15 +160,62 @@ def test_gpu_ball_terminal_velocity():
 
 
 @pytest.mark.gpu
-def test_gradients_refuse_fluid_models():
-  """The adjoint does not differentiate fluid forces: the call is refused
-  before any launch."""
+@pytest.mark.parametrize('inverse', ['cholesky', 'newton_schulz'])
+def test_gpu_swimmer_gradient(inverse):
+  """The gradient through the fluid forces (the inertia-box drag of
+  fluid.py:53-82 added to the passive forces, dynamics.py:198-211): the
+  swimmer, 8 envs, 3 env steps of 5 frames, d loss / d (qd0, actions)
+  against FP64 central differences of the FP64 rollout (the median of steps
+  1e-5, 1e-6, 1e-7 per env)."""
   torch = pytest.importorskip('torch')
   if not torch.cuda.is_available():
     pytest.skip('no CUDA device')
   from brax_gb300 import pipeline as P
-  sys = _ball(1.0, 0.0)
-  q = torch.as_tensor(np.tile(sys.init_q, (2, 1)).astype(np.float32), device='cuda')
-  with pytest.raises(NotImplementedError, match='fluid'):
-    P.rollout_grad(sys, q, torch.zeros(2, 6, device='cuda'), torch.zeros(4, 2, 0, device='cuda'),
-                   ckpt_every=2)
+  sys = mjcf.loads(_SWIMMER)
+  n, H, F = 8, 3, 5
+  q, qd = _seeded(sys, n, 5)
+  rng = np.random.default_rng(6)
+  u = rng.uniform(-1, 1, (H, n, sys.act_size())).astype(np.float32)
+  q_bar = rng.normal(size=(H, n, sys.q_size()))
+  qd_bar = rng.normal(size=(H, n, sys.qd_size()))
+  exact = inverse == 'cholesky'
+  mode = P.CHOLESKY if exact else P.NEWTON_SCHULZ
+  t = lambda x: torch.as_tensor(np.asarray(x, np.float32), device='cuda')
+  r = P.rollout_grad(sys, t(q), t(qd), t(u), t(q_bar), t(qd_bar), n_frames=F, ckpt_every=1, trajectory=True,
+                     inverse_mode=mode)
+  s0 = P.bare_state(t(q), t(qd)) if exact else P.init(sys, t(q), t(qd))
+  _, (rq, rqd) = P.rollout(sys, s0, t(u), n_frames=F, inverse_mode=mode, trajectory=True)
+  torch.cuda.synchronize()
+  assert (r[3].cpu().numpy() == 0).all()
+  torch.testing.assert_close(r[4][0], rq, rtol=0, atol=0)
+  torch.testing.assert_close(r[4][1], rqd, rtol=0, atol=0)
+  o = Oracle(sys, np.float64, exact_inverse=exact)
+  q64, qd64, u64 = q.astype(np.float64), qd.astype(np.float64), u.astype(np.float64)
+
+  def loss(qd0, uu):
+    st = o.init(q64, qd0)
+    tot = np.zeros(n)
+    for k in range(H):
+      st = o.env_step(st, uu[k], F)
+      tot += np.sum(q_bar[k] * st.q, -1) + np.sum(qd_bar[k] * st.qd, -1)
+    return tot
+
+  def fd(f, x, idx):
+    est = []
+    for eps in (1e-5, 1e-6, 1e-7):
+      a, b = x.copy(), x.copy()
+      a[idx] += eps
+      b[idx] -= eps
+      est.append((f(a) - f(b)) / (2 * eps))
+    return np.median(np.stack(est), 0)
+
+  g_qd = np.stack([fd(lambda x: loss(x, u64), qd64, (slice(None), j)) for j in range(sys.qd_size())], 1)
+  g_u = np.stack([np.stack([fd(lambda x: loss(qd64, x), u64, (k, slice(None), j)) for j in range(sys.act_size())], 1)
+                  for k in range(H)], 0)
+  rel = lambda a, b: np.abs(a - b).reshape(n, -1).max(-1) / np.maximum(np.abs(b).reshape(n, -1).max(-1), 1e-6)
+  eq = rel(r[2].cpu().numpy(), g_qd)
+  eu = rel(np.swapaxes(r[0].cpu().numpy(), 0, 1), np.swapaxes(g_u, 0, 1))
+  print(f'swimmer {inverse} gradient vs FP64 FD: qd0 per env {" ".join(f"{v:.2e}" for v in eq)}; '
+        f'act per env {" ".join(f"{v:.2e}" for v in eu)}')
+  for e in (eq, eu):
+    assert np.median(e) <= 1e-4 and e.max() <= 1e-3

@@ -113,10 +113,10 @@ def test_gpu_step_matches_oracle(name, inverse):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize('name', sorted(n for n in MODELS if n != 'swimmer'))
+@pytest.mark.parametrize('name', sorted(MODELS))
 def test_gpu_rollout_gradient(name):
-  """APG's gradient on each of the reference's env models but the swimmer
-  (fluid forces, which the gradient refuses): 4 envs, 2 env steps, the
+  """APG's gradient on each of the reference's env models (the swimmer's
+  through its fluid forces): 4 envs, 2 env steps, the
   gradient kernel's forward equal to the plain rollout bit for bit, no env
   flagged, and d loss / d qd0 against FP64 central differences of the FP64
   rollout (the median of steps 1e-5, 1e-6, 1e-7 per env; median env within
