@@ -713,12 +713,59 @@ def bench_humanoid(torch, pipeline, dev, rank, n=16384, steps=20, warmup=3):
     e1.synchronize()
     t += e0.elapsed_time(e1) / 1e3
   last = bufs[(warmup + steps) % 2]
+  grad = bench_humanoid_grad(torch, pipeline, sys_, dev, rank)
   return {'workload': f'humanoid-like nq 28 nv 27 nu 17, 27 contact slots, {n} envs, env step = '
                       f'{N_FRAMES} x {sys_.dt} s, actions N(0, 0.3) clipped, Cholesky mode',
           'env_steps_per_s': round(steps * n / t, 1), 'ms_per_step': round(1e3 * t / steps, 4),
           'launch_shape': dict(zip(('threads_per_env', 'envs_per_cta', 'smem_bytes'),
                                    model.launch_shape(pipeline.CHOLESKY, n_env=n))),
-          'env_status_nonzero': int((last.status != 0).sum().item()), 'gpu_launches_per_step': 1}
+          'env_status_nonzero': int((last.status != 0).sum().item()), 'gpu_launches_per_step': 1,
+          'gradient': grad}
+
+
+def bench_humanoid_grad(torch, pipeline, sys_, dev, rank, n=512, horizon=32, ckpt=8, reps=3):
+  """APG's gradient on the humanoid-like model (27 dofs, the feet's
+  capsule-capsule pair, most solves above 32 rows once it falls): 512 envs,
+  32 env steps of 5 frames, loss -mean(torso x-velocity), the fused forward +
+  adjoint launch against the plain forward rollout, exact inverse."""
+  rng = np.random.default_rng(710 + rank)
+  q0 = (sys_.init_q + rng.uniform(-0.01, 0.01, (n, sys_.q_size()))).astype(np.float32)
+  q0[:, 3:7] /= np.linalg.norm(q0[:, 3:7], axis=1, keepdims=True)
+  q0 = torch.tensor(q0, device=dev)
+  qd0 = torch.tensor((0.01 * rng.normal(size=(n, sys_.qd_size()))).astype(np.float32), device=dev)
+  u = torch.tensor(np.clip(rng.normal(0.0, 0.3, (horizon, n, sys_.act_size())), -1, 1).astype(np.float32),
+                   device=dev)
+  qd_bar = torch.zeros(horizon, n, sys_.qd_size(), device=dev)
+  qd_bar[:, :, 0] = -1.0 / horizon
+  stream = torch.cuda.current_stream(dev)
+  status = [None]
+
+  def fwd():
+    pipeline.rollout(sys_, pipeline.bare_state(q0, qd0), u, n_frames=N_FRAMES, inverse_mode=pipeline.CHOLESKY,
+                     trajectory=True)
+
+  def fwd_adj():
+    status[0] = pipeline.rollout_grad(sys_, q0, qd0, u, None, qd_bar, n_frames=N_FRAMES, ckpt_every=ckpt)[3]
+
+  def timed(fn):
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+      e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+      e0.record(stream)
+      fn()
+      e1.record(stream)
+      torch.cuda.synchronize()
+      ts.append(e0.elapsed_time(e1) / 1e3)
+    return statistics.median(ts)
+
+  t_f, t_b = timed(fwd), timed(fwd_adj)
+  return {'workload': f'humanoid-like, {n} envs, {horizon} env steps x {N_FRAMES} frames, checkpoint every {ckpt}',
+          'fwd_ms': round(1e3 * t_f, 3), 'fwd_adj_ms': round(1e3 * t_b, 3),
+          'fwd_adj_env_steps_per_s': round(n * horizon / t_b, 1),
+          'cost_ratio_fwd_adj_over_fwd': round(t_b / t_f, 3),
+          'envs_without_gradient': int((status[0] != 0).sum().item())}
 
 
 def bench_chain3(torch, pipeline, dev, rank, n=128, n_steps=1000):
