@@ -1278,8 +1278,9 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
     const float r1 = md.F(BXM_O_CON_G1SIZE)[3 * kc], h1 = md.F(BXM_O_CON_G1SIZE)[3 * kc + 1];
     float rad = md.F(BXM_O_CON_G2SIZE)[3 * kc], hl = md.F(BXM_O_CON_G2SIZE)[3 * kc + 1];
     f3 n, axis = mk3(R2[2], R2[5], R2[8]);
-    f3 wv = mk3(0.f, 0.f, 0.f), t1, t2, pos;
+    f3 wv = mk3(0.f, 0.f, 0.f), t1, t2, pos, bvl = mk3(0.f, 0.f, 0.f);
     float dist, bn = 1.f;
+    int bvert = -1;
     if (two) {
       f3 ca = p1, cb = p2;
       if (kind == BXM_CON_SPHERE_CAPSULE) {
@@ -1297,6 +1298,16 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
     } else {  // the world plane as geom1
       n = mk3(R1[2], R1[5], R1[8]);
       f3 center = p2;
+      if (kind == BXM_CON_PLANE_BOX) {  // the slot's manifold vertex, a point of the box (radius 0)
+        float dd;
+        f3 pp;
+        const f3 hb = ld3(md.F(BXM_O_CON_G2SIZE) + 3 * kc);
+        plane_box(p1, n, p2, R2, hb, sub, dd, pp, &bvert);
+        bvl = box_vertex(bvert < 0 ? 0 : bvert, hb);
+        center = p2 + mk3(R2[0] * bvl.x + R2[1] * bvl.y + R2[2] * bvl.z, R2[3] * bvl.x + R2[4] * bvl.y + R2[5] * bvl.z,
+                          R2[6] * bvl.x + R2[7] * bvl.y + R2[8] * bvl.z);
+        rad = 0.f;
+      }
       if (kind == BXM_CON_PLANE_CAPSULE) {
         center = sub == 0 ? p2 + axis * hl : p2 - axis * hl;
         wv = axis - n * dot3(n, axis);
@@ -1406,6 +1417,11 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
         centerb = centerb + n * db2;
         f3 p2b = centerb;
         float R2b[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (kind == BXM_CON_PLANE_BOX) {  // center = p2 + R2 v: R2b = centerb v^T
+          const float cb[3] = {centerb.x, centerb.y, centerb.z}, vv[3] = {bvl.x, bvl.y, bvl.z};
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) R2b[3 * i + j] = cb[i] * vv[j];
+        }
         if (kind == BXM_CON_PLANE_CAPSULE) {
           f3 axisb = centerb * (sub == 0 ? hl : -hl);
           if (bn >= 0.5f) {

@@ -122,11 +122,12 @@ static int run_vjp(const braxg_model* m, void* stream, int n_env, int n_steps, i
   if (m->dims.nv > 32) return fail(BRAXG_ERR_UNSUPPORTED, "gradients support nv <= 32");
   for (int k = 0; k < m->dims.ncon; ++k) {
     const int kind = m->h[m->h[BXM_O_CON_KIND] + k], la = m->h[m->h[BXM_O_CON_LA] + k];
-    const bool plane = (kind == BXM_CON_PLANE_SPHERE || kind == BXM_CON_PLANE_CAPSULE) && la < 0;
+    const bool plane =
+        (kind == BXM_CON_PLANE_SPHERE || kind == BXM_CON_PLANE_CAPSULE || kind == BXM_CON_PLANE_BOX) && la < 0;
     const bool two = kind == BXM_CON_SPHERE_SPHERE || kind == BXM_CON_SPHERE_CAPSULE || kind == BXM_CON_CAPSULE_CAPSULE;
     if (!plane && !two)
       return fail(BRAXG_ERR_UNSUPPORTED,
-                  "gradients support world-plane sphere/capsule contacts and sphere/capsule pairs only");
+                  "gradients support world-plane sphere/capsule/box contacts and sphere/capsule pairs only");
   }
   // as many trailing segments resident as the workspace holds
   const int n_ckpt = vjp_n_ckpt(n_steps, ckpt_every);

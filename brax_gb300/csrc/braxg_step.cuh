@@ -1104,7 +1104,8 @@ __device__ __forceinline__ void closest_seg_seg(f3 a0, f3 a1, f3 b0, f3 b1, f3& 
 __device__ __forceinline__ f3 box_vertex(int v, f3 h) {
   return mk3((v & 4) ? h.x : -h.x, (v & 2) ? h.y : -h.y, (v & 1) ? h.z : -h.z);
 }
-__device__ __forceinline__ void plane_box(f3 p1, f3 n, f3 p2, const float* R2, f3 h, int sub, float& dist, f3& pos) {
+__device__ __forceinline__ void plane_box(f3 p1, f3 n, f3 p2, const float* R2, f3 h, int sub, float& dist, f3& pos,
+                                          int* vert = nullptr) {
   const f3 dp = p1 - p2;  // box frame: R2^T (p1 - p2), R2^T n
   const f3 rel = mk3(R2[0] * dp.x + R2[3] * dp.y + R2[6] * dp.z, R2[1] * dp.x + R2[4] * dp.y + R2[7] * dp.z,
                      R2[2] * dp.x + R2[5] * dp.y + R2[8] * dp.z);
@@ -1163,6 +1164,7 @@ __device__ __forceinline__ void plane_box(f3 p1, f3 n, f3 p2, const float* R2, f
   bool unique = true;
   for (int j = 0; j < sub; ++j) unique = unique && idx[j] != i;
   dist = unique ? -support[i] : 1.f;
+  if (vert != nullptr) *vert = unique ? i : -1;  // the slot's vertex (box frame, box_vertex order)
   const f3 vl = box_vertex(i, h);
   const f3 vw = mk3(R2[0] * vl.x + R2[1] * vl.y + R2[2] * vl.z, R2[3] * vl.x + R2[4] * vl.y + R2[5] * vl.z,
                     R2[6] * vl.x + R2[7] * vl.y + R2[8] * vl.z);

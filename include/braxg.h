@@ -300,11 +300,10 @@ int braxg_rollout_vjp_workspace_mode(const braxg_model* model, int n_env, int n_
  * shared memory per env: 12 KB up to 16 dofs, 48 KB up to 32, so a model
  * that no longer fits the launch gets BRAXG_ERR_UNSUPPORTED in that mode
  * only).  Status bits as braxg_env_flags.
- * Supports hinge/slide/free joints, world-plane sphere and capsule contacts,
- * sphere / capsule pairs between two moving geoms, joint limits and fluid
- * drag, with either constraint-solve path (A formed explicitly up to 32
- * active rows, applied implicitly above); box-plane contacts return
- * BRAXG_ERR_UNSUPPORTED. */
+ * Supports hinge/slide/free joints, every contact kind of the forward
+ * (world-plane sphere, capsule and box; sphere / capsule pairs between two
+ * moving geoms), joint limits and fluid drag, with either constraint-solve
+ * path (A formed explicitly up to 32 active rows, applied implicitly above). */
 int braxg_rollout_vjp(const braxg_model* model, void* stream, int n_env, int n_steps, int n_frames,
                       int ckpt_every, const float* act_seq, const float* q0, const float* qd0,
                       const float* q_bar, const float* qd_bar, float* act_bar, float* q0_bar,

@@ -596,3 +596,84 @@ def test_two_geom_contact_gradient(pair, mode):
     print(f'{pair} {mode} gradient vs FP64 FD ({k}; rows {rows.tolist()}): per env {" ".join(f"{v:.2e}" for v in e)}')
   for e in errs.values():
     assert np.median(e) <= 1e-3 and e.max() <= 1e-2
+
+
+@pytest.mark.parametrize('mode', ['exact', 'newton_schulz'])
+def test_box_plane_gradient(mode):
+  """The reverse of mjx's plane-box contact (the slot's manifold vertex, a
+  point of the box, against the plane; the vertex choice piecewise
+  constant): 16 randomly oriented boxes with their lowest vertex 2-6 mm into
+  the plane, 2 env steps of 2 frames, against FP64 central differences of
+  the FP64 rollout on the envs where those are determined."""
+  P = _P()
+  from brax_gb300 import mjcf
+  from oracle.pipeline import Oracle
+  from tests.test_gpu_parity import BOX_XML
+  sys_ = mjcf.loads(BOX_XML)
+  n, H, F = 16, 2, 2
+  rng = np.random.default_rng(93)
+  qv = rng.normal(size=(n, 4))
+  qv /= np.linalg.norm(qv, axis=1, keepdims=True)
+  h = np.array([0.2, 0.15, 0.1])
+  verts = np.array([[sx, sy, sz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)]) * h
+  q0 = np.zeros((n, 7))
+  for e in range(n):  # the lowest vertex's height sets the box's
+    w, x, y, z = qv[e]
+    R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                  [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                  [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+    low = (verts @ R.T)[:, 2].min()
+    q0[e] = [rng.uniform(-0.5, 0.5), rng.uniform(-0.5, 0.5), -low - rng.uniform(0.002, 0.006), w, x, y, z]
+  qd0 = 0.05 * rng.normal(size=(n, 6))
+  q0, qd0 = q0.astype(np.float32).astype(np.float64), qd0.astype(np.float32).astype(np.float64)
+  u = np.zeros((H, n, 0))
+  q_bar = rng.normal(size=(H, n, 7))
+  qd_bar = rng.normal(size=(H, n, 6))
+  inv = P.CHOLESKY if mode == 'exact' else P.NEWTON_SCHULZ
+  fused = P.rollout_grad(sys_, _t(q0), _t(qd0), _t(u), _t(q_bar), _t(qd_bar), n_frames=F, ckpt_every=1,
+                         trajectory=True, inverse_mode=inv)
+  s0 = P.bare_state(_t(q0), _t(qd0)) if mode == 'exact' else P.init(sys_, _t(q0), _t(qd0))
+  _, (rq, rqd) = P.rollout(sys_, s0, _t(u), n_frames=F, inverse_mode=inv, trajectory=True)
+  full = P.init(sys_, _t(q0), _t(qd0), full=True)
+  torch.cuda.synchronize()
+  rows = (full.con_diag.cpu().numpy() != 0).sum(-1)
+  assert (rows > 0).all(), rows
+  assert (fused[3] == 0).all(), fused[3]
+  torch.testing.assert_close(fused[4][0], rq, rtol=0, atol=0)
+  torch.testing.assert_close(fused[4][1], rqd, rtol=0, atol=0)
+  o = Oracle(sys_, np.float64, exact_inverse=mode == 'exact')
+
+  def loss(q0_, qd0_):
+    s = o.init(q0_, qd0_)
+    tot = np.zeros(n)
+    for t in range(H):
+      s = o.env_step(s, u[t], F)
+      tot += np.sum(q_bar[t] * s.q, -1) + np.sum(qd_bar[t] * s.qd, -1)
+    return tot
+
+  # a box on one corner is often near the solve's stopping test: its loss has
+  # kinks below 1e-5, and differences at 1e-5, 1e-6 and 1e-7 disagree; the
+  # gradient is checked on the envs whose three differences agree to 1e-3
+  errs, det = {}, np.ones(n, bool)
+  for which, (x0, got) in enumerate(((q0, fused[1]), (qd0, fused[2]))):
+    f = (lambda x: loss(x, qd0)) if which == 0 else (lambda x: loss(q0, x))
+    est = []
+    for eps in (1e-5, 1e-6, 1e-7):
+      cols = []
+      for jj in range(x0.shape[1]):
+        a_, b_ = x0.copy(), x0.copy()
+        a_[:, jj] += eps
+        b_[:, jj] -= eps
+        cols.append((f(a_) - f(b_)) / (2 * eps))
+      est.append(np.stack(cols, 1))
+    est = np.stack(est)
+    fd = np.median(est, 0)
+    spread = (est.max(0) - est.min(0)).max(-1) / np.maximum(np.abs(fd).max(-1), 1e-6)
+    det &= spread <= 1e-3
+    errs[['q0', 'qd0'][which]] = _rel(got.cpu().numpy(), fd)
+  for k_, e in errs.items():
+    print(f'box-plane {mode} gradient vs FP64 FD ({k_}; determined envs {det.astype(int).tolist()}): '
+          f'per env {" ".join(f"{v:.2e}" for v in e)}')
+  assert det.sum() >= 3, det
+  for e in errs.values():  # as the two-body pairs: FP32 and FP64 solves may stop apart
+    assert np.median(e[det]) <= 1e-3 and e[det].max() <= 1e-2
