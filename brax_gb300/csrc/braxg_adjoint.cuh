@@ -1214,6 +1214,135 @@ __device__ __noinline__ void rev_crba(const int* mw, Ws w, AWs a) {
 }
 
 // ---------------------------------------------------------------------------
+// The reverse of one active contact between two moving geoms (a sphere /
+// capsule pair: contact.py:28-67 with the mjx primitives, constraint.py:
+// 135-176), rows c0..c0+3 of slot kc: its rows hold both links' point
+// Jacobians (J_b - J_a at the contact point), reversed into both links' cdof
+// and root com; its geometry is differentiated by two_geom_contact_vjp and
+// sent back through both geoms' poses.  Out of line: the plane contacts of
+// rev_rows do not carry its code.
+// ---------------------------------------------------------------------------
+template <int T>
+__device__ __noinline__ void rev_contact_pair(const int* mw, Ws w, AWs a, int c0, int kc) {
+  const Model md(mw);
+  const Team<T> tm;
+  const Layout& L = *w.L;
+  const AdjLayout& A = *a.A;
+  const int nv = md.nv, ldj = L.ldj;
+  const float* qd = a.at(A.qd0);
+  const float* Jb = a.at(A.Jb);
+  const float* diagb = a.at(A.diagb);
+  const float* arefb = a.at(A.arefb);
+  float* qdb = a.at(A.qdb);
+  const float* rc = w.at(L.rc);
+  const float* cdof = w.at(L.cdof);
+  const float* xp = w.at(L.xp);
+  const float* xr = w.at(L.xr);
+  float* cdofb = a.at(A.cdofb);
+  float* rcb = a.at(A.rcb);
+  float* xpb = a.at(A.xpb);
+  float* xrb = a.at(A.xrb);
+  const int kind = md.I(BXM_O_CON_KIND)[kc];
+  const int la = md.I(BXM_O_CON_LA)[kc], lb = md.I(BXM_O_CON_LB)[kc];
+  f3 p1, p2;
+  float R1[9], R2[9];
+  geom_pose(xp, xr, la, md.F(BXM_O_CON_G1POS) + 3 * kc, md.F(BXM_O_CON_G1QUAT) + 4 * kc, p1, R1);
+  geom_pose(xp, xr, lb, md.F(BXM_O_CON_G2POS) + 3 * kc, md.F(BXM_O_CON_G2QUAT) + 4 * kc, p2, R2);
+  const float r1 = md.F(BXM_O_CON_G1SIZE)[3 * kc], h1 = md.F(BXM_O_CON_G1SIZE)[3 * kc + 1];
+  const float r2 = md.F(BXM_O_CON_G2SIZE)[3 * kc], h2 = md.F(BXM_O_CON_G2SIZE)[3 * kc + 1];
+  const f3 u1 = mk3(R1[2], R1[5], R1[8]), u2 = mk3(R2[2], R2[5], R2[8]);
+  float c[13];
+  two_geom_contact(kind, p1, u1, r1, h1, p2, u2, r2, h2, c);
+  const float dist = c[0];
+  const f3 pos = ld3(c + 1), n = ld3(c + 4), t1 = ld3(c + 7), t2 = ld3(c + 10);
+  const float mu = md.F(BXM_O_CON_FRIC)[kc], tw = md.F(BXM_O_CON_INVW)[kc];
+  float imp, dimp, bco, kco;
+  imp_parts(md.F(BXM_O_CON_SOLP) + 7 * kc, dist, imp, dimp, bco, kco);
+  const f3 vq[4] = {(-t1) * (-mu) + n, (-t1) * mu + n, (-t2) * (-mu) + n, (-t2) * mu + n};
+  float velb[4];
+  float distb = 0.f;
+  for (int qq = 0; qq < 4; ++qq) {
+    const float ab = arefb[c0 + qq], db = diagb[c0 + qq];
+    velb[qq] = -bco * ab;
+    const float impb = -kco * dist * ab + db * (tw + mu * mu * tw) * 2.f * mu * mu * ddiag_dimp(imp);
+    distb += -kco * imp * ab + impb * dimp;
+  }
+  // rows (J_b(pos) - J_a(pos)) . v_q, J_l(pos) = cdof_v - (pos - root_com_l) x cdof_a
+  // over the dofs of l's ancestors (none for a world geom)
+  const uint64_t mb = md.anc(lb), ma = la >= 0 ? md.anc(la) : 0ull;
+  const f3 offb = pos - ld3(rc + 3 * lb);
+  const f3 offa = la >= 0 ? pos - ld3(rc + 3 * la) : mk3(0.f, 0.f, 0.f);
+  f3 obp = mk3(0.f, 0.f, 0.f), oap = obp, v0b = obp, v1b = obp, v2b = obp, v3b = obp;
+  for (int d = tm.lane; d < nv; d += T) {
+    float jr[4];
+    for (int qq = 0; qq < 4; ++qq) {
+      jr[qq] = Jb[(c0 + qq) * ldj + d] + velb[qq] * qd[d];
+      qdb[d] += velb[qq] * w.jrow(c0 + qq)[d];
+    }
+    const bool inb = (mb >> d) & 1ull, ina = (ma >> d) & 1ull;
+    if (!inb && !ina) continue;
+    const f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
+    f3 diff = mk3(0.f, 0.f, 0.f);
+    if (inb) diff = cv - cross3(offb, ca);
+    if (ina) diff = diff - (cv - cross3(offa, ca));
+    v0b = v0b + diff * jr[0];
+    v1b = v1b + diff * jr[1];
+    v2b = v2b + diff * jr[2];
+    v3b = v3b + diff * jr[3];
+    const f3 diffb = vq[0] * jr[0] + vq[1] * jr[1] + vq[2] * jr[2] + vq[3] * jr[3];
+    if (inb) {
+      add3(cdofb + 6 * d + 3, diffb);
+      add3(cdofb + 6 * d, -cross3(diffb, offb));
+      obp = obp - cross3(ca, diffb);
+    }
+    if (ina) {
+      add3(cdofb + 6 * d + 3, -diffb);
+      add3(cdofb + 6 * d, cross3(diffb, offa));
+      oap = oap + cross3(ca, diffb);
+    }
+  }
+  const f3 offbb = mk3(tm.sum(obp.x), tm.sum(obp.y), tm.sum(obp.z));
+  const f3 offab = mk3(tm.sum(oap.x), tm.sum(oap.y), tm.sum(oap.z));
+  v0b = mk3(tm.sum(v0b.x), tm.sum(v0b.y), tm.sum(v0b.z));
+  v1b = mk3(tm.sum(v1b.x), tm.sum(v1b.y), tm.sum(v1b.z));
+  v2b = mk3(tm.sum(v2b.x), tm.sum(v2b.y), tm.sum(v2b.z));
+  v3b = mk3(tm.sum(v3b.x), tm.sum(v3b.y), tm.sum(v3b.z));
+  if (tm.lane == 0) {
+    add3(rcb + 3 * lb, -offbb);
+    if (la >= 0) add3(rcb + 3 * la, -offab);
+    const f3 t1b = mu * (v0b - v1b), t2b = mu * (v2b - v3b);
+    const f3 posb = offbb + offab, nb = v0b + v1b + v2b + v3b;
+    const float cot[13] = {distb, posb.x, posb.y, posb.z, nb.x, nb.y, nb.z,
+                           t1b.x, t1b.y, t1b.z, t2b.x, t2b.y, t2b.z};
+    float inb[kContactIn];
+    two_geom_contact_vjp(kind, p1, u1, r1, h1, p2, u2, r2, h2, cot, inb);
+    // each geom: p = x_pos + rotate(geom_pos, x_rot), u = third column of
+    // quat_to_3x3(x_rot * geom_quat)
+    for (int g = 0; g < 2; ++g) {
+      const int l = g == 0 ? la : lb;
+      if (l < 0) continue;  // a world geom does not move
+      const f3 gp = ld3(md.F(g == 0 ? BXM_O_CON_G1POS : BXM_O_CON_G2POS) + 3 * kc);
+      const q4 gqr = ld4(md.F(g == 0 ? BXM_O_CON_G1QUAT : BXM_O_CON_G2QUAT) + 4 * kc);
+      const q4 xl = ld4(xr + 4 * l);
+      const f3 pb = mk3(inb[6 * g], inb[6 * g + 1], inb[6 * g + 2]);
+      float Rb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      Rb[2] = inb[6 * g + 3];
+      Rb[5] = inb[6 * g + 4];
+      Rb[8] = inb[6 * g + 5];
+      const q4 gq = qmul(xl, gqr);
+      const q4 gqb = quat_to_3x3_vjp(gq, Rb);
+      q4 xrb1, gqt, xrb2;
+      f3 gpb;
+      qmul_vjp(xl, gqr, gqb, xrb1, gqt);
+      rotate_vjp(gp, xl, pb, gpb, xrb2);
+      add3(xpb + 3 * l, pb);
+      add4(xrb + 4 * l, qadd(xrb1, xrb2));
+    }
+  }
+  tm.sync();
+}
+
+// ---------------------------------------------------------------------------
 // constraint rows reverse (constraint.py:68-176): limit rows -> q, qd;
 // contact rows -> qd, cdof, root_com, and the contact geometry -> x.
 // ---------------------------------------------------------------------------
@@ -1267,63 +1396,49 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
     if (orig >= 4 * ncon) break;  // contact rows come first
     int kc = orig >> 2;
     int kind = md.I(BXM_O_CON_KIND)[kc], sub = md.I(BXM_O_CON_SUB)[kc];
-    int la = md.I(BXM_O_CON_LA)[kc], lb = md.I(BXM_O_CON_LB)[kc];
-    // two moving geoms (sphere / capsule pairs) or a geom against the world plane
-    const bool two = kind == BXM_CON_SPHERE_SPHERE || kind == BXM_CON_SPHERE_CAPSULE || kind == BXM_CON_CAPSULE_CAPSULE;
-    // recompute the contact
-    f3 p1, p2;
+    if (kind == BXM_CON_SPHERE_SPHERE || kind == BXM_CON_SPHERE_CAPSULE || kind == BXM_CON_CAPSULE_CAPSULE) {
+      rev_contact_pair<T>(mw, w, a, c0, kc);  // two moving geoms
+      continue;
+    }
+    int lb = md.I(BXM_O_CON_LB)[kc];
+    // recompute the contact (world plane as geom1)
+    f3 p1 = ld3(md.F(BXM_O_CON_G1POS) + 3 * kc);
     float R1[9], R2[9];
-    geom_pose(xp, xr, la, md.F(BXM_O_CON_G1POS) + 3 * kc, md.F(BXM_O_CON_G1QUAT) + 4 * kc, p1, R1);
-    geom_pose(xp, xr, lb, md.F(BXM_O_CON_G2POS) + 3 * kc, md.F(BXM_O_CON_G2QUAT) + 4 * kc, p2, R2);
-    const float r1 = md.F(BXM_O_CON_G1SIZE)[3 * kc], h1 = md.F(BXM_O_CON_G1SIZE)[3 * kc + 1];
+    quat_to_3x3(ld4(md.F(BXM_O_CON_G1QUAT) + 4 * kc), R1);
+    f3 n = mk3(R1[2], R1[5], R1[8]);
+    q4 xrl = ld4(xr + 4 * lb);
+    f3 gpos = ld3(md.F(BXM_O_CON_G2POS) + 3 * kc);
+    q4 gquat = ld4(md.F(BXM_O_CON_G2QUAT) + 4 * kc);
+    f3 p2 = ld3(xp + 3 * lb) + rotate(gpos, xrl);
+    q4 gq = qmul(xrl, gquat);
+    quat_to_3x3(gq, R2);
     float rad = md.F(BXM_O_CON_G2SIZE)[3 * kc], hl = md.F(BXM_O_CON_G2SIZE)[3 * kc + 1];
-    f3 n, axis = mk3(R2[2], R2[5], R2[8]);
-    f3 wv = mk3(0.f, 0.f, 0.f), t1, t2, pos, bvl = mk3(0.f, 0.f, 0.f);
-    float dist, bn = 1.f;
-    int bvert = -1;
-    if (two) {
-      f3 ca = p1, cb = p2;
-      if (kind == BXM_CON_SPHERE_CAPSULE) {
-        cb = closest_segment_point(p2 - axis * hl, p2 + axis * hl, p1);
-      } else if (kind == BXM_CON_CAPSULE_CAPSULE) {
-        const f3 s1 = mk3(R1[2], R1[5], R1[8]) * h1;
-        closest_seg_seg(p1 - s1, p1 + s1, p2 - axis * hl, p2 + axis * hl, ca, cb);
-      }
-      sphere_sphere(ca, r1, cb, rad, dist, pos, n);
+    f3 axis = mk3(R2[2], R2[5], R2[8]);
+    f3 center = p2, wv = mk3(0.f, 0.f, 0.f), t1, t2, bvl = mk3(0.f, 0.f, 0.f);
+    float bn = 1.f;
+    if (kind == BXM_CON_PLANE_BOX) {  // the slot's manifold vertex, a point of the box (radius 0)
+      const f3 hb = ld3(md.F(BXM_O_CON_G2SIZE) + 3 * kc);
+      const int bvert = plane_box_vertex(p1, n, p2, R2, hb, sub);
+      bvl = box_vertex(bvert < 0 ? 0 : bvert, hb);
+      center = p2 + mk3(R2[0] * bvl.x + R2[1] * bvl.y + R2[2] * bvl.z, R2[3] * bvl.x + R2[4] * bvl.y + R2[5] * bvl.z,
+                        R2[6] * bvl.x + R2[7] * bvl.y + R2[8] * bvl.z);
+      rad = 0.f;
+    }
+    if (kind == BXM_CON_PLANE_CAPSULE) {
+      center = sub == 0 ? p2 + axis * hl : p2 - axis * hl;
+      wv = axis - n * dot3(n, axis);
+      f3 bvec = normalize_with_norm(wv, bn);
+      if (bn < 0.5f) bvec = (-0.5f < n.y && n.y < 0.5f) ? mk3(0.f, 1.f, 0.f) : mk3(0.f, 0.f, 1.f);
+      t1 = bvec;
+      t2 = cross3(n, bvec);
+    } else {
       float F[9];
       make_frame(n, F);
-      n = ld3(F);
       t1 = ld3(F + 3);
       t2 = ld3(F + 6);
-    } else {  // the world plane as geom1
-      n = mk3(R1[2], R1[5], R1[8]);
-      f3 center = p2;
-      if (kind == BXM_CON_PLANE_BOX) {  // the slot's manifold vertex, a point of the box (radius 0)
-        float dd;
-        f3 pp;
-        const f3 hb = ld3(md.F(BXM_O_CON_G2SIZE) + 3 * kc);
-        plane_box(p1, n, p2, R2, hb, sub, dd, pp, &bvert);
-        bvl = box_vertex(bvert < 0 ? 0 : bvert, hb);
-        center = p2 + mk3(R2[0] * bvl.x + R2[1] * bvl.y + R2[2] * bvl.z, R2[3] * bvl.x + R2[4] * bvl.y + R2[5] * bvl.z,
-                          R2[6] * bvl.x + R2[7] * bvl.y + R2[8] * bvl.z);
-        rad = 0.f;
-      }
-      if (kind == BXM_CON_PLANE_CAPSULE) {
-        center = sub == 0 ? p2 + axis * hl : p2 - axis * hl;
-        wv = axis - n * dot3(n, axis);
-        f3 bvec = normalize_with_norm(wv, bn);
-        if (bn < 0.5f) bvec = (-0.5f < n.y && n.y < 0.5f) ? mk3(0.f, 1.f, 0.f) : mk3(0.f, 0.f, 1.f);
-        t1 = bvec;
-        t2 = cross3(n, bvec);
-      } else {
-        float F[9];
-        make_frame(n, F);
-        t1 = ld3(F + 3);
-        t2 = ld3(F + 6);
-      }
-      dist = dot3(center - p1, n) - rad;
-      pos = center - n * (rad + 0.5f * dist);
     }
+    float dist = dot3(center - p1, n) - rad;
+    f3 pos = center - n * (rad + 0.5f * dist);
     float mu = md.F(BXM_O_CON_FRIC)[kc], tw = md.F(BXM_O_CON_INVW)[kc];
     const float* params = md.F(BXM_O_CON_SOLP) + 7 * kc;
     float imp, dimp, bco, kco;
@@ -1337,43 +1452,29 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
       float impb = -kco * dist * ab + db * (tw + mu * mu * tw) * 2.f * mu * mu * ddiag_dimp(imp);
       distb += -kco * imp * ab + impb * dimp;
     }
-    // the rows are (J_b(pos) - J_a(pos)) . v_q with J_l(pos) = cdof_v - (pos - root_com_l) x cdof_a
-    // over the dofs of l's ancestors (link a: none for the world plane)
-    f3 offb_part = mk3(0.f, 0.f, 0.f), offa_part = offb_part;
+    f3 offb_part = mk3(0.f, 0.f, 0.f);
     f3 v0b = mk3(0.f, 0.f, 0.f), v1b = v0b, v2b = v0b, v3b = v0b;
-    uint64_t mb = md.anc(lb), ma = la >= 0 ? md.anc(la) : 0ull;
+    uint64_t mb = md.anc(lb);
     f3 off = pos - ld3(rc + 3 * lb);
-    f3 offa = la >= 0 ? pos - ld3(rc + 3 * la) : mk3(0.f, 0.f, 0.f);
     for (int d = tm.lane; d < nv; d += T) {
       float jr[4];
       for (int qq = 0; qq < 4; ++qq) {
         jr[qq] = Jb[(c0 + qq) * ldj + d] + velb[qq] * qd[d];
         qdb[d] += velb[qq] * w.jrow(c0 + qq)[d];
       }
-      const bool inb = (mb >> d) & 1ull, ina = (ma >> d) & 1ull;
-      if (!inb && !ina) continue;
+      if (!((mb >> d) & 1ull)) continue;
       f3 ca = ld3(cdof + 6 * d), cv = ld3(cdof + 6 * d + 3);
-      f3 diff = mk3(0.f, 0.f, 0.f);
-      if (inb) diff = cv - cross3(off, ca);
-      if (ina) diff = diff - (cv - cross3(offa, ca));
+      f3 diff = cv - cross3(off, ca);
       v0b = v0b + diff * jr[0];
       v1b = v1b + diff * jr[1];
       v2b = v2b + diff * jr[2];
       v3b = v3b + diff * jr[3];
       f3 diffb = vq[0] * jr[0] + vq[1] * jr[1] + vq[2] * jr[2] + vq[3] * jr[3];
-      if (inb) {
-        add3(cdofb + 6 * d + 3, diffb);
-        add3(cdofb + 6 * d, -cross3(diffb, off));
-        offb_part = offb_part - cross3(ca, diffb);
-      }
-      if (ina) {
-        add3(cdofb + 6 * d + 3, -diffb);
-        add3(cdofb + 6 * d, cross3(diffb, offa));
-        offa_part = offa_part + cross3(ca, diffb);
-      }
+      add3(cdofb + 6 * d + 3, diffb);
+      add3(cdofb + 6 * d, -cross3(diffb, off));
+      offb_part = offb_part - cross3(ca, diffb);
     }
     f3 offb = mk3(tm.sum(offb_part.x), tm.sum(offb_part.y), tm.sum(offb_part.z));
-    f3 offab = mk3(tm.sum(offa_part.x), tm.sum(offa_part.y), tm.sum(offa_part.z));
     v0b = mk3(tm.sum(v0b.x), tm.sum(v0b.y), tm.sum(v0b.z));
     v1b = mk3(tm.sum(v1b.x), tm.sum(v1b.y), tm.sum(v1b.z));
     v2b = mk3(tm.sum(v2b.x), tm.sum(v2b.y), tm.sum(v2b.z));
@@ -1381,71 +1482,36 @@ __device__ __noinline__ void rev_rows(const int* mw, Ws w, AWs a) {
     if (tm.lane == 0) {
       add3(rcb + 3 * lb, -offb);
       f3 t1b = mu * (v0b - v1b), t2b = mu * (v2b - v3b);
-      if (two) {
-        if (la >= 0) add3(rcb + 3 * la, -offab);
-        const f3 posb = offb + offab, nb = v0b + v1b + v2b + v3b;
-        const float cot[13] = {distb, posb.x, posb.y, posb.z, nb.x, nb.y, nb.z,
-                               t1b.x, t1b.y, t1b.z, t2b.x, t2b.y, t2b.z};
-        float inb[kContactIn];
-        two_geom_contact_vjp(kind, p1, mk3(R1[2], R1[5], R1[8]), r1, h1, p2, axis, rad, hl, cot, inb);
-        // each geom: p = x_pos + rotate(geom_pos, x_rot), u = third column of
-        // quat_to_3x3(x_rot * geom_quat)
-        for (int g = 0; g < 2; ++g) {
-          const int l = g == 0 ? la : lb;
-          if (l < 0) continue;  // a world geom does not move
-          const f3 gp = ld3(md.F(g == 0 ? BXM_O_CON_G1POS : BXM_O_CON_G2POS) + 3 * kc);
-          const q4 gqr = ld4(md.F(g == 0 ? BXM_O_CON_G1QUAT : BXM_O_CON_G2QUAT) + 4 * kc);
-          const q4 xl = ld4(xr + 4 * l);
-          const f3 pb = mk3(inb[6 * g], inb[6 * g + 1], inb[6 * g + 2]);
-          float Rb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-          Rb[2] = inb[6 * g + 3];
-          Rb[5] = inb[6 * g + 4];
-          Rb[8] = inb[6 * g + 5];
-          const q4 gq = qmul(xl, gqr);
-          const q4 gqb = quat_to_3x3_vjp(gq, Rb);
-          q4 xrb1, gqt, xrb2;
-          f3 gpb;
-          qmul_vjp(xl, gqr, gqb, xrb1, gqt);
-          rotate_vjp(gp, xl, pb, gpb, xrb2);
-          add3(xpb + 3 * l, pb);
-          add4(xrb + 4 * l, qadd(xrb1, xrb2));
-        }
-      } else {
-        // pos = center - n (r + 0.5 dist); dist = (center - p1) . n - r
-        f3 centerb = offb;
-        float db2 = distb - 0.5f * dot3(offb, n);
-        centerb = centerb + n * db2;
-        f3 p2b = centerb;
-        float R2b[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        if (kind == BXM_CON_PLANE_BOX) {  // center = p2 + R2 v: R2b = centerb v^T
-          const float cb[3] = {centerb.x, centerb.y, centerb.z}, vv[3] = {bvl.x, bvl.y, bvl.z};
-          for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) R2b[3 * i + j] = cb[i] * vv[j];
-        }
-        if (kind == BXM_CON_PLANE_CAPSULE) {
-          f3 axisb = centerb * (sub == 0 ? hl : -hl);
-          if (bn >= 0.5f) {
-            f3 bb = t1b + cross3(t2b, n);
-            f3 wb = normalize3_vjp(wv, bb);
-            axisb = axisb + wb - n * dot3(n, wb);
-          }
-          R2b[2] = axisb.x;
-          R2b[5] = axisb.y;
-          R2b[8] = axisb.z;
-        }
-        const q4 xrl = ld4(xr + 4 * lb);
-        const f3 gpos = ld3(md.F(BXM_O_CON_G2POS) + 3 * kc);
-        const q4 gquat = ld4(md.F(BXM_O_CON_G2QUAT) + 4 * kc);
-        const q4 gq = qmul(xrl, gquat);
-        q4 gqb = quat_to_3x3_vjp(gq, R2b);
-        q4 xrb1, gqt;
-        qmul_vjp(xrl, gquat, gqb, xrb1, gqt);
-        f3 gpb;
-        q4 xrb2;
-        rotate_vjp(gpos, xrl, p2b, gpb, xrb2);
-        add3(xpb + 3 * lb, p2b);
-        add4(xrb + 4 * lb, qadd(xrb1, xrb2));
+      // pos = center - n (r + 0.5 dist); dist = (center - p1) . n - r
+      f3 centerb = offb;
+      float db2 = distb - 0.5f * dot3(offb, n);
+      centerb = centerb + n * db2;
+      f3 p2b = centerb;
+      float R2b[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+      if (kind == BXM_CON_PLANE_BOX) {  // center = p2 + R2 v: R2b = centerb v^T
+        const float cb[3] = {centerb.x, centerb.y, centerb.z}, vv[3] = {bvl.x, bvl.y, bvl.z};
+        for (int i = 0; i < 3; ++i)
+          for (int j = 0; j < 3; ++j) R2b[3 * i + j] = cb[i] * vv[j];
       }
+      if (kind == BXM_CON_PLANE_CAPSULE) {
+        f3 axisb = centerb * (sub == 0 ? hl : -hl);
+        if (bn >= 0.5f) {
+          f3 bb = t1b + cross3(t2b, n);
+          f3 wb = normalize3_vjp(wv, bb);
+          axisb = axisb + wb - n * dot3(n, wb);
+        }
+        R2b[2] = axisb.x;
+        R2b[5] = axisb.y;
+        R2b[8] = axisb.z;
+      }
+      q4 gqb = quat_to_3x3_vjp(gq, R2b);
+      q4 xrb1, gqt;
+      qmul_vjp(xrl, gquat, gqb, xrb1, gqt);
+      f3 gpb;
+      q4 xrb2;
+      rotate_vjp(gpos, xrl, p2b, gpb, xrb2);
+      add3(xpb + 3 * lb, p2b);
+      add4(xrb + 4 * lb, qadd(xrb1, xrb2));
     }
     tm.sync();
   }

@@ -215,4 +215,32 @@ static __device__ __noinline__ void two_geom_contact_vjp(int kind, f3 p1v, f3 u1
   }
 }
 
+// The contact of a two-geom slot (values, as stage_contacts computes them):
+// dist, pos and the frame rows n, t1, t2.  Out of line: the constraint-row
+// reverse calls it only for such slots.
+static __device__ __noinline__ void two_geom_contact(int kind, f3 p1, f3 u1, float r1, float h1, f3 p2, f3 u2,
+                                                     float r2, float h2, float* out) {
+  f3 ca = p1, cb = p2, n, pos;
+  float dist;
+  if (kind == BXM_CON_SPHERE_CAPSULE) {
+    cb = closest_segment_point(p2 - u2 * h2, p2 + u2 * h2, p1);
+  } else if (kind == BXM_CON_CAPSULE_CAPSULE) {
+    closest_seg_seg(p1 - u1 * h1, p1 + u1 * h1, p2 - u2 * h2, p2 + u2 * h2, ca, cb);
+  }
+  sphere_sphere(ca, r1, cb, r2, dist, pos, n);
+  out[0] = dist;
+  st3(out + 1, pos);
+  make_frame(n, out + 4);  // rows n, t1, t2
+}
+
+// The manifold vertex of a plane-box slot (box frame; -1: the slot repeats
+// an earlier vertex and is inactive).  Out of line, as two_geom_contact.
+static __device__ __noinline__ int plane_box_vertex(f3 p1, f3 n, f3 p2, const float* R2, f3 h, int sub) {
+  float dd;
+  f3 pp;
+  int v = -1;
+  plane_box(p1, n, p2, R2, h, sub, dd, pp, &v);
+  return v;
+}
+
 }  // namespace braxg
