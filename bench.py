@@ -404,49 +404,56 @@ def run_braxg(args):
   h_act.copy_(acts[args.warmup:].cpu())
   h_q = torch.empty(n, nq_, dtype=torch.float32).pin_memory()
   h_qd = torch.empty(n, nv_, dtype=torch.float32).pin_memory()
-  d_act = torch.empty(n, nu_, dtype=torch.float32, device=dev)
-  # the same trajectory segment as the device-timed loop: a fresh reset, the
-  # same warm-up steps, then the timed steps with the actions read from host
-  st = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev),
-                      cache=args.state_cache)
-  st2 = pipeline._alloc(model, n, False, dev, cache=args.state_cache)
-  for k in range(args.warmup):
-    pipeline.step(sys_, st, acts[k], n_frames=N_FRAMES, out=st2, **kw)
-    st, st2 = st2, st
-  cs = [pipeline._cstate(st), pipeline._cstate(st2)]  # ping-pong: in = cs[k % 2], out = the other
-  states = [st, st2]
-  c_opt = pipeline._opts(mode, args.threads_per_env, args.envs_per_cta)
-  c_stream = ctypes.c_void_p(stream.cuda_stream)
-  torch.cuda.synchronize()
-  if world > 1:
-    dist.barrier()
-  e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-  api_s = 0.0
-  t0 = time.perf_counter()
-  for k in range(args.steps):
-    e_ev[k][0].record(stream)
-    d_act.copy_(h_act[k], non_blocking=True)
-    ta = time.perf_counter()
-    rc = lib.braxg_step(model.handle, c_stream, n, N_FRAMES, d_act.data_ptr(), ctypes.byref(cs[k % 2]),
-                        ctypes.byref(cs[1 - k % 2]), ctypes.byref(c_opt))
-    api_s += time.perf_counter() - ta
-    if rc != 0:
-      _native.check(rc, 'braxg_step')
-    out_s = states[1 - k % 2]
-    h_q.copy_(out_s.q, non_blocking=True)
-    h_qd.copy_(out_s.qd, non_blocking=True)
-    e_ev[k][1].record(stream)
-    stream.synchronize()
-  t_e2e = max_over_ranks(time.perf_counter() - t0, dev)
-  gpu_e2e = sum(a.elapsed_time(b) for a, b in e_ev) / 1e3
-  e2e = {'value': whole_job_rate(args.steps * n, world, t_e2e), 'unit': 'env-steps/s',
-         'ms_per_step_wall': round(1e3 * t_e2e / args.steps, 4),
-         'ms_per_step_gpu': round(1e3 * gpu_e2e / args.steps, 4),
-         'ms_per_step_api_call': round(1e3 * api_s / args.steps, 4),
-         'path': 'braxg_step through ctypes; actions H2D from pinned memory, q and qd D2H to pinned memory',
-         'h2d_bytes_per_step': n * nu_ * 4,
-         'd2h_bytes_per_step': n * (nq_ + nv_) * 4}
+  def measure_e2e(mode_, kw_):
+    """Env-steps/s of the host-buffer path in one inverse mode."""
+    d_act = torch.empty(n, nu_, dtype=torch.float32, device=dev)
+    # the same trajectory segment as the device-timed loop: a fresh reset, the
+    # same warm-up steps, then the timed steps with the actions read from host
+    st = pipeline.init(sys_, torch.tensor(q0, device=dev), torch.tensor(qd0, device=dev),
+                        cache=args.state_cache)
+    st2 = pipeline._alloc(model, n, False, dev, cache=args.state_cache)
+    for k in range(args.warmup):
+      pipeline.step(sys_, st, acts[k], n_frames=N_FRAMES, out=st2, **kw_)
+      st, st2 = st2, st
+    cs = [pipeline._cstate(st), pipeline._cstate(st2)]  # ping-pong: in = cs[k % 2], out = the other
+    states = [st, st2]
+    c_opt = pipeline._opts(mode_, args.threads_per_env, args.envs_per_cta)
+    c_stream = ctypes.c_void_p(stream.cuda_stream)
+    torch.cuda.synchronize()
+    if world > 1:
+      dist.barrier()
+    e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            for _ in range(args.steps)]
+    api_s = 0.0
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+      e_ev[k][0].record(stream)
+      d_act.copy_(h_act[k], non_blocking=True)
+      ta = time.perf_counter()
+      rc = lib.braxg_step(model.handle, c_stream, n, N_FRAMES, d_act.data_ptr(), ctypes.byref(cs[k % 2]),
+                          ctypes.byref(cs[1 - k % 2]), ctypes.byref(c_opt))
+      api_s += time.perf_counter() - ta
+      if rc != 0:
+        _native.check(rc, 'braxg_step')
+      out_s = states[1 - k % 2]
+      h_q.copy_(out_s.q, non_blocking=True)
+      h_qd.copy_(out_s.qd, non_blocking=True)
+      e_ev[k][1].record(stream)
+      stream.synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, dev)
+    gpu_e2e = sum(a.elapsed_time(b) for a, b in e_ev) / 1e3
+    e2e = {'value': whole_job_rate(args.steps * n, world, t_e2e), 'unit': 'env-steps/s',
+           'ms_per_step_wall': round(1e3 * t_e2e / args.steps, 4),
+           'ms_per_step_gpu': round(1e3 * gpu_e2e / args.steps, 4),
+           'ms_per_step_api_call': round(1e3 * api_s / args.steps, 4),
+           'path': 'braxg_step through ctypes; actions H2D from pinned memory, q and qd D2H to pinned memory',
+           'h2d_bytes_per_step': n * nu_ * 4,
+           'd2h_bytes_per_step': n * (nq_ + nv_) * 4}
+
+    return e2e
+
+  e2e = measure_e2e(mode, kw)
+  other_mode['e2e'] = measure_e2e(other, kw_o)
 
   # ---- roofline -----------------------------------------------------------
   nmv = load_nmv()[WORKLOAD]
