@@ -110,7 +110,7 @@ __device__ __forceinline__ void inertia_mul_vjp(const float* I, f3 p, float m, f
 // (ra, rv) = motion_cross(sa, sv, oa, ov)
 __device__ __forceinline__ void motion_cross_vjp(f3 sa, f3 sv, f3 oa, f3 ov, f3 rab, f3 rvb, f3& sab, f3& svb,
                                                  f3& oab, f3& ovb) {
-  f3 s1, o1, s2, o2, o3;
+  f3 s1, o1, s2, o3;
   cross_vjp(sa, oa, rab, s1, o1);
   cross_vjp(sa, ov, rvb, s2, ovb);
   cross_vjp(sv, oa, rvb, svb, o3);

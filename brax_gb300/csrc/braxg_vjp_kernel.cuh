@@ -93,6 +93,16 @@ __device__ __forceinline__ void snap_save(const Team<T>& tm, float* slot, const 
   for (int i = tm.lane; i < arena_words / 4; i += T) d[i] = x[i];
   for (int i = tm.lane; i < used / 4; i += T) d[arena_words / 4 + i] = t[i];
 }
+// 16 bytes global -> shared without a register round trip; every copy a lane
+// issues is in flight at once until its cp.async.wait_all.
+__device__ __forceinline__ void copy16_async(float4* smem_dst, const float4* gmem_src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem_src) : "memory");
+}
+// The arena and the tape are in shared memory; the snapshot, the arena and
+// the tape start on 16-byte boundaries (the checked build verifies the first
+// two and the slot stride).  The caller's team sync makes the copies visible
+// to the other lanes.
 template <int T>
 __device__ __forceinline__ void snap_load(const Team<T>& tm, const float* slot, float* arena, int arena_words,
                                           float* tape, int tape_cap) {
@@ -100,8 +110,9 @@ __device__ __forceinline__ void snap_load(const Team<T>& tm, const float* slot, 
   float4* x = reinterpret_cast<float4*>(arena);
   float4* t = reinterpret_cast<float4*>(tape);
   const int used = tape_used(slot + arena_words, tape_cap);
-  for (int i = tm.lane; i < arena_words / 4; i += T) x[i] = d[i];
-  for (int i = tm.lane; i < used / 4; i += T) t[i] = d[arena_words / 4 + i];
+  for (int i = tm.lane; i < arena_words / 4; i += T) copy16_async(x + i, d + i);
+  for (int i = tm.lane; i < used / 4; i += T) copy16_async(t + i, d + arena_words / 4 + i);
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 template <int T, int NVB>
