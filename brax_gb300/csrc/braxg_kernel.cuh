@@ -104,6 +104,17 @@ __device__ __forceinline__ void copy_arena(const Team<T>& tm, float* dst, const 
   const float4* s = reinterpret_cast<const float4*>(src);
   for (int i = tm.lane; i < words / 4; i += T) d[i] = s[i];
 }
+// copy_arena from global into shared memory as cp.async 16-byte copies, all in
+// flight at once, waited for before it returns (the caller's team sync makes
+// them visible to the other lanes)
+template <int T>
+__device__ __forceinline__ void copy_arena_to_shared(const Team<T>& tm, float* dst, const float* src, int words) {
+  for (int i = tm.lane; i < words / 4; i += T) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst + 4 * i);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src + 4 * i) : "memory");
+  }
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
 
 // Copies the words of an arena that hold position-level terms: everything
 // before the scratch region, the mass matrix (in scratch unless the
@@ -113,14 +124,24 @@ __device__ __forceinline__ void copy_arena(const Team<T>& tm, float* dst, const 
 // The active row count is read from `arena` (the destination on a restore,
 // the source on a store) once the part before scratch is there, and clamped
 // to the model's row count.
-template <int T>
+// kRestore: `dst` is the env's arena in shared memory and `src` its global
+// cache slot.
+template <int T, bool kRestore>
 __device__ __forceinline__ void copy_position_terms(const Team<T>& tm, float* dst, const float* src, const Layout& L,
                                                     int nv, int m, const float* arena, float* ovf_dst,
                                                     const float* ovf_src) {
-  copy_arena<T>(tm, dst, src, L.scr);
+  if (kRestore)
+    copy_arena_to_shared<T>(tm, dst, src, L.scr);
+  else
+    copy_arena<T>(tm, dst, src, L.scr);
   tm.sync();
   const int nrow = min(max(reinterpret_cast<const int*>(arena + L.misc)[0], 0), m);
-  if (L.M >= L.scr) copy_arena<T>(tm, dst + L.M, src + L.M, al4(nv * L.ldm));
+  if (L.M >= L.scr) {
+    if (kRestore)
+      copy_arena_to_shared<T>(tm, dst + L.M, src + L.M, al4(nv * L.ldm));
+    else
+      copy_arena<T>(tm, dst + L.M, src + L.M, al4(nv * L.ldm));
+  }
   const int novf = nrow - L.jcap;
   if (novf > 0 && ovf_dst != ovf_src) {
     const int o0 = L.jovf & ~3, o1 = al4(L.jovf + novf * L.ldj);
@@ -151,7 +172,7 @@ __device__ __noinline__ bool restore_cache(const StepArgs& a, const EnvBase& B, 
   // checked build: a misaligned slot is not used (and is flagged by the caller)
   if (kChecked && ((reinterpret_cast<uintptr_t>(slot) | reinterpret_cast<uintptr_t>(w.b)) & 15u) != 0u) return false;
   // overflow rows: into the arena, or from the input's cache slot to the output's
-  copy_position_terms<T>(tm, w.b, slot, *w.L, md.nv, md.m, w.b, w.L->ovf_g ? w.g : w.b, slot);
+  copy_position_terms<T, true>(tm, w.b, slot, *w.L, md.nv, md.m, w.b, w.L->ovf_g ? w.g : w.b, slot);
   tm.sync();
   const int tag = reinterpret_cast<const int*>(w.at(w.L->misc))[11];
   const int want = cache_tag<T>(*w.L, true);
@@ -171,7 +192,7 @@ __device__ __noinline__ void store_cache(const StepArgs& a, const EnvBase& B, co
   float* slot = a.out.cache + (B.env + env) * a.cache_stride;
   if (bx_misaligned<T>(w, slot, w.b)) return;
   // overflow rows: from the arena's scratch end, or already in this slot
-  copy_position_terms<T>(tm, slot, w.b, *w.L, md.nv, md.m, w.b, slot, w.L->ovf_g ? slot : w.b);
+  copy_position_terms<T, false>(tm, slot, w.b, *w.L, md.nv, md.m, w.b, slot, w.L->ovf_g ? slot : w.b);
 }
 
 // Per-stage cycle accumulation (only when a profile buffer is passed): lane 0
